@@ -1,0 +1,399 @@
+/*
+ * swr.h — C ABI of the GB300 per-frame rasterization pipeline.
+ *
+ * This library replaces the per-frame render path of swraster-viewer
+ * (Rust) with hand-written sm_103a CUDA kernels. Every entry point is plain C:
+ * opaque handles, plain pointers and sizes, a status code, no exceptions, no
+ * aborts. A Rust crate (or ctypes, cgo, JNI) binds to it verbatim.
+ *
+ * Reference interface each entry point replaces (paths inside the reference
+ * project):
+ *   swr_scene_create       Scene::from_gltf                   src/scene.rs:145-354
+ *                          (+ load-time precompute driven by load_scene,
+ *                           src/main.rs:100-291)
+ *   swr_camera_init        RenderCamera::new                  src/rendercamera.rs:28-63
+ *   swr_camera_update      RenderCamera::update_matrices      src/rendercamera.rs:78-86
+ *   swr_renderer_create    Renderer::new                      src/renderer.rs:165-198
+ *   swr_render_frame       Renderer::render_scene             src/renderer.rs:201-256
+ *                        + Renderer::update_auto_exposure     src/renderer.rs:258-290
+ *   swr_blit               Renderer::blit_to_buffer           src/renderer.rs:293-355
+ *   swr_read_visbuffer     (no reference counterpart: the reference keeps a
+ *                           per-tile packet index, src/tilerasterizer.rs:33-36;
+ *                           this exports primitive + triangle ID per pixel)
+ *
+ * Conventions
+ *   - Every call returns swr_status; swr_last_error() gives a message for the
+ *     calling thread's last failure.
+ *   - A scene is immutable after creation and may be shared by any number of
+ *     renderers and streams. A renderer is single-threaded: one per
+ *     thread/stream (the reference wraps its renderer in a Mutex,
+ *     src/main.rs:312).
+ *   - `stream` arguments are cudaStream_t values passed as void* (NULL = the
+ *     legacy default stream).
+ *   - Matrices are column-major float[16] (glam's layout).
+ *   - RGBA8 pixels pack R in the most significant byte:
+ *     r<<24 | g<<16 | b<<8 | a  (src/util.rs:98-100).
+ */
+#ifndef SWR_H
+#define SWR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SWR_ABI_VERSION 1
+
+typedef enum swr_status {
+    SWR_OK = 0,
+    SWR_INVALID_ARG = 1,
+    SWR_NO_MEMORY = 2,
+    SWR_OVERFLOW = 3,     /* a device capacity (bins, clip output) was exceeded */
+    SWR_TIMEOUT = 4,      /* a bounded device wait gave up */
+    SWR_CUDA_ERROR = 5,
+    SWR_IO_ERROR = 6,
+    SWR_BAD_SCENE = 7,
+    SWR_UNSUPPORTED = 8,
+    SWR_BUSY = 9          /* admission refused: memory budget or slots exhausted */
+} swr_status;
+
+/* Texture types, src/texture.rs:19-26. They select the mip filter. */
+enum {
+    SWR_TEX_SRGB = 0,
+    SWR_TEX_NORMAL = 1,
+    SWR_TEX_METALLIC_ROUGHNESS = 2,
+    SWR_TEX_CUBEMAP = 3,
+    SWR_TEX_LINEAR = 4
+};
+
+/* Wrap modes, src/texture.rs:554-558. */
+enum {
+    SWR_WRAP_REPEAT = 0,
+    SWR_WRAP_MIRRORED_REPEAT = 1,
+    SWR_WRAP_CLAMP_TO_EDGE = 2
+};
+
+/* Reciprocal square root used by Vec3x4::normalize (src/math.rs:10-49).
+ * AARCH64 reproduces FRSQRTE + one FRSQRTS step (the reference as built on
+ * Arm hosts such as Grace); IEEE is 1/sqrt(x) with two correctly rounded
+ * operations (the reference's portable fallback). */
+enum {
+    SWR_RSQRT_IEEE = 0,
+    SWR_RSQRT_AARCH64 = 1
+};
+
+/* ------------------------------------------------------------------ */
+/* Scene description (in-memory; the synthetic-scene and glTF loaders  */
+/* both produce this).                                                 */
+/* ------------------------------------------------------------------ */
+
+typedef struct swr_texture_desc {
+    uint32_t width;
+    uint32_t height;
+    uint32_t type;            /* SWR_TEX_* */
+    uint32_t reserved;
+    const uint32_t* rgba8;    /* width*height texels, R in MSB */
+} swr_texture_desc;
+
+typedef struct swr_texref {
+    int32_t texture;          /* index into swr_scene_desc.textures, -1 = none */
+    uint32_t wrap_s;          /* SWR_WRAP_* */
+    uint32_t wrap_t;
+    uint32_t reserved;
+} swr_texref;
+
+/* glTF pbrMetallicRoughness material as read by Material::from_gltf,
+ * src/scene.rs:690-780. */
+typedef struct swr_material_desc {
+    float base_color_factor[4];
+    float metallic_factor;
+    float roughness_factor;
+    float emissive_factor[3];
+    float occlusion_strength;   /* default 1 */
+    float alpha_cutoff;         /* default 0.5 */
+    float transmission;         /* KHR_materials_transmission factor */
+    uint32_t alpha_mask;        /* glTF alphaMode == MASK */
+    uint32_t has_transmission;  /* KHR_materials_transmission present -> translucent */
+    swr_texref base_color;
+    swr_texref metallic_roughness;
+    swr_texref normal;
+    swr_texref emissive;
+    swr_texref occlusion;
+    swr_texref transmission_texture;
+} swr_material_desc;
+
+/* One glTF primitive (src/scene.rs:439-495). normals/tangents/texcoords
+ * may be NULL: normals are then generated (compute_smooth_normals), tangents
+ * generated (compute_tangents) and texcoords zero-filled, as the reference
+ * loader does. */
+typedef struct swr_primitive_desc {
+    uint32_t vertex_count;
+    uint32_t index_count;       /* multiple of 3 */
+    const float* positions;     /* vertex_count * 3 */
+    const float* normals;       /* vertex_count * 3, or NULL */
+    const float* tangents;      /* vertex_count * 4, or NULL */
+    const float* texcoords;     /* vertex_count * 2, or NULL */
+    const uint32_t* indices;    /* index_count */
+    int32_t material;           /* -1 = material 0, as src/scene.rs:493 */
+    uint32_t reserved;
+} swr_primitive_desc;
+
+typedef struct swr_mesh_desc {
+    uint32_t primitive_count;
+    uint32_t reserved;
+    const swr_primitive_desc* primitives;
+} swr_mesh_desc;
+
+/* A flattened node. `world` is the final (parent-composed) transform;
+ * `local` is the node's own transform, which the reference uses as the
+ * initial bounding-sphere centre (src/scene.rs:384-394). For root nodes
+ * both are equal. */
+typedef struct swr_node_desc {
+    float world[16];
+    float local[16];
+    int32_t mesh;               /* -1 = no mesh */
+    uint32_t reserved;
+} swr_node_desc;
+
+typedef struct swr_scene_desc {
+    uint32_t mesh_count;
+    uint32_t node_count;
+    uint32_t material_count;
+    uint32_t texture_count;
+    const swr_mesh_desc* meshes;
+    const swr_node_desc* nodes;
+    const swr_material_desc* materials;
+    const swr_texture_desc* textures;
+    /* Environment cubemap faces in +X,-X,+Y,-Y,+Z,-Z order, each
+     * size*size RGBA8 (the unpacked cross of src/texture.rs:922-971). */
+    uint32_t cubemap_face_size;
+    uint32_t voxel_grid_size;   /* 128 in the reference (src/main.rs:228) */
+    const uint32_t* cubemap_faces;
+    uint32_t specular_samples;  /* GGX prefilter samples, 64 (src/scene.rs:179) */
+    uint32_t brdf_lut_size;     /* 128 (src/scene.rs:221) */
+    float gi_sh_scale;          /* 0.25 (src/main.rs:54) */
+    float sky_visibility;       /* 1.0 (src/main.rs:280) */
+    uint32_t host_threads;      /* precompute threads, 0 = all cores */
+    uint32_t flags;             /* SWR_SCENE_* */
+} swr_scene_desc;
+
+/* swr_scene_desc.flags */
+#define SWR_SCENE_HOST_ONLY 1u  /* build and precompute only; no device copy
+                                   (swr_scene_export works, rendering does not) */
+
+typedef struct swr_scene swr_scene;
+
+swr_status swr_scene_create(const swr_scene_desc* desc, swr_scene** out);
+void swr_scene_destroy(swr_scene* scene);
+
+typedef struct swr_scene_info {
+    uint64_t triangle_count;    /* sum over nodes of their mesh's triangles */
+    uint64_t vertex_count;
+    uint64_t device_bytes;      /* HBM held by the scene */
+    uint32_t node_count;
+    uint32_t draw_count;        /* (node, primitive) pairs */
+    float bounds_min[3];
+    float bounds_max[3];
+    float bounds_center[3];
+    float bounds_diagonal;
+} swr_scene_info;
+
+swr_status swr_scene_get_info(const swr_scene* scene, swr_scene_info* out);
+
+/* Read-only host view of the processed scene (generated normals and
+ * tangents, mip chains, prefiltered cubemap, BRDF LUT, voxel grid). Test
+ * infrastructure uses it to feed a CPU implementation the same inputs the
+ * kernels consume. Pointers stay valid until swr_scene_destroy. */
+typedef struct swr_texture_view {
+    uint32_t width;
+    uint32_t height;
+    uint32_t type;
+    uint32_t mip_count;         /* max_mip_level + 1 */
+    const uint32_t* data;       /* all mips and faces */
+    uint64_t data_len;          /* texels */
+    const uint32_t* mip_offsets;
+    const uint32_t* mip_widths;
+    const uint32_t* mip_heights;
+    const uint32_t* array_stride;
+    float width_height_vec[4];
+} swr_texture_view;
+
+typedef struct swr_primitive_view {
+    uint32_t vertex_count;
+    uint32_t index_count;
+    const float* positions;     /* vertex_count * 4 (x, y, z, 1) */
+    const float* normals;       /* vertex_count * 4 (x, y, z, 0) */
+    const float* tangents;      /* vertex_count * 4 */
+    const float* texcoords;     /* vertex_count * 2 */
+    const uint32_t* indices;
+    uint32_t material;
+    uint32_t triangle_id_base;  /* static ID of triangle 0 (per mesh) */
+    float sphere[4];            /* bounding sphere centre xyz, radius */
+} swr_primitive_view;
+
+typedef struct swr_mesh_view {
+    uint32_t primitive_count;
+    uint32_t opaque_count;
+    uint32_t translucent_count;
+    uint32_t reserved;
+    const uint32_t* primitives;       /* index into swr_scene_host_view.primitives */
+    const uint32_t* opaque;           /* local primitive indices, src/scene.rs:276-284 */
+    const uint32_t* translucent;
+} swr_mesh_view;
+
+typedef struct swr_node_view {
+    float transform[16];
+    float sphere[4];            /* bounding_sphere_world */
+    int32_t mesh;
+    uint32_t triangle_id_base;  /* static ID of this node's first triangle */
+} swr_node_view;
+
+typedef struct swr_material_view {
+    float base_color_factor[4];
+    float metallic_factor;
+    float roughness_factor;
+    float emissive_factor[3];
+    float occlusion_strength;
+    float alpha_cutoff;
+    float transmission;
+    uint32_t is_alpha_tested;
+    uint32_t is_translucent;
+    int32_t tex[6];             /* base, metallic-roughness, normal, emissive, occlusion, transmission; -1 = none */
+    uint32_t wrap_s[6];
+    uint32_t wrap_t[6];
+} swr_material_view;
+
+typedef struct swr_scene_host_view {
+    uint32_t primitive_count;
+    uint32_t mesh_count;
+    uint32_t node_count;
+    uint32_t material_count;
+    uint32_t texture_count;
+    uint32_t voxel_size;        /* grid is voxel_size^3 */
+    const swr_primitive_view* primitives;
+    const swr_mesh_view* meshes;
+    const swr_node_view* nodes;
+    const swr_material_view* materials;
+    const swr_texture_view* textures;
+    swr_texture_view cubemap;
+    swr_texture_view cubemap_specular;
+    swr_texture_view brdf_lut;
+    float irradiance_sh[4][3];
+    float light_direction[3];
+    float light_color[3];
+    float voxel_world_min[3];
+    float voxel_world_max[3];
+    const float* voxel_light_intensity;   /* voxel_size^3 (sun visibility, blurred) */
+    float voxel_gi_sh4_const[4][4];       /* per-voxel SH4 rgb (+w filled per voxel) */
+} swr_scene_host_view;
+
+swr_status swr_scene_export(const swr_scene* scene, swr_scene_host_view* out);
+
+/* ------------------------------------------------------------------ */
+/* Camera (src/rendercamera.rs). Host maths, same operation order as  */
+/* glam 0.30.                                                          */
+/* ------------------------------------------------------------------ */
+
+typedef struct swr_camera {
+    float position[3];
+    float fov;
+    float width;
+    float height;
+    float one_over_width;
+    float one_over_height;
+    float near_plane;
+    float far_plane;
+    float yaw;
+    float pitch;
+    float roll;
+    float view_normal[3];
+    float view[16];
+    float projection[16];
+    float view_project[16];
+    float inverse_view_project[16];
+    float skybox_transposed[16];
+    float view_clip_planes[6][4];
+} swr_camera;
+
+swr_status swr_camera_init(swr_camera* cam, const float position[3], const float look_at[3],
+                           float fov, float width, float height, float far_plane);
+swr_status swr_camera_update(swr_camera* cam);
+
+/* ------------------------------------------------------------------ */
+/* Plain per-frame renderer                                            */
+/* ------------------------------------------------------------------ */
+
+typedef struct swr_renderer_opts {
+    uint32_t rsqrt_mode;        /* SWR_RSQRT_*, default AARCH64 */
+    uint32_t sched_tile;        /* raster scheduling tile: 8, 16, 32 or 64 (0 = 64) */
+    uint64_t bin_capacity;      /* initial (triangle, tile) pair capacity, 0 = auto */
+    uint32_t raster_warps;      /* warps per raster CTA, 0 = default */
+    uint32_t flags;             /* reserved, 0 */
+} swr_renderer_opts;
+
+typedef struct swr_renderer swr_renderer;
+
+swr_status swr_renderer_create(int32_t width, int32_t height, const swr_renderer_opts* opts,
+                               swr_renderer** out);
+void swr_renderer_destroy(swr_renderer* r);
+
+/* render_scene + update_auto_exposure(dt). Enqueued on `stream`; returns
+ * once the frame is enqueued (and, when dt > 0, after the exposure step's
+ * host callback is enqueued). Bin overflow is detected on the device and
+ * the frame is re-rendered with a larger capacity on the next call to
+ * swr_renderer_sync, swr_blit or swr_read_visbuffer. */
+swr_status swr_render_frame(swr_renderer* r, const swr_scene* scene, const swr_camera* camera,
+                            float dt, void* stream);
+
+/* Waits for the frame and reports device-side errors (overflow retries
+ * happen here). */
+swr_status swr_renderer_sync(swr_renderer* r);
+
+/* Copies the tonemapped RGBA8 frame into `pixels` (host or device memory),
+ * row_stride in pixels (0 = width). For an odd height the last row is left
+ * untouched, as blit_to_buffer's chunks_exact drops it (src/renderer.rs:298). */
+swr_status swr_blit(swr_renderer* r, uint32_t* pixels, size_t row_stride, void* stream);
+
+/* Visibility buffer, width*height entries: (static triangle ID << 3) | fan
+ * index for covered pixels, UINT64_MAX where depth stayed +inf. Static
+ * triangle IDs number triangles in scene order (node, primitive, triangle);
+ * see swr_node_view.triangle_id_base. */
+swr_status swr_read_visbuffer(swr_renderer* r, uint64_t* ids, void* stream);
+
+/* Device pointers to the renderer's own outputs (valid until the next
+ * frame or destroy). */
+swr_status swr_renderer_device_outputs(swr_renderer* r, const uint32_t** rgba8,
+                                       const uint64_t** vis);
+
+swr_status swr_renderer_get_exposure(const swr_renderer* r, float* exposure);
+swr_status swr_renderer_set_exposure(swr_renderer* r, float exposure);
+
+typedef struct swr_frame_stats {
+    uint64_t triangles_in;      /* triangles entering the front end */
+    uint64_t triangles_clipped; /* triangles that went through the clipper */
+    uint64_t setup_triangles;   /* triangles after clip/cull with >= 1 tile */
+    uint64_t bin_pairs;         /* (triangle, tile) pairs */
+    uint64_t bin_capacity;
+    uint32_t tiles;
+    uint32_t overflow_retries;
+    float tile_luminance_mean;
+    float exposure;
+} swr_frame_stats;
+
+swr_status swr_renderer_get_stats(swr_renderer* r, swr_frame_stats* out);
+
+/* Per-tile centre luminance of the last frame (tiles_x * tiles_y floats,
+ * 64-pixel reference tiles), the auto-exposure meter input
+ * (src/tilerasterizer.rs:103-106). */
+swr_status swr_renderer_get_tile_luminance(swr_renderer* r, float* out, uint32_t count);
+
+const char* swr_last_error(void);
+int32_t swr_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SWR_H */

@@ -1,0 +1,80 @@
+"""ctypes binding of the CPU oracle (test infrastructure only).
+
+The oracle restates the reference's per-frame path on the CPU; tests, the
+smoke check and bench.py's CPU-baseline leg use it to check or time against
+the CUDA path. The product never imports this module.
+"""
+import ctypes as C
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "swr_oracle.cpp")
+LIB = os.path.join(HERE, "liboracle.so")
+ROOT = os.path.dirname(HERE)
+sys.path.insert(0, os.path.join(ROOT, "swraster-viewer_gb300"))
+import swr  # noqa: E402  (structure definitions only)
+
+# -ffp-contract=off: the reference never fuses multiply and add.
+FLAGS = ["-O3", "-std=c++17", "-fPIC", "-shared", "-pthread", "-ffp-contract=off", "-fno-fast-math"]
+
+
+def build(force=False):
+    deps = [SRC, os.path.join(ROOT, "include", "swr.h")]
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(d) for d in deps):
+        cmd = ["g++"] + FLAGS + [SRC, "-o", LIB]
+        p = subprocess.run(cmd, capture_output=True, text=True)
+        if p.returncode != 0:
+            raise RuntimeError("oracle build failed:\n" + p.stderr)
+    return LIB
+
+
+class Opts(C.Structure):
+    _fields_ = [("rsqrt_mode", C.c_uint32), ("threads", C.c_uint32), ("dt", C.c_float), ("ev", C.c_float)]
+
+
+class Result(C.Structure):
+    _fields_ = [("ev", C.c_float), ("exposure", C.c_float), ("target", C.c_float), ("tiles", C.c_uint32),
+                ("packets", C.c_uint64), ("triangles_in", C.c_uint64)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB)
+        L.oracle_render.argtypes = [C.POINTER(swr.SceneHostView), C.POINTER(swr.Camera), C.c_int32, C.c_int32,
+                                    C.POINTER(Opts), C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(Result)]
+        L.oracle_render.restype = C.c_int
+        for n in ("oracle_frsqrte", "oracle_rsqrt_aarch64"):
+            getattr(L, n).argtypes = [C.c_float]
+            getattr(L, n).restype = C.c_float
+        L.oracle_frsqrts.argtypes = [C.c_float, C.c_float]
+        L.oracle_frsqrts.restype = C.c_float
+        _lib = L
+    return _lib
+
+
+def render(view, cam, width, height, rsqrt_mode=swr.RSQRT_AARCH64, threads=1, dt=0.0, ev=1.0):
+    """Returns (rgba8 (H,W) u32, vis (H,W) u64, tile_lum, Result)."""
+    rgba = np.zeros((height, width), np.uint32)
+    vis = np.zeros((height, width), np.uint64)
+    tl = np.zeros(((width + 63) // 64) * ((height + 63) // 64), np.float32)
+    res = Result()
+    o = Opts(rsqrt_mode, threads, dt, ev)
+    rc = lib().oracle_render(C.byref(view), C.byref(cam), width, height, C.byref(o),
+                             rgba.ctypes.data_as(C.c_void_p), vis.ctypes.data_as(C.c_void_p),
+                             tl.ctypes.data_as(C.c_void_p), C.byref(res))
+    if rc != 0:
+        raise RuntimeError("oracle_render failed")
+    return rgba, vis, tl, res
+
+
+if __name__ == "__main__":
+    print(build(force=True))

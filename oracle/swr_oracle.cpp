@@ -1,0 +1,1179 @@
+// CPU oracle for the per-frame rasterization path of swraster-viewer.
+//
+// TEST INFRASTRUCTURE ONLY. This file restates, in plain C++, the reference's
+// per-frame path (Renderer::render_scene + update_auto_exposure +
+// blit_to_buffer) so tests can check the CUDA kernels against it. Nothing in
+// the product links, imports or calls it; only tests/, the smoke check and
+// bench.py's CPU-baseline leg do.
+//
+// Parity status: unpinned against the reference binary. The reference is
+// Rust; no Rust toolchain or vendored crates exist here, so it cannot be run
+// and it ships no tests or golden images. Fidelity is argued line by line
+// (every function cites the reference file:line it follows) and pinned where
+// possible by known-answer tests derived from the reference's formulas and by
+// checking the Arm FRSQRTE/FRSQRTS emulation against the real instructions on
+// an aarch64 host.
+//
+// Structure follows the reference: 4-wide "Vec4" lanes are float[4] with
+// per-lane IEEE operations in the reference's order (glam never fuses a
+// multiply and an add; this file must be compiled with -ffp-contract=off),
+// tiles of 64x64 pixels hold 2x2-quad buffers (color, depth, packet index,
+// barycentrics), packets are queued per tile in the canonical sequential order
+// (node rank after the stable distance sort, opaque primitive, triangle, fan)
+// when run single-threaded, and in rayon-like nondeterministic order when run
+// multi-threaded (the timed CPU baseline).
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+#include <numeric>
+#include <thread>
+#include <vector>
+
+#include "../include/swr.h"
+
+namespace orc {
+
+// ---------------------------------------------------------------- lanes
+struct F4 {
+    float l[4];
+};
+static inline F4 splat(float v) { return {{v, v, v, v}}; }
+static inline F4 mk(float a, float b, float c, float d) { return {{a, b, c, d}}; }
+#define LANEWISE(op)                                                                           \
+    static inline F4 operator op(F4 a, F4 b) {                                                 \
+        return {{a.l[0] op b.l[0], a.l[1] op b.l[1], a.l[2] op b.l[2], a.l[3] op b.l[3]}};   \
+    }
+LANEWISE(+)
+LANEWISE(-)
+LANEWISE(*)
+LANEWISE(/)
+#undef LANEWISE
+static inline F4 operator+(F4 a, float s) { return a + splat(s); }
+static inline F4 operator-(F4 a, float s) { return a - splat(s); }
+static inline F4 operator*(F4 a, float s) { return a * splat(s); }
+static inline F4 operator+(float s, F4 a) { return splat(s) + a; }
+static inline F4 operator-(float s, F4 a) { return splat(s) - a; }
+static inline F4 operator/(float s, F4 a) { return splat(s) / a; }
+// glam max/min/clamp with IEEE maxNum/minNum semantics (scalar f32::max).
+static inline F4 vmax(F4 a, F4 b) {
+    F4 r;
+    for (int i = 0; i < 4; ++i) r.l[i] = std::fmax(a.l[i], b.l[i]);
+    return r;
+}
+static inline F4 vmin(F4 a, F4 b) {
+    F4 r;
+    for (int i = 0; i < 4; ++i) r.l[i] = std::fmin(a.l[i], b.l[i]);
+    return r;
+}
+static inline F4 vclamp(F4 v, F4 lo, F4 hi) { return vmin(vmax(v, lo), hi); }
+static inline F4 vfloor(F4 a) {
+    F4 r;
+    for (int i = 0; i < 4; ++i) r.l[i] = std::floor(a.l[i]);
+    return r;
+}
+static inline F4 vround(F4 a) {
+    F4 r;
+    for (int i = 0; i < 4; ++i) r.l[i] = std::round(a.l[i]);
+    return r;
+}
+typedef bool B4[4];
+
+struct V3x4 {
+    F4 x, y, z;
+};
+static inline V3x4 operator+(V3x4 a, V3x4 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+static inline V3x4 operator-(V3x4 a, V3x4 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+static inline V3x4 operator*(V3x4 a, V3x4 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+static inline V3x4 operator*(V3x4 a, F4 s) { return {a.x * s, a.y * s, a.z * s}; }
+static inline V3x4 operator*(V3x4 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+static inline V3x4 operator-(V3x4 a, float s) { return {a.x - s, a.y - s, a.z - s}; }
+static inline V3x4 operator+(V3x4 a, float s) { return {a.x + s, a.y + s, a.z + s}; }
+static inline V3x4 operator/(V3x4 a, V3x4 b) { return {a.x / b.x, a.y / b.y, a.z / b.z}; }
+static inline V3x4 v3splat(float v) { return {splat(v), splat(v), splat(v)}; }
+static inline V3x4 v3f(float x, float y, float z) { return {splat(x), splat(y), splat(z)}; }
+// Vec3x4::dot (src/math.rs:88-90).
+static inline F4 dot(V3x4 a, V3x4 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+static inline V3x4 cross(V3x4 a, V3x4 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+static inline V3x4 v3select(const B4 m, V3x4 a, V3x4 b) {
+    V3x4 r;
+    for (int i = 0; i < 4; ++i) {
+        r.x.l[i] = m[i] ? a.x.l[i] : b.x.l[i];
+        r.y.l[i] = m[i] ? a.y.l[i] : b.y.l[i];
+        r.z.l[i] = m[i] ? a.z.l[i] : b.z.l[i];
+    }
+    return r;
+}
+
+// ---------------------------------------------------------------- rsqrt
+// Arm FRSQRTE (FPRSqrtEstimate, FPCR.AH = 0, no increased precision) and
+// FRSQRTS (FPRSqrtStepFused), restated from the Arm Architecture Reference
+// Manual pseudocode.
+static int recip_sqrt_estimate(int a) {
+    if (a < 256) {
+        a = a * 2 + 1;
+    } else {
+        a = (a >> 1) << 1;
+        a = (a + 1) * 2;
+    }
+    long long b = 512;
+    while ((long long)a * (b + 1) * (b + 1) < (1LL << 28)) b++;
+    return (int)((b + 1) / 2);
+}
+static uint8_t g_est[512];
+static std::once_flag g_est_once;
+static void init_est() {
+    for (int a = 128; a < 512; ++a) g_est[a] = (uint8_t)(recip_sqrt_estimate(a) & 0xFF);
+}
+static float frsqrte(float x) {
+    std::call_once(g_est_once, init_est);
+    uint32_t b;
+    std::memcpy(&b, &x, 4);
+    if (std::isnan(x)) {
+        b |= 0x00400000u;
+        float r;
+        std::memcpy(&r, &b, 4);
+        return r;
+    }
+    if (x == 0.0f) return std::copysign(INFINITY, x);
+    if (b >> 31) return NAN;
+    if (std::isinf(x)) return 0.0f;
+    int e = (int)((b >> 23) & 0xFF);
+    uint64_t frac = (uint64_t)(b & 0x7FFFFF) << 29;
+    if (e == 0) {
+        while (!((frac >> 51) & 1)) {
+            frac <<= 1;
+            e -= 1;
+        }
+        frac = (frac << 1) & ((1ULL << 52) - 1);
+    }
+    const int scaled = (e & 1) == 0 ? (int)(256 | (frac >> 44)) : (int)(128 | (frac >> 45));
+    const int rexp = (380 - e) / 2;
+    const uint32_t out = ((uint32_t)(rexp & 0xFF) << 23) | ((uint32_t)g_est[scaled] << 15);
+    float r;
+    std::memcpy(&r, &out, 4);
+    return r;
+}
+static float frsqrts(float a, float b) {
+    if (std::isnan(a)) return a;
+    if (std::isnan(b)) return b;
+    if ((std::isinf(a) && b == 0.0f) || (a == 0.0f && std::isinf(b))) return 1.5f;
+    if (std::isinf(a) || std::isinf(b)) return (std::signbit(a) != std::signbit(b)) ? INFINITY : -INFINITY;
+    // (3 - a*b) / 2 with one rounding: the product is exact in double, the
+    // sum is rounded once by fmaf, halving is exact.
+    return std::fmaf(-a, b, 3.0f) * 0.5f;
+}
+static int g_rsqrt_mode = SWR_RSQRT_AARCH64;
+// rsqrt_vec (src/math.rs:17-49).
+static F4 rsqrt_vec(F4 v) {
+    F4 r;
+    for (int i = 0; i < 4; ++i) {
+        const float x = v.l[i];
+        if (g_rsqrt_mode == SWR_RSQRT_AARCH64) {
+            const float y0 = frsqrte(x);
+            r.l[i] = y0 * frsqrts(x * y0, y0);
+        } else {
+            r.l[i] = 1.0f / std::sqrt(x);
+        }
+    }
+    return r;
+}
+// Vec3x4::normalize (src/math.rs:101-108).
+static inline V3x4 normalize(V3x4 a) {
+    const F4 ol = rsqrt_vec((a.x * a.x + a.y * a.y) + a.z * a.z);
+    return {a.x * ol, a.y * ol, a.z * ol};
+}
+
+// ---------------------------------------------------------------- casts
+static inline uint32_t as_u32(float x) {
+    if (!(x > 0.0f)) return 0u;
+    if (x >= 4294967296.0f) return 0xFFFFFFFFu;
+    return (uint32_t)x;
+}
+static inline int32_t as_i32(float x) {
+    if (x != x) return 0;
+    if (x >= 2147483648.0f) return INT32_MAX;
+    if (x <= -2147483648.0f) return INT32_MIN;
+    return (int32_t)x;
+}
+static inline uint8_t as_u8(float x) {
+    if (!(x > 0.0f)) return 0;
+    if (x >= 255.0f) return 255;
+    return (uint8_t)x;
+}
+static inline int32_t wsub(int32_t a, int32_t b) { return (int32_t)((uint32_t)a - (uint32_t)b); }
+static inline int32_t wadd(int32_t a, int32_t b) { return (int32_t)((uint32_t)a + (uint32_t)b); }
+static inline int32_t wmul(int32_t a, int32_t b) { return (int32_t)((uint32_t)a * (uint32_t)b); }
+
+// ---------------------------------------------------------------- util.rs
+static inline float unorm(uint32_t c, int shift) { return (float)((c >> shift) & 0xFFu) / 255.0f; }
+// srgb_to_linear_fast (src/util.rs:111-113).
+static inline V3x4 srgb_fast(V3x4 x) { return x * (x * (x * 0.305306011f + 0.682171111f) + 0.012522878f); }
+// tonemap (src/util.rs:37-41).
+static inline V3x4 tonemap(V3x4 c) {
+    const float k = 0.2f;
+    return (c / (c + k)) * (1.0f + k);
+}
+
+// ScalarInterpolator / Vec3Interpolator (src/util.rs:149-194).
+struct SI {
+    float a, da, db;
+    static SI from3(float x, float y, float z) { return {x, y - x, z - x}; }
+    F4 interp(F4 b1, F4 b2) const { return (a + b1 * da) + b2 * db; }
+};
+struct VI {
+    SI c[3];
+    V3x4 interp(F4 b1, F4 b2) const { return {c[0].interp(b1, b2), c[1].interp(b1, b2), c[2].interp(b1, b2)}; }
+};
+
+// ---------------------------------------------------------------- texture.rs
+struct Tex {
+    const swr_texture_view* t;
+    uint32_t wrap_s, wrap_t;
+};
+static inline float mipw(const swr_texture_view* t, uint32_t m) { return (float)t->mip_widths[m]; }
+static inline float miph(const swr_texture_view* t, uint32_t m) { return (float)t->mip_heights[m]; }
+// apply_wrap_mode (src/texture.rs:578-589).
+static F4 apply_wrap(F4 texel, F4 dim, uint32_t mode) {
+    F4 t = texel;
+    if (mode == SWR_WRAP_REPEAT) {
+        t = texel - vfloor(texel / dim) * dim;
+    } else if (mode == SWR_WRAP_MIRRORED_REPEAT) {
+        const F4 two = dim * 2.0f;
+        const F4 m = texel - vfloor(texel / two) * two;
+        t = vmin(m, two - m);
+    }
+    return vmin(t, dim - 1.0f);
+}
+// compute_mip_level (src/texture.rs:851-863).
+static uint32_t compute_mip_level(const swr_texture_view* t, F4 du_dv) {
+    const F4 d = du_dv * mk(t->width_height_vec[0], t->width_height_vec[1], t->width_height_vec[2],
+                            t->width_height_vec[3]);
+    const float dx2 = d.l[0] * d.l[0] + d.l[2] * d.l[2];
+    const float dy2 = d.l[1] * d.l[1] + d.l[3] * d.l[3];
+    const float fp = (dx2 + dy2) * 0.5f;
+    const uint32_t u = as_u32(std::fmax(fp, 1.0f));
+    uint32_t lg = 0;
+    while ((u >> (lg + 1)) != 0) ++lg;
+    const uint32_t mip = lg >> 1;
+    const uint32_t mx = t->mip_count - 1;
+    return mip < mx ? mip : mx;
+}
+static V3x4 gather_rgb(const swr_texture_view* t, const uint32_t idx[4]) {
+    V3x4 r;
+    for (int i = 0; i < 4; ++i) {
+        const uint32_t c = t->data[idx[i]];
+        r.x.l[i] = unorm(c, 24);
+        r.y.l[i] = unorm(c, 16);
+        r.z.l[i] = unorm(c, 8);
+    }
+    return r;
+}
+// sample4_rgb / sample4_alpha (src/texture.rs:680-714).
+static void sample4_index(const Tex& tx, F4 u, F4 v, F4 du_dv, uint32_t idx[4]) {
+    const swr_texture_view* t = tx.t;
+    const uint32_t m = compute_mip_level(t, du_dv);
+    const F4 wf = splat(mipw(t, m)), hf = splat(miph(t, m));
+    const F4 x = apply_wrap(vfloor(u * wf), wf, tx.wrap_s);
+    const F4 y = apply_wrap(vfloor(v * hf), hf, tx.wrap_t);
+    for (int i = 0; i < 4; ++i) idx[i] = t->mip_offsets[m] + as_u32(y.l[i]) * t->mip_widths[m] + as_u32(x.l[i]);
+}
+static V3x4 sample4_rgb(const Tex& tx, F4 u, F4 v, F4 du_dv) {
+    uint32_t idx[4];
+    sample4_index(tx, u, v, du_dv, idx);
+    return gather_rgb(tx.t, idx);
+}
+static F4 sample4_alpha(const Tex& tx, F4 u, F4 v, F4 du_dv) {
+    uint32_t idx[4];
+    sample4_index(tx, u, v, du_dv, idx);
+    F4 r;
+    for (int i = 0; i < 4; ++i) r.l[i] = unorm(tx.t->data[idx[i]], 0);
+    return r;
+}
+// cubemap_uv_from_normal (src/texture.rs:593-644).
+static void cubemap_uv(V3x4 n, F4& uf, F4& vf, uint32_t slice[4]) {
+    for (int i = 0; i < 4; ++i) {
+        const float nx = n.x.l[i], ny = n.y.l[i], nz = n.z.l[i];
+        const float ax = std::fabs(nx), ay = std::fabs(ny), az = std::fabs(nz);
+        const bool mx = ax >= ay && ax >= az;
+        const bool my = ay > ax && ay >= az;
+        const float sx = nx >= 0.0f ? 1.0f : -1.0f;
+        const float sy = ny >= 0.0f ? 1.0f : -1.0f;
+        const float sz = nz >= 0.0f ? 1.0f : -1.0f;
+        const float u = mx ? (-nz * sx) : (my ? nx : nx * sz);
+        const float v = mx ? -ny : (my ? nz * sy : -ny);
+        float den = mx ? ax : (my ? ay : az);
+        den = std::fmax(den, 1.0e-19f);
+        uf.l[i] = 0.5f * (u / den + 1.0f);
+        vf.l[i] = 0.5f * (v / den + 1.0f);
+        const float fx = nx >= 0.0f ? 0.0f : 1.0f;
+        const float fy = ny >= 0.0f ? 2.0f : 3.0f;
+        const float fz = nz >= 0.0f ? 4.0f : 5.0f;
+        slice[i] = as_u32(mx ? fx : (my ? fy : fz));
+    }
+}
+// sample_cubemap_rgb (src/texture.rs:646-663).
+static V3x4 sample_cubemap_rgb(const swr_texture_view* t, V3x4 n, const uint32_t mip_in[4]) {
+    F4 u, v;
+    uint32_t slice[4];
+    cubemap_uv(n, u, v, slice);
+    uint32_t idx[4];
+    for (int i = 0; i < 4; ++i) {
+        const uint32_t mx = t->mip_count - 1;
+        const uint32_t m = mip_in[i] < mx ? mip_in[i] : mx;
+        const float wf = mipw(t, m), hf = miph(t, m);
+        float x = std::round(u.l[i] * (wf - 1.0f));
+        float y = std::round(v.l[i] * (hf - 1.0f));
+        x = std::fmin(std::fmax(x, 0.0f), wf - 1.0f);
+        y = std::fmin(std::fmax(y, 0.0f), hf - 1.0f);
+        idx[i] = t->mip_offsets[m] + slice[i] * t->array_stride[m] + as_u32(y) * t->mip_widths[m] + as_u32(x);
+    }
+    return gather_rgb(t, idx);
+}
+// sample_cubemap_trilinear_rgb (src/texture.rs:665-678).
+static V3x4 sample_cubemap_trilinear(const swr_texture_view* t, V3x4 n, F4 mip) {
+    const F4 mxv = splat((float)(t->mip_count - 1));
+    const F4 m = vclamp(mip, splat(0.0f), mxv);
+    const F4 m0 = vfloor(m);
+    const F4 m1 = vmin(m0 + 1.0f, mxv);
+    const F4 tt = m - m0;
+    uint32_t i0[4], i1[4];
+    for (int i = 0; i < 4; ++i) {
+        i0[i] = as_u32(m0.l[i]);
+        i1[i] = as_u32(m1.l[i]);
+    }
+    const V3x4 c0 = sample_cubemap_rgb(t, n, i0);
+    const V3x4 c1 = sample_cubemap_rgb(t, n, i1);
+    return {c0.x + (c1.x - c0.x) * tt, c0.y + (c1.y - c0.y) * tt, c0.z + (c1.z - c0.z) * tt};
+}
+// sample_bilinear_rgb, mip 0, slice 0, ClampToEdge (src/texture.rs:730-790).
+static V3x4 sample_bilinear_rgb(const swr_texture_view* t, F4 u, F4 v) {
+    const F4 wf = splat(mipw(t, 0)), hf = splat(miph(t, 0));
+    const F4 xf = u * wf - 0.5f, yf = v * hf - 0.5f;
+    const F4 x0 = vfloor(xf), y0 = vfloor(yf);
+    const F4 x1 = x0 + 1.0f, y1 = y0 + 1.0f;
+    const F4 fx = xf - x0, fy = yf - y0;
+    const F4 ofx = 1.0f - fx, ofy = 1.0f - fy;
+    const F4 cx0 = apply_wrap(x0, wf, SWR_WRAP_CLAMP_TO_EDGE), cy0 = apply_wrap(y0, hf, SWR_WRAP_CLAMP_TO_EDGE);
+    const F4 cx1 = apply_wrap(x1, wf, SWR_WRAP_CLAMP_TO_EDGE), cy1 = apply_wrap(y1, hf, SWR_WRAP_CLAMP_TO_EDGE);
+    uint32_t i00[4], i10[4], i01[4], i11[4];
+    const uint32_t w = t->mip_widths[0], off = t->mip_offsets[0];
+    for (int i = 0; i < 4; ++i) {
+        i00[i] = off + as_u32(cy0.l[i]) * w + as_u32(cx0.l[i]);
+        i10[i] = off + as_u32(cy0.l[i]) * w + as_u32(cx1.l[i]);
+        i01[i] = off + as_u32(cy1.l[i]) * w + as_u32(cx0.l[i]);
+        i11[i] = off + as_u32(cy1.l[i]) * w + as_u32(cx1.l[i]);
+    }
+    const V3x4 p00 = gather_rgb(t, i00), p10 = gather_rgb(t, i10), p01 = gather_rgb(t, i01), p11 = gather_rgb(t, i11);
+    const F4 w00 = ofx * ofy, w10 = fx * ofy, w01 = ofx * fy, w11 = fx * fy;
+    return {((p00.x * w00 + p10.x * w10) + p01.x * w01) + p11.x * w11,
+            ((p00.y * w00 + p10.y * w10) + p01.y * w01) + p11.y * w11,
+            ((p00.z * w00 + p10.z * w10) + p01.z * w01) + p11.z * w11};
+}
+
+// ---------------------------------------------------------------- voxel
+struct Voxel {
+    uint32_t n;
+    float min[3], vs[3];
+    const float* light;
+    float gi[4][4];
+};
+// get_filtered_gi_sh4_packed_vec (src/voxelgrid.rs:264-368) over a grid whose
+// voxels all hold gi[c] except w of coefficient 0 (light intensity).
+static void voxel_gi(const Voxel& g, V3x4 p, V3x4 out_rgb[4], F4 out_w[4]) {
+    const F4 vx = (p.x - g.min[0]) / splat(g.vs[0]);
+    const F4 vy = (p.y - g.min[1]) / splat(g.vs[1]);
+    const F4 vz = (p.z - g.min[2]) / splat(g.vs[2]);
+    const F4 x0f = vfloor(vx), y0f = vfloor(vy), z0f = vfloor(vz);
+    uint64_t x0[4], y0[4], z0[4], x1[4], y1[4], z1[4];
+    const uint64_t nm1 = g.n - 1;
+    for (int i = 0; i < 4; ++i) {
+        auto us = [](float f) -> uint64_t {
+            if (!(f > 0.0f)) return 0;
+            if (f >= 1.8446744e19f) return UINT64_MAX;
+            return (uint64_t)f;
+        };
+        x0[i] = std::min(us(x0f.l[i]), nm1);
+        y0[i] = std::min(us(y0f.l[i]), nm1);
+        z0[i] = std::min(us(z0f.l[i]), nm1);
+        x1[i] = std::min(x0[i] + 1, nm1);
+        y1[i] = std::min(y0[i] + 1, nm1);
+        z1[i] = std::min(z0[i] + 1, nm1);
+    }
+    const F4 fx = vx - x0f, fy = vy - y0f, fz = vz - z0f;
+    auto coeff = [&](int c, int comp, const uint64_t* X, const uint64_t* Y, const uint64_t* Z) {
+        F4 r;
+        for (int i = 0; i < 4; ++i) {
+            if (c == 0 && comp == 3)
+                r.l[i] = g.light[Z[i] * g.n * g.n + Y[i] * g.n + X[i]];
+            else
+                r.l[i] = g.gi[c][comp];
+        }
+        return r;
+    };
+    auto tri = [&](int c, int comp) {
+        const F4 v000 = coeff(c, comp, x0, y0, z0), v001 = coeff(c, comp, x0, y0, z1);
+        const F4 v010 = coeff(c, comp, x0, y1, z0), v011 = coeff(c, comp, x0, y1, z1);
+        const F4 v100 = coeff(c, comp, x1, y0, z0), v101 = coeff(c, comp, x1, y0, z1);
+        const F4 v110 = coeff(c, comp, x1, y1, z0), v111 = coeff(c, comp, x1, y1, z1);
+        const F4 v00 = v000 * (1.0f - fx) + v100 * fx;
+        const F4 v01 = v001 * (1.0f - fx) + v101 * fx;
+        const F4 v10 = v010 * (1.0f - fx) + v110 * fx;
+        const F4 v11 = v011 * (1.0f - fx) + v111 * fx;
+        const F4 v0 = v00 * (1.0f - fy) + v10 * fy;
+        const F4 v1 = v01 * (1.0f - fy) + v11 * fy;
+        return v0 * (1.0f - fz) + v1 * fz;
+    };
+    for (int c = 0; c < 4; ++c) {
+        out_rgb[c] = {tri(c, 0), tri(c, 1), tri(c, 2)};
+        out_w[c] = tri(c, 3);
+    }
+}
+
+// ---------------------------------------------------------------- glam mats
+struct M4 {
+    float m[16];  // column-major
+};
+static inline void mat_vec(const float* m, const float v[4], float o[4]) {
+    for (int r = 0; r < 4; ++r) o[r] = ((m[r] * v[0] + m[4 + r] * v[1]) + m[8 + r] * v[2]) + m[12 + r] * v[3];
+}
+static inline M4 mat_mul(const float* a, const float* b) {
+    M4 r;
+    for (int c = 0; c < 4; ++c) mat_vec(a, b + 4 * c, r.m + 4 * c);
+    return r;
+}
+static inline float len4(const float* c) { return std::sqrt((c[0] * c[0] + c[1] * c[1]) + (c[2] * c[2] + c[3] * c[3])); }
+static inline float dot4(const float* a, const float* b) { return (a[0] * b[0] + a[1] * b[1]) + (a[2] * b[2] + a[3] * b[3]); }
+
+// ---------------------------------------------------------------- renderer.rs
+struct IV2 {
+    int32_t x, y;
+};
+struct Vertex {
+    float pos_clip[4];
+    float pos_world[3];
+    float normal[3];
+    float tangent[4];
+    float uv[2];
+};
+// RasterPacket (src/renderer.rs:58-76) plus the triangle identity this build
+// exports in its visibility buffer.
+struct Packet {
+    IV2 min, max;
+    IV2 p[3];
+    SI zow, oow;
+    VI normals, tangents;
+    SI tsign, uow, vow;
+    VI pww;
+    float ooa;
+    uint32_t material;
+    float du_dv[4];
+    uint32_t static_id, fan;
+};
+
+constexpr int TILE = 64;
+
+// BumpQueue-like per-tile queue: lock-free slot allocation, 1024-packet blocks.
+struct Queue {
+    std::atomic<size_t> count{0};
+    std::vector<Packet*> blocks;
+    std::mutex lock;
+    void push(const Packet& p) {
+        const size_t i = count.fetch_add(1, std::memory_order_relaxed);
+        const size_t b = i / 1024;
+        Packet* blk;
+        {
+            std::lock_guard<std::mutex> g(lock);
+            while (blocks.size() <= b) blocks.push_back(new Packet[1024]);
+            blk = blocks[b];
+        }
+        blk[i % 1024] = p;
+    }
+    const Packet& get(size_t i) const { return blocks[i / 1024][i % 1024]; }
+    size_t size() const { return count.load(std::memory_order_relaxed); }
+    ~Queue() {
+        for (Packet* b : blocks) delete[] b;
+    }
+};
+
+struct Tile {
+    IV2 smin, smax;
+    Queue opaque;
+    std::vector<V3x4> color;
+    std::vector<F4> depth;
+    std::vector<uint32_t> pidx;  // 4 per quad
+    std::vector<F4> bary1, bary2;
+    float center_luminance = 1.0f;
+};
+
+struct Frame {
+    const swr_scene_host_view* s;
+    const swr_camera* cam;
+    int width, height, tiles_x, tiles_y;
+    float width_f, height_f;
+    std::vector<Tile*> tiles;
+    Voxel vox;
+};
+
+static Tex texof(const Frame& f, const swr_material_view& m, int slot) {
+    return {&f.s->textures[m.tex[slot]], m.wrap_s[slot], m.wrap_t[slot]};
+}
+
+// clip_to_screen_subpixels (src/renderer.rs:834-846).
+static IV2 to_screen(const Frame& f, const float* v) {
+    const float nx = v[0] / v[3], ny = v[1] / v[3];
+    const float sx = ((nx + 1.0f) * f.width_f) / 2.0f;
+    const float sy = ((1.0f - ny) * f.height_f) / 2.0f;
+    return {as_i32(std::round(sx * 16.0f)), as_i32(std::round(sy * 16.0f))};
+}
+
+// bin_triangle (src/renderer.rs:668-831), opaque mode.
+static void bin_triangle(Frame& f, const Vertex* v, uint32_t material, uint32_t static_id, uint32_t fan) {
+    const IV2 p0 = to_screen(f, v[0].pos_clip), p1 = to_screen(f, v[1].pos_clip), p2 = to_screen(f, v[2].pos_clip);
+    const int32_t area = wsub(wmul(wsub(p1.x, p0.x), wsub(p2.y, p0.y)), wmul(wsub(p2.x, p0.x), wsub(p1.y, p0.y)));
+    if (area > 0) return;
+    const int32_t wsp = f.width * 16, hsp = f.height * 16;
+    const IV2 mns = {std::max(std::min(std::min(p0.x, p1.x), p2.x), 0), std::max(std::min(std::min(p0.y, p1.y), p2.y), 0)};
+    const IV2 mxs = {std::min(std::max(std::max(p0.x, p1.x), p2.x), wsp),
+                     std::min(std::max(std::max(p0.y, p1.y), p2.y), hsp)};
+    const IV2 mnp = {mns.x >> 4, mns.y >> 4};
+    const IV2 mxp = {wadd(mxs.x, 16) >> 4, wadd(mxs.y, 16) >> 4};
+    const int32_t aa = area < 0 ? (int32_t)(0u - (uint32_t)area) : area;
+    Packet pk;
+    pk.ooa = 1.0f / (float)aa;
+    float oow[3], zow[3], uow[3], vow[3];
+    for (int k = 0; k < 3; ++k) {
+        oow[k] = 1.0f / v[k].pos_clip[3];
+        zow[k] = v[k].pos_clip[2] * oow[k];
+        uow[k] = v[k].uv[0] * oow[k];
+        vow[k] = v[k].uv[1] * oow[k];
+    }
+    pk.zow = SI::from3(zow[0], zow[1], zow[2]);
+    pk.oow = SI::from3(oow[0], oow[1], oow[2]);
+    for (int c = 0; c < 3; ++c) {
+        pk.normals.c[c] = SI::from3(v[0].normal[c], v[1].normal[c], v[2].normal[c]);
+        pk.tangents.c[c] = SI::from3(v[0].tangent[c], v[1].tangent[c], v[2].tangent[c]);
+        pk.pww.c[c] = SI::from3(v[0].pos_world[c] * oow[0], v[1].pos_world[c] * oow[1], v[2].pos_world[c] * oow[2]);
+    }
+    pk.tsign = SI::from3(v[0].tangent[3], v[1].tangent[3], v[2].tangent[3]);
+    pk.uow = SI::from3(uow[0], uow[1], uow[2]);
+    pk.vow = SI::from3(vow[0], vow[1], vow[2]);
+    const float dx1 = (float)wsub(p1.x, p0.x), dx2 = (float)wsub(p2.x, p0.x);
+    const float dy1 = (float)wsub(p1.y, p0.y), dy2 = (float)wsub(p2.y, p0.y);
+    const float du1 = uow[1] - uow[0], du2 = uow[2] - uow[0], dv1 = vow[1] - vow[0], dv2 = vow[2] - vow[0];
+    const float sc = pk.ooa * 16.0f;
+    pk.du_dv[0] = (du1 * dy2 - du2 * dy1) * sc;
+    pk.du_dv[1] = (du2 * dx1 - du1 * dx2) * sc;
+    pk.du_dv[2] = (dv1 * dy2 - dv2 * dy1) * sc;
+    pk.du_dv[3] = (dv2 * dx1 - dv1 * dx2) * sc;
+    pk.p[0] = p0;
+    pk.p[1] = p1;
+    pk.p[2] = p2;
+    pk.material = material;
+    pk.static_id = static_id;
+    pk.fan = fan;
+    const int32_t bx0 = mnp.x / TILE, by0 = mnp.y / TILE;
+    const int32_t bx1 = (mxp.x + TILE - 1) / TILE, by1 = (mxp.y + TILE - 1) / TILE;
+    const int32_t ntiles = (int32_t)f.tiles.size();
+    for (int32_t y = by0; y < by1; ++y) {
+        for (int32_t x = bx0; x < bx1; ++x) {
+            const int32_t bi = y * f.tiles_x + x;
+            if (bi < 0 || bi >= ntiles) continue;
+            Tile* t = f.tiles[bi];
+            const IV2 cmin = {std::max(mnp.x, t->smin.x), std::max(mnp.y, t->smin.y)};
+            const IV2 cmax = {std::min(mxp.x, t->smax.x), std::min(mxp.y, t->smax.y)};
+            if (cmax.x - cmin.x < 1 || cmax.y - cmin.y < 1) continue;
+            pk.min = cmin;
+            pk.max = cmax;
+            t->opaque.push(pk);
+        }
+    }
+}
+
+// clip_against_frustum (src/renderer.rs:579-665).
+static void clip_triangle(Frame& f, const Vertex* tri, uint32_t material, uint32_t static_id) {
+    static const float planes[6][4] = {{0, 0, 1, 1}, {0, 0, -1, 1}, {1, 0, 0, 1},
+                                       {-1, 0, 0, 1}, {0, 1, 0, 1}, {0, -1, 0, 1}};
+    Vertex poly[16], np[16];
+    int len = 3;
+    poly[0] = tri[0];
+    poly[1] = tri[1];
+    poly[2] = tri[2];
+    auto lerp = [](const Vertex& a, const Vertex& b, float t) {
+        Vertex o;
+        for (int i = 0; i < 4; ++i) o.pos_clip[i] = a.pos_clip[i] + (b.pos_clip[i] - a.pos_clip[i]) * t;
+        for (int i = 0; i < 3; ++i) o.pos_world[i] = a.pos_world[i] + (b.pos_world[i] - a.pos_world[i]) * t;
+        for (int i = 0; i < 3; ++i) o.normal[i] = a.normal[i] + (b.normal[i] - a.normal[i]) * t;
+        for (int i = 0; i < 4; ++i) o.tangent[i] = a.tangent[i] + (b.tangent[i] - a.tangent[i]) * t;
+        for (int i = 0; i < 2; ++i) o.uv[i] = a.uv[i] + (b.uv[i] - a.uv[i]) * t;
+        return o;
+    };
+    for (int p = 0; p < 6; ++p) {
+        if (len == 0) return;
+        int nl = 0;
+        for (int i = 0; i < len; ++i) {
+            const Vertex& cur = poly[i];
+            const Vertex& prv = poly[(i + len - 1) % len];
+            const float dc = dot4(planes[p], cur.pos_clip), dp = dot4(planes[p], prv.pos_clip);
+            if (dc >= 0.0f) {
+                if (!(dp >= 0.0f)) np[nl++] = lerp(prv, cur, dp / (dp - dc));
+                np[nl++] = cur;
+            } else if (dp >= 0.0f) {
+                np[nl++] = lerp(prv, cur, dp / (dp - dc));
+            }
+        }
+        for (int i = 0; i < nl; ++i) poly[i] = np[i];
+        len = nl;
+    }
+    if (len < 3) return;
+    for (int i = 1; i < len - 1; ++i) {
+        const Vertex t3[3] = {poly[0], poly[i], poly[i + 1]};
+        bin_triangle(f, t3, material, static_id, (uint32_t)(i - 1));
+    }
+}
+
+// render_primitive_inner (src/renderer.rs:470-574) for one triangle.
+static void process_triangle(Frame& f, const swr_primitive_view& p, const float* model, const float* mvp, bool clip,
+                             uint32_t t, uint32_t static_base) {
+    Vertex v[3];
+    for (int k = 0; k < 3; ++k) {
+        const uint32_t i = p.indices[3 * t + k];
+        const float* pos = p.positions + 4 * (size_t)i;
+        const float* n = p.normals + 4 * (size_t)i;
+        const float* tg = p.tangents + 4 * (size_t)i;
+        float world[4];
+        mat_vec(model, pos, world);
+        mat_vec(mvp, pos, v[k].pos_clip);
+        for (int c = 0; c < 3; ++c) {
+            v[k].pos_world[c] = world[c];
+            v[k].normal[c] = (model[c] * n[0] + model[4 + c] * n[1]) + model[8 + c] * n[2];
+            v[k].tangent[c] = (model[c] * tg[0] + model[4 + c] * tg[1]) + model[8 + c] * tg[2];
+        }
+        v[k].tangent[3] = tg[3];
+        v[k].uv[0] = p.texcoords[2 * (size_t)i];
+        v[k].uv[1] = p.texcoords[2 * (size_t)i + 1];
+    }
+    if (clip)
+        clip_triangle(f, v, p.material, static_base + t);
+    else
+        bin_triangle(f, v, p.material, static_base + t, 0);
+}
+
+// ---------------------------------------------------------------- tilerasterizer.rs
+static inline size_t qindex(const Tile& t, IV2 px) {
+    const int32_t lx = (px.x - t.smin.x) / 2, ly = (px.y - t.smin.y) / 2;
+    const int32_t wq = (t.smax.x - t.smin.x) / 2;
+    return (size_t)(ly * wq + lx);
+}
+
+struct Edges {
+    F4 a01, b01, c01, a12, b12, c12, a20, b20, c20;
+    F4 sx01, sx12, sx20, sy01, sy12, sy20;
+};
+
+static void fine_raster(const Frame& f, Tile& t, const Packet& pk, const Edges& e, size_t packet_index, int32_t xs,
+                        int32_t ys, int32_t xe, int32_t ye) {
+    const swr_material_view& mat = f.s->materials[pk.material];
+    const F4 x = mk((float)(xs + 8), (float)(xs + 24), (float)(xs + 8), (float)(xs + 24));
+    const F4 y = mk((float)(ys + 8), (float)(ys + 8), (float)(ys + 24), (float)(ys + 24));
+    F4 w0r = (e.a12 * x + e.b12 * y) + e.c12;
+    F4 w1r = (e.a20 * x + e.b20 * y) + e.c20;
+    F4 w2r = (e.a01 * x + e.b01 * y) + e.c01;
+    const F4 ooa = splat(pk.ooa);
+    for (int32_t py = ys; py < ye; py += 32) {
+        F4 w0 = w0r, w1 = w1r, w2 = w2r;
+        for (int32_t px = xs; px < xe; px += 32) {
+            B4 mask;
+            bool any = false;
+            for (int i = 0; i < 4; ++i) {
+                mask[i] = w0.l[i] >= 0.0f && w1.l[i] >= 0.0f && w2.l[i] >= 0.0f;
+                any |= mask[i];
+            }
+            if (any) {
+                const F4 b1 = w1 * ooa, b2 = w2 * ooa;
+                const F4 w = 1.0f / pk.oow.interp(b1, b2);
+                const F4 z = pk.zow.interp(b1, b2) * w;
+                const IV2 pix = {px >> 4, py >> 4};
+                const size_t qi = qindex(t, pix);
+                // depth_test (src/tilerasterizer.rs:511-523).
+                const F4 cur = t.depth[qi];
+                B4 fm;
+                bool anyp = false;
+                for (int i = 0; i < 4; ++i) {
+                    fm[i] = mask[i] && (z.l[i] <= cur.l[i]);
+                    anyp |= fm[i];
+                }
+                if (anyp) {
+                    // VBufferOpaqueShader::shade (src/shader.rs:32-63).
+                    if (mat.is_alpha_tested) {
+                        const Tex tx = texof(f, mat, 0);
+                        const F4 u = pk.uow.interp(b1, b2) * w, v = pk.vow.interp(b1, b2) * w;
+                        const F4 a = sample4_alpha(tx, u, v, mk(pk.du_dv[0], pk.du_dv[1], pk.du_dv[2], pk.du_dv[3]));
+                        for (int i = 0; i < 4; ++i) fm[i] = fm[i] && (a.l[i] >= mat.alpha_cutoff);
+                    }
+                    for (int i = 0; i < 4; ++i) {
+                        if (!fm[i]) continue;
+                        t.pidx[4 * qi + i] = (uint32_t)packet_index;
+                        t.bary1[qi].l[i] = b1.l[i];
+                        t.bary2[qi].l[i] = b2.l[i];
+                        t.depth[qi].l[i] = z.l[i];
+                    }
+                }
+            }
+            w0 = w0 + e.sx12;
+            w1 = w1 + e.sx20;
+            w2 = w2 + e.sx01;
+        }
+        w0r = w0r + e.sy12;
+        w1r = w1r + e.sy20;
+        w2r = w2r + e.sy01;
+    }
+}
+
+// rasterize_packet + coarse_raster (src/tilerasterizer.rs:114-291).
+static void rasterize_packet(const Frame& f, Tile& t, const Packet& pk, size_t packet_index) {
+    const IV2 p0 = pk.p[0], p1 = pk.p[1], p2 = pk.p[2];
+    auto bias = [](int32_t a, int32_t b) { return (a < 0 || (a == 0 && b > 0)) ? 0 : -1; };
+    const int32_t a01 = wsub(p1.y, p0.y), b01 = wsub(p0.x, p1.x);
+    const int32_t c01 = wadd(wsub(wmul(p1.x, p0.y), wmul(p0.x, p1.y)), bias(a01, b01));
+    const int32_t a12 = wsub(p2.y, p1.y), b12 = wsub(p1.x, p2.x);
+    const int32_t c12 = wadd(wsub(wmul(p2.x, p1.y), wmul(p1.x, p2.y)), bias(a12, b12));
+    const int32_t a20 = wsub(p0.y, p2.y), b20 = wsub(p2.x, p0.x);
+    const int32_t c20 = wadd(wsub(wmul(p0.x, p2.y), wmul(p2.x, p0.y)), bias(a20, b20));
+    Edges e;
+    e.a01 = splat((float)a01); e.b01 = splat((float)b01); e.c01 = splat((float)c01);
+    e.a12 = splat((float)a12); e.b12 = splat((float)b12); e.c12 = splat((float)c12);
+    e.a20 = splat((float)a20); e.b20 = splat((float)b20); e.c20 = splat((float)c20);
+    e.sx01 = splat((float)wmul(a01, 32)); e.sx12 = splat((float)wmul(a12, 32)); e.sx20 = splat((float)wmul(a20, 32));
+    e.sy01 = splat((float)wmul(b01, 32)); e.sy12 = splat((float)wmul(b12, 32)); e.sy20 = splat((float)wmul(b20, 32));
+    const int32_t wp = pk.max.x - pk.min.x, hp = pk.max.y - pk.min.y;
+    const int32_t xs = (pk.min.x & ~1) * 16, ys = (pk.min.y & ~1) * 16;
+    const int32_t xe = pk.max.x * 16, ye = pk.max.y * 16;
+    if (wp > 16 || hp > 16) {
+        for (int32_t by = ys; by < ye; by += 256) {
+            for (int32_t bx = xs; bx < xe; bx += 256) {
+                const F4 cx = mk((float)(bx + 8), (float)(bx + 256 - 8), (float)(bx + 8), (float)(bx + 256 - 8));
+                const F4 cy = mk((float)(by + 8), (float)(by + 8), (float)(by + 256 - 8), (float)(by + 256 - 8));
+                const F4 w0c = (e.a12 * cx + e.b12 * cy) + e.c12;
+                const F4 w1c = (e.a20 * cx + e.b20 * cy) + e.c20;
+                const F4 w2c = (e.a01 * cx + e.b01 * cy) + e.c01;
+                auto maxel = [](F4 v) { return std::fmax(std::fmax(v.l[0], v.l[1]), std::fmax(v.l[2], v.l[3])); };
+                if (maxel(w0c) < 0.0f || maxel(w1c) < 0.0f || maxel(w2c) < 0.0f) continue;
+                fine_raster(f, t, pk, e, packet_index, bx, by, std::min(bx + 256, xe), std::min(by + 256, ye));
+            }
+        }
+    } else {
+        fine_raster(f, t, pk, e, packet_index, xs, ys, xe, ye);
+    }
+}
+
+// pbr_shader<false> (src/shader.rs:110-309).
+static V3x4 pbr_shader(const Frame& f, const Packet& pk, F4 b1, F4 b2) {
+    const swr_material_view& m = f.s->materials[pk.material];
+    const float PI = 3.14159265358979f;
+    const F4 EPS = splat(1e-6f);
+    const F4 w = 1.0f / pk.oow.interp(b1, b2);
+    const V3x4 in_n = normalize(pk.normals.interp(b1, b2));
+    const V3x4 in_t = normalize(pk.tangents.interp(b1, b2));
+    const F4 tsign = pk.tsign.interp(b1, b2);
+    const V3x4 pw = pk.pww.interp(b1, b2) * w;
+    const F4 uvx = pk.uow.interp(b1, b2) * w;
+    const F4 uvy = pk.vow.interp(b1, b2) * w;
+    const F4 du_dv = mk(pk.du_dv[0], pk.du_dv[1], pk.du_dv[2], pk.du_dv[3]) * w;
+    const V3x4 tw = normalize(in_t - in_n * dot(in_n, in_t));
+    F4 hand;
+    for (int i = 0; i < 4; ++i) hand.l[i] = tsign.l[i] >= 0.0f ? 1.0f : -1.0f;
+    const V3x4 bw = cross(in_n, tw) * hand;
+    V3x4 nw = normalize(in_n);
+    if (m.tex[2] >= 0) {
+        const V3x4 tsn = sample4_rgb(texof(f, m, 2), uvx, uvy, du_dv) * 2.0f - 1.0f;
+        nw = (tw * tsn.x + bw * tsn.y) + in_n * tsn.z;
+        nw = normalize(nw);
+    }
+    const V3x4 ld = v3f(f.s->light_direction[0], f.s->light_direction[1], f.s->light_direction[2]);
+    const V3x4 lc = v3f(f.s->light_color[0], f.s->light_color[1], f.s->light_color[2]);
+    const V3x4 vd = v3f(f.cam->position[0], f.cam->position[1], f.cam->position[2]) - pw;
+    const V3x4 vn = normalize(vd);
+    const F4 ndl = vmax(dot(nw, ld), splat(0.0f));
+    const V3x4 hv = normalize(ld + vn);
+    const F4 ndh = vmax(dot(nw, hv), splat(0.0f));
+    const F4 ndv = vmax(dot(nw, vn), splat(1.0e-4f));
+    const F4 vdh = vmax(dot(vn, hv), splat(0.0f));
+    V3x4 gi_rgb[4];
+    F4 gi_w[4];
+    voxel_gi(f.vox, pw, gi_rgb, gi_w);
+    const F4 vli = vclamp(gi_w[0], splat(0.0f), splat(1.0f));
+    const F4 skyv = vclamp(gi_w[1], splat(0.0f), splat(1.0f));
+    V3x4 bc = v3f(m.base_color_factor[0], m.base_color_factor[1], m.base_color_factor[2]);
+    if (m.tex[0] >= 0) bc = bc * srgb_fast(sample4_rgb(texof(f, m, 0), uvx, uvy, du_dv));
+    F4 rough = splat(m.roughness_factor), metal = splat(m.metallic_factor);
+    if (m.tex[1] >= 0) {
+        const V3x4 mr = sample4_rgb(texof(f, m, 1), uvx, uvy, du_dv);
+        rough = rough * mr.y;
+        metal = metal * mr.z;
+    }
+    rough = vclamp(rough, splat(0.045f), splat(1.0f));
+    metal = vclamp(metal, splat(0.0f), splat(1.0f));
+    F4 ao = splat(1.0f);
+    if (m.tex[4] >= 0) {
+        ao = sample4_rgb(texof(f, m, 4), uvx, uvy, du_dv).x;
+        ao = 1.0f + (ao - 1.0f) * splat(m.occlusion_strength);
+    }
+    const V3x4 f0 = {0.04f + (bc.x - 0.04f) * metal, 0.04f + (bc.y - 0.04f) * metal, 0.04f + (bc.z - 0.04f) * metal};
+    const F4 omvh = 1.0f - vdh;
+    const F4 omvh2 = omvh * omvh;
+    const F4 omvh4 = omvh2 * omvh2;
+    const F4 omvh5 = omvh4 * omvh;
+    const V3x4 fd = f0 + (v3splat(1.0f) - f0) * omvh5;
+    const F4 alpha = rough * rough;
+    const F4 alpha2 = alpha * alpha;
+    const F4 ndh2 = ndh * ndh;
+    const F4 den_d = ndh2 * (alpha2 - 1.0f) + 1.0f;
+    const F4 brdf_d = alpha2 / (splat(PI) * (den_d * den_d) + EPS);
+    F4 k = rough + 1.0f;
+    k = (k * k) * 0.125f;
+    const F4 gv = ndv / ((ndv * (1.0f - k) + k) + EPS);
+    const F4 gl = ndl / ((ndl * (1.0f - k) + k) + EPS);
+    const F4 brdf_g = gv * gl;
+    const F4 spec_dg = (brdf_d * brdf_g) / ((splat(4.0f) * ndl) * ndv + EPS);
+    const V3x4 kd = (v3splat(1.0f) - fd) * (1.0f - metal);
+    const V3x4 lambert = bc * splat(1.0f / PI);
+    const V3x4 cdd = (((lc * kd) * lambert) * ndl) * vli;
+    const V3x4 cds = (((lc * fd) * spec_dg) * ndl) * vli;
+    const V3x4 kdi = (v3splat(1.0f) - f0) * (1.0f - metal);
+    // eval_irradiance_sh_vec (src/shader.rs:102-108).
+    V3x4 irr = ((gi_rgb[0] + gi_rgb[1] * nw.y) + gi_rgb[2] * nw.z) + gi_rgb[3] * nw.x;
+    irr = {vmax(irr.x, splat(0.0f)), vmax(irr.y, splat(0.0f)), vmax(irr.z, splat(0.0f))};
+    const V3x4 cid = ((irr * bc) * kdi) * splat(1.0f / PI);
+    // reflect (src/math.rs:118-120).
+    const V3x4 iv = vn * -1.0f;
+    const V3x4 rd = iv - (nw * dot(iv, nw)) * 2.0f;
+    const F4 spec_mip = rough * splat((float)(f.s->cubemap_specular.mip_count - 1));
+    const V3x4 env = sample_cubemap_trilinear(&f.s->cubemap_specular, rd, spec_mip);
+    const V3x4 lut = sample_bilinear_rgb(&f.s->brdf_lut, vclamp(ndv, splat(0.0f), splat(1.0f)),
+                                         vclamp(rough, splat(0.0f), splat(1.0f)));
+    V3x4 bsf = f0 * lut.x;
+    bsf = {bsf.x + lut.y, bsf.y + lut.y, bsf.z + lut.y};
+    V3x4 cis = env * bsf;
+    const F4 ao_spec = 1.0f + (ao - 1.0f) * 0.5f;
+    cis = cis * (ao_spec * skyv);
+    V3x4 color = ((cdd + cds) + cid) + cis;
+    V3x4 em = v3splat(1.0f);
+    if (m.tex[3] >= 0) em = srgb_fast(sample4_rgb(texof(f, m, 3), uvx, uvy, du_dv));
+    color = color + em * v3f(m.emissive_factor[0], m.emissive_factor[1], m.emissive_factor[2]);
+    return color;
+}
+
+// compute_skybox (src/tilerasterizer.rs:478-508).
+static V3x4 compute_skybox(const Frame& f, IV2 pixel) {
+    const float sx = (float)pixel.x, sy = (float)pixel.y;
+    const F4 px = mk(sx + 0.5f, sx + 1.5f, sx + 0.5f, sx + 1.5f);
+    const F4 py = mk(sy + 0.5f, sy + 0.5f, sy + 1.5f, sy + 1.5f);
+    const F4 ndc_x = (px * f.cam->one_over_width) * 2.0f - 1.0f;
+    const F4 ndc_y = (1.0f - py * f.cam->one_over_height) * 2.0f - 1.0f;
+    const float* m = f.cam->skybox_transposed;
+    const F4 one = splat(1.0f);
+    const V3x4 d = {((ndc_x * m[0] + ndc_y * m[1]) + one * m[2]) + m[3],
+                    ((ndc_x * m[4] + ndc_y * m[5]) + one * m[6]) + m[7],
+                    ((ndc_x * m[8] + ndc_y * m[9]) + one * m[10]) + m[11]};
+    const uint32_t mip0[4] = {0, 0, 0, 0};
+    return srgb_fast(sample_cubemap_rgb(&f.s->cubemap, normalize(d), mip0));
+}
+
+// shade_vbuffer (src/tilerasterizer.rs:386-476).
+static void shade_vbuffer(const Frame& f, Tile& t, bool skybox_only) {
+    const int32_t tw = t.smax.x - t.smin.x, th = t.smax.y - t.smin.y;
+    const int32_t wq = tw / 2;
+    for (int32_t y = 0; y < th / 2; ++y) {
+        const int32_t sy = t.smin.y + y * 2;
+        for (int32_t qx = 0; qx < wq; ++qx) {
+            const IV2 pixel = {t.smin.x + qx * 2, sy};
+            const size_t qi = qindex(t, pixel);
+            if (skybox_only) {
+                t.color[qi] = compute_skybox(f, pixel);
+                continue;
+            }
+            const uint32_t* pi = &t.pidx[4 * qi];
+            const F4 depth = t.depth[qi];
+            B4 dm;
+            bool anyd = false, alld = true;
+            for (int i = 0; i < 4; ++i) {
+                dm[i] = depth.l[i] != INFINITY;
+                anyd |= dm[i];
+                alld &= dm[i];
+            }
+            V3x4 out = v3splat(0.0f);
+            if (anyd) {
+                B4 rem = {dm[0], dm[1], dm[2], dm[3]};
+                for (;;) {
+                    int lane = -1;
+                    for (int i = 0; i < 4; ++i)
+                        if (rem[i]) {
+                            lane = i;
+                            break;
+                        }
+                    if (lane < 0) break;
+                    const uint32_t p = pi[lane];
+                    B4 mask;
+                    for (int i = 0; i < 4; ++i) mask[i] = pi[i] == p;
+                    const Packet& pk = t.opaque.get(p);
+                    const V3x4 c = pbr_shader(f, pk, t.bary1[qi], t.bary2[qi]);
+                    out = v3select(mask, c, out);
+                    for (int i = 0; i < 4; ++i) rem[i] = rem[i] && !mask[i];
+                }
+            }
+            if (!alld) out = v3select(dm, out, compute_skybox(f, pixel));
+            t.color[qi] = out;
+        }
+    }
+}
+
+// render_tile (src/tilerasterizer.rs:72-111), opaque path.
+static void render_tile(const Frame& f, Tile& t) {
+    for (F4& d : t.depth) d = splat(INFINITY);
+    const size_t n = t.opaque.size();
+    for (size_t i = 0; i < n; ++i) rasterize_packet(f, t, t.opaque.get(i), i);
+    shade_vbuffer(f, t, n == 0);
+    const V3x4 cq = t.color[t.color.size() / 2];
+    const F4 lx = (cq.x * 0.2126f + cq.y * 0.7152f) + cq.z * 0.0722f;
+    t.center_luminance = (((lx.l[0] + lx.l[1]) + lx.l[2]) + lx.l[3]) * 0.25f;
+}
+
+template <typename F>
+static void par_for(size_t n, unsigned threads, F fn) {
+    if (threads <= 1) {
+        for (size_t i = 0; i < n; ++i) fn(i);
+        return;
+    }
+    std::atomic<size_t> next{0};
+    auto w = [&]() {
+        for (;;) {
+            const size_t i = next.fetch_add(1);
+            if (i >= n) break;
+            fn(i);
+        }
+    };
+    std::vector<std::thread> pool;
+    for (unsigned k = 1; k < threads; ++k) pool.emplace_back(w);
+    w();
+    for (auto& th : pool) th.join();
+}
+
+}  // namespace orc
+
+extern "C" {
+
+typedef struct oracle_opts {
+    uint32_t rsqrt_mode;
+    uint32_t threads;     /* 1 = canonical sequential order */
+    float dt;
+    float ev;             /* exposure state in: log2 of the current exposure (1.0 fresh) */
+} oracle_opts;
+
+typedef struct oracle_result {
+    float ev;             /* exposure state out */
+    float exposure;       /* exposure the blit used */
+    float target;
+    uint32_t tiles;
+    uint64_t packets;     /* (triangle, tile) pairs queued */
+    uint64_t triangles_in;
+} oracle_result;
+
+// Renderer::render_scene + update_auto_exposure + blit_to_buffer for a fresh
+// Renderer (its vbuffer bary/packet index start at zero). rgba8 (height rows
+// of width; an odd last row is not written, as chunks_exact drops it), vis
+// (width*height) and tile_lum (tiles_x*tiles_y) may be NULL.
+int oracle_render(const swr_scene_host_view* s, const swr_camera* cam, int32_t width, int32_t height,
+                  const oracle_opts* o, uint32_t* rgba8, uint64_t* vis, float* tile_lum, oracle_result* res) {
+    using namespace orc;
+    if (!s || !cam || width <= 0 || height <= 0 || !o) return 1;
+    g_rsqrt_mode = (int)o->rsqrt_mode;
+    const unsigned threads = o->threads ? o->threads : 1;
+    Frame f;
+    f.s = s;
+    f.cam = cam;
+    f.width = width;
+    f.height = height;
+    f.width_f = (float)width;
+    f.height_f = (float)height;
+    f.tiles_x = (width + TILE - 1) / TILE;
+    f.tiles_y = (height + TILE - 1) / TILE;
+    f.vox.n = s->voxel_size;
+    for (int k = 0; k < 3; ++k) {
+        f.vox.min[k] = s->voxel_world_min[k];
+        f.vox.vs[k] = (s->voxel_world_max[k] - s->voxel_world_min[k]) / (float)s->voxel_size;
+    }
+    f.vox.light = s->voxel_light_intensity;
+    std::memcpy(f.vox.gi, s->voxel_gi_sh4_const, sizeof(f.vox.gi));
+    for (int ty = 0; ty < f.tiles_y; ++ty)
+        for (int tx = 0; tx < f.tiles_x; ++tx) {
+            Tile* t = new Tile();
+            t->smin = {tx * TILE, ty * TILE};
+            t->smax = {(tx + 1) * TILE, (ty + 1) * TILE};
+            const size_t nq = (TILE / 2) * (TILE / 2);
+            t->color.assign(nq, v3splat(0.0f));
+            t->depth.assign(nq, splat(INFINITY));
+            t->pidx.assign(4 * nq, 0u);
+            t->bary1.assign(nq, splat(0.0f));
+            t->bary2.assign(nq, splat(0.0f));
+            f.tiles.push_back(t);
+        }
+    // compute_nodes_by_distance (src/renderer.rs:357-367).
+    std::vector<uint32_t> order(s->node_count);
+    std::iota(order.begin(), order.end(), 0u);
+    std::vector<float> key(s->node_count);
+    for (uint32_t i = 0; i < s->node_count; ++i) {
+        const float* c = s->nodes[i].sphere;
+        const float dx = cam->position[0] - c[0], dy = cam->position[1] - c[1], dz = cam->position[2] - c[2];
+        key[i] = (dx * dx + dy * dy) + dz * dz;
+    }
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+        const float x = key[a], y = key[b];
+        if (x != x) return false;
+        if (y != y) return true;
+        return x < y;
+    });
+    // Front end work items: (primitive, model, mvp, clip, 128-triangle batch).
+    struct Item {
+        const swr_primitive_view* p;
+        M4 mvp;
+        const float* model;
+        bool clip;
+        uint32_t t0, t1, static_base;
+    };
+    std::vector<Item> items;
+    uint64_t tri_in = 0;
+    for (uint32_t ni : order) {
+        const swr_node_view& n = s->nodes[ni];
+        if (n.mesh < 0) continue;
+        // render_node: mvp = VP * model (src/renderer.rs:369-384).
+        const M4 mvp = mat_mul(cam->view_project, n.transform);
+        const swr_mesh_view& mesh = s->meshes[n.mesh];
+        for (uint32_t k = 0; k < mesh.opaque_count; ++k) {
+            const swr_primitive_view& p = s->primitives[mesh.primitives[mesh.opaque[k]]];
+            // Mat4 * &BoundingSphere (src/scene.rs:53-63) and
+            // test_sphere_frustum (src/renderer.rs:130-142).
+            const float* M = n.transform;
+            const float scale = ((len4(M) + len4(M + 4)) + len4(M + 8)) / 3.0f;
+            float c[3];
+            for (int r = 0; r < 3; ++r) c[r] = ((M[r] * p.sphere[0] + M[4 + r] * p.sphere[1]) + M[8 + r] * p.sphere[2]) + M[12 + r];
+            const float radius = p.sphere[3] * scale;
+            const float cw[4] = {c[0], c[1], c[2], 1.0f};
+            float cv[4];
+            mat_vec(cam->view, cw, cv);
+            int result = 0;  // 0 inside, 1 intersecting, 2 outside
+            for (int pl = 0; pl < 6; ++pl) {
+                const float d = dot4(cam->view_clip_planes[pl], cv);
+                if (d < -radius) {
+                    result = 2;
+                    break;
+                } else if (d < radius) {
+                    result = 1;
+                }
+            }
+            if (result == 2) continue;
+            const uint32_t nt = p.index_count / 3;
+            tri_in += nt;
+            for (uint32_t t0 = 0; t0 < nt; t0 += 128)
+                items.push_back({&p, mvp, n.transform, result == 1, t0, std::min(nt, t0 + 128),
+                                 n.triangle_id_base + p.triangle_id_base});
+        }
+    }
+    par_for(items.size(), threads, [&](size_t i) {
+        const Item& it = items[i];
+        for (uint32_t t = it.t0; t < it.t1; ++t) process_triangle(f, *it.p, it.model, it.mvp.m, it.clip, t, it.static_base);
+    });
+    uint64_t packets = 0;
+    for (Tile* t : f.tiles) packets += t->opaque.size();
+    par_for(f.tiles.size(), threads, [&](size_t i) { render_tile(f, *f.tiles[i]); });
+    // update_auto_exposure (src/renderer.rs:258-290).
+    float ev = o->ev;
+    float exposure, target = 0.0f;
+    {
+        const size_t n = f.tiles.size();
+        std::vector<float> smp(n);
+        for (size_t i = 0; i < n; ++i) smp[i] = std::log2(std::fmax(f.tiles[i]->center_luminance, 1e-4f));
+        std::sort(smp.begin(), smp.end());
+        size_t trim = (size_t)std::floor((float)n * 0.10f);
+        trim = std::min(trim, (n - 1) / 2);
+        float sum = 0.0f;
+        for (size_t i = trim; i < n - trim; ++i) sum += smp[i];
+        const float mean = sum / (float)(n - 2 * trim);
+        const float y = 0.45f;
+        const float meter = std::fmax((y * 0.2f) / std::fmax((1.0f + 0.2f) - y, 1e-6f), 1e-4f);
+        const float tev0 = std::log2(meter) - mean;
+        target = std::fmin(std::fmax(std::exp2(tev0), 0.05f), 32.0f);
+        const float tev = std::log2(target);
+        const float alpha = 1.0f - std::exp(-(std::fmax(o->dt, 0.0f) / std::fmax(1.0f, 1e-4f)));
+        ev += (tev - ev) * alpha;
+        exposure = std::exp2(ev);
+    }
+    // blit_to_buffer (src/renderer.rs:293-355).
+    if (rgba8) {
+        const int rows2 = height / 2;
+        par_for((size_t)rows2, threads, [&](size_t qy) {
+            const int py = (int)qy * 2;
+            const int ty = py / TILE;
+            for (int tx = 0; tx < f.tiles_x; ++tx) {
+                const Tile& t = *f.tiles[ty * f.tiles_x + tx];
+                const int lq = (py - t.smin.y) / 2;
+                const int wq = (t.smax.x - t.smin.x) / 2;
+                for (int qx = 0; qx < wq; ++qx) {
+                    const int bx = t.smin.x + qx * 2;
+                    V3x4 c = t.color[(size_t)(lq * wq + qx)];
+                    c = c * splat(exposure);
+                    c = tonemap(c);
+                    for (int sy = 0; sy < 2; ++sy)
+                        for (int sx = 0; sx < 2; ++sx) {
+                            const int x = bx + sx;
+                            if (x >= width) continue;
+                            const int ln = sy * 2 + sx;
+                            const uint32_t r = as_u8(c.x.l[ln] * 255.0f), g = as_u8(c.y.l[ln] * 255.0f),
+                                           b = as_u8(c.z.l[ln] * 255.0f);
+                            rgba8[(size_t)(py + sy) * width + x] = (r << 24) | (g << 16) | (b << 8) | 0xFFu;
+                        }
+                }
+            }
+        });
+    }
+    if (vis) {
+        for (int y = 0; y < height; ++y)
+            for (int x = 0; x < width; ++x) {
+                const Tile& t = *f.tiles[(y / TILE) * f.tiles_x + (x / TILE)];
+                const size_t qi = qindex(t, {x & ~1, y & ~1});
+                const int ln = (y & 1) * 2 + (x & 1);
+                uint64_t v = ~0ull;
+                if (t.depth[qi].l[ln] != INFINITY) {
+                    const Packet& pk = t.opaque.get(t.pidx[4 * qi + ln]);
+                    v = ((uint64_t)pk.static_id << 3) | pk.fan;
+                }
+                vis[(size_t)y * width + x] = v;
+            }
+    }
+    if (tile_lum)
+        for (size_t i = 0; i < f.tiles.size(); ++i) tile_lum[i] = f.tiles[i]->center_luminance;
+    if (res) {
+        res->ev = ev;
+        res->exposure = exposure;
+        res->target = target;
+        res->tiles = (uint32_t)f.tiles.size();
+        res->packets = packets;
+        res->triangles_in = tri_in;
+    }
+    for (Tile* t : f.tiles) delete t;
+    return 0;
+}
+
+// Arm FRSQRTE/FRSQRTS emulation, exposed for the known-answer tests.
+float oracle_frsqrte(float x) { return orc::frsqrte(x); }
+float oracle_frsqrts(float a, float b) { return orc::frsqrts(a, b); }
+float oracle_rsqrt_aarch64(float x) {
+    const float y0 = orc::frsqrte(x);
+    return y0 * orc::frsqrts(x * y0, y0);
+}
+
+}  // extern "C"

@@ -1,0 +1,228 @@
+// Internal data layout shared by the host runtime and the CUDA kernels.
+//
+// HBM layout (one scene):
+//   vertices   DVertex[V]   48 B/vertex  {pos.xyz, u} {normal.xyz, v} {tangent.xyzw}
+//   indices    u32[3T]      primitive-local, rebased by DPrimitive.vtx_base
+//   prims      DPrimitive[] nodes DNode[] materials DMaterial[] textures DTexture[]
+//   texels     u32 pool     RGBA8, R in MSB, every mip of every texture
+//   voxel      f32[N^3]     blurred sun visibility (the only per-voxel data the
+//                           non-GI shading path reads; the SH part is constant)
+//
+// Per frame (renderer-owned):
+//   draws      DDraw[D]     (node, primitive) pairs in canonical order, + MVP
+//   chunks     DChunk[]     256-triangle slices of draws, one CTA each
+//   tri_state  u8[T]        0 none, 1 record in slot g, 2 clipped
+//   rec_r      RecRaster[T + extra]   80 B: screen vertices, bbox, z/w, 1/w
+//   rec_s      RecShade [T + extra]  176 B: shading interpolators
+//   fan_base   u32[T]       first extra slot of a clipped triangle's fans 1..6
+//   bins       u32[cap]     record indices grouped by scheduling tile
+//   keys       u64[pitch*rows] per view: orderable(z) << 32 | ~(seq8 + 1)
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace swr {
+
+constexpr int kRefTile = 64;          // reference tile size, src/renderer.rs:14
+constexpr int kSubpixelScale = 16;    // src/tilerasterizer.rs:10
+constexpr int kSubpixelShift = 4;
+constexpr int kChunkTris = 256;       // triangles per front-end CTA
+constexpr uint64_t kEmptyKey = 0xFF800000FFFFFFFFull;  // orderable(+inf) << 32 | 0xFFFFFFFF
+
+struct alignas(16) DVertex {
+    float px, py, pz, u;
+    float nx, ny, nz, v;
+    float tx, ty, tz, tw;
+};
+
+struct alignas(16) DPrimitive {
+    uint32_t vtx_base;
+    uint32_t idx_base;
+    uint32_t tri_count;
+    uint32_t material;
+};
+
+struct alignas(16) DTexture {
+    const uint32_t* data;      // device pointer to mip 0 of this texture
+    uint32_t width, height;
+    uint32_t max_mip;
+    uint32_t pad0;
+    float whv[4];              // width_height_vec
+    uint32_t mip_offset[16];   // relative to data
+    uint32_t mip_w[16];
+    uint32_t mip_h[16];
+    uint32_t array_stride[16];
+    float mip_wf[16];
+    float mip_hf[16];
+};
+
+enum : uint32_t {
+    MAT_ALPHA_TESTED = 1u,
+    MAT_TRANSLUCENT = 2u,
+};
+
+// Texture slots inside DMaterial.tex.
+enum { TS_BASE = 0, TS_MR = 1, TS_NORMAL = 2, TS_EMISSIVE = 3, TS_OCCLUSION = 4, TS_TRANSMISSION = 5 };
+
+struct alignas(16) DMaterial {
+    float base_color[4];
+    float metallic, roughness, occlusion_strength, alpha_cutoff;
+    float emissive[3];
+    uint32_t flags;
+    int32_t tex[6];            // index into scene texture table, -1 none
+    uint32_t wrap_s[6];
+    uint32_t wrap_t[6];
+    float transmission;
+    uint32_t pad[1];
+};
+
+// Scene-wide device constants. The per-voxel SH4 of the non-GI path is
+// the same for every voxel (src/gi.rs:123-149): rgb = irradiance_sh * scale,
+// w0 = light intensity (per voxel), w1 = sky visibility, w2 = w3 = 0.
+struct alignas(16) DScene {
+    const DVertex* vertices;
+    const uint32_t* indices;
+    const DPrimitive* prims;
+    const float* node_xform;   // 16 floats per node
+    const DMaterial* materials;
+    const DTexture* textures;  // scene textures, then cubemap, specular, brdf lut
+    const float* voxel_light;  // voxel_n^3
+    uint32_t tex_cubemap, tex_specular, tex_brdf_lut, voxel_n;
+    float voxel_min[3];
+    float voxel_size_f[3];     // (max - min) / n per axis
+    float gi_rgb[4][3];
+    float sky_visibility;
+    float light_dir[3];
+    float light_color[3];
+    float pad[3];
+};
+
+// One view (camera + resolution + outputs).
+struct alignas(16) DView {
+    float skybox_t[16];        // RenderCamera::skybox_matrix_transposed
+    float cam_pos[3];
+    float one_over_width, one_over_height;
+    float width_f, height_f;
+    float exposure;
+    int32_t width, height;
+    int32_t tiles_x, tiles_y;  // 64-px reference tiles
+    int32_t stiles_x, stiles_y;// scheduling tiles
+    uint32_t stile_base;       // first bin of this view
+    uint32_t scene;            // index into the DScene table
+    uint32_t quad_base;        // first shading quad of this view
+    uint32_t quad_pitch;       // tiles_x * 32
+    uint32_t rsqrt_mode;
+    uint32_t flags;            // 1: write linear colour instead of RGBA8
+    uint64_t key_offset;       // into the key buffer (u64 elements)
+    uint64_t key_pitch;        // tiles_x * 64
+    uint32_t* rgba8;           // width*height, row pitch out_pitch
+    uint64_t* vis;             // width*height
+    float* color;              // width*height*3 when flags&1
+    float* tile_lum;           // tiles_x*tiles_y
+    uint32_t out_pitch;
+    uint32_t pad2[3];
+};
+
+struct alignas(16) DDraw {
+    float mvp[16];
+    uint32_t node;
+    uint32_t prim;
+    uint32_t view;
+    uint32_t clip;             // primitive's sphere intersects the frustum
+    uint32_t tri_begin;        // global triangle index of this draw's triangle 0
+    uint32_t tri_count;
+    uint32_t static_base;      // static triangle ID of triangle 0
+    uint32_t scene;
+};
+
+struct DChunk {
+    uint32_t draw;
+    uint32_t tri_start;        // local to the draw
+};
+
+// Raster-side triangle record (one per emitted, non-culled triangle).
+struct alignas(16) RecRaster {
+    int32_t p[6];              // screen subpixel positions p0, p1, p2
+    int32_t bb[4];             // screen_min_pixels.xy, screen_max_pixels.xy
+    float ooa;                 // one_over_area
+    float zow[3];              // z_over_w interpolator (a, da, db)
+    float oow[3];              // one_over_w interpolator
+    uint32_t seq8;             // (global triangle index << 3) | fan
+    uint32_t material;
+    uint32_t view;
+};
+static_assert(sizeof(RecRaster) == 80, "RecRaster layout");
+
+// Shading-side record.
+struct alignas(16) RecShade {
+    float nrm[9];              // normals a.xyz, da.xyz, db.xyz
+    float tan[9];
+    float tsign[3];
+    float uow[3];
+    float vow[3];
+    float pww[9];              // pos_world_over_w
+    float du_dv[4];
+    uint32_t static_id;
+    uint32_t pad[3];
+};
+static_assert(sizeof(RecShade) == 176, "RecShade layout");
+
+// Device status word bits.
+enum : uint32_t {
+    ST_BIN_OVERFLOW = 1u,
+    ST_CLIP_OVERFLOW = 2u,
+    ST_QUEUE_OVERFLOW = 4u,
+    ST_TIMEOUT = 8u,
+};
+
+// Frame-level counters (device).
+struct alignas(16) DCounters {
+    uint32_t status;
+    uint32_t clip_queue;       // triangles queued for clipping
+    uint32_t extra_used;       // extra record slots taken by fans 1..6
+    uint32_t setup_tris;       // records written
+    unsigned long long pairs;  // (triangle, tile) pairs counted
+    uint32_t work_next;        // persistent raster work cursor
+    uint32_t pad[3];
+};
+
+// Everything a frame's kernels need, passed by value.
+struct FrameArgs {
+    const DScene* scenes;
+    const DView* views;
+    uint32_t n_views;
+    const DDraw* draws;
+    const DChunk* chunks;
+    uint32_t n_chunks;
+    uint32_t tri_total;        // T: main record slots
+    uint32_t extra_cap;        // extra record slots
+    uint32_t clip_cap;         // clip queue capacity
+    uint32_t n_stiles;         // bins over all views
+    uint64_t bin_cap;
+    uint32_t sched_tile;       // S
+    uint32_t pad0;
+    uint8_t* tri_state;
+    RecRaster* rec_r;
+    RecShade* rec_s;
+    uint32_t* fan_base;
+    uint2* clip_queue;         // (g, draw)
+    uint32_t* tile_count;      // n_stiles
+    uint32_t* tile_offset;     // n_stiles + 1
+    uint32_t* tile_cursor;     // n_stiles
+    uint32_t* bins;
+    unsigned long long* keys;
+    DCounters* counters;
+    const uint8_t* rsqrt_table;// 512 entries, FRSQRTE estimates
+    uint32_t total_quads;      // shading work over all views
+    uint32_t max_view_pixels;  // largest width * (height & ~1) over views
+    const float* exposure_dev; // exposure computed by the host step (dt > 0)
+};
+
+// Launch wrappers (kernels.cu).
+void launch_frame(const FrameArgs& a, void* stream, int num_sms);
+void launch_reset(const FrameArgs& a, void* stream);
+void launch_resolve(const FrameArgs& a, void* stream);
+
+}  // namespace swr

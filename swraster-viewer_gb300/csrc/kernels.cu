@@ -1,0 +1,1113 @@
+// GB300 (sm_103a) kernels for the per-frame rasterization path.
+//
+// Frame = reset -> frontend -> clip -> scan -> scatter -> raster -> shade.
+// All kernels are batched over views: the plain path is a batch of one.
+//
+//   k_frontend  one thread per input triangle (256-triangle chunks of a draw):
+//               vertex transform (src/renderer.rs:470-574), trivial clip
+//               classification, triangle setup (bin_triangle,
+//               src/renderer.rs:668-831), per-tile pair counts with
+//               warp-aggregated atomics.
+//   k_clip      Sutherland-Hodgman for triangles with a vertex outside a plane
+//               (clip_against_frustum, src/renderer.rs:579-665), fan setup.
+//   k_scan      exclusive scan of tile counts -> bin offsets, overflow check.
+//   k_scatter   record indices into per-tile bins (warp-aggregated cursors);
+//               replaces BumpQueue::push (src/bumpqueue.rs:96-112).
+//   k_raster    one CTA per scheduling tile: the reference's coarse/fine
+//               traversal and f32 edge stepping (src/tilerasterizer.rs:114-383)
+//               with a 64-bit (depth, sequence) atomicMin per pixel in shared
+//               memory; keys go to HBM (the visibility buffer).
+//   k_shade     one thread per pixel, 4 per 2x2 quad: barycentrics rebuilt
+//               from the winning record, quad-coupled mip selection,
+//               pbr_shader / skybox (src/shader.rs:110-309,
+//               src/tilerasterizer.rs:386-508), tile-centre luminance,
+//               exposure + tonemap + RGBA8 pack (src/renderer.rs:293-355).
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "devmath.cuh"
+#include "internal.h"
+
+namespace swr {
+
+// --------------------------------------------------------------------------
+// Small vector helpers (one lane of Vec3x4 / Vec4).
+// --------------------------------------------------------------------------
+struct f3 {
+    float x, y, z;
+};
+__device__ __forceinline__ f3 mk3(float x, float y, float z) { return {x, y, z}; }
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ f3 operator*(f3 a, f3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+__device__ __forceinline__ f3 operator*(f3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ float dot(f3 a, f3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+__device__ __forceinline__ f3 cross(f3 a, f3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ f3 normalize(f3 a, uint32_t mode, const uint8_t* tab) {
+    const float l2 = (a.x * a.x + a.y * a.y) + a.z * a.z;
+    const float r = rsqrt_mode(l2, mode, tab);
+    return {a.x * r, a.y * r, a.z * r};
+}
+// glam Vec4::clamp = max(min).min(max); scalar IEEE max/min.
+__device__ __forceinline__ float clampf(float v, float lo, float hi) { return fminf(fmaxf(v, lo), hi); }
+
+// ScalarInterpolator::interpolate: (a + b1*da) + b2*db (src/util.rs:169-171).
+__device__ __forceinline__ float interp(const float* s, float b1, float b2) { return (s[0] + b1 * s[1]) + b2 * s[2]; }
+__device__ __forceinline__ f3 interp3(const float* s, float b1, float b2) {
+    return {(s[0] + b1 * s[3]) + b2 * s[6], (s[1] + b1 * s[4]) + b2 * s[7], (s[2] + b1 * s[5]) + b2 * s[8]};
+}
+
+__constant__ float c_unorm8[256];  // i / 255.0 (src/util.rs:83-89)
+
+__device__ __forceinline__ f3 unpack_rgb(uint32_t t) {
+    return {c_unorm8[(t >> 24) & 0xFFu], c_unorm8[(t >> 16) & 0xFFu], c_unorm8[(t >> 8) & 0xFFu]};
+}
+
+// srgb_to_linear_fast (src/util.rs:111-113).
+__device__ __forceinline__ float srgb_fast(float x) { return x * (x * (x * 0.305306011f + 0.682171111f) + 0.012522878f); }
+__device__ __forceinline__ f3 srgb_fast3(f3 c) { return {srgb_fast(c.x), srgb_fast(c.y), srgb_fast(c.z)}; }
+
+// --------------------------------------------------------------------------
+// Texture sampling (src/texture.rs:578-863)
+// --------------------------------------------------------------------------
+__device__ __forceinline__ float apply_wrap(float texel, float dim, uint32_t mode) {
+    float t = texel;
+    if (mode == 0u) {  // Repeat
+        t = texel - floorf(texel / dim) * dim;
+    } else if (mode == 1u) {  // MirroredRepeat
+        const float two = dim * 2.0f;
+        const float m = texel - floorf(texel / two) * two;
+        t = fminf(m, two - m);
+    }
+    return fminf(t, dim - 1.0f);
+}
+
+// compute_mip_level (src/texture.rs:851-863): one mip per quad.
+__device__ __forceinline__ uint32_t mip_level(const DTexture& t, float d0, float d1, float d2, float d3) {
+    const float tx = d0 * t.whv[0], ty = d1 * t.whv[1], tz = d2 * t.whv[2], tw = d3 * t.whv[3];
+    const float dx2 = tx * tx + tz * tz;
+    const float dy2 = ty * ty + tw * tw;
+    const float fp = (dx2 + dy2) * 0.5f;
+    const uint32_t u = f2u_sat(fmaxf(fp, 1.0f));
+    const uint32_t mip = (31u - (uint32_t)__clz(u)) >> 1;
+    return mip < t.max_mip ? mip : t.max_mip;
+}
+
+__device__ __forceinline__ uint32_t sample_texel(const DTexture& t, float u, float v, uint32_t mip, uint32_t ws,
+                                                 uint32_t wt) {
+    const float wf = t.mip_wf[mip], hf = t.mip_hf[mip];
+    const uint32_t x = f2u_sat(apply_wrap(floorf(u * wf), wf, ws));
+    const uint32_t y = f2u_sat(apply_wrap(floorf(v * hf), hf, wt));
+    const uint32_t idx = t.mip_offset[mip] + y * t.mip_w[mip] + x;
+    return __ldg(t.data + idx);
+}
+
+// cubemap_uv_from_normal (src/texture.rs:593-644).
+__device__ __forceinline__ void cube_uv(f3 n, float& uf, float& vf, uint32_t& slice) {
+    const float ax = fabsf(n.x), ay = fabsf(n.y), az = fabsf(n.z);
+    const bool mx = (ax >= ay) && (ax >= az);
+    const bool my = (ay > ax) && (ay >= az);
+    const float sx = n.x >= 0.0f ? 1.0f : -1.0f;
+    const float sy = n.y >= 0.0f ? 1.0f : -1.0f;
+    const float sz = n.z >= 0.0f ? 1.0f : -1.0f;
+    const float u_x = -n.z * sx, v_x = -n.y;
+    const float u_y = n.x, v_y = n.z * sy;
+    const float u_z = n.x * sz, v_z = -n.y;
+    const float u = mx ? u_x : (my ? u_y : u_z);
+    const float v = mx ? v_x : (my ? v_y : v_z);
+    float den = mx ? ax : (my ? ay : az);
+    den = fmaxf(den, 1.0e-19f);
+    uf = 0.5f * (u / den + 1.0f);
+    vf = 0.5f * (v / den + 1.0f);
+    const uint32_t ix = n.x >= 0.0f ? 0u : 1u;
+    const uint32_t iy = n.y >= 0.0f ? 2u : 3u;
+    const uint32_t iz = n.z >= 0.0f ? 4u : 5u;
+    slice = mx ? ix : (my ? iy : iz);
+}
+
+// sample_cubemap_rgb (src/texture.rs:646-663): nearest texel at one mip.
+__device__ __forceinline__ f3 sample_cube(const DTexture& t, float uf, float vf, uint32_t slice, uint32_t mip) {
+    if (mip > t.max_mip) mip = t.max_mip;
+    const float wf = t.mip_wf[mip], hf = t.mip_hf[mip];
+    const uint32_t off = t.mip_offset[mip] + slice * t.array_stride[mip];
+    float x = round_away(uf * (wf - 1.0f));
+    float y = round_away(vf * (hf - 1.0f));
+    x = clampf(x, 0.0f, wf - 1.0f);
+    y = clampf(y, 0.0f, hf - 1.0f);
+    const uint32_t idx = off + f2u_sat(y) * t.mip_w[mip] + f2u_sat(x);
+    return unpack_rgb(__ldg(t.data + idx));
+}
+
+// sample_bilinear_rgb at mip 0, slice 0 (src/texture.rs:730-790); ClampToEdge.
+__device__ __forceinline__ f3 sample_bilinear(const DTexture& t, float u, float v) {
+    const float wf = t.mip_wf[0], hf = t.mip_hf[0];
+    const uint32_t wi = t.mip_w[0];
+    const float xf = u * wf - 0.5f;
+    const float yf = v * hf - 0.5f;
+    const float x0 = floorf(xf), y0 = floorf(yf);
+    const float x1 = x0 + 1.0f, y1 = y0 + 1.0f;
+    const float fx = xf - x0, fy = yf - y0;
+    const float ofx = 1.0f - fx, ofy = 1.0f - fy;
+    const uint32_t x0i = f2u_sat(apply_wrap(x0, wf, 2u));
+    const uint32_t y0i = f2u_sat(apply_wrap(y0, hf, 2u));
+    const uint32_t x1i = f2u_sat(apply_wrap(x1, wf, 2u));
+    const uint32_t y1i = f2u_sat(apply_wrap(y1, hf, 2u));
+    const uint32_t off = t.mip_offset[0];
+    const f3 p00 = unpack_rgb(__ldg(t.data + off + y0i * wi + x0i));
+    const f3 p10 = unpack_rgb(__ldg(t.data + off + y0i * wi + x1i));
+    const f3 p01 = unpack_rgb(__ldg(t.data + off + y1i * wi + x0i));
+    const f3 p11 = unpack_rgb(__ldg(t.data + off + y1i * wi + x1i));
+    const float w00 = ofx * ofy, w10 = fx * ofy, w01 = ofx * fy, w11 = fx * fy;
+    return {((p00.x * w00 + p10.x * w10) + p01.x * w01) + p11.x * w11,
+            ((p00.y * w00 + p10.y * w10) + p01.y * w01) + p11.y * w11,
+            ((p00.z * w00 + p10.z * w10) + p01.z * w01) + p11.z * w11};
+}
+
+// --------------------------------------------------------------------------
+// Edge functions (src/tilerasterizer.rs:136-164)
+// --------------------------------------------------------------------------
+__device__ __forceinline__ int32_t top_left_bias(int32_t a, int32_t b) { return (a < 0 || (a == 0 && b > 0)) ? 0 : -1; }
+
+struct Edge {
+    float a, b, c, sx, sy;
+};
+// Edge (xi, yi) -> (xj, yj): a = yj - yi, b = xi - xj, c = xj*yi - xi*yj + bias.
+__device__ __forceinline__ Edge make_edge(int32_t xi, int32_t yi, int32_t xj, int32_t yj) {
+    const int32_t a = wsub(yj, yi);
+    const int32_t b = wsub(xi, xj);
+    const int32_t c = wadd(wsub(wmul(xj, yi), wmul(xi, yj)), top_left_bias(a, b));
+    Edge e;
+    e.a = i2f(a);
+    e.b = i2f(b);
+    e.c = i2f(c);
+    e.sx = i2f(wmul(a, 32));
+    e.sy = i2f(wmul(b, 32));
+    return e;
+}
+__device__ __forceinline__ float edge_eval(const Edge& e, float x, float y) { return (e.a * x + e.b * y) + e.c; }
+
+// Traversal origin of a (record, 64-px reference tile) packet for one pixel:
+// the quad-aligned clipped bbox min (fine path) or the 16-px block holding
+// the pixel (coarse path), src/tilerasterizer.rs:191-291.
+struct Origin {
+    int32_t ox, oy;  // subpixels
+};
+__device__ __forceinline__ void clipped_rect(const RecRaster& r, int32_t tx0, int32_t ty0, int32_t& x0, int32_t& y0,
+                                             int32_t& x1, int32_t& y1) {
+    x0 = max(r.bb[0], tx0);
+    y0 = max(r.bb[1], ty0);
+    x1 = min(r.bb[2], tx0 + kRefTile);
+    y1 = min(r.bb[3], ty0 + kRefTile);
+}
+
+// Rebuild bary1/bary2 of pixel (px, py) exactly as fine_raster produced them.
+__device__ __forceinline__ void rebuild_bary(const RecRaster& r, int32_t px, int32_t py, float& b1, float& b2) {
+    const int32_t tx0 = (px >> 6) << 6, ty0 = (py >> 6) << 6;
+    int32_t x0, y0, x1, y1;
+    clipped_rect(r, tx0, ty0, x0, y0, x1, y1);
+    const bool coarse = (x1 - x0 > 16) || (y1 - y0 > 16);
+    const int32_t xs = (x0 & ~1) * kSubpixelScale, ys = (y0 & ~1) * kSubpixelScale;
+    int32_t ox = xs, oy = ys;
+    if (coarse) {
+        ox = xs + ((px * kSubpixelScale - xs) >> 8) * 256;
+        oy = ys + ((py * kSubpixelScale - ys) >> 8) * 256;
+    }
+    const int32_t qi = (px * kSubpixelScale - ox) >> 5;
+    const int32_t qj = (py * kSubpixelScale - oy) >> 5;
+    const float lx = i2f(ox + ((px & 1) ? 24 : 8));
+    const float ly = i2f(oy + ((py & 1) ? 24 : 8));
+    const Edge e20 = make_edge(r.p[4], r.p[5], r.p[0], r.p[1]);
+    const Edge e01 = make_edge(r.p[0], r.p[1], r.p[2], r.p[3]);
+    float w1 = edge_eval(e20, lx, ly);
+    float w2 = edge_eval(e01, lx, ly);
+    for (int j = 0; j < qj; ++j) {
+        w1 += e20.sy;
+        w2 += e01.sy;
+    }
+    for (int i = 0; i < qi; ++i) {
+        w1 += e20.sx;
+        w2 += e01.sx;
+    }
+    b1 = w1 * r.ooa;
+    b2 = w2 * r.ooa;
+}
+
+// --------------------------------------------------------------------------
+// Front end
+// --------------------------------------------------------------------------
+struct Vtx {
+    float cx, cy, cz, cw;  // pos_clip
+    float wx, wy, wz;      // pos_world
+    float nx, ny, nz;      // normal
+    float tx, ty, tz, tw;  // tangent
+    float u, v;
+};
+
+__device__ __forceinline__ Vtx transform_vertex(const DVertex* __restrict__ vb, uint32_t vi, const float* model,
+                                                const float* mvp) {
+    const float4 a = __ldg(reinterpret_cast<const float4*>(vb + vi));
+    const float4 b = __ldg(reinterpret_cast<const float4*>(vb + vi) + 1);
+    const float4 c = __ldg(reinterpret_cast<const float4*>(vb + vi) + 2);
+    Vtx o;
+    // Mat4 * Vec4 with w = 1: ((c0*x + c1*y) + c2*z) + c3*1 (src/renderer.rs:504-511).
+    o.cx = ((mvp[0] * a.x + mvp[4] * a.y) + mvp[8] * a.z) + mvp[12];
+    o.cy = ((mvp[1] * a.x + mvp[5] * a.y) + mvp[9] * a.z) + mvp[13];
+    o.cz = ((mvp[2] * a.x + mvp[6] * a.y) + mvp[10] * a.z) + mvp[14];
+    o.cw = ((mvp[3] * a.x + mvp[7] * a.y) + mvp[11] * a.z) + mvp[15];
+    o.wx = ((model[0] * a.x + model[4] * a.y) + model[8] * a.z) + model[12];
+    o.wy = ((model[1] * a.x + model[5] * a.y) + model[9] * a.z) + model[13];
+    o.wz = ((model[2] * a.x + model[6] * a.y) + model[10] * a.z) + model[14];
+    // Mat3A * Vec3A: (c0*x + c1*y) + c2*z (src/renderer.rs:514-521).
+    o.nx = (model[0] * b.x + model[4] * b.y) + model[8] * b.z;
+    o.ny = (model[1] * b.x + model[5] * b.y) + model[9] * b.z;
+    o.nz = (model[2] * b.x + model[6] * b.y) + model[10] * b.z;
+    o.tx = (model[0] * c.x + model[4] * c.y) + model[8] * c.z;
+    o.ty = (model[1] * c.x + model[5] * c.y) + model[9] * c.z;
+    o.tz = (model[2] * c.x + model[6] * c.y) + model[10] * c.z;
+    o.tw = c.w;
+    o.u = a.w;
+    o.v = b.w;
+    return o;
+}
+
+// clip_to_screen_subpixels (src/renderer.rs:834-846).
+__device__ __forceinline__ void to_screen(const Vtx& v, float wf, float hf, int32_t& sx, int32_t& sy) {
+    const float nx = v.cx / v.cw;
+    const float ny = v.cy / v.cw;
+    const float fx = ((nx + 1.0f) * wf) / 2.0f;
+    const float fy = ((1.0f - ny) * hf) / 2.0f;
+    sx = f2i_sat(round_away(fx * 16.0f));
+    sy = f2i_sat(round_away(fy * 16.0f));
+}
+
+// Warp-aggregated atomicAdd of 1 on counter[idx].
+__device__ __forceinline__ void agg_inc(uint32_t* counter, uint32_t idx) {
+    const uint32_t active = __activemask();
+    const uint32_t peers = __match_any_sync(active, idx);
+    const int leader = __ffs(peers) - 1;
+    if ((int)(threadIdx.x & 31) == leader) atomicAdd(counter + idx, (uint32_t)__popc(peers));
+}
+
+// Iterate the scheduling tiles a setup triangle touches. f(stile) is called
+// once per (triangle, scheduling tile) pair. Mirrors the bin loop of
+// bin_triangle (src/renderer.rs:756-830) restricted to real tiles (the
+// reference's x == tiles_x column aliases into the next row's tile 0 and only
+// ever yields an empty rect or an exact duplicate packet).
+template <typename F>
+__device__ __forceinline__ void for_each_stile(const DView& v, int32_t S, int32_t mnx, int32_t mny, int32_t mxx,
+                                               int32_t mxy, F f) {
+    const int32_t bx0 = mnx / kRefTile, by0 = mny / kRefTile;
+    const int32_t bx1 = min((mxx + kRefTile - 1) / kRefTile, v.tiles_x);
+    const int32_t by1 = min((mxy + kRefTile - 1) / kRefTile, v.tiles_y);
+    for (int32_t ty = by0; ty < by1; ++ty) {
+        for (int32_t tx = bx0; tx < bx1; ++tx) {
+            const int32_t x0 = max(mnx, tx * kRefTile), y0 = max(mny, ty * kRefTile);
+            const int32_t x1 = min(mxx, tx * kRefTile + kRefTile), y1 = min(mxy, ty * kRefTile + kRefTile);
+            if (x1 - x0 < 1 || y1 - y0 < 1) continue;
+            const int32_t sx0 = x0 / S, sx1 = (x1 - 1) / S;
+            const int32_t sy0 = y0 / S, sy1 = (y1 - 1) / S;
+            for (int32_t sy = sy0; sy <= sy1; ++sy)
+                for (int32_t sx = sx0; sx <= sx1; ++sx) f(v.stile_base + (uint32_t)(sy * v.stiles_x + sx));
+        }
+    }
+}
+
+// bin_triangle (src/renderer.rs:668-831): setup + count. Returns true when a
+// record was written to `slot`.
+__device__ bool setup_triangle(const FrameArgs& a, const DView& view, const Vtx& v0, const Vtx& v1, const Vtx& v2,
+                               uint32_t slot, uint32_t seq8, uint32_t static_id, uint32_t material,
+                               uint32_t view_idx) {
+    int32_t p0x, p0y, p1x, p1y, p2x, p2y;
+    to_screen(v0, view.width_f, view.height_f, p0x, p0y);
+    to_screen(v1, view.width_f, view.height_f, p1x, p1y);
+    to_screen(v2, view.width_f, view.height_f, p2x, p2y);
+    const int32_t area = wsub(wmul(wsub(p1x, p0x), wsub(p2y, p0y)), wmul(wsub(p2x, p0x), wsub(p1y, p0y)));
+    if (area > 0) return false;  // back-facing (CW front faces after the y flip)
+    const int32_t wsub_px = view.width * kSubpixelScale, hsub_px = view.height * kSubpixelScale;
+    const int32_t mns_x = max(min(min(p0x, p1x), p2x), 0);
+    const int32_t mns_y = max(min(min(p0y, p1y), p2y), 0);
+    const int32_t mxs_x = min(max(max(p0x, p1x), p2x), wsub_px);
+    const int32_t mxs_y = min(max(max(p0y, p1y), p2y), hsub_px);
+    const int32_t mnx = mns_x >> kSubpixelShift, mny = mns_y >> kSubpixelShift;
+    const int32_t mxx = wadd(mxs_x, kSubpixelScale) >> kSubpixelShift;
+    const int32_t mxy = wadd(mxs_y, kSubpixelScale) >> kSubpixelShift;
+
+    uint32_t n = 0;
+    const int32_t S = (int32_t)a.sched_tile;
+    for_each_stile(view, S, mnx, mny, mxx, mxy, [&](uint32_t) { ++n; });
+    if (n == 0) return false;
+
+    // Interpolator setup (src/renderer.rs:699-754).
+    const float ooa = 1.0f / i2f(wabs(area));
+    const float oow0 = 1.0f / v0.cw, oow1 = 1.0f / v1.cw, oow2 = 1.0f / v2.cw;
+    const float zow0 = v0.cz * oow0, zow1 = v1.cz * oow1, zow2 = v2.cz * oow2;
+    const float u0 = v0.u * oow0, u1 = v1.u * oow1, u2 = v2.u * oow2;
+    const float w0 = v0.v * oow0, w1 = v1.v * oow1, w2 = v2.v * oow2;
+    const float dx1 = i2f(wsub(p1x, p0x)), dx2 = i2f(wsub(p2x, p0x));
+    const float dy1 = i2f(wsub(p1y, p0y)), dy2 = i2f(wsub(p2y, p0y));
+    const float du1 = u1 - u0, du2 = u2 - u0, dv1 = w1 - w0, dv2 = w2 - w0;
+    const float du_dx = du1 * dy2 - du2 * dy1;
+    const float du_dy = du2 * dx1 - du1 * dx2;
+    const float dv_dx = dv1 * dy2 - dv2 * dy1;
+    const float dv_dy = dv2 * dx1 - dv1 * dx2;
+    const float s = ooa * 16.0f;
+
+    RecRaster r;
+    r.p[0] = p0x; r.p[1] = p0y; r.p[2] = p1x; r.p[3] = p1y; r.p[4] = p2x; r.p[5] = p2y;
+    r.bb[0] = mnx; r.bb[1] = mny; r.bb[2] = mxx; r.bb[3] = mxy;
+    r.ooa = ooa;
+    r.zow[0] = zow0; r.zow[1] = zow1 - zow0; r.zow[2] = zow2 - zow0;
+    r.oow[0] = oow0; r.oow[1] = oow1 - oow0; r.oow[2] = oow2 - oow0;
+    r.seq8 = seq8;
+    r.material = material;
+    r.view = view_idx;
+    RecShade q;
+    q.nrm[0] = v0.nx; q.nrm[1] = v0.ny; q.nrm[2] = v0.nz;
+    q.nrm[3] = v1.nx - v0.nx; q.nrm[4] = v1.ny - v0.ny; q.nrm[5] = v1.nz - v0.nz;
+    q.nrm[6] = v2.nx - v0.nx; q.nrm[7] = v2.ny - v0.ny; q.nrm[8] = v2.nz - v0.nz;
+    q.tan[0] = v0.tx; q.tan[1] = v0.ty; q.tan[2] = v0.tz;
+    q.tan[3] = v1.tx - v0.tx; q.tan[4] = v1.ty - v0.ty; q.tan[5] = v1.tz - v0.tz;
+    q.tan[6] = v2.tx - v0.tx; q.tan[7] = v2.ty - v0.ty; q.tan[8] = v2.tz - v0.tz;
+    q.tsign[0] = v0.tw; q.tsign[1] = v1.tw - v0.tw; q.tsign[2] = v2.tw - v0.tw;
+    q.uow[0] = u0; q.uow[1] = u1 - u0; q.uow[2] = u2 - u0;
+    q.vow[0] = w0; q.vow[1] = w1 - w0; q.vow[2] = w2 - w0;
+    const float px0 = v0.wx * oow0, py0 = v0.wy * oow0, pz0 = v0.wz * oow0;
+    const float px1 = v1.wx * oow1, py1 = v1.wy * oow1, pz1 = v1.wz * oow1;
+    const float px2 = v2.wx * oow2, py2 = v2.wy * oow2, pz2 = v2.wz * oow2;
+    q.pww[0] = px0; q.pww[1] = py0; q.pww[2] = pz0;
+    q.pww[3] = px1 - px0; q.pww[4] = py1 - py0; q.pww[5] = pz1 - pz0;
+    q.pww[6] = px2 - px0; q.pww[7] = py2 - py0; q.pww[8] = pz2 - pz0;
+    q.du_dv[0] = du_dx * s; q.du_dv[1] = du_dy * s; q.du_dv[2] = dv_dx * s; q.du_dv[3] = dv_dy * s;
+    q.static_id = static_id;
+    q.pad[0] = q.pad[1] = q.pad[2] = 0;
+
+    {
+        const float4* src = reinterpret_cast<const float4*>(&r);
+        float4* dst = reinterpret_cast<float4*>(a.rec_r + slot);
+#pragma unroll
+        for (int i = 0; i < 5; ++i) dst[i] = src[i];
+    }
+    {
+        const float4* src = reinterpret_cast<const float4*>(&q);
+        float4* dst = reinterpret_cast<float4*>(a.rec_s + slot);
+#pragma unroll
+        for (int i = 0; i < 11; ++i) dst[i] = src[i];
+    }
+    for_each_stile(view, S, mnx, mny, mxx, mxy, [&](uint32_t st) { agg_inc(a.tile_count, st); });
+    atomicAdd(&a.counters->pairs, (unsigned long long)n);
+    return true;
+}
+
+__global__ void k_reset(FrameArgs a) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < a.n_stiles) a.tile_count[i] = 0u;
+    if (i == 0) {
+        a.counters->status = 0u;
+        a.counters->clip_queue = 0u;
+        a.counters->extra_used = 0u;
+        a.counters->setup_tris = 0u;
+        a.counters->pairs = 0ull;
+        a.counters->work_next = 0u;
+    }
+}
+
+__device__ __forceinline__ bool vtx_inside_all(const Vtx& v) {
+    // plane.dot(pos_clip) >= 0 for the six planes of src/renderer.rs:581-588;
+    // every product is by 0 or +-1, so the dot is exactly +-c + w.
+    return (v.cz + v.cw >= 0.0f) && (-v.cz + v.cw >= 0.0f) && (v.cx + v.cw >= 0.0f) && (-v.cx + v.cw >= 0.0f) &&
+           (v.cy + v.cw >= 0.0f) && (-v.cy + v.cw >= 0.0f);
+}
+
+__global__ void __launch_bounds__(kChunkTris) k_frontend(FrameArgs a) {
+    const DChunk ch = a.chunks[blockIdx.x];
+    const DDraw& d = a.draws[ch.draw];
+    const uint32_t local = ch.tri_start + threadIdx.x;
+    if (local >= d.tri_count) return;
+    const uint32_t g = d.tri_begin + local;
+    const DScene& sc = a.scenes[d.scene];
+    const DView& view = a.views[d.view];
+    const DPrimitive pr = sc.prims[d.prim];
+    const float* model = sc.node_xform + 16u * d.node;
+    const uint32_t* ib = sc.indices + pr.idx_base + 3u * local;
+    const uint32_t i0 = __ldg(ib), i1 = __ldg(ib + 1), i2 = __ldg(ib + 2);
+    const Vtx v0 = transform_vertex(sc.vertices, pr.vtx_base + i0, model, d.mvp);
+    const Vtx v1 = transform_vertex(sc.vertices, pr.vtx_base + i1, model, d.mvp);
+    const Vtx v2 = transform_vertex(sc.vertices, pr.vtx_base + i2, model, d.mvp);
+    if (d.clip && !(vtx_inside_all(v0) && vtx_inside_all(v1) && vtx_inside_all(v2))) {
+        const uint32_t q = atomicAdd(&a.counters->clip_queue, 1u);
+        if (q < a.clip_cap) {
+            a.clip_queue[q] = make_uint2(g, ch.draw);
+        } else {
+            atomicOr(&a.counters->status, ST_QUEUE_OVERFLOW);
+        }
+        a.tri_state[g] = 2;
+        return;
+    }
+    // All three vertices inside: the clipper would return the triangle unchanged.
+    const bool ok = setup_triangle(a, view, v0, v1, v2, g, g << 3, d.static_base + local, pr.material, d.view);
+    a.tri_state[g] = ok ? 1 : 0;
+    if (ok) atomicAdd(&a.counters->setup_tris, 1u);
+}
+
+// intersect (src/renderer.rs:598-609).
+__device__ __forceinline__ Vtx lerp_vtx(const Vtx& a, const Vtx& b, float t) {
+    Vtx o;
+    o.cx = a.cx + (b.cx - a.cx) * t; o.cy = a.cy + (b.cy - a.cy) * t;
+    o.cz = a.cz + (b.cz - a.cz) * t; o.cw = a.cw + (b.cw - a.cw) * t;
+    o.wx = a.wx + (b.wx - a.wx) * t; o.wy = a.wy + (b.wy - a.wy) * t; o.wz = a.wz + (b.wz - a.wz) * t;
+    o.nx = a.nx + (b.nx - a.nx) * t; o.ny = a.ny + (b.ny - a.ny) * t; o.nz = a.nz + (b.nz - a.nz) * t;
+    o.tx = a.tx + (b.tx - a.tx) * t; o.ty = a.ty + (b.ty - a.ty) * t;
+    o.tz = a.tz + (b.tz - a.tz) * t; o.tw = a.tw + (b.tw - a.tw) * t;
+    o.u = a.u + (b.u - a.u) * t; o.v = a.v + (b.v - a.v) * t;
+    return o;
+}
+__device__ __forceinline__ float plane_dist(const Vtx& v, int p) {
+    switch (p) {
+        case 0: return v.cz + v.cw;   // near:   z + w
+        case 1: return -v.cz + v.cw;  // far:   -z + w
+        case 2: return v.cx + v.cw;   // right:  x + w
+        case 3: return -v.cx + v.cw;  // left:  -x + w
+        case 4: return v.cy + v.cw;   // top:    y + w
+        default: return -v.cy + v.cw; // bottom: -y + w
+    }
+}
+
+__global__ void __launch_bounds__(128) k_clip(FrameArgs a) {
+    const uint32_t nq = min(a.counters->clip_queue, a.clip_cap);
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
+        const uint2 e = a.clip_queue[q];
+        const uint32_t g = e.x;
+        const DDraw& d = a.draws[e.y];
+        const uint32_t local = g - d.tri_begin;
+        const DScene& sc = a.scenes[d.scene];
+        const DView& view = a.views[d.view];
+        const DPrimitive pr = sc.prims[d.prim];
+        const float* model = sc.node_xform + 16u * d.node;
+        const uint32_t* ib = sc.indices + pr.idx_base + 3u * local;
+        Vtx poly[16], np[16];
+        poly[0] = transform_vertex(sc.vertices, pr.vtx_base + __ldg(ib), model, d.mvp);
+        poly[1] = transform_vertex(sc.vertices, pr.vtx_base + __ldg(ib + 1), model, d.mvp);
+        poly[2] = transform_vertex(sc.vertices, pr.vtx_base + __ldg(ib + 2), model, d.mvp);
+        int len = 3;
+        for (int p = 0; p < 6 && len > 0; ++p) {
+            int nl = 0;
+            for (int i = 0; i < len; ++i) {
+                const Vtx& cur = poly[i];
+                const Vtx& prv = poly[(i + len - 1) % len];
+                const float dc = plane_dist(cur, p), dp = plane_dist(prv, p);
+                const bool cin = dc >= 0.0f, pin = dp >= 0.0f;
+                if (cin) {
+                    if (!pin) np[nl++] = lerp_vtx(prv, cur, dp / (dp - dc));
+                    np[nl++] = cur;
+                } else if (pin) {
+                    np[nl++] = lerp_vtx(prv, cur, dp / (dp - dc));
+                }
+            }
+            for (int i = 0; i < nl; ++i) poly[i] = np[i];
+            len = nl;
+        }
+        uint32_t any = 0;
+        if (len >= 3) {
+            const int fans = len - 2;
+            uint32_t base = 0;
+            if (fans > 1) {
+                base = atomicAdd(&a.counters->extra_used, (uint32_t)(fans - 1));
+                if (base + (uint32_t)(fans - 1) > a.extra_cap) {
+                    atomicOr(&a.counters->status, ST_CLIP_OVERFLOW);
+                    a.tri_state[g] = 0;
+                    continue;
+                }
+                a.fan_base[g] = a.tri_total + base;
+            }
+            for (int f = 0; f < fans; ++f) {
+                const uint32_t slot = f == 0 ? g : a.tri_total + base + (uint32_t)(f - 1);
+                const bool ok = setup_triangle(a, view, poly[0], poly[f + 1], poly[f + 2], slot, (g << 3) | (uint32_t)f,
+                                               d.static_base + local, pr.material, d.view);
+                if (ok) {
+                    atomicAdd(&a.counters->setup_tris, 1u);
+                    if (f == 0) any = 1;
+                } else if (f > 0) {
+                    // Mark the unused extra slot so the scatter skips it.
+                    a.rec_r[slot].view = 0xFFFFFFFFu;
+                }
+            }
+        }
+        a.tri_state[g] = any ? 1 : 3;
+    }
+}
+
+// Exclusive scan of tile counts (single CTA). Also seeds the scatter cursors.
+__global__ void __launch_bounds__(1024) k_scan(FrameArgs a) {
+    __shared__ uint32_t part[1024];
+    const uint32_t n = a.n_stiles;
+    const uint32_t per = (n + 1023u) / 1024u;
+    const uint32_t b = threadIdx.x * per;
+    const uint32_t e = min(b + per, n);
+    uint32_t s = 0;
+    for (uint32_t i = b; i < e; ++i) s += a.tile_count[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (uint32_t off = 1; off < 1024u; off <<= 1) {
+        uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    uint32_t run = part[threadIdx.x] - s;
+    for (uint32_t i = b; i < e; ++i) {
+        a.tile_offset[i] = run;
+        a.tile_cursor[i] = run;
+        run += a.tile_count[i];
+    }
+    if (threadIdx.x == 1023) {
+        a.tile_offset[n] = part[1023];
+        if ((uint64_t)part[1023] > a.bin_cap) atomicOr(&a.counters->status, ST_BIN_OVERFLOW);
+    }
+}
+
+__global__ void k_scatter(FrameArgs a) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a.counters->status & (ST_BIN_OVERFLOW | ST_CLIP_OVERFLOW | ST_QUEUE_OVERFLOW)) return;
+    uint32_t slot;
+    if (i < a.tri_total) {
+        if (a.tri_state[i] != 1) return;
+        slot = i;
+    } else {
+        const uint32_t x = i - a.tri_total;
+        if (x >= min(a.counters->extra_used, a.extra_cap)) return;
+        slot = i;
+        if (a.rec_r[slot].view == 0xFFFFFFFFu) return;
+    }
+    const RecRaster& r = a.rec_r[slot];
+    const DView& view = a.views[r.view];
+    for_each_stile(view, (int32_t)a.sched_tile, r.bb[0], r.bb[1], r.bb[2], r.bb[3], [&](uint32_t st) {
+        const uint32_t active = __activemask();
+        const uint32_t peers = __match_any_sync(active, st);
+        const int leader = __ffs(peers) - 1;
+        const uint32_t lane = threadIdx.x & 31u;
+        uint32_t base = 0;
+        if ((int)lane == leader) base = atomicAdd(a.tile_cursor + st, (uint32_t)__popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+        a.bins[base + rank] = slot;
+    });
+}
+
+// --------------------------------------------------------------------------
+// Raster
+// --------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t find_view_by_stile(const FrameArgs& a, uint32_t st) {
+    uint32_t lo = 0, hi = a.n_views - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (a.views[mid].stile_base <= st) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Alpha test of one lane (get_alpha_test_mask, src/shader.rs:311-329): the
+// mip comes from the packet's du_dv without the per-lane w scale.
+__device__ __forceinline__ bool alpha_pass(const DScene& sc, const DMaterial& m, const RecShade& q, float b1, float b2,
+                                           float w, uint32_t mip) {
+    const DTexture& t = sc.textures[m.tex[TS_BASE]];
+    const float u = interp(q.uow, b1, b2) * w;
+    const float v = interp(q.vow, b1, b2) * w;
+    const uint32_t tx = sample_texel(t, u, v, mip, m.wrap_s[TS_BASE], m.wrap_t[TS_BASE]);
+    return c_unorm8[tx & 0xFFu] >= m.alpha_cutoff;
+}
+
+// One warp rasterizes one fine region (a whole small packet, or one 16-px
+// block of a coarse packet). Lane = (quad row j, lane-in-quad k); each lane
+// walks its row along x with the reference's sequential f32 additions.
+template <int S>
+__device__ __forceinline__ void fine_region(unsigned long long* sk, const Edge& e12, const Edge& e20, const Edge& e01,
+                                            const RecRaster& r, int32_t ox, int32_t oy, int32_t xe, int32_t ye,
+                                            int32_t sx0, int32_t sy0, const DScene* sc, const DMaterial* mat,
+                                            const RecShade* qs, uint32_t amip) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const int32_t k = (int32_t)(lane & 3u);
+    const int32_t kx = k & 1, ky = k >> 1;
+    const float lx = i2f(ox + (kx ? 24 : 8));
+    const float ly = i2f(oy + (ky ? 24 : 8));
+    const int32_t nrow = (ye - oy + 31) >> 5;
+    const int32_t ncol = (xe - ox + 31) >> 5;
+    for (int32_t j = (int32_t)(lane >> 2); j < nrow; j += 8) {
+        const int32_t py = (oy >> 4) + 2 * j + ky;
+        float w0 = edge_eval(e12, lx, ly), w1 = edge_eval(e20, lx, ly), w2 = edge_eval(e01, lx, ly);
+        for (int32_t s = 0; s < j; ++s) {
+            w0 += e12.sy;
+            w1 += e20.sy;
+            w2 += e01.sy;
+        }
+        const bool row_in = (uint32_t)(py - sy0) < (uint32_t)S;
+        if (!row_in) continue;
+        for (int32_t i = 0; i < ncol; ++i) {
+            const int32_t px = (ox >> 4) + 2 * i + kx;
+            if ((uint32_t)(px - sx0) < (uint32_t)S && w0 >= 0.0f && w1 >= 0.0f && w2 >= 0.0f) {
+                const float b1 = w1 * r.ooa, b2 = w2 * r.ooa;
+                const float w = 1.0f / interp(r.oow, b1, b2);
+                const float z = interp(r.zow, b1, b2) * w;
+                bool pass = (z == z);
+                if (pass && mat) pass = alpha_pass(*sc, *mat, *qs, b1, b2, w, amip);
+                if (pass) {
+                    const unsigned long long key = make_key(z, r.seq8);
+                    unsigned long long* slot = sk + (py - sy0) * S + (px - sx0);
+                    if (key < *slot) atomicMin(slot, key);
+                }
+            }
+            w0 += e12.sx;
+            w1 += e20.sx;
+            w2 += e01.sx;
+        }
+    }
+}
+
+template <int S>
+__global__ void __launch_bounds__(256) k_raster(FrameArgs a) {
+    __shared__ unsigned long long sk[S * S];
+    const uint32_t st = blockIdx.x;
+    const uint32_t vi = find_view_by_stile(a, st);
+    const DView& view = a.views[vi];
+    const uint32_t local = st - view.stile_base;
+    const int32_t sx0 = (int32_t)(local % (uint32_t)view.stiles_x) * S;
+    const int32_t sy0 = (int32_t)(local / (uint32_t)view.stiles_x) * S;
+    const int32_t tx0 = (sx0 / kRefTile) * kRefTile, ty0 = (sy0 / kRefTile) * kRefTile;
+    for (int i = threadIdx.x; i < S * S; i += blockDim.x) sk[i] = kEmptyKey;
+    __syncthreads();
+    const bool bad = (a.counters->status & (ST_BIN_OVERFLOW | ST_CLIP_OVERFLOW | ST_QUEUE_OVERFLOW)) != 0u;
+    if (!bad) {
+        const uint32_t b0 = a.tile_offset[st], b1 = a.tile_offset[st + 1];
+        const uint32_t warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+        const DScene& sc = a.scenes[view.scene];
+        for (uint32_t p = b0 + warp; p < b1; p += nwarps) {
+            const uint32_t slot = a.bins[p];
+            RecRaster r;
+            {
+                const float4* src = reinterpret_cast<const float4*>(a.rec_r + slot);
+                float4* dst = reinterpret_cast<float4*>(&r);
+#pragma unroll
+                for (int i = 0; i < 5; ++i) dst[i] = __ldg(src + i);
+            }
+            const Edge e01 = make_edge(r.p[0], r.p[1], r.p[2], r.p[3]);
+            const Edge e12 = make_edge(r.p[2], r.p[3], r.p[4], r.p[5]);
+            const Edge e20 = make_edge(r.p[4], r.p[5], r.p[0], r.p[1]);
+            int32_t x0, y0, x1, y1;
+            clipped_rect(r, tx0, ty0, x0, y0, x1, y1);
+            const DMaterial* mat = nullptr;
+            const RecShade* qs = nullptr;
+            uint32_t amip = 0;
+            {
+                const DMaterial& m = sc.materials[r.material];
+                if (m.flags & MAT_ALPHA_TESTED) {
+                    mat = &m;
+                    qs = a.rec_s + slot;
+                    amip = mip_level(sc.textures[m.tex[TS_BASE]], qs->du_dv[0], qs->du_dv[1], qs->du_dv[2],
+                                     qs->du_dv[3]);
+                }
+            }
+            const int32_t xs = (x0 & ~1) * kSubpixelScale, ys = (y0 & ~1) * kSubpixelScale;
+            const int32_t xe = x1 * kSubpixelScale, ye = y1 * kSubpixelScale;
+            if ((x1 - x0 > 16) || (y1 - y0 > 16)) {
+                // coarse_raster (src/tilerasterizer.rs:220-291): 16-px blocks.
+                for (int32_t by = ys; by < ye; by += 256) {
+                    if (by + 256 <= sy0 * 16 || by >= (sy0 + S) * 16) continue;
+                    for (int32_t bx = xs; bx < xe; bx += 256) {
+                        if (bx + 256 <= sx0 * 16 || bx >= (sx0 + S) * 16) continue;
+                        const float cx0 = i2f(bx + 8), cx1 = i2f(bx + 256 - 8);
+                        const float cy0 = i2f(by + 8), cy1 = i2f(by + 256 - 8);
+                        const float m0 = fmaxf(fmaxf(edge_eval(e12, cx0, cy0), edge_eval(e12, cx1, cy0)),
+                                               fmaxf(edge_eval(e12, cx0, cy1), edge_eval(e12, cx1, cy1)));
+                        const float m1 = fmaxf(fmaxf(edge_eval(e20, cx0, cy0), edge_eval(e20, cx1, cy0)),
+                                               fmaxf(edge_eval(e20, cx0, cy1), edge_eval(e20, cx1, cy1)));
+                        const float m2 = fmaxf(fmaxf(edge_eval(e01, cx0, cy0), edge_eval(e01, cx1, cy0)),
+                                               fmaxf(edge_eval(e01, cx0, cy1), edge_eval(e01, cx1, cy1)));
+                        if (m0 < 0.0f || m1 < 0.0f || m2 < 0.0f) continue;
+                        fine_region<S>(sk, e12, e20, e01, r, bx, by, min(bx + 256, xe), min(by + 256, ye), sx0, sy0,
+                                       &sc, mat, qs, amip);
+                    }
+                }
+            } else {
+                fine_region<S>(sk, e12, e20, e01, r, xs, ys, xe, ye, sx0, sy0, &sc, mat, qs, amip);
+            }
+        }
+    }
+    __syncthreads();
+    unsigned long long* dst = a.keys + view.key_offset;
+    for (int i = threadIdx.x; i < S * S; i += blockDim.x) {
+        const int32_t ly = i / S, lx = i % S;
+        dst[(uint64_t)(sy0 + ly) * view.key_pitch + (uint64_t)(sx0 + lx)] = sk[i];
+    }
+}
+
+// --------------------------------------------------------------------------
+// Shading
+// --------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t find_view_by_quad(const FrameArgs& a, uint32_t q) {
+    uint32_t lo = 0, hi = a.n_views - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (a.views[mid].quad_base <= q) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// compute_skybox for one lane (src/tilerasterizer.rs:478-508).
+__device__ f3 skybox(const DView& v, const DScene& sc, int32_t qx_screen, int32_t qy_screen, int32_t kx, int32_t ky,
+                     const uint8_t* tab) {
+    const float pxf = i2f(qx_screen) + (kx ? 1.5f : 0.5f);
+    const float pyf = i2f(qy_screen) + (ky ? 1.5f : 0.5f);
+    const float ndc_x = ((pxf * v.one_over_width) * 2.0f) - 1.0f;
+    const float ndc_y = ((1.0f - pyf * v.one_over_height) * 2.0f) - 1.0f;
+    const float* m = v.skybox_t;
+    f3 d;
+    d.x = ((ndc_x * m[0] + ndc_y * m[1]) + 1.0f * m[2]) + m[3];
+    d.y = ((ndc_x * m[4] + ndc_y * m[5]) + 1.0f * m[6]) + m[7];
+    d.z = ((ndc_x * m[8] + ndc_y * m[9]) + 1.0f * m[10]) + m[11];
+    const f3 n = normalize(d, v.rsqrt_mode, tab);
+    float uf, vf;
+    uint32_t slice;
+    cube_uv(n, uf, vf, slice);
+    return srgb_fast3(sample_cube(sc.textures[sc.tex_cubemap], uf, vf, slice, 0u));
+}
+
+// get_filtered_gi_sh4_packed_vec (src/voxelgrid.rs:264-368) for the
+// constant-SH voxel grid: w0 from the light grid, the rest constant.
+__device__ void voxel_gi(const DScene& sc, f3 pos, f3 sh[4], float& w0, float& w1) {
+    const uint32_t n = sc.voxel_n;
+    const float vx = (pos.x - sc.voxel_min[0]) / sc.voxel_size_f[0];
+    const float vy = (pos.y - sc.voxel_min[1]) / sc.voxel_size_f[1];
+    const float vz = (pos.z - sc.voxel_min[2]) / sc.voxel_size_f[2];
+    const float x0f = floorf(vx), y0f = floorf(vy), z0f = floorf(vz);
+    uint32_t x0 = f2u_sat(x0f), y0 = f2u_sat(y0f), z0 = f2u_sat(z0f);
+    x0 = min(x0, n - 1u); y0 = min(y0, n - 1u); z0 = min(z0, n - 1u);
+    const uint32_t x1 = min(x0 + 1u, n - 1u), y1 = min(y0 + 1u, n - 1u), z1 = min(z0 + 1u, n - 1u);
+    const float fx = vx - x0f, fy = vy - y0f, fz = vz - z0f;
+    const float ofx = 1.0f - fx, ofy = 1.0f - fy, ofz = 1.0f - fz;
+    const float* L = sc.voxel_light;
+    const uint32_t nn = n * n;
+    const float w000 = __ldg(L + z0 * nn + y0 * n + x0), w001 = __ldg(L + z1 * nn + y0 * n + x0);
+    const float w010 = __ldg(L + z0 * nn + y1 * n + x0), w011 = __ldg(L + z1 * nn + y1 * n + x0);
+    const float w100 = __ldg(L + z0 * nn + y0 * n + x1), w101 = __ldg(L + z1 * nn + y0 * n + x1);
+    const float w110 = __ldg(L + z0 * nn + y1 * n + x1), w111 = __ldg(L + z1 * nn + y1 * n + x1);
+    {
+        const float v00 = w000 * ofx + w100 * fx, v01 = w001 * ofx + w101 * fx;
+        const float v10 = w010 * ofx + w110 * fx, v11 = w011 * ofx + w111 * fx;
+        const float v0 = v00 * ofy + v10 * fy, v1 = v01 * ofy + v11 * fy;
+        w0 = v0 * ofz + v1 * fz;
+    }
+    {
+        const float c = sc.sky_visibility;
+        const float v00 = c * ofx + c * fx;
+        const float v0 = v00 * ofy + v00 * fy;
+        w1 = v0 * ofz + v0 * fz;
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        float o[3];
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+            const float c = sc.gi_rgb[i][ch];
+            const float v00 = c * ofx + c * fx;
+            const float v0 = v00 * ofy + v00 * fy;
+            o[ch] = v0 * ofz + v0 * fz;
+        }
+        sh[i] = mk3(o[0], o[1], o[2]);
+    }
+}
+
+// pbr_shader<false> for one lane (src/shader.rs:110-309). du_dv already holds
+// packet.du_dv * w with component i scaled by lane i's w (Q6 quirk).
+__device__ f3 pbr_lane(const DScene& sc, const DView& v, const DMaterial& m, const RecShade& q, const RecRaster& r,
+                       float b1, float b2, const float du_dv[4], const uint8_t* tab) {
+    const uint32_t md = v.rsqrt_mode;
+    const float PI = 3.14159265358979f;
+    const float EPS = 1e-6f;
+    const float INV_PI = 1.0f / 3.14159265358979f;
+    const float w = 1.0f / interp(r.oow, b1, b2);
+    const f3 in_n = normalize(interp3(q.nrm, b1, b2), md, tab);
+    const f3 in_t = normalize(interp3(q.tan, b1, b2), md, tab);
+    const float tsign = interp(q.tsign, b1, b2);
+    const f3 pw = interp3(q.pww, b1, b2) * w;
+    const float uvx = interp(q.uow, b1, b2) * w;
+    const float uvy = interp(q.vow, b1, b2) * w;
+    const f3 tw = normalize(in_t - in_n * dot(in_n, in_t), md, tab);
+    const float hand = tsign >= 0.0f ? 1.0f : -1.0f;
+    const f3 bw = cross(in_n, tw) * hand;
+    f3 nw = normalize(in_n, md, tab);
+    if (m.tex[TS_NORMAL] >= 0) {
+        const DTexture& t = sc.textures[m.tex[TS_NORMAL]];
+        const uint32_t mip = mip_level(t, du_dv[0], du_dv[1], du_dv[2], du_dv[3]);
+        const f3 s = unpack_rgb(sample_texel(t, uvx, uvy, mip, m.wrap_s[TS_NORMAL], m.wrap_t[TS_NORMAL]));
+        const f3 tsn = mk3(s.x * 2.0f - 1.0f, s.y * 2.0f - 1.0f, s.z * 2.0f - 1.0f);
+        nw = (tw * tsn.x + bw * tsn.y) + in_n * tsn.z;
+        nw = normalize(nw, md, tab);
+    }
+    const f3 ld = mk3(sc.light_dir[0], sc.light_dir[1], sc.light_dir[2]);
+    const f3 lc = mk3(sc.light_color[0], sc.light_color[1], sc.light_color[2]);
+    const f3 vd = mk3(v.cam_pos[0], v.cam_pos[1], v.cam_pos[2]) - pw;
+    const f3 vn = normalize(vd, md, tab);
+    const float ndl = fmaxf(dot(nw, ld), 0.0f);
+    const f3 hv = normalize(ld + vn, md, tab);
+    const float ndh = fmaxf(dot(nw, hv), 0.0f);
+    const float ndv = fmaxf(dot(nw, vn), 1.0e-4f);
+    const float vdh = fmaxf(dot(vn, hv), 0.0f);
+    f3 sh[4];
+    float gw0, gw1;
+    voxel_gi(sc, pw, sh, gw0, gw1);
+    const float vli = clampf(gw0, 0.0f, 1.0f);
+    const float skyv = clampf(gw1, 0.0f, 1.0f);
+    f3 bc = mk3(m.base_color[0], m.base_color[1], m.base_color[2]);
+    if (m.tex[TS_BASE] >= 0) {
+        const DTexture& t = sc.textures[m.tex[TS_BASE]];
+        const uint32_t mip = mip_level(t, du_dv[0], du_dv[1], du_dv[2], du_dv[3]);
+        bc = bc * srgb_fast3(unpack_rgb(sample_texel(t, uvx, uvy, mip, m.wrap_s[TS_BASE], m.wrap_t[TS_BASE])));
+    }
+    float rough = m.roughness, metal = m.metallic;
+    if (m.tex[TS_MR] >= 0) {
+        const DTexture& t = sc.textures[m.tex[TS_MR]];
+        const uint32_t mip = mip_level(t, du_dv[0], du_dv[1], du_dv[2], du_dv[3]);
+        const f3 s = unpack_rgb(sample_texel(t, uvx, uvy, mip, m.wrap_s[TS_MR], m.wrap_t[TS_MR]));
+        rough = rough * s.y;
+        metal = metal * s.z;
+    }
+    rough = clampf(rough, 0.045f, 1.0f);
+    metal = clampf(metal, 0.0f, 1.0f);
+    float ao = 1.0f;
+    if (m.tex[TS_OCCLUSION] >= 0) {
+        const DTexture& t = sc.textures[m.tex[TS_OCCLUSION]];
+        const uint32_t mip = mip_level(t, du_dv[0], du_dv[1], du_dv[2], du_dv[3]);
+        ao = unpack_rgb(sample_texel(t, uvx, uvy, mip, m.wrap_s[TS_OCCLUSION], m.wrap_t[TS_OCCLUSION])).x;
+        ao = 1.0f + (ao - 1.0f) * m.occlusion_strength;
+    }
+    const f3 f0 = mk3(0.04f + (bc.x - 0.04f) * metal, 0.04f + (bc.y - 0.04f) * metal, 0.04f + (bc.z - 0.04f) * metal);
+    const float omvh = 1.0f - vdh;
+    const float omvh2 = omvh * omvh;
+    const float omvh4 = omvh2 * omvh2;
+    const float omvh5 = omvh4 * omvh;
+    const f3 one = mk3(1.0f, 1.0f, 1.0f);
+    const f3 fd = f0 + (one - f0) * omvh5;
+    const float alpha = rough * rough;
+    const float alpha2 = alpha * alpha;
+    const float ndh2 = ndh * ndh;
+    const float den_d = ndh2 * (alpha2 - 1.0f) + 1.0f;
+    const float brdf_d = alpha2 / (PI * (den_d * den_d) + EPS);
+    float k = rough + 1.0f;
+    k = (k * k) * 0.125f;
+    const float gv = ndv / ((ndv * (1.0f - k) + k) + EPS);
+    const float gl = ndl / ((ndl * (1.0f - k) + k) + EPS);
+    const float brdf_g = gv * gl;
+    const float spec_dg = (brdf_d * brdf_g) / ((4.0f * ndl) * ndv + EPS);
+    const f3 kd = (one - fd) * (1.0f - metal);
+    const f3 lambert = bc * INV_PI;
+    const f3 cdd = (((lc * kd) * lambert) * ndl) * vli;
+    const f3 cds = (((lc * fd) * spec_dg) * ndl) * vli;
+    const f3 kdi = (one - f0) * (1.0f - metal);
+    f3 irr;
+    irr.x = fmaxf(((sh[0].x + sh[1].x * nw.y) + sh[2].x * nw.z) + sh[3].x * nw.x, 0.0f);
+    irr.y = fmaxf(((sh[0].y + sh[1].y * nw.y) + sh[2].y * nw.z) + sh[3].y * nw.x, 0.0f);
+    irr.z = fmaxf(((sh[0].z + sh[1].z * nw.y) + sh[2].z * nw.z) + sh[3].z * nw.x, 0.0f);
+    const f3 cid = ((irr * bc) * kdi) * INV_PI;
+    // reflect: self - normal * self.dot(normal) * 2 (src/math.rs:118-120).
+    const f3 iv = vn * -1.0f;
+    const f3 rd = iv - (nw * dot(iv, nw)) * 2.0f;
+    const DTexture& spec = sc.textures[sc.tex_specular];
+    const float spec_mip = rough * (float)spec.max_mip;
+    f3 env;
+    {
+        const float mx = (float)spec.max_mip;
+        const float mp = clampf(spec_mip, 0.0f, mx);
+        const float m0 = floorf(mp);
+        const float m1 = fminf(m0 + 1.0f, mx);
+        const float t = mp - m0;
+        float uf, vf;
+        uint32_t slice;
+        cube_uv(rd, uf, vf, slice);
+        const f3 c0 = sample_cube(spec, uf, vf, slice, f2u_sat(m0));
+        const f3 c1 = sample_cube(spec, uf, vf, slice, f2u_sat(m1));
+        env = mk3(c0.x + (c1.x - c0.x) * t, c0.y + (c1.y - c0.y) * t, c0.z + (c1.z - c0.z) * t);
+    }
+    const f3 lut = sample_bilinear(sc.textures[sc.tex_brdf_lut], clampf(ndv, 0.0f, 1.0f), clampf(rough, 0.0f, 1.0f));
+    f3 bsf = f0 * lut.x;
+    bsf = mk3(bsf.x + lut.y, bsf.y + lut.y, bsf.z + lut.y);
+    f3 cis = env * bsf;
+    const float ao_spec = 1.0f + (ao - 1.0f) * 0.5f;
+    cis = cis * (ao_spec * skyv);
+    f3 col = ((cdd + cds) + cid) + cis;
+    f3 em = one;
+    if (m.tex[TS_EMISSIVE] >= 0) {
+        const DTexture& t = sc.textures[m.tex[TS_EMISSIVE]];
+        const uint32_t mip = mip_level(t, du_dv[0], du_dv[1], du_dv[2], du_dv[3]);
+        em = srgb_fast3(unpack_rgb(sample_texel(t, uvx, uvy, mip, m.wrap_s[TS_EMISSIVE], m.wrap_t[TS_EMISSIVE])));
+    }
+    col = col + em * mk3(m.emissive[0], m.emissive[1], m.emissive[2]);
+    return col;
+}
+
+__device__ __forceinline__ uint32_t tonemap_pack(f3 c, float exposure) {
+    // blit_to_buffer (src/renderer.rs:325-348) and tonemap (src/util.rs:37-41).
+    const float k = 0.2f;
+    const float kk = 1.0f + k;
+    c = c * exposure;
+    c = mk3((c.x / (c.x + k)) * kk, (c.y / (c.y + k)) * kk, (c.z / (c.z + k)) * kk);
+    const uint32_t r = f2u8_sat(c.x * 255.0f), g = f2u8_sat(c.y * 255.0f), b = f2u8_sat(c.z * 255.0f);
+    return (r << 24) | (g << 16) | (b << 8) | 0xFFu;
+}
+
+__global__ void __launch_bounds__(256) k_shade(FrameArgs a) {
+    __shared__ uint8_t tab[512];
+    for (int i = threadIdx.x; i < 512; i += blockDim.x) tab[i] = a.rsqrt_table[i];
+    __syncthreads();
+    const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t gq = gt >> 2;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t qmask = 0xFu << (lane & ~3u);
+    const bool live = gq < a.total_quads;
+    const uint32_t vi = find_view_by_quad(a, live ? gq : 0u);
+    const DView& v = a.views[vi];
+    const DScene& sc = a.scenes[v.scene];
+    const uint32_t lq = gq - v.quad_base;
+    const int32_t qx = (int32_t)(lq % v.quad_pitch), qy = (int32_t)(lq / v.quad_pitch);
+    const int32_t k = (int32_t)(gt & 3u), kx = k & 1, ky = k >> 1;
+    const int32_t px = 2 * qx + kx, py = 2 * qy + ky;
+    const bool centre = ((qx & 31) == 0) && ((qy & 31) == 16);
+    const bool needed = live && ((2 * qx < v.width && 2 * qy < v.height) || centre);
+
+    // Winner of this lane.
+    unsigned long long key = kEmptyKey;
+    if (needed) key = a.keys[v.key_offset + (uint64_t)py * v.key_pitch + (uint64_t)px];
+    const bool writer = key != kEmptyKey;
+    const float z = ordered_to_float((uint32_t)(key >> 32));
+    const bool covered = writer && !(z == __int_as_float(0x7F800000));
+    uint32_t slot = 0;
+    RecRaster r;
+    float b1 = 0.0f, b2 = 0.0f;
+    if (writer) {
+        const uint32_t s8 = key_seq8(key);
+        const uint32_t g = s8 >> 3, f = s8 & 7u;
+        slot = f == 0 ? g : a.fan_base[g] + f - 1u;
+        const float4* src = reinterpret_cast<const float4*>(a.rec_r + slot);
+        float4* dst = reinterpret_cast<float4*>(&r);
+#pragma unroll
+        for (int i = 0; i < 5; ++i) dst[i] = __ldg(src + i);
+        rebuild_bary(r, px, py, b1, b2);
+    }
+    // bary1/bary2 of all four lanes of the quad (uncovered lanes hold 0, the
+    // contents of a fresh renderer's vbuffer; src/tilerasterizer.rs:114-118).
+    float qb1[4], qb2[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        qb1[i] = __shfl_sync(0xFFFFFFFFu, b1, (int)((lane & ~3u) + (uint32_t)i));
+        qb2[i] = __shfl_sync(0xFFFFFFFFu, b2, (int)((lane & ~3u) + (uint32_t)i));
+    }
+    f3 col = mk3(0.0f, 0.0f, 0.0f);
+    uint32_t vis_hi = 0xFFFFFFFFu, vis_fan = 0;
+    if (needed) {
+        if (covered) {
+            RecShade q;
+            {
+                const float4* src = reinterpret_cast<const float4*>(a.rec_s + slot);
+                float4* dst = reinterpret_cast<float4*>(&q);
+#pragma unroll
+                for (int i = 0; i < 11; ++i) dst[i] = __ldg(src + i);
+            }
+            float dd[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) dd[i] = q.du_dv[i] * (1.0f / interp(r.oow, qb1[i], qb2[i]));
+            const DMaterial& m = sc.materials[r.material];
+            col = pbr_lane(sc, v, m, q, r, b1, b2, dd, tab);
+            vis_hi = q.static_id;
+            vis_fan = r.seq8 & 7u;
+        } else {
+            col = skybox(v, sc, 2 * qx, 2 * qy, kx, ky, tab);
+        }
+    }
+    // Tile-centre luminance (src/tilerasterizer.rs:103-106): quad (0, 16).
+    const float lum = (col.x * 0.2126f + col.y * 0.7152f) + col.z * 0.0722f;
+    const float l0 = __shfl_sync(0xFFFFFFFFu, lum, (int)(lane & ~3u));
+    const float l1 = __shfl_sync(0xFFFFFFFFu, lum, (int)((lane & ~3u) + 1u));
+    const float l2 = __shfl_sync(0xFFFFFFFFu, lum, (int)((lane & ~3u) + 2u));
+    const float l3 = __shfl_sync(0xFFFFFFFFu, lum, (int)((lane & ~3u) + 3u));
+    (void)qmask;
+    if (needed && centre && k == 0) {
+        const uint32_t tile = (uint32_t)(qy >> 5) * (uint32_t)v.tiles_x + (uint32_t)(qx >> 5);
+        v.tile_lum[tile] = (((l0 + l1) + l2) + l3) * 0.25f;
+    }
+    if (!needed) return;
+    if (px < v.width && py < v.height) {
+        v.vis[(uint64_t)py * (uint64_t)v.width + (uint64_t)px] =
+            covered ? (((unsigned long long)vis_hi << 3) | vis_fan) : ~0ull;
+    }
+    if (px < v.width && py < (v.height & ~1)) {
+        if (v.flags & 1u) {
+            float* c = v.color + ((uint64_t)py * (uint64_t)v.width + (uint64_t)px) * 3u;
+            c[0] = col.x;
+            c[1] = col.y;
+            c[2] = col.z;
+        } else {
+            v.rgba8[(uint64_t)py * v.out_pitch + (uint64_t)px] = tonemap_pack(col, v.exposure);
+        }
+    }
+}
+
+// Exposure applied after the host's update_auto_exposure (dt > 0 path).
+__global__ void k_resolve(FrameArgs a) {
+    const uint32_t vi = blockIdx.y;
+    const DView& v = a.views[vi];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t w = (uint32_t)v.width, h = (uint32_t)(v.height & ~1);
+    if (i >= w * h || !(v.flags & 1u)) return;
+    const uint32_t x = i % w, y = i / w;
+    const float* c = v.color + (uint64_t)i * 3u;
+    const float e = a.exposure_dev ? *a.exposure_dev : v.exposure;
+    v.rgba8[(uint64_t)y * v.out_pitch + x] = tonemap_pack(mk3(c[0], c[1], c[2]), e);
+}
+
+// --------------------------------------------------------------------------
+// Host launch wrappers
+// --------------------------------------------------------------------------
+static bool g_const_init = false;
+static void init_constants() {
+    if (g_const_init) return;
+    float t[256];
+    for (int i = 0; i < 256; ++i) t[i] = (float)i / 255.0f;
+    cudaMemcpyToSymbol(c_unorm8, t, sizeof(t));
+    g_const_init = true;
+}
+
+void launch_reset(const FrameArgs& a, void* stream) {
+    init_constants();
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t n = a.n_stiles > 0 ? a.n_stiles : 1u;
+    k_reset<<<(n + 255) / 256, 256, 0, s>>>(a);
+}
+
+void launch_frame(const FrameArgs& a, void* stream, int num_sms) {
+    cudaStream_t s = (cudaStream_t)stream;
+    launch_reset(a, stream);
+    if (a.n_chunks > 0) k_frontend<<<a.n_chunks, kChunkTris, 0, s>>>(a);
+    k_clip<<<num_sms * 4, 128, 0, s>>>(a);
+    k_scan<<<1, 1024, 0, s>>>(a);
+    {
+        const uint64_t n = (uint64_t)a.tri_total + a.extra_cap;
+        if (n > 0) k_scatter<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
+    }
+    switch (a.sched_tile) {
+        case 8: k_raster<8><<<a.n_stiles, 64, 0, s>>>(a); break;
+        case 16: k_raster<16><<<a.n_stiles, 128, 0, s>>>(a); break;
+        case 32: k_raster<32><<<a.n_stiles, 256, 0, s>>>(a); break;
+        default: k_raster<64><<<a.n_stiles, 256, 0, s>>>(a); break;
+    }
+    if (a.total_quads > 0) k_shade<<<(a.total_quads * 4 + 255) / 256, 256, 0, s>>>(a);
+}
+
+void launch_resolve(const FrameArgs& a, void* stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t maxpx = a.max_view_pixels > 0 ? a.max_view_pixels : 1u;
+    dim3 grid((maxpx + 255) / 256, a.n_views);
+    k_resolve<<<grid, 256, 0, s>>>(a);
+}
+
+}  // namespace swr

@@ -1,0 +1,277 @@
+// Per-frame host runtime: node sort, sphere/frustum classification, draw
+// and chunk tables, device capacities, kernel launch, exposure.
+#include "renderer.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+namespace swr {
+
+namespace {
+
+enum class Frustum { Inside, Outside, Intersecting };
+
+// test_sphere_frustum (src/renderer.rs:130-142).
+Frustum test_sphere_frustum(const float sphere[4], const swr_camera& cam) {
+    const M4 view = from_array(cam.view);
+    const V4 cv = mulmv(view, {sphere[0], sphere[1], sphere[2], 1.0f});
+    Frustum r = Frustum::Inside;
+    for (int i = 0; i < 6; ++i) {
+        const V4 pl = {cam.view_clip_planes[i][0], cam.view_clip_planes[i][1], cam.view_clip_planes[i][2],
+                       cam.view_clip_planes[i][3]};
+        const float d = dot4(pl, cv);
+        if (d < -sphere[3]) return Frustum::Outside;
+        if (d < sphere[3]) r = Frustum::Intersecting;
+    }
+    return r;
+}
+
+// OrderedFloat ordering: NaN sorts after everything.
+inline bool ordered_less(float a, float b) {
+    if (a != a) return false;
+    if (b != b) return true;
+    return a < b;
+}
+
+}  // namespace
+
+void build_view_draws(const SceneImpl& s, const swr_camera& cam, uint32_t view_idx, uint32_t scene_idx,
+                      uint32_t& tri_cursor, std::vector<DDraw>& draws, std::vector<DChunk>& chunks) {
+    // compute_nodes_by_distance: stable sort by squared distance.
+    const size_t nn = s.nodes.size();
+    std::vector<uint32_t> order(nn);
+    std::iota(order.begin(), order.end(), 0u);
+    std::vector<float> key(nn);
+    const V3 cp = {cam.position[0], cam.position[1], cam.position[2]};
+    for (size_t i = 0; i < nn; ++i) {
+        const V3 d = sub(cp, {s.nodes[i].sphere[0], s.nodes[i].sphere[1], s.nodes[i].sphere[2]});
+        key[i] = dot3(d, d);
+    }
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return ordered_less(key[a], key[b]); });
+    const M4 vp = from_array(cam.view_project);
+    for (uint32_t ni : order) {
+        const HNode& n = s.nodes[ni];
+        if (n.mesh < 0) continue;
+        const M4 mvp = mulmm(vp, n.transform);
+        const HMesh& m = s.meshes[n.mesh];
+        for (uint32_t lp : m.opaque) {
+            const uint32_t gp = m.prims[lp];
+            const HPrimitive& p = s.prims[gp];
+            float ws[4];
+            {
+                const float max_scale =
+                    ((length4(n.transform.c[0]) + length4(n.transform.c[1])) + length4(n.transform.c[2])) / 3.0f;
+                const V3 c = transform_point3(n.transform, {p.sphere[0], p.sphere[1], p.sphere[2]});
+                ws[0] = c.x;
+                ws[1] = c.y;
+                ws[2] = c.z;
+                ws[3] = p.sphere[3] * max_scale;
+            }
+            const Frustum f = test_sphere_frustum(ws, cam);
+            if (f == Frustum::Outside) continue;
+            const uint32_t tc = (uint32_t)(p.idx.size() / 3);
+            if (tc == 0) continue;
+            DDraw d{};
+            to_array(mvp, d.mvp);
+            d.node = ni;
+            d.prim = gp;
+            d.view = view_idx;
+            d.clip = f == Frustum::Intersecting ? 1u : 0u;
+            d.tri_begin = tri_cursor;
+            d.tri_count = tc;
+            d.static_base = n.tri_id_base + p.tri_id_base;
+            d.scene = scene_idx;
+            const uint32_t di = (uint32_t)draws.size();
+            draws.push_back(d);
+            for (uint32_t t = 0; t < tc; t += kChunkTris) chunks.push_back({di, t});
+            tri_cursor += tc;
+        }
+    }
+}
+
+void init_view(DView& v, const swr_camera& cam, int32_t width, int32_t height, uint32_t S) {
+    std::memcpy(v.skybox_t, cam.skybox_transposed, sizeof(v.skybox_t));
+    v.cam_pos[0] = cam.position[0];
+    v.cam_pos[1] = cam.position[1];
+    v.cam_pos[2] = cam.position[2];
+    v.one_over_width = cam.one_over_width;
+    v.one_over_height = cam.one_over_height;
+    v.width_f = (float)width;
+    v.height_f = (float)height;
+    v.width = width;
+    v.height = height;
+    v.tiles_x = (width + kRefTile - 1) / kRefTile;
+    v.tiles_y = (height + kRefTile - 1) / kRefTile;
+    v.stiles_x = v.tiles_x * (kRefTile / (int32_t)S);
+    v.stiles_y = v.tiles_y * (kRefTile / (int32_t)S);
+    v.quad_pitch = (uint32_t)v.tiles_x * 32u;
+    v.key_pitch = (uint64_t)v.tiles_x * kRefTile;
+}
+
+void ExposureState::update(const float* lum, size_t n, float dt) {
+    if (n == 0) return;
+    std::vector<float> s(n);
+    for (size_t i = 0; i < n; ++i) s[i] = std::log2(std::fmax(lum[i], 1e-4f));
+    // total_cmp order (no NaN can appear after max with 1e-4).
+    std::sort(s.begin(), s.end());
+    size_t trim = (size_t)std::floor((float)n * 0.10f);
+    trim = std::min(trim, (n - 1) / 2);
+    float sum = 0.0f;
+    for (size_t i = trim; i < n - trim; ++i) sum += s[i];
+    const float mean = sum / (float)(n - 2 * trim);
+    // tonemap_inverse_scalar(0.45) (src/util.rs:43-47).
+    const float y = std::fmin(std::fmax(0.45f, 0.0f), 1.0f);
+    const float den = std::fmax(1.0f + 0.2f - y, 1e-6f);
+    const float meter_key = std::fmax((y * 0.2f) / den, 1e-4f);
+    const float target_ev = std::log2(meter_key) - mean;
+    const float t = std::exp2(target_ev);
+    target = std::fmin(std::fmax(t, 0.05f), 32.0f);
+    const float tev = std::log2(target);
+    const float tau = std::fmax(1.0f, 1e-4f);
+    const float alpha = 1.0f - std::exp(-(std::fmax(dt, 0.0f) / tau));
+    ev += (tev - ev) * alpha;
+    exposure = std::exp2(ev);
+}
+
+swr_status FrameEngine::init(std::string& err) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && sms > 0) num_sms = sms;
+    if (rsqrt_tab.ensure(512) != cudaSuccess || counters.ensure(sizeof(DCounters)) != cudaSuccess) {
+        err = "cudaMalloc failed";
+        return SWR_NO_MEMORY;
+    }
+    uint8_t tab[512];
+    build_rsqrt_table(tab);
+    if (cudaMemcpy(rsqrt_tab.p, tab, 512, cudaMemcpyHostToDevice) != cudaSuccess) {
+        err = "cudaMemcpy failed";
+        return SWR_CUDA_ERROR;
+    }
+    if (cudaEventCreateWithFlags(&stage_done, cudaEventDisableTiming) != cudaSuccess) {
+        err = "cudaEventCreate failed";
+        return SWR_CUDA_ERROR;
+    }
+    return SWR_OK;
+}
+
+void FrameEngine::release() {
+    for (DBuf* b : {&scene_tab, &views, &draws, &chunks, &tri_state, &rec_r, &rec_s, &fan_base, &clip_queue, &tile_count,
+                    &tile_offset, &tile_cursor, &bins, &keys, &counters, &rsqrt_tab})
+        b->release();
+    h_stage.release();
+    if (stage_done) cudaEventDestroy(stage_done);
+    stage_done = nullptr;
+}
+
+swr_status FrameEngine::run(const std::vector<const SceneImpl*>& scenes, std::vector<DView>& vws,
+                            const std::vector<const swr_camera*>& cams, cudaStream_t stream, FrameArgs* out,
+                            std::string& err) {
+    // Draw lists for every view, canonical order within a view.
+    std::vector<DDraw> hdraws;
+    std::vector<DChunk> hchunks;
+    uint32_t tri_cursor = 0;
+    uint32_t stile_cursor = 0, quad_cursor = 0, max_px = 0;
+    uint64_t key_cursor = 0;
+    for (size_t i = 0; i < vws.size(); ++i) {
+        DView& v = vws[i];
+        build_view_draws(*scenes[v.scene], *cams[i], (uint32_t)i, v.scene, tri_cursor, hdraws, hchunks);
+        v.stile_base = stile_cursor;
+        stile_cursor += (uint32_t)(v.stiles_x * v.stiles_y);
+        v.quad_base = quad_cursor;
+        quad_cursor += v.quad_pitch * (uint32_t)v.tiles_y * 32u;
+        v.key_offset = key_cursor;
+        max_px = std::max<uint32_t>(max_px, (uint32_t)v.width * (uint32_t)(v.height & ~1));
+        key_cursor += v.key_pitch * (uint64_t)v.tiles_y * kRefTile;
+    }
+    const uint32_t T = tri_cursor;
+    if (extra_cap == 0) extra_cap = std::max<uint64_t>(4096, T / 4);
+    if (bin_cap == 0) bin_cap = std::max<uint64_t>(65536, (uint64_t)T * 2 + stile_cursor * 4ull);
+    // Capacities.
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t x) {
+        if (x != cudaSuccess && e == cudaSuccess) e = x;
+    };
+    const size_t slots = (size_t)T + extra_cap;
+    chk(scene_tab.ensure(scenes.size() * sizeof(DScene)));
+    chk(views.ensure(vws.size() * sizeof(DView)));
+    chk(draws.ensure(std::max<size_t>(1, hdraws.size()) * sizeof(DDraw)));
+    chk(chunks.ensure(std::max<size_t>(1, hchunks.size()) * sizeof(DChunk)));
+    chk(tri_state.ensure(std::max<size_t>(1, T)));
+    chk(rec_r.ensure(std::max<size_t>(1, slots) * sizeof(RecRaster)));
+    chk(rec_s.ensure(std::max<size_t>(1, slots) * sizeof(RecShade)));
+    chk(fan_base.ensure(std::max<size_t>(1, T) * sizeof(uint32_t)));
+    chk(clip_queue.ensure(std::max<size_t>(1, T) * sizeof(uint2)));
+    chk(tile_count.ensure((stile_cursor + 1) * sizeof(uint32_t)));
+    chk(tile_offset.ensure((stile_cursor + 1) * sizeof(uint32_t)));
+    chk(tile_cursor.ensure((stile_cursor + 1) * sizeof(uint32_t)));
+    chk(bins.ensure(bin_cap * sizeof(uint32_t)));
+    chk(keys.ensure(std::max<uint64_t>(1, key_cursor) * sizeof(unsigned long long)));
+    if (e != cudaSuccess) {
+        err = std::string("device allocation failed: ") + cudaGetErrorString(e);
+        cudaGetLastError();
+        return e == cudaErrorMemoryAllocation ? SWR_NO_MEMORY : SWR_CUDA_ERROR;
+    }
+    // Stage tables through pinned memory (wait for the previous frame's copy).
+    if (stage_pending) {
+        cudaEventSynchronize(stage_done);
+        stage_pending = false;
+    }
+    const size_t sb = scenes.size() * sizeof(DScene);
+    const size_t vb = vws.size() * sizeof(DView), db = hdraws.size() * sizeof(DDraw), cb = hchunks.size() * sizeof(DChunk);
+    const size_t so = 0, vo = (sb + 255) & ~size_t(255), dof = (vo + vb + 255) & ~size_t(255),
+                 co = (dof + db + 255) & ~size_t(255);
+    if (h_stage.ensure(co + cb) != cudaSuccess) {
+        err = "pinned allocation failed";
+        return SWR_NO_MEMORY;
+    }
+    uint8_t* hs = static_cast<uint8_t*>(h_stage.p);
+    for (size_t i = 0; i < scenes.size(); ++i) std::memcpy(hs + so + i * sizeof(DScene), &scenes[i]->dscene, sizeof(DScene));
+    std::memcpy(hs + vo, vws.data(), vb);
+    if (db) std::memcpy(hs + dof, hdraws.data(), db);
+    if (cb) std::memcpy(hs + co, hchunks.data(), cb);
+    chk(cudaMemcpyAsync(scene_tab.p, hs + so, sb, cudaMemcpyHostToDevice, stream));
+    chk(cudaMemcpyAsync(views.p, hs + vo, vb, cudaMemcpyHostToDevice, stream));
+    if (db) chk(cudaMemcpyAsync(draws.p, hs + dof, db, cudaMemcpyHostToDevice, stream));
+    if (cb) chk(cudaMemcpyAsync(chunks.p, hs + co, cb, cudaMemcpyHostToDevice, stream));
+    chk(cudaEventRecord(stage_done, stream));
+    stage_pending = true;
+    if (e != cudaSuccess) {
+        err = std::string("upload failed: ") + cudaGetErrorString(e);
+        return SWR_CUDA_ERROR;
+    }
+    FrameArgs a{};
+    a.views = views.as<DView>();
+    a.n_views = (uint32_t)vws.size();
+    a.draws = draws.as<DDraw>();
+    a.chunks = chunks.as<DChunk>();
+    a.n_chunks = (uint32_t)hchunks.size();
+    a.tri_total = T;
+    a.extra_cap = (uint32_t)extra_cap;
+    a.clip_cap = std::max<uint32_t>(1, T);
+    a.n_stiles = stile_cursor;
+    a.bin_cap = bin_cap;
+    a.sched_tile = sched_tile;
+    a.tri_state = tri_state.as<uint8_t>();
+    a.rec_r = rec_r.as<RecRaster>();
+    a.rec_s = rec_s.as<RecShade>();
+    a.fan_base = fan_base.as<uint32_t>();
+    a.clip_queue = clip_queue.as<uint2>();
+    a.tile_count = tile_count.as<uint32_t>();
+    a.tile_offset = tile_offset.as<uint32_t>();
+    a.tile_cursor = tile_cursor.as<uint32_t>();
+    a.bins = bins.as<uint32_t>();
+    a.keys = keys.as<unsigned long long>();
+    a.counters = counters.as<DCounters>();
+    a.rsqrt_table = rsqrt_tab.as<uint8_t>();
+    a.total_quads = quad_cursor;
+    a.max_view_pixels = max_px;
+    a.exposure_dev = nullptr;
+    a.scenes = scene_tab.as<DScene>();
+    *out = a;
+    return SWR_OK;
+}
+
+}  // namespace swr

@@ -1,0 +1,124 @@
+// Host runtime of the per-frame renderer: draw-list construction, device
+// buffer management, exposure state (Renderer, src/renderer.rs:144-198).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/swr.h"
+#include "internal.h"
+#include "scene.h"
+
+namespace swr {
+
+// Grow-only device buffer.
+struct DBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t n) {
+        if (n <= bytes) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        size_t want = n + n / 4;
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) bytes = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <typename T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+// Pinned host staging buffer.
+struct HBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t n) {
+        if (n <= bytes) return cudaSuccess;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+        size_t want = n + n / 4 + 256;
+        cudaError_t e = cudaHostAlloc(&p, want, cudaHostAllocDefault);
+        if (e == cudaSuccess) bytes = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+    }
+};
+
+// Reusable frame engine: everything a batch of views needs on the device.
+struct FrameEngine {
+    int num_sms = 148;
+    uint32_t sched_tile = 64;
+    uint64_t bin_cap = 0, extra_cap = 0;
+    DBuf scene_tab, views, draws, chunks, tri_state, rec_r, rec_s, fan_base, clip_queue;
+    DBuf tile_count, tile_offset, tile_cursor, bins, keys, counters, rsqrt_tab;
+    HBuf h_stage;
+    cudaEvent_t stage_done = nullptr;
+    bool stage_pending = false;
+    uint32_t retries = 0;
+    DCounters last{};
+
+    swr_status init(std::string& err);
+    void release();
+    // Build, upload and launch one frame over `views` (views[i].scene indexes
+    // `scenes`). Returns after enqueueing.
+    swr_status run(const std::vector<const SceneImpl*>& scenes, std::vector<DView>& views,
+                   const std::vector<const swr_camera*>& cams, cudaStream_t stream, FrameArgs* out_args,
+                   std::string& err);
+};
+
+// Per-frame draw list for one view (render_scene's front half,
+// src/renderer.rs:201-210 and 357-468).
+void build_view_draws(const SceneImpl& s, const swr_camera& cam, uint32_t view_idx, uint32_t scene_idx,
+                      uint32_t& tri_cursor, std::vector<DDraw>& draws, std::vector<DChunk>& chunks);
+
+// Fill the view-geometry fields of a DView (tiles, pitches, camera).
+void init_view(DView& v, const swr_camera& cam, int32_t width, int32_t height, uint32_t sched_tile);
+
+// update_auto_exposure (src/renderer.rs:258-290).
+struct ExposureState {
+    float exposure = 2.0f;
+    float target = 2.0f;
+    float ev = 1.0f;  // log2(2.0)
+    void update(const float* tile_lum, size_t n, float dt);
+};
+
+}  // namespace swr
+
+struct swr_renderer {
+    int32_t width = 0, height = 0;
+    swr_renderer_opts opts{};
+    swr::FrameEngine eng;
+    swr::DBuf rgba8, vis, color, tile_lum;
+    swr::ExposureState expo;
+    // Mapped pinned memory for the dt > 0 exposure step.
+    float* h_lum = nullptr;
+    uint32_t* h_status = nullptr;
+    float* h_expo = nullptr;
+    float* d_expo = nullptr;
+    cudaEvent_t expo_done = nullptr;
+    bool expo_pending = false;
+    float pending_dt = 0.0f;
+    // Last frame, kept for overflow re-runs.
+    const swr_scene* last_scene = nullptr;
+    swr_camera last_cam{};
+    float last_dt = 0.0f;
+    cudaStream_t last_stream = nullptr;
+    bool have_frame = false;
+    bool checked = true;
+    swr::FrameArgs last_args{};
+    uint32_t tiles_x = 0, tiles_y = 0;
+};

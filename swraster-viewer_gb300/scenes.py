@@ -1,0 +1,155 @@
+"""Seeded synthetic scenes with the shapes of the benchmark configurations.
+
+No glTF sample assets are available, so scenes are generated: icospheres and
+displaced grids with f32 positions/normals/UVs and u32 indices, seeded
+value-noise textures and a seeded RGBA8 cubemap (fed as raw faces instead of
+the reference's JPEG cross, because JPEG decoding is not bit-reproducible).
+
+A scene is a plain dict consumed by swr.Scene:
+  meshes:    [[{positions (V,3), normals (V,3)|None, texcoords (V,2)|None,
+                indices (3T,), material}]]
+  nodes:     [{world (16,) column-major, local, mesh}]
+  materials: [{base_color_factor, metallic, roughness, base_color: (tex, wrap_s, wrap_t), ...}]
+  textures:  [{width, height, type, rgba8 (H*W,) uint32 R-in-MSB}]
+  cubemap, cubemap_face_size, voxel_grid_size, specular_samples, brdf_lut_size
+"""
+import math
+
+import numpy as np
+
+TEX_SRGB, TEX_NORMAL, TEX_METALLIC_ROUGHNESS, TEX_CUBEMAP, TEX_LINEAR = 0, 1, 2, 3, 4
+WRAP_REPEAT = 0
+
+
+def icosphere(subdiv):
+    """Unit icosphere, counter-clockwise outward faces (glTF front faces)."""
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+         (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    verts = [np.array(p, np.float64) / np.linalg.norm(p) for p in v]
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+             (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11),
+             (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    for _ in range(subdiv):
+        cache = {}
+        nf = []
+
+        def mid(a, b):
+            key = (min(a, b), max(a, b))
+            if key not in cache:
+                m = verts[a] + verts[b]
+                verts.append(m / np.linalg.norm(m))
+                cache[key] = len(verts) - 1
+            return cache[key]
+
+        for a, b, c in faces:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        faces = nf
+    P = np.array(verts, np.float32)
+    F = np.array(faces, np.uint32).reshape(-1)
+    return P, F
+
+
+def spherical_uv(P):
+    u = 0.5 + np.arctan2(P[:, 2], P[:, 0]) / (2.0 * math.pi)
+    v = 0.5 - np.arcsin(np.clip(P[:, 1], -1.0, 1.0)) / math.pi
+    return np.stack([u, v], 1).astype(np.float32)
+
+
+def grid(n, m):
+    """Unit grid in the xy plane, z = 0, facing +z (counter-clockwise)."""
+    xs = np.linspace(-0.5, 0.5, n + 1, dtype=np.float32)
+    ys = np.linspace(-0.5, 0.5, m + 1, dtype=np.float32)
+    X, Y = np.meshgrid(xs, ys)
+    P = np.stack([X.ravel(), Y.ravel(), np.zeros(X.size, np.float32)], 1).astype(np.float32)
+    UV = np.stack([(X.ravel() + 0.5), (0.5 - Y.ravel())], 1).astype(np.float32)
+    i = np.arange(n)[None, :] + (n + 1) * np.arange(m)[:, None]
+    a, b, c, d = i, i + 1, i + n + 1, i + n + 2
+    F = np.stack([a, b, d, a, d, c], -1).reshape(-1).astype(np.uint32)
+    return P, UV, F
+
+
+def value_noise(rng, size, cells, channels=3):
+    """Bilinear value noise in [0, 1]: (size, size, channels) float32."""
+    lat = rng.random((cells + 1, cells + 1, channels), dtype=np.float32)
+    x = np.linspace(0, cells, size, endpoint=False, dtype=np.float32)
+    i = np.floor(x).astype(np.int64)
+    f = (x - i)[:, None]
+    f = f * f * (3 - 2 * f)
+    row0 = lat[i] * (1 - f[:, :, None]) + lat[i + 1] * f[:, :, None]
+    out = row0[:, i] * (1 - f[None, :, :]) + row0[:, i + 1] * f[None, :, :]
+    return out.astype(np.float32)
+
+
+def pack_rgba8(rgb, alpha=255):
+    c = np.clip(np.round(rgb * 255.0), 0, 255).astype(np.uint32)
+    a = np.full(c.shape[:-1], alpha, np.uint32)
+    return ((c[..., 0] << 24) | (c[..., 1] << 16) | (c[..., 2] << 8) | a).reshape(-1).astype(np.uint32)
+
+
+def noise_texture(rng, size, cells=16, tint=None):
+    n = value_noise(rng, size, cells)
+    if tint is not None:
+        n = 0.35 + 0.65 * n * np.asarray(tint, np.float32)
+    return {"width": size, "height": size, "type": TEX_SRGB, "rgba8": pack_rgba8(n)}
+
+
+def cubemap_faces(rng, size):
+    """Six seeded faces (+X,-X,+Y,-Y,+Z,-Z): a vertical sky gradient plus noise."""
+    faces = []
+    for face in range(6):
+        n = value_noise(rng, size, 8)
+        base = np.array([0.45, 0.6, 0.85], np.float32) if face != 3 else np.array([0.25, 0.22, 0.2], np.float32)
+        if face == 2:
+            base = np.array([0.7, 0.8, 1.0], np.float32)
+        ramp = np.linspace(1.1, 0.7, size, dtype=np.float32)[:, None, None]
+        img = np.clip(base[None, None, :] * ramp + 0.35 * (n - 0.5), 0.0, 1.0)
+        faces.append(pack_rgba8(img))
+    return np.concatenate(faces)
+
+
+def translate_scale(center, s):
+    m = np.eye(4, dtype=np.float32)
+    m[0, 0] = m[1, 1] = m[2, 2] = s
+    m[:3, 3] = center
+    return m.T.reshape(16).copy()  # column-major
+
+
+def spheres_scene(seed=1, count=64, subdiv=3, box=10.0, radius=(0.5, 2.0), tex_size=256, cube_size=128,
+                  voxel=128, specular_samples=64, brdf_lut_size=128):
+    """Plain method, small: `count` icospheres (subdivision `subdiv`) with
+    centres uniform in [-box, box]^3, radii uniform in `radius` (node scale),
+    one shared value-noise base-colour texture, per-mesh metallic/roughness
+    uniform in [0, 1], a seeded cubemap."""
+    rng = np.random.default_rng(seed)
+    P, F = icosphere(subdiv)
+    UV = spherical_uv(P)
+    tex = noise_texture(rng, tex_size)
+    meshes, nodes, mats = [], [], []
+    centers = rng.uniform(-box, box, (count, 3)).astype(np.float32)
+    radii = rng.uniform(radius[0], radius[1], count).astype(np.float32)
+    for i in range(count):
+        mats.append({"base_color_factor": (1.0, 1.0, 1.0, 1.0), "metallic": float(rng.random()),
+                     "roughness": float(rng.random()), "base_color": (0, WRAP_REPEAT, WRAP_REPEAT)})
+        meshes.append([{"positions": P, "normals": P.copy(), "texcoords": UV, "indices": F, "material": i}])
+        w = translate_scale(centers[i], radii[i])
+        nodes.append({"world": w, "local": w, "mesh": i})
+    return {"meshes": meshes, "nodes": nodes, "materials": mats, "textures": [tex],
+            "cubemap": cubemap_faces(rng, cube_size), "cubemap_face_size": cube_size, "voxel_grid_size": voxel,
+            "specular_samples": specular_samples, "brdf_lut_size": brdf_lut_size}
+
+
+def default_camera_params(info, width, height, fov=math.pi / 3.0):
+    """load_scene's default camera (src/main.rs:210-225): distance = scene
+    diagonal along +z from the bounds centre, far = 2 * diagonal."""
+    c = np.array(info.bounds_center[:], np.float32)
+    d = float(info.bounds_diagonal)
+    pos = (float(c[0]), float(c[1]), float(c[2] + np.float32(d)))
+    return pos, (float(c[0]), float(c[1]), float(c[2])), fov, width, height, float(np.float32(d) * np.float32(2.0))
+
+
+def small_scene(seed=7, count=6, subdiv=2, tex_size=64, cube_size=16, voxel=32):
+    """A quick scene for tests: few spheres, small textures and grids."""
+    return spheres_scene(seed=seed, count=count, subdiv=subdiv, box=4.0, radius=(0.5, 2.0), tex_size=tex_size,
+                         cube_size=cube_size, voxel=voxel, specular_samples=16, brdf_lut_size=32)
