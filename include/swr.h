@@ -389,6 +389,14 @@ swr_status swr_renderer_get_stats(swr_renderer* r, swr_frame_stats* out);
  * (src/tilerasterizer.rs:103-106). */
 swr_status swr_renderer_get_tile_luminance(swr_renderer* r, float* out, uint32_t count);
 
+/* Stage timing with CUDA events recorded on the frame's stream between the
+ * kernels: reset, frontend, clip, scan, scatter, raster, shade, resolve.
+ * swr_renderer_get_profile waits for outstanding frames and returns the mean
+ * milliseconds per stage over the frames since profiling was enabled. */
+#define SWR_STAGES 8
+swr_status swr_renderer_set_profiling(swr_renderer* r, int32_t enable);
+swr_status swr_renderer_get_profile(swr_renderer* r, float* stage_ms, int32_t n, uint32_t* frames);
+
 const char* swr_last_error(void);
 int32_t swr_abi_version(void);
 

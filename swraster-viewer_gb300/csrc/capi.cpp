@@ -45,7 +45,7 @@ swr_status swr_scene_create(const swr_scene_desc* desc, swr_scene** out) {
     swr_status st;
     try {
         st = build_scene(desc, &s->impl, err);
-        if (st == SWR_OK && !(desc->flags & SWR_SCENE_HOST_ONLY)) st = upload_scene(&s->impl, err);
+        if (st == SWR_OK) st = upload_scene(&s->impl, err, !(desc->flags & SWR_SCENE_HOST_ONLY));
     } catch (const std::bad_alloc&) {
         st = SWR_NO_MEMORY;
         err = "out of host memory";
@@ -220,10 +220,31 @@ void swr_renderer_destroy(swr_renderer* r) {
     if (r->h_expo) cudaFreeHost(r->h_expo);
     if (r->h_status) cudaFreeHost(r->h_status);
     if (r->expo_done) cudaEventDestroy(r->expo_done);
+    for (auto& set : r->prof_ev)
+        for (cudaEvent_t& e : set)
+            if (e) cudaEventDestroy(e);
     delete r;
 }
 
 namespace {
+
+void prof_collect(swr_renderer* r, int slot) {
+    if (!r->prof_pending[slot]) return;
+    cudaEvent_t* ev = r->prof_ev[slot];
+    const int last = r->prof_resolve[slot] ? 9 : 7;
+    cudaEventSynchronize(ev[last]);
+    for (int i = 0; i < 7; ++i) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, ev[i], ev[i + 1]) == cudaSuccess) r->prof_ms[i] += ms;
+    }
+    if (r->prof_resolve[slot]) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, ev[8], ev[9]) == cudaSuccess) r->prof_ms[7] += ms;
+    }
+    cudaGetLastError();
+    r->prof_frames += 1;
+    r->prof_pending[slot] = false;
+}
 
 void CUDART_CB exposure_callback(void* p) {
     swr_renderer* r = static_cast<swr_renderer*>(p);
@@ -268,7 +289,17 @@ swr_status enqueue_frame(swr_renderer* r, const swr_scene* scene, const swr_came
     FrameArgs a{};
     swr_status st = r->eng.run(scenes, views, cams, stream, &a, err);
     if (st != SWR_OK) return fail(st, err);
-    launch_frame(a, stream, r->eng.num_sms);
+    cudaEvent_t* ev = nullptr;
+    int slot = -1;
+    if (r->profiling) {
+        slot = r->prof_next;
+        r->prof_next = (r->prof_next + 1) % swr_renderer::kProfRing;
+        prof_collect(r, slot);
+        ev = r->prof_ev[slot];
+        r->prof_pending[slot] = true;
+        r->prof_resolve[slot] = deferred;
+    }
+    launch_frame(a, stream, r->eng.num_sms, ev);
     if (deferred) {
         const size_t nt = (size_t)r->tiles_x * r->tiles_y;
         cudaMemcpyAsync(r->h_lum, r->tile_lum.p, nt * sizeof(float), cudaMemcpyDeviceToHost, stream);
@@ -276,7 +307,9 @@ swr_status enqueue_frame(swr_renderer* r, const swr_scene* scene, const swr_came
         r->pending_dt = dt;
         cudaLaunchHostFunc(stream, exposure_callback, r);
         a.exposure_dev = r->d_expo;
+        if (ev) cudaEventRecord(ev[8], stream);
         launch_resolve(a, stream);
+        if (ev) cudaEventRecord(ev[9], stream);
         cudaEventRecord(r->expo_done, stream);
         r->expo_pending = true;
     }
@@ -401,6 +434,29 @@ swr_status swr_renderer_get_stats(swr_renderer* r, swr_frame_stats* o) {
     o->tiles = r->tiles_x * r->tiles_y;
     o->overflow_retries = r->eng.retries;
     o->exposure = r->expo.exposure;
+    return SWR_OK;
+}
+
+swr_status swr_renderer_set_profiling(swr_renderer* r, int32_t enable) {
+    if (!r) return fail(SWR_INVALID_ARG, "null argument");
+    if (enable && !r->prof_ev[0][0]) {
+        for (auto& set : r->prof_ev)
+            for (cudaEvent_t& e : set)
+                if (cudaEventCreate(&e) != cudaSuccess) return cuda_fail(cudaGetLastError(), "profiling events");
+    }
+    for (int i = 0; i < swr_renderer::kProfRing; ++i) r->prof_pending[i] = false;
+    for (double& m : r->prof_ms) m = 0.0;
+    r->prof_frames = 0;
+    r->profiling = enable != 0;
+    return SWR_OK;
+}
+
+swr_status swr_renderer_get_profile(swr_renderer* r, float* stage_ms, int32_t n, uint32_t* frames) {
+    if (!r || !stage_ms) return fail(SWR_INVALID_ARG, "null argument");
+    for (int i = 0; i < swr_renderer::kProfRing; ++i) prof_collect(r, i);
+    for (int i = 0; i < n && i < SWR_STAGES; ++i)
+        stage_ms[i] = r->prof_frames ? (float)(r->prof_ms[i] / r->prof_frames) : 0.0f;
+    if (frames) *frames = r->prof_frames;
     return SWR_OK;
 }
 

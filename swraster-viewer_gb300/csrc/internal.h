@@ -220,8 +220,9 @@ struct FrameArgs {
     const float* exposure_dev; // exposure computed by the host step (dt > 0)
 };
 
-// Launch wrappers (kernels.cu).
-void launch_frame(const FrameArgs& a, void* stream, int num_sms);
+// Launch wrappers (kernels.cu). `ev`, when given, holds 8 events recorded
+// before reset, frontend, clip, scan, scatter, raster, shade and after shade.
+void launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t* ev = nullptr);
 void launch_reset(const FrameArgs& a, void* stream);
 void launch_resolve(const FrameArgs& a, void* stream);
 

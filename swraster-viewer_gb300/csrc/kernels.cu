@@ -1084,23 +1084,34 @@ void launch_reset(const FrameArgs& a, void* stream) {
     k_reset<<<(n + 255) / 256, 256, 0, s>>>(a);
 }
 
-void launch_frame(const FrameArgs& a, void* stream, int num_sms) {
+void launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t* ev) {
     cudaStream_t s = (cudaStream_t)stream;
+    auto mark = [&](int i) {
+        if (ev) cudaEventRecord(ev[i], s);
+    };
+    mark(0);
     launch_reset(a, stream);
+    mark(1);
     if (a.n_chunks > 0) k_frontend<<<a.n_chunks, kChunkTris, 0, s>>>(a);
+    mark(2);
     k_clip<<<num_sms * 4, 128, 0, s>>>(a);
+    mark(3);
     k_scan<<<1, 1024, 0, s>>>(a);
+    mark(4);
     {
         const uint64_t n = (uint64_t)a.tri_total + a.extra_cap;
         if (n > 0) k_scatter<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
     }
+    mark(5);
     switch (a.sched_tile) {
         case 8: k_raster<8><<<a.n_stiles, 64, 0, s>>>(a); break;
         case 16: k_raster<16><<<a.n_stiles, 128, 0, s>>>(a); break;
         case 32: k_raster<32><<<a.n_stiles, 256, 0, s>>>(a); break;
         default: k_raster<64><<<a.n_stiles, 256, 0, s>>>(a); break;
     }
+    mark(6);
     if (a.total_quads > 0) k_shade<<<(a.total_quads * 4 + 255) / 256, 256, 0, s>>>(a);
+    mark(7);
 }
 
 void launch_resolve(const FrameArgs& a, void* stream) {

@@ -121,4 +121,13 @@ struct swr_renderer {
     bool checked = true;
     swr::FrameArgs last_args{};
     uint32_t tiles_x = 0, tiles_y = 0;
+    // Stage profiling: a ring of event sets, one per in-flight frame.
+    static constexpr int kProfRing = 64;
+    bool profiling = false;
+    cudaEvent_t prof_ev[kProfRing][10] = {};
+    bool prof_pending[kProfRing] = {};
+    bool prof_resolve[kProfRing] = {};
+    int prof_next = 0;
+    double prof_ms[SWR_STAGES] = {};
+    uint32_t prof_frames = 0;
 };

@@ -976,13 +976,13 @@ struct Arena {
     uint64_t add(const void* p, size_t bytes) {
         const uint64_t off = (host.size() + 255) & ~uint64_t(255);
         host.resize(off + bytes);
-        if (bytes) std::memcpy(host.data() + off, p, bytes);
+        if (bytes && p) std::memcpy(host.data() + off, p, bytes);
         return off;
     }
 };
-DTexture to_dtex(const HTexture& t, uint64_t off_in_block, uint8_t* dbase) {
+DTexture to_dtex(const HTexture& t, uintptr_t addr) {
     DTexture d{};
-    d.data = reinterpret_cast<const uint32_t*>(dbase + off_in_block);
+    d.data = reinterpret_cast<const uint32_t*>(addr);
     d.width = t.width;
     d.height = t.height;
     d.max_mip = t.max_mip;
@@ -999,7 +999,7 @@ DTexture to_dtex(const HTexture& t, uint64_t off_in_block, uint8_t* dbase) {
 }
 }  // namespace
 
-swr_status upload_scene(SceneImpl* s, std::string& err) {
+swr_status upload_scene(SceneImpl* s, std::string& err, bool to_device) {
     Arena ar;
     // Vertices, indices, primitive table.
     std::vector<DVertex> verts;
@@ -1063,24 +1063,30 @@ swr_status upload_scene(SceneImpl* s, std::string& err) {
     const uint64_t o_dtex = ar.add(nullptr, all_tex.size() * sizeof(DTexture));
     const uint64_t o_dscene = ar.add(nullptr, sizeof(DScene));
     void* dblock = nullptr;
-    cudaError_t e = cudaMalloc(&dblock, ar.host.size());
-    if (e != cudaSuccess) {
-        err = std::string("cudaMalloc(scene): ") + cudaGetErrorString(e);
-        return e == cudaErrorMemoryAllocation ? SWR_NO_MEMORY : SWR_CUDA_ERROR;
+    cudaError_t e = cudaSuccess;
+    if (to_device) {
+        e = cudaMalloc(&dblock, ar.host.size());
+        if (e != cudaSuccess) {
+            err = std::string("cudaMalloc(scene): ") + cudaGetErrorString(e);
+            cudaGetLastError();
+            return e == cudaErrorMemoryAllocation ? SWR_NO_MEMORY : SWR_CUDA_ERROR;
+        }
     }
-    uint8_t* db = static_cast<uint8_t*>(dblock);
+    // Host-only scenes are packed against a zero base so the layout code runs.
+    const uintptr_t base = reinterpret_cast<uintptr_t>(dblock);
+    auto at = [&](uint64_t off) { return base + (uintptr_t)off; };
     std::vector<DTexture> dtex;
-    for (size_t i = 0; i < all_tex.size(); ++i) dtex.push_back(to_dtex(*all_tex[i], o_tex[i], db));
+    for (size_t i = 0; i < all_tex.size(); ++i) dtex.push_back(to_dtex(*all_tex[i], at(o_tex[i])));
     std::memcpy(ar.host.data() + o_dtex, dtex.data(), dtex.size() * sizeof(DTexture));
     DScene& ds = s->dscene;
     ds = DScene{};
-    ds.vertices = reinterpret_cast<const DVertex*>(db + o_vert);
-    ds.indices = reinterpret_cast<const uint32_t*>(db + o_idx);
-    ds.prims = reinterpret_cast<const DPrimitive*>(db + o_prim);
-    ds.node_xform = reinterpret_cast<const float*>(db + o_xf);
-    ds.materials = reinterpret_cast<const DMaterial*>(db + o_mat);
-    ds.textures = reinterpret_cast<const DTexture*>(db + o_dtex);
-    ds.voxel_light = reinterpret_cast<const float*>(db + o_vox);
+    ds.vertices = reinterpret_cast<const DVertex*>(at(o_vert));
+    ds.indices = reinterpret_cast<const uint32_t*>(at(o_idx));
+    ds.prims = reinterpret_cast<const DPrimitive*>(at(o_prim));
+    ds.node_xform = reinterpret_cast<const float*>(at(o_xf));
+    ds.materials = reinterpret_cast<const DMaterial*>(at(o_mat));
+    ds.textures = reinterpret_cast<const DTexture*>(at(o_dtex));
+    ds.voxel_light = reinterpret_cast<const float*>(at(o_vox));
     ds.tex_cubemap = (uint32_t)s->textures.size();
     ds.tex_specular = ds.tex_cubemap + 1;
     ds.tex_brdf_lut = ds.tex_cubemap + 2;
@@ -1103,6 +1109,8 @@ swr_status upload_scene(SceneImpl* s, std::string& err) {
     ds.light_color[1] = s->light_color.y;
     ds.light_color[2] = s->light_color.z;
     std::memcpy(ar.host.data() + o_dscene, &ds, sizeof(DScene));
+    s->d_bytes = ar.host.size();
+    if (!to_device) return SWR_OK;
     e = cudaMemcpy(dblock, ar.host.data(), ar.host.size(), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         cudaFree(dblock);
@@ -1111,7 +1119,7 @@ swr_status upload_scene(SceneImpl* s, std::string& err) {
     }
     s->d_block = dblock;
     s->d_bytes = ar.host.size();
-    s->d_scene = reinterpret_cast<DScene*>(db + o_dscene);
+    s->d_scene = reinterpret_cast<DScene*>(at(o_dscene));
     return SWR_OK;
 }
 

@@ -77,7 +77,7 @@ struct SceneImpl {
 };
 
 swr_status build_scene(const swr_scene_desc* desc, SceneImpl* s, std::string& err);
-swr_status upload_scene(SceneImpl* s, std::string& err);
+swr_status upload_scene(SceneImpl* s, std::string& err, bool to_device);
 void free_scene_device(SceneImpl* s);
 void export_scene(const SceneImpl* s, swr_scene_host_view* out);
 

@@ -153,3 +153,109 @@ def small_scene(seed=7, count=6, subdiv=2, tex_size=64, cube_size=16, voxel=32):
     """A quick scene for tests: few spheres, small textures and grids."""
     return spheres_scene(seed=seed, count=count, subdiv=subdiv, box=4.0, radius=(0.5, 2.0), tex_size=tex_size,
                          cube_size=cube_size, voxel=voxel, specular_samples=16, brdf_lut_size=32)
+
+
+_ICO_CACHE = {}
+
+
+def _ico(subdiv):
+    if subdiv not in _ICO_CACHE:
+        P, F = icosphere(subdiv)
+        _ICO_CACHE[subdiv] = (P, spherical_uv(P), F)
+    return _ICO_CACHE[subdiv]
+
+
+def _look_rotation(forward, up=(0.0, 1.0, 0.0)):
+    f = forward / np.linalg.norm(forward)
+    r = np.cross(f, up)
+    if np.linalg.norm(r) < 1e-6:
+        r = np.cross(f, (1.0, 0.0, 0.0))
+    r /= np.linalg.norm(r)
+    u = np.cross(r, f)
+    return np.stack([r, u, -f], 1)  # columns: local x, y, z (z toward -forward)
+
+
+def stress_scene(seed=2, triangles=2_000_000, width=3840, height=2160, fov=math.pi / 3.0, far=400.0,
+                 n_textures=8, tex_size=2048, cube_size=128, voxel=128, area=(0.5, 5000.0), side_fraction=0.15,
+                 specular_samples=64, brdf_lut_size=128):
+    """Plain method, large: `triangles` triangles in icospheres and displaced
+    grids seen by a camera at the origin looking down -z.
+
+    Each object draws its mean front-facing triangle screen area A
+    log-uniformly from `area` px and gets about c / sqrt(A) triangles, so the
+    per-object triangle area is log-uniform over 0.5-5000 px while the total
+    coverage stays near 8x the screen. About `side_fraction` of the objects
+    straddle a frustum side or the near plane. `n_textures` value-noise
+    textures of `tex_size`^2 (full mip chains) are shared by the materials.
+    Returns (scene dict, camera params)."""
+    rng = np.random.default_rng(seed)
+    near = far * 0.01
+    fpx = (height / 2.0) / math.tan(fov / 2.0)
+    aspect = width / height
+    textures = [noise_texture(rng, tex_size, cells=32, tint=rng.uniform(0.4, 1.0, 3)) for _ in range(n_textures)]
+    meshes, nodes, mats = [], [], []
+    total = 0
+    # c such that E[c / sqrt(A)] * objects ~= triangles with ~1000 tris per object.
+    lo, hi = math.log(area[0]), math.log(area[1])
+    e_inv_sqrt = (area[0] ** -0.5 - area[1] ** -0.5) / (0.5 * (hi - lo))
+    c = 1000.0 / e_inv_sqrt
+    while total < triangles:
+        A = math.exp(rng.uniform(lo, hi))
+        T = int(max(8, min(8192, round(c / math.sqrt(A)))))
+        if total + T > triangles:
+            T = max(8, triangles - total)
+        edge = rng.random() < side_fraction
+        z = math.exp(rng.uniform(math.log(near * 3.0), math.log(far * 0.8)))
+        if edge:
+            if rng.random() < 0.3:
+                z = near * rng.uniform(0.6, 2.0)  # crosses the near plane
+                nx, ny = rng.uniform(-0.8, 0.8), rng.uniform(-0.8, 0.8)
+            else:
+                side = rng.integers(4)
+                nx, ny = rng.uniform(-1.0, 1.0), rng.uniform(-1.0, 1.0)
+                if side == 0: nx = rng.uniform(0.95, 1.1)
+                elif side == 1: nx = -rng.uniform(0.95, 1.1)
+                elif side == 2: ny = rng.uniform(0.95, 1.1)
+                else: ny = -rng.uniform(0.95, 1.1)
+        else:
+            nx, ny = rng.uniform(-0.95, 0.95), rng.uniform(-0.95, 0.95)
+        center = np.array([nx * z * aspect * math.tan(fov / 2), ny * z * math.tan(fov / 2), -z], np.float32)
+        sphere = rng.random() < 0.5
+        ti = int(rng.integers(n_textures))
+        mats.append({"base_color_factor": (1.0, 1.0, 1.0, 1.0), "metallic": float(rng.random()),
+                     "roughness": float(rng.random()), "base_color": (ti, WRAP_REPEAT, WRAP_REPEAT)})
+        if sphere:
+            sub = int(np.clip(round(math.log(max(T, 20) / 20.0, 4)), 0, 5))
+            P, UV, F = _ico(sub)
+            T = F.size // 3
+            r_px = math.sqrt(A * T / (2.0 * math.pi))
+            r = r_px * z / fpx
+            M = np.eye(4, dtype=np.float32)
+            M[:3, :3] *= r
+            M[:3, 3] = center
+            prim = {"positions": P, "normals": P.copy(), "texcoords": UV, "indices": F, "material": len(mats) - 1}
+        else:
+            n = max(2, int(round(math.sqrt(T / 2.0))))
+            P, UV, F = grid(n, n)
+            T = F.size // 3
+            L_px = math.sqrt(A * T)
+            L = L_px * z / fpx
+            P = P.copy()
+            P[:, 2] = 0.08 * np.sin(P[:, 0] * rng.uniform(4, 12)) * np.cos(P[:, 1] * rng.uniform(4, 12))
+            UV = UV * np.float32(rng.integers(1, 6))
+            to_cam = -center / np.linalg.norm(center)
+            tilt = rng.normal(0, 0.5, 3)
+            R = _look_rotation(-(to_cam + 0.6 * tilt))
+            M = np.eye(4, dtype=np.float32)
+            M[:3, :3] = R * L
+            M[:3, 3] = center
+            prim = {"positions": P, "normals": None, "texcoords": UV, "indices": F, "material": len(mats) - 1}
+        meshes.append([prim])
+        w = M.T.reshape(16).astype(np.float32).copy()
+        nodes.append({"world": w, "local": w, "mesh": len(meshes) - 1})
+        total += T
+    sd = {"meshes": meshes, "nodes": nodes, "materials": mats, "textures": textures,
+          "cubemap": cubemap_faces(rng, cube_size), "cubemap_face_size": cube_size, "voxel_grid_size": voxel,
+          "specular_samples": specular_samples, "brdf_lut_size": brdf_lut_size}
+    cam = ((0.0, 0.0, 0.0), (0.0, 0.0, -1.0), fov, width, height, far)
+    return sd, cam

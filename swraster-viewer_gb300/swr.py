@@ -138,8 +138,9 @@ EXPORTS = [
     "swr_camera_update", "swr_renderer_create", "swr_renderer_destroy", "swr_render_frame", "swr_renderer_sync",
     "swr_blit", "swr_read_visbuffer", "swr_renderer_device_outputs", "swr_renderer_get_exposure",
     "swr_renderer_set_exposure", "swr_renderer_get_stats", "swr_renderer_get_tile_luminance", "swr_last_error",
-    "swr_abi_version",
+    "swr_abi_version", "swr_renderer_set_profiling", "swr_renderer_get_profile",
 ]
+STAGES = ["reset", "frontend", "clip", "scan", "scatter", "raster", "shade", "resolve"]
 
 _lib = None
 
@@ -171,6 +172,8 @@ def lib():
         "swr_renderer_set_exposure": ([vp, C.c_float], C.c_int),
         "swr_renderer_get_stats": ([vp, C.POINTER(FrameStats)], C.c_int),
         "swr_renderer_get_tile_luminance": ([vp, f32p, C.c_uint32], C.c_int),
+        "swr_renderer_set_profiling": ([vp, C.c_int32], C.c_int),
+        "swr_renderer_get_profile": ([vp, f32p, C.c_int32, C.POINTER(C.c_uint32)], C.c_int),
         "swr_last_error": ([], C.c_char_p),
         "swr_abi_version": ([], C.c_int32),
     }
@@ -358,6 +361,16 @@ class Renderer:
         out = np.zeros(tx * ty, np.float32)
         check(lib().swr_renderer_get_tile_luminance(self.handle, _fp(out), out.size))
         return out
+
+    def set_profiling(self, on=True):
+        check(lib().swr_renderer_set_profiling(self.handle, 1 if on else 0))
+
+    def profile(self):
+        """Mean ms per stage since profiling was enabled, and the frame count."""
+        out = np.zeros(8, np.float32)
+        n = C.c_uint32()
+        check(lib().swr_renderer_get_profile(self.handle, _fp(out), 8, C.byref(n)))
+        return dict(zip(STAGES, out.tolist())), n.value
 
     def close(self):
         if getattr(self, "handle", None):

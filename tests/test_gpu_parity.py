@@ -24,11 +24,12 @@ def compare(scene, cam, w, h, **kw):
     bad = int((vis != ovis).sum())
     assert bad == 0, "visibility differs in %d of %d pixels" % (bad, vis.size)
     rows = h & ~1
-    a = rgba[:rows].view(np.uint8).astype(np.int32)
-    b = orgba[:rows].view(np.uint8).astype(np.int32)
-    d = np.abs(a - b)
-    print("max %d mean %.6f exact %.6f" % (d.max(), d.mean(), (d == 0).mean()))
-    assert d.max() <= TOL
+    if rows > 0:
+        a = rgba[:rows].view(np.uint8).astype(np.int32)
+        b = orgba[:rows].view(np.uint8).astype(np.int32)
+        d = np.abs(a - b)
+        print("max %d mean %.6f exact %.6f" % (d.max(), d.mean(), (d == 0).mean()))
+        assert d.max() <= TOL
     np.testing.assert_array_equal(tl, otl)
     r.close()
     return rgba, vis
