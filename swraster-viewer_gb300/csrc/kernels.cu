@@ -283,6 +283,23 @@ __device__ __forceinline__ void to_screen(const Vtx& v, float wf, float hf, int3
     sy = f2i_sat(round_away(fy * 16.0f));
 }
 
+// One atomic per warp: returns a distinct slot of *counter to every active lane.
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter) {
+    const uint32_t active = __activemask();
+    const int leader = __ffs(active) - 1;
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t base = 0;
+    if ((int)lane == leader) base = atomicAdd(counter, (uint32_t)__popc(active));
+    base = __shfl_sync(active, base, leader);
+    return base + (uint32_t)__popc(active & ((1u << lane) - 1u));
+}
+// One atomic per warp: adds the number of active lanes with `pred` set.
+__device__ __forceinline__ void warp_count(uint32_t* counter, bool pred) {
+    const uint32_t active = __activemask();
+    const uint32_t b = __ballot_sync(active, pred);
+    if ((int)(threadIdx.x & 31u) == __ffs(active) - 1 && b) atomicAdd(counter, (uint32_t)__popc(b));
+}
+
 // Warp-aggregated atomicAdd of 1 on counter[idx].
 __device__ __forceinline__ void agg_inc(uint32_t* counter, uint32_t idx) {
     const uint32_t active = __activemask();
@@ -397,7 +414,6 @@ __device__ bool setup_triangle(const FrameArgs& a, const DView& view, const Vtx&
         for (int i = 0; i < 11; ++i) dst[i] = src[i];
     }
     for_each_stile(view, S, mnx, mny, mxx, mxy, [&](uint32_t st) { agg_inc(a.tile_count, st); });
-    atomicAdd(&a.counters->pairs, (unsigned long long)n);
     return true;
 }
 
@@ -437,7 +453,7 @@ __global__ void __launch_bounds__(kChunkTris) k_frontend(FrameArgs a) {
     const Vtx v1 = transform_vertex(sc.vertices, pr.vtx_base + i1, model, d.mvp);
     const Vtx v2 = transform_vertex(sc.vertices, pr.vtx_base + i2, model, d.mvp);
     if (d.clip && !(vtx_inside_all(v0) && vtx_inside_all(v1) && vtx_inside_all(v2))) {
-        const uint32_t q = atomicAdd(&a.counters->clip_queue, 1u);
+        const uint32_t q = warp_append(&a.counters->clip_queue);
         if (q < a.clip_cap) {
             a.clip_queue[q] = make_uint2(g, ch.draw);
         } else {
@@ -449,7 +465,7 @@ __global__ void __launch_bounds__(kChunkTris) k_frontend(FrameArgs a) {
     // All three vertices inside: the clipper would return the triangle unchanged.
     const bool ok = setup_triangle(a, view, v0, v1, v2, g, g << 3, d.static_base + local, pr.material, d.view);
     a.tri_state[g] = ok ? 1 : 0;
-    if (ok) atomicAdd(&a.counters->setup_tris, 1u);
+    warp_count(&a.counters->setup_tris, ok);
 }
 
 // intersect (src/renderer.rs:598-609).
@@ -564,6 +580,7 @@ __global__ void __launch_bounds__(1024) k_scan(FrameArgs a) {
     }
     if (threadIdx.x == 1023) {
         a.tile_offset[n] = part[1023];
+        a.counters->pairs = part[1023];
         if ((uint64_t)part[1023] > a.bin_cap) atomicOr(&a.counters->status, ST_BIN_OVERFLOW);
     }
 }
@@ -665,9 +682,138 @@ __device__ __forceinline__ void fine_region(unsigned long long* sk, const Edge& 
     }
 }
 
+// One thread rasterizes a whole fine region (a small packet, or one 16-px
+// block), stepping its four quad lanes with the reference's sequential f32
+// additions: row starts accumulate step_y, quads accumulate step_x.
+template <int S>
+__device__ __forceinline__ void fine_thread(unsigned long long* sk, const Edge& e12, const Edge& e20, const Edge& e01,
+                                            const RecRaster& r, int32_t ox, int32_t oy, int32_t xe, int32_t ye,
+                                            int32_t sx0, int32_t sy0, const DScene* sc, const DMaterial* mat,
+                                            const RecShade* qs, uint32_t amip) {
+    float r0[4], r1[4], r2[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float lx = i2f(ox + ((k & 1) ? 24 : 8));
+        const float ly = i2f(oy + ((k >> 1) ? 24 : 8));
+        r0[k] = edge_eval(e12, lx, ly);
+        r1[k] = edge_eval(e20, lx, ly);
+        r2[k] = edge_eval(e01, lx, ly);
+    }
+    for (int32_t y = oy; y < ye; y += 32) {
+        const int32_t py0 = y >> 4;
+        if (py0 + 1 >= sy0 && py0 < sy0 + S) {
+            float w0[4], w1[4], w2[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                w0[k] = r0[k];
+                w1[k] = r1[k];
+                w2[k] = r2[k];
+            }
+            for (int32_t x = ox; x < xe; x += 32) {
+                const int32_t px0 = x >> 4;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int32_t px = px0 + (k & 1), py = py0 + (k >> 1);
+                    if (w0[k] >= 0.0f && w1[k] >= 0.0f && w2[k] >= 0.0f && (uint32_t)(px - sx0) < (uint32_t)S &&
+                        (uint32_t)(py - sy0) < (uint32_t)S) {
+                        const float b1 = w1[k] * r.ooa, b2 = w2[k] * r.ooa;
+                        const float w = 1.0f / interp(r.oow, b1, b2);
+                        const float z = interp(r.zow, b1, b2) * w;
+                        bool pass = (z == z);
+                        if (pass && mat) pass = alpha_pass(*sc, *mat, *qs, b1, b2, w, amip);
+                        if (pass) {
+                            const unsigned long long key = make_key(z, r.seq8);
+                            unsigned long long* slot = sk + (py - sy0) * S + (px - sx0);
+                            if (key < *slot) atomicMin(slot, key);
+                        }
+                    }
+                    w0[k] += e12.sx;
+                    w1[k] += e20.sx;
+                    w2[k] += e01.sx;
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            r0[k] += e12.sy;
+            r1[k] += e20.sy;
+            r2[k] += e01.sy;
+        }
+    }
+}
+
+// coarse_raster's block reject (src/tilerasterizer.rs:238-269): the block is
+// skipped when any edge is negative at all four corner pixel centres.
+__device__ __forceinline__ bool block_rejected(const Edge& e12, const Edge& e20, const Edge& e01, int32_t bx,
+                                               int32_t by) {
+    const float cx0 = i2f(bx + 8), cx1 = i2f(bx + 256 - 8);
+    const float cy0 = i2f(by + 8), cy1 = i2f(by + 256 - 8);
+    const float m0 = fmaxf(fmaxf(edge_eval(e12, cx0, cy0), edge_eval(e12, cx1, cy0)),
+                           fmaxf(edge_eval(e12, cx0, cy1), edge_eval(e12, cx1, cy1)));
+    const float m1 = fmaxf(fmaxf(edge_eval(e20, cx0, cy0), edge_eval(e20, cx1, cy0)),
+                           fmaxf(edge_eval(e20, cx0, cy1), edge_eval(e20, cx1, cy1)));
+    const float m2 = fmaxf(fmaxf(edge_eval(e01, cx0, cy0), edge_eval(e01, cx1, cy0)),
+                           fmaxf(edge_eval(e01, cx0, cy1), edge_eval(e01, cx1, cy1)));
+    return m0 < 0.0f || m1 < 0.0f || m2 < 0.0f;
+}
+
+struct PacketCtx {
+    RecRaster r;
+    Edge e01, e12, e20;
+    int32_t xs, ys, xe, ye;
+    bool coarse;
+    const DMaterial* mat;
+    const RecShade* qs;
+    uint32_t amip;
+};
+
+__device__ __forceinline__ void load_packet(const FrameArgs& a, const DScene& sc, uint32_t slot, int32_t tx0,
+                                            int32_t ty0, PacketCtx& c) {
+    const float4* src = reinterpret_cast<const float4*>(a.rec_r + slot);
+    float4* dst = reinterpret_cast<float4*>(&c.r);
+#pragma unroll
+    for (int i = 0; i < 5; ++i) dst[i] = __ldg(src + i);
+    c.e01 = make_edge(c.r.p[0], c.r.p[1], c.r.p[2], c.r.p[3]);
+    c.e12 = make_edge(c.r.p[2], c.r.p[3], c.r.p[4], c.r.p[5]);
+    c.e20 = make_edge(c.r.p[4], c.r.p[5], c.r.p[0], c.r.p[1]);
+    int32_t x0, y0, x1, y1;
+    clipped_rect(c.r, tx0, ty0, x0, y0, x1, y1);
+    c.coarse = (x1 - x0 > 16) || (y1 - y0 > 16);
+    c.xs = (x0 & ~1) * kSubpixelScale;
+    c.ys = (y0 & ~1) * kSubpixelScale;
+    c.xe = x1 * kSubpixelScale;
+    c.ye = y1 * kSubpixelScale;
+    c.mat = nullptr;
+    c.qs = nullptr;
+    c.amip = 0;
+    const DMaterial& m = sc.materials[c.r.material];
+    if (m.flags & MAT_ALPHA_TESTED) {
+        c.mat = &m;
+        c.qs = a.rec_s + slot;
+        c.amip = mip_level(sc.textures[m.tex[TS_BASE]], c.qs->du_dv[0], c.qs->du_dv[1], c.qs->du_dv[2],
+                           c.qs->du_dv[3]);
+    }
+}
+
+// Block index ranges of a coarse packet's 16-px blocks that overlap the
+// scheduling tile [s0, s0 + S).
+__device__ __forceinline__ void block_range(int32_t start, int32_t end, int32_t s0, int32_t S, int32_t& lo,
+                                            int32_t& hi) {
+    const int32_t nb = (end - start + 255) >> 8;
+    lo = 0;
+    hi = nb;  // exclusive
+    const int32_t t0 = s0 * 16, t1 = (s0 + S) * 16;
+    while (lo < hi && start + 256 * lo + 256 <= t0) ++lo;
+    while (hi > lo && start + 256 * (hi - 1) >= t1) --hi;
+}
+
+constexpr int kUnitCap = 1024;  // queued (packet, block) units per tile pass
+
 template <int S>
 __global__ void __launch_bounds__(256) k_raster(FrameArgs a) {
     __shared__ unsigned long long sk[S * S];
+    __shared__ uint2 units[kUnitCap];
+    __shared__ uint32_t n_units;
     const uint32_t st = blockIdx.x;
     const uint32_t vi = find_view_by_stile(a, st);
     const DView& view = a.views[vi];
@@ -676,62 +822,60 @@ __global__ void __launch_bounds__(256) k_raster(FrameArgs a) {
     const int32_t sy0 = (int32_t)(local / (uint32_t)view.stiles_x) * S;
     const int32_t tx0 = (sx0 / kRefTile) * kRefTile, ty0 = (sy0 / kRefTile) * kRefTile;
     for (int i = threadIdx.x; i < S * S; i += blockDim.x) sk[i] = kEmptyKey;
+    if (threadIdx.x == 0) n_units = 0;
     __syncthreads();
     const bool bad = (a.counters->status & (ST_BIN_OVERFLOW | ST_CLIP_OVERFLOW | ST_QUEUE_OVERFLOW)) != 0u;
     if (!bad) {
         const uint32_t b0 = a.tile_offset[st], b1 = a.tile_offset[st + 1];
-        const uint32_t warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
         const DScene& sc = a.scenes[view.scene];
-        for (uint32_t p = b0 + warp; p < b1; p += nwarps) {
+        // Pass 1: one thread per packet. Small packets are rasterized here;
+        // large ones are split into 16-px block units for pass 2.
+        for (uint32_t p = b0 + threadIdx.x; p < b1; p += blockDim.x) {
             const uint32_t slot = a.bins[p];
-            RecRaster r;
-            {
-                const float4* src = reinterpret_cast<const float4*>(a.rec_r + slot);
-                float4* dst = reinterpret_cast<float4*>(&r);
-#pragma unroll
-                for (int i = 0; i < 5; ++i) dst[i] = __ldg(src + i);
+            PacketCtx c;
+            load_packet(a, sc, slot, tx0, ty0, c);
+            if (!c.coarse) {
+                fine_thread<S>(sk, c.e12, c.e20, c.e01, c.r, c.xs, c.ys, c.xe, c.ye, sx0, sy0, &sc, c.mat, c.qs,
+                               c.amip);
+                continue;
             }
-            const Edge e01 = make_edge(r.p[0], r.p[1], r.p[2], r.p[3]);
-            const Edge e12 = make_edge(r.p[2], r.p[3], r.p[4], r.p[5]);
-            const Edge e20 = make_edge(r.p[4], r.p[5], r.p[0], r.p[1]);
-            int32_t x0, y0, x1, y1;
-            clipped_rect(r, tx0, ty0, x0, y0, x1, y1);
-            const DMaterial* mat = nullptr;
-            const RecShade* qs = nullptr;
-            uint32_t amip = 0;
-            {
-                const DMaterial& m = sc.materials[r.material];
-                if (m.flags & MAT_ALPHA_TESTED) {
-                    mat = &m;
-                    qs = a.rec_s + slot;
-                    amip = mip_level(sc.textures[m.tex[TS_BASE]], qs->du_dv[0], qs->du_dv[1], qs->du_dv[2],
-                                     qs->du_dv[3]);
-                }
-            }
-            const int32_t xs = (x0 & ~1) * kSubpixelScale, ys = (y0 & ~1) * kSubpixelScale;
-            const int32_t xe = x1 * kSubpixelScale, ye = y1 * kSubpixelScale;
-            if ((x1 - x0 > 16) || (y1 - y0 > 16)) {
-                // coarse_raster (src/tilerasterizer.rs:220-291): 16-px blocks.
-                for (int32_t by = ys; by < ye; by += 256) {
-                    if (by + 256 <= sy0 * 16 || by >= (sy0 + S) * 16) continue;
-                    for (int32_t bx = xs; bx < xe; bx += 256) {
-                        if (bx + 256 <= sx0 * 16 || bx >= (sx0 + S) * 16) continue;
-                        const float cx0 = i2f(bx + 8), cx1 = i2f(bx + 256 - 8);
-                        const float cy0 = i2f(by + 8), cy1 = i2f(by + 256 - 8);
-                        const float m0 = fmaxf(fmaxf(edge_eval(e12, cx0, cy0), edge_eval(e12, cx1, cy0)),
-                                               fmaxf(edge_eval(e12, cx0, cy1), edge_eval(e12, cx1, cy1)));
-                        const float m1 = fmaxf(fmaxf(edge_eval(e20, cx0, cy0), edge_eval(e20, cx1, cy0)),
-                                               fmaxf(edge_eval(e20, cx0, cy1), edge_eval(e20, cx1, cy1)));
-                        const float m2 = fmaxf(fmaxf(edge_eval(e01, cx0, cy0), edge_eval(e01, cx1, cy0)),
-                                               fmaxf(edge_eval(e01, cx0, cy1), edge_eval(e01, cx1, cy1)));
-                        if (m0 < 0.0f || m1 < 0.0f || m2 < 0.0f) continue;
-                        fine_region<S>(sk, e12, e20, e01, r, bx, by, min(bx + 256, xe), min(by + 256, ye), sx0, sy0,
-                                       &sc, mat, qs, amip);
-                    }
-                }
+            int32_t bxl, bxh, byl, byh;
+            block_range(c.xs, c.xe, sx0, S, bxl, bxh);
+            block_range(c.ys, c.ye, sy0, S, byl, byh);
+            const int32_t nb = (bxh - bxl) * (byh - byl);
+            if (nb <= 0) continue;
+            const uint32_t base = atomicAdd(&n_units, (uint32_t)nb);
+            if (base + (uint32_t)nb <= (uint32_t)kUnitCap) {
+                uint32_t u = base;
+                for (int32_t by = byl; by < byh; ++by)
+                    for (int32_t bx = bxl; bx < bxh; ++bx) units[u++] = make_uint2(slot, (uint32_t)((by << 8) | bx));
             } else {
-                fine_region<S>(sk, e12, e20, e01, r, xs, ys, xe, ye, sx0, sy0, &sc, mat, qs, amip);
+                // Queue full: mark the part of the reservation that fits as
+                // empty, then walk the packet's blocks in this thread.
+                for (uint32_t u = base; u < (uint32_t)kUnitCap; ++u) units[u] = make_uint2(0xFFFFFFFFu, 0u);
+                for (int32_t by = byl; by < byh; ++by)
+                    for (int32_t bx = bxl; bx < bxh; ++bx) {
+                        const int32_t ox = c.xs + 256 * bx, oy = c.ys + 256 * by;
+                        if (block_rejected(c.e12, c.e20, c.e01, ox, oy)) continue;
+                        fine_thread<S>(sk, c.e12, c.e20, c.e01, c.r, ox, oy, min(ox + 256, c.xe), min(oy + 256, c.ye),
+                                       sx0, sy0, &sc, c.mat, c.qs, c.amip);
+                    }
             }
+        }
+        __syncthreads();
+        // Pass 2: one warp per queued 16-px block of a large packet.
+        const uint32_t nu = min(n_units, (uint32_t)kUnitCap);
+        const uint32_t warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+        for (uint32_t u = warp; u < nu; u += nwarps) {
+            const uint2 un = units[u];
+            if (un.x == 0xFFFFFFFFu) continue;
+            PacketCtx c;
+            load_packet(a, sc, un.x, tx0, ty0, c);
+            const int32_t bx = (int32_t)(un.y & 0xFFu), by = (int32_t)(un.y >> 8);
+            const int32_t ox = c.xs + 256 * bx, oy = c.ys + 256 * by;
+            if (block_rejected(c.e12, c.e20, c.e01, ox, oy)) continue;
+            fine_region<S>(sk, c.e12, c.e20, c.e01, c.r, ox, oy, min(ox + 256, c.xe), min(oy + 256, c.ye), sx0, sy0,
+                           &sc, c.mat, c.qs, c.amip);
         }
     }
     __syncthreads();
@@ -1104,7 +1248,7 @@ void launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t* ev
     }
     mark(5);
     switch (a.sched_tile) {
-        case 8: k_raster<8><<<a.n_stiles, 64, 0, s>>>(a); break;
+        case 8: k_raster<8><<<a.n_stiles, 128, 0, s>>>(a); break;
         case 16: k_raster<16><<<a.n_stiles, 128, 0, s>>>(a); break;
         case 32: k_raster<32><<<a.n_stiles, 256, 0, s>>>(a); break;
         default: k_raster<64><<<a.n_stiles, 256, 0, s>>>(a); break;

@@ -98,3 +98,57 @@ def test_repeat_frames_identical(small):
     np.testing.assert_array_equal(a[0], b[0])
     np.testing.assert_array_equal(a[1], b[1])
     r.close()
+
+
+def quad_stack_scene(n=120, dup_every=10):
+    """n screen-covering 2-triangle quads at increasing depth; every
+    `dup_every`-th quad is duplicated exactly (same node transform), so the
+    two copies tie on depth at every pixel and the later node must win."""
+    rng = np.random.default_rng(11)
+    P, UV, F = scenes.grid(1, 1)
+    tex = scenes.noise_texture(rng, 32)
+    meshes, nodes, mats = [], [], []
+    for i in range(n):
+        mats.append({"metallic": float(rng.random()), "roughness": float(rng.random()), "base_color": (0, 0, 0)})
+        meshes.append([{"positions": P, "normals": None, "texcoords": UV, "indices": F, "material": i}])
+        z = -2.0 - 0.05 * i
+        m = np.eye(4, dtype=np.float32)
+        m[0, 0] = m[1, 1] = 8.0 + 0.01 * i
+        m[:3, 3] = (0.01 * i, -0.02 * i, z)
+        w = m.T.reshape(16).copy()
+        nodes.append({"world": w, "local": w, "mesh": i})
+        if i % dup_every == 0:
+            nodes.append({"world": w, "local": w, "mesh": i})
+    return {"meshes": meshes, "nodes": nodes, "materials": mats, "textures": [tex],
+            "cubemap": scenes.cubemap_faces(rng, 8), "cubemap_face_size": 8, "voxel_grid_size": 16,
+            "specular_samples": 8, "brdf_lut_size": 16}
+
+
+@pytest.mark.parametrize("tile", [64, 16])
+def test_overlapping_large_quads_and_depth_ties(tile):
+    s = swr.Scene(quad_stack_scene())
+    cam = swr.make_camera((0.0, 0.0, 3.0), (0.0, 0.0, 0.0), 1.0, 192, 128, 40.0)
+    rgba, vis = compare(s, cam, 192, 128, sched_tile=tile)
+    # The nearest quad is node 0 (triangles 0, 1) with an exact duplicate,
+    # node 1 (triangles 2, 3): equal depth everywhere, and the duplicate comes
+    # later in the canonical order, so only its triangles are visible.
+    covered = vis[vis != np.uint64(2 ** 64 - 1)] >> np.uint64(3)
+    assert covered.size > 0 and set(np.unique(covered).tolist()) == {2, 3}
+    s.close()
+
+
+def test_stress_workload_reduced():
+    sd, cp = scenes.stress_scene(seed=4, triangles=150_000, width=960, height=540, n_textures=2, tex_size=256,
+                                 cube_size=32, voxel=32, specular_samples=16, brdf_lut_size=32)
+    s = swr.Scene(sd)
+    cam = swr.make_camera(*cp)
+    compare(s, cam, 960, 540)
+    s.close()
+
+
+def test_stress_workload_full_4k():
+    sd, cp = scenes.stress_scene()
+    s = swr.Scene(sd)
+    cam = swr.make_camera(*cp)
+    compare(s, cam, 3840, 2160)
+    s.close()
