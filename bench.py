@@ -42,6 +42,7 @@ def parse():
     ap.add_argument("--workload", default="4k", choices=["4k", "small"])
     ap.add_argument("--cpu-frames", type=int, default=3, help="frames in the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sched-tile", type=int, default=64, help="raster scheduling tile (8, 16, 32, 64)")
     return ap.parse_args()
 
 
@@ -175,7 +176,7 @@ def main():
     scene = swr.Scene(sd)
     cam = swr.make_camera(*cam_params) if cam_params else swr.make_camera(
         *scenes.default_camera_params(scene.info(), W, H))
-    r = swr.Renderer(W, H)
+    r = swr.Renderer(W, H, sched_tile=args.sched_tile)
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
 
@@ -254,7 +255,7 @@ def main():
             "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded scene of the configured shape; inputs larger than L2)",
-            "config": dict(cfg, parallelism="replicas" if world > 1 else "single"),
+            "config": dict(cfg, parallelism="replicas" if world > 1 else "single", sched_tile=args.sched_tile),
             "gtri_per_s": fps * cfg["triangles"] / 1e9, "gpix_per_s": fps * W * H / 1e9,
             "stage_ms": {k: round(v, 4) for k, v in prof.items()},
             "frame_stats": {"triangles_in": st.triangles_in, "clipped": st.triangles_clipped,

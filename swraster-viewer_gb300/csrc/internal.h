@@ -142,6 +142,9 @@ struct DChunk {
     uint32_t tri_start;        // local to the draw
 };
 
+// RecRaster.material carries the alpha-test flag in its top bit.
+constexpr uint32_t kRecAlphaBit = 0x80000000u;
+
 // Raster-side triangle record (one per emitted, non-culled triangle).
 struct alignas(16) RecRaster {
     int32_t p[6];              // screen subpixel positions p0, p1, p2

@@ -463,7 +463,8 @@ __global__ void __launch_bounds__(kChunkTris) k_frontend(FrameArgs a) {
         return;
     }
     // All three vertices inside: the clipper would return the triangle unchanged.
-    const bool ok = setup_triangle(a, view, v0, v1, v2, g, g << 3, d.static_base + local, pr.material, d.view);
+    const uint32_t mword = pr.material | ((sc.materials[pr.material].flags & MAT_ALPHA_TESTED) ? kRecAlphaBit : 0u);
+    const bool ok = setup_triangle(a, view, v0, v1, v2, g, g << 3, d.static_base + local, mword, d.view);
     a.tri_state[g] = ok ? 1 : 0;
     warp_count(&a.counters->setup_tris, ok);
 }
@@ -501,6 +502,7 @@ __global__ void __launch_bounds__(128) k_clip(FrameArgs a) {
         const DScene& sc = a.scenes[d.scene];
         const DView& view = a.views[d.view];
         const DPrimitive pr = sc.prims[d.prim];
+        const uint32_t mword = pr.material | ((sc.materials[pr.material].flags & MAT_ALPHA_TESTED) ? kRecAlphaBit : 0u);
         const float* model = sc.node_xform + 16u * d.node;
         const uint32_t* ib = sc.indices + pr.idx_base + 3u * local;
         Vtx poly[16], np[16];
@@ -541,7 +543,7 @@ __global__ void __launch_bounds__(128) k_clip(FrameArgs a) {
             for (int f = 0; f < fans; ++f) {
                 const uint32_t slot = f == 0 ? g : a.tri_total + base + (uint32_t)(f - 1);
                 const bool ok = setup_triangle(a, view, poly[0], poly[f + 1], poly[f + 2], slot, (g << 3) | (uint32_t)f,
-                                               d.static_base + local, pr.material, d.view);
+                                               d.static_base + local, mword, d.view);
                 if (ok) {
                     atomicAdd(&a.counters->setup_tris, 1u);
                     if (f == 0) any = 1;
@@ -659,11 +661,15 @@ __device__ __forceinline__ void fine_region(unsigned long long* sk, const Edge& 
             w1 += e20.sy;
             w2 += e01.sy;
         }
-        const bool row_in = (uint32_t)(py - sy0) < (uint32_t)S;
+        const bool row_in = S == kRefTile || (uint32_t)(py - sy0) < (uint32_t)S;
         if (!row_in) continue;
+        const bool dec0 = !(e12.sx > 0.0f), dec1 = !(e20.sx > 0.0f), dec2 = !(e01.sx > 0.0f);
         for (int32_t i = 0; i < ncol; ++i) {
             const int32_t px = (ox >> 4) + 2 * i + kx;
-            if ((uint32_t)(px - sx0) < (uint32_t)S && w0 >= 0.0f && w1 >= 0.0f && w2 >= 0.0f) {
+            // Monotone rounding: an edge with x step <= 0 that is negative
+            // stays negative for the rest of this lane's row.
+            if ((dec0 && w0 < 0.0f) || (dec1 && w1 < 0.0f) || (dec2 && w2 < 0.0f)) break;
+            if ((S == kRefTile || (uint32_t)(px - sx0) < (uint32_t)S) && w0 >= 0.0f && w1 >= 0.0f && w2 >= 0.0f) {
                 const float b1 = w1 * r.ooa, b2 = w2 * r.ooa;
                 const float w = 1.0f / interp(r.oow, b1, b2);
                 const float z = interp(r.zow, b1, b2) * w;
@@ -699,9 +705,14 @@ __device__ __forceinline__ void fine_thread(unsigned long long* sk, const Edge& 
         r1[k] = edge_eval(e20, lx, ly);
         r2[k] = edge_eval(e01, lx, ly);
     }
+    // Rounding is monotone, so along a row an edge whose x step is <= 0 never
+    // grows: once it is negative in all four lanes the rest of the row is
+    // outside the triangle and the walk stops (the values it would have
+    // computed are never used).
+    const bool dec0 = !(e12.sx > 0.0f), dec1 = !(e20.sx > 0.0f), dec2 = !(e01.sx > 0.0f);
     for (int32_t y = oy; y < ye; y += 32) {
         const int32_t py0 = y >> 4;
-        if (py0 + 1 >= sy0 && py0 < sy0 + S) {
+        if (S == kRefTile || (py0 + 1 >= sy0 && py0 < sy0 + S)) {
             float w0[4], w1[4], w2[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
@@ -711,22 +722,39 @@ __device__ __forceinline__ void fine_thread(unsigned long long* sk, const Edge& 
             }
             for (int32_t x = ox; x < xe; x += 32) {
                 const int32_t px0 = x >> 4;
+                bool any = false;
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    const int32_t px = px0 + (k & 1), py = py0 + (k >> 1);
-                    if (w0[k] >= 0.0f && w1[k] >= 0.0f && w2[k] >= 0.0f && (uint32_t)(px - sx0) < (uint32_t)S &&
-                        (uint32_t)(py - sy0) < (uint32_t)S) {
-                        const float b1 = w1[k] * r.ooa, b2 = w2[k] * r.ooa;
-                        const float w = 1.0f / interp(r.oow, b1, b2);
-                        const float z = interp(r.zow, b1, b2) * w;
-                        bool pass = (z == z);
-                        if (pass && mat) pass = alpha_pass(*sc, *mat, *qs, b1, b2, w, amip);
-                        if (pass) {
-                            const unsigned long long key = make_key(z, r.seq8);
-                            unsigned long long* slot = sk + (py - sy0) * S + (px - sx0);
-                            if (key < *slot) atomicMin(slot, key);
+                    const bool cov = w0[k] >= 0.0f && w1[k] >= 0.0f && w2[k] >= 0.0f;
+                    any |= cov;
+                }
+                if (any) {
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const int32_t px = px0 + (k & 1), py = py0 + (k >> 1);
+                        const bool in_tile = S == kRefTile || ((uint32_t)(px - sx0) < (uint32_t)S &&
+                                                               (uint32_t)(py - sy0) < (uint32_t)S);
+                        if (w0[k] >= 0.0f && w1[k] >= 0.0f && w2[k] >= 0.0f && in_tile) {
+                            const float b1 = w1[k] * r.ooa, b2 = w2[k] * r.ooa;
+                            const float w = 1.0f / interp(r.oow, b1, b2);
+                            const float z = interp(r.zow, b1, b2) * w;
+                            bool pass = (z == z);
+                            if (pass && mat) pass = alpha_pass(*sc, *mat, *qs, b1, b2, w, amip);
+                            if (pass) {
+                                const unsigned long long key = make_key(z, r.seq8);
+                                unsigned long long* slot = sk + (py - sy0) * S + (px - sx0);
+                                if (key < *slot) atomicMin(slot, key);
+                            }
                         }
                     }
+                } else {
+                    const bool out0 = dec0 && w0[0] < 0.0f && w0[1] < 0.0f && w0[2] < 0.0f && w0[3] < 0.0f;
+                    const bool out1 = dec1 && w1[0] < 0.0f && w1[1] < 0.0f && w1[2] < 0.0f && w1[3] < 0.0f;
+                    const bool out2 = dec2 && w2[0] < 0.0f && w2[1] < 0.0f && w2[2] < 0.0f && w2[3] < 0.0f;
+                    if (out0 || out1 || out2) break;
+                }
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
                     w0[k] += e12.sx;
                     w1[k] += e20.sx;
                     w2[k] += e01.sx;
@@ -786,8 +814,8 @@ __device__ __forceinline__ void load_packet(const FrameArgs& a, const DScene& sc
     c.mat = nullptr;
     c.qs = nullptr;
     c.amip = 0;
-    const DMaterial& m = sc.materials[c.r.material];
-    if (m.flags & MAT_ALPHA_TESTED) {
+    if (c.r.material & kRecAlphaBit) {
+        const DMaterial& m = sc.materials[c.r.material & ~kRecAlphaBit];
         c.mat = &m;
         c.qs = a.rec_s + slot;
         c.amip = mip_level(sc.textures[m.tex[TS_BASE]], c.qs->du_dv[0], c.qs->du_dv[1], c.qs->du_dv[2],
@@ -1160,7 +1188,7 @@ __global__ void __launch_bounds__(256) k_shade(FrameArgs a) {
             float dd[4];
 #pragma unroll
             for (int i = 0; i < 4; ++i) dd[i] = q.du_dv[i] * (1.0f / interp(r.oow, qb1[i], qb2[i]));
-            const DMaterial& m = sc.materials[r.material];
+            const DMaterial& m = sc.materials[r.material & ~kRecAlphaBit];
             col = pbr_lane(sc, v, m, q, r, b1, b2, dd, tab);
             vis_hi = q.static_id;
             vis_fan = r.seq8 & 7u;

@@ -10,7 +10,7 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIBPATH = os.path.join(HERE, "libswr.so")
+LIBPATH = os.environ.get("SWR_LIBRARY") or os.path.join(HERE, "libswr.so")
 
 SWR_OK, SWR_INVALID_ARG, SWR_NO_MEMORY, SWR_OVERFLOW, SWR_TIMEOUT = 0, 1, 2, 3, 4
 SWR_CUDA_ERROR, SWR_IO_ERROR, SWR_BAD_SCENE, SWR_UNSUPPORTED, SWR_BUSY = 5, 6, 7, 8, 9
