@@ -397,6 +397,25 @@ swr_status swr_renderer_get_tile_luminance(swr_renderer* r, float* out, uint32_t
 swr_status swr_renderer_set_profiling(swr_renderer* r, int32_t enable);
 swr_status swr_renderer_get_profile(swr_renderer* r, float* stage_ms, int32_t n, uint32_t* frames);
 
+/* Allocation-free frame. No counterpart in the reference: an addition for
+ * callers that cannot allocate device memory while they render (code running
+ * under CUDA stream capture, processes whose device memory belongs to another
+ * allocator, real-time loops that cannot afford a synchronizing cudaMalloc).
+ * Renders `scene` (already resident) from `camera` into the caller's device
+ * buffers rgba8 (width*height, row pitch width; an odd last row is left
+ * untouched) and vis (width*height), with a fixed `exposure` (2.0 is a fresh
+ * renderer's) and without allocating anything: all per-frame work buffers
+ * live in one fixed __device__ array of about 9 MB. Limits: width, height
+ * <= 512, at most 16384 triangles passing the frustum test, 4096 nodes, 4096
+ * draws, 65536 (triangle, tile) pairs; larger inputs return SWR_INVALID_ARG,
+ * capacity overflow on the device returns SWR_OVERFLOW. Returns after the
+ * frame has finished. The first call on each device looks up the array's
+ * address and must come before any stream capture; all calls share the array,
+ * so calls whose GPU work overlaps race. */
+swr_status swr_render_frame_noalloc(const swr_scene* scene, const swr_camera* camera, int32_t width,
+                                    int32_t height, float exposure, uint32_t rsqrt_mode, uint32_t* rgba8,
+                                    uint64_t* vis, void* stream);
+
 const char* swr_last_error(void);
 int32_t swr_abi_version(void);
 

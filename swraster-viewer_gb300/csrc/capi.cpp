@@ -29,6 +29,11 @@ swr_status cuda_fail(cudaError_t e, const char* what) {
 
 }  // namespace
 
+namespace swr {
+// Lets entry points outside this file report through swr_last_error().
+void set_last_error(const char* msg) { g_err = msg; }
+}  // namespace swr
+
 extern "C" {
 
 const char* swr_last_error(void) { return g_err.c_str(); }

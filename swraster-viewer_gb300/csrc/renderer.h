@@ -88,6 +88,9 @@ void build_view_draws(const SceneImpl& s, const swr_camera& cam, uint32_t view_i
 // Fill the view-geometry fields of a DView (tiles, pitches, camera).
 void init_view(DView& v, const swr_camera& cam, int32_t width, int32_t height, uint32_t sched_tile);
 
+// Sets the calling thread's swr_last_error() message.
+void set_last_error(const char* msg);
+
 // update_auto_exposure (src/renderer.rs:258-290).
 struct ExposureState {
     float exposure = 2.0f;

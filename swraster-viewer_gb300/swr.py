@@ -138,7 +138,7 @@ EXPORTS = [
     "swr_camera_update", "swr_renderer_create", "swr_renderer_destroy", "swr_render_frame", "swr_renderer_sync",
     "swr_blit", "swr_read_visbuffer", "swr_renderer_device_outputs", "swr_renderer_get_exposure",
     "swr_renderer_set_exposure", "swr_renderer_get_stats", "swr_renderer_get_tile_luminance", "swr_last_error",
-    "swr_abi_version", "swr_renderer_set_profiling", "swr_renderer_get_profile",
+    "swr_abi_version", "swr_renderer_set_profiling", "swr_renderer_get_profile", "swr_render_frame_noalloc",
 ]
 STAGES = ["reset", "frontend", "clip", "scan", "scatter", "raster", "shade", "resolve"]
 
@@ -174,6 +174,8 @@ def lib():
         "swr_renderer_get_tile_luminance": ([vp, f32p, C.c_uint32], C.c_int),
         "swr_renderer_set_profiling": ([vp, C.c_int32], C.c_int),
         "swr_renderer_get_profile": ([vp, f32p, C.c_int32, C.POINTER(C.c_uint32)], C.c_int),
+        "swr_render_frame_noalloc": ([vp, C.POINTER(Camera), C.c_int32, C.c_int32, C.c_float, C.c_uint32, vp, vp, vp],
+                                     C.c_int),
         "swr_last_error": ([], C.c_char_p),
         "swr_abi_version": ([], C.c_int32),
     }
