@@ -397,6 +397,109 @@ swr_status swr_renderer_get_tile_luminance(swr_renderer* r, float* out, uint32_t
 swr_status swr_renderer_set_profiling(swr_renderer* r, int32_t enable);
 swr_status swr_renderer_get_profile(swr_renderer* r, float* stage_ms, int32_t n, uint32_t* frames);
 
+/* ------------------------------------------------------------------ */
+/* Batched form: many views of one or more resident scenes rendered by */
+/* one launch sequence (no reference counterpart; the reference renders */
+/* one view per frame).                                                 */
+/* ------------------------------------------------------------------ */
+
+typedef struct swr_view_desc {
+    const swr_scene* scene;
+    const swr_camera* camera;
+    int32_t width;
+    int32_t height;
+    float exposure;             /* 2.0 = a fresh renderer's exposure */
+    uint32_t rsqrt_mode;        /* SWR_RSQRT_* */
+    uint32_t* rgba8;            /* device output (width*height) or NULL: batch-owned */
+    uint64_t* vis;              /* device output (width*height) or NULL: batch-owned */
+} swr_view_desc;
+
+typedef struct swr_batch_opts {
+    uint32_t sched_tile;        /* 8, 16, 32, 64; 0 = autotuned choice for the batch's class */
+    uint32_t use_graph;         /* replay the frame as a CUDA graph */
+    uint64_t bin_capacity;      /* initial pair capacity, 0 = auto */
+} swr_batch_opts;
+
+typedef struct swr_batch swr_batch;
+
+swr_status swr_batch_create(const swr_batch_opts* opts, swr_batch** out);
+void swr_batch_destroy(swr_batch* b);
+/* Enqueues all views on `stream` (the tables are uploaded with one copy and
+ * the seven kernels run once for the whole batch; the raster kernel is
+ * persistent and pulls (view, tile) items from a device work counter). */
+swr_status swr_batch_render(swr_batch* b, const swr_view_desc* views, int32_t n, void* stream);
+/* Waits for the last batch; re-renders it after growing capacities if bins
+ * overflowed. */
+swr_status swr_batch_sync(swr_batch* b);
+swr_status swr_batch_output(swr_batch* b, int32_t view, const uint32_t** rgba8, const uint64_t** vis);
+/* Times every scheduling tile size on these views and keeps the fastest for
+ * the batch's class (pixel count, triangle count, view count). */
+swr_status swr_batch_autotune(swr_batch* b, const swr_view_desc* views, int32_t n, void* stream,
+                              uint32_t* best_tile, float* best_ms);
+/* Milliseconds of the last synced batch on the device (CUDA events). */
+swr_status swr_batch_last_ms(swr_batch* b, float* ms);
+
+/* ------------------------------------------------------------------ */
+/* Served form: a request loop over resident scenes with memory-budget */
+/* admission and continuous batching (no reference counterpart).        */
+/* ------------------------------------------------------------------ */
+
+typedef struct swr_server_opts {
+    uint64_t memory_budget;     /* HBM bytes for resident scenes + pooled framebuffers */
+    uint32_t max_batch_views;   /* views per batch (default 64) */
+    uint32_t max_queue;         /* pending requests before submit returns SWR_BUSY (default 4096) */
+    uint32_t inflight;          /* batches in flight on separate streams (default 2) */
+    uint32_t sched_tile;        /* 0 = autotuned choice */
+    uint32_t rsqrt_mode;
+    uint32_t use_graph;
+} swr_server_opts;
+
+typedef struct swr_request {
+    int32_t scene;              /* id from swr_server_add_scene */
+    int32_t width;
+    int32_t height;
+    float exposure;
+    swr_camera camera;
+    uint64_t tag;
+} swr_request;
+
+typedef struct swr_completion {
+    uint64_t ticket;
+    uint64_t tag;
+    int32_t status;
+    int32_t width;
+    int32_t height;
+    int32_t batch_views;        /* size of the batch this request ran in */
+    const uint32_t* rgba8;      /* device; valid until swr_server_release(ticket) */
+    const uint64_t* vis;
+    double queue_ms;            /* submit -> batch launch */
+    double latency_ms;          /* submit -> completion */
+} swr_completion;
+
+typedef struct swr_server_stats {
+    uint64_t submitted, completed, rejected, batches;
+    uint64_t device_bytes;      /* scenes + framebuffers + engines */
+    uint64_t budget;
+} swr_server_stats;
+
+typedef struct swr_server swr_server;
+
+swr_status swr_server_create(const swr_server_opts* opts, swr_server** out);
+void swr_server_destroy(swr_server* s);
+/* Makes a scene resident for the server; SWR_BUSY if it does not fit the
+ * budget. The scene must outlive the server. */
+swr_status swr_server_add_scene(swr_server* s, const swr_scene* scene, int32_t* id);
+swr_status swr_server_submit(swr_server* s, const swr_request* req, uint64_t* ticket);
+/* Up to `max` completions; waits up to wait_ms for the first one. */
+swr_status swr_server_poll(swr_server* s, swr_completion* out, int32_t max, int32_t* n, int32_t wait_ms);
+/* Returns a completed request's framebuffers to the pool. */
+swr_status swr_server_release(swr_server* s, uint64_t ticket);
+swr_status swr_server_get_stats(swr_server* s, swr_server_stats* out);
+
+/* Copies `bytes` from device memory (batch or server outputs) into host
+ * memory `dst`, ordered on `stream`; returns when the copy is done. */
+swr_status swr_copy_to_host(void* dst, const void* src_device, size_t bytes, void* stream);
+
 /* Allocation-free frame. No counterpart in the reference: an addition for
  * callers that cannot allocate device memory while they render (code running
  * under CUDA stream capture, processes whose device memory belongs to another

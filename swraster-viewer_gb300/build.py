@@ -46,7 +46,13 @@ def _compile(src, force):
     return obj, p.stderr
 
 
-def build(force=False, verbose=False):
+def build(force=False, verbose=False, defines=(), out=None, lib=None):
+    """defines: extra -D flags (variants for experiments build into `out`/`lib`)."""
+    global OUT, LIB
+    if out:
+        OUT, LIB = out, lib
+    if defines:
+        NVCC_FLAGS.extend("-D" + d for d in defines)
     os.makedirs(OUT, exist_ok=True)
     srcs = sorted(os.path.join(SRC, f) for f in os.listdir(SRC) if f.endswith((".cu", ".cpp")))
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 1))) as ex:

@@ -291,9 +291,6 @@ swr_status enqueue_frame(swr_renderer* r, const swr_scene* scene, const swr_came
         r->expo.exposure = v.exposure;
     }
     std::vector<const swr_camera*> cams = {cam};
-    FrameArgs a{};
-    swr_status st = r->eng.run(scenes, views, cams, stream, &a, err);
-    if (st != SWR_OK) return fail(st, err);
     cudaEvent_t* ev = nullptr;
     int slot = -1;
     if (r->profiling) {
@@ -304,7 +301,9 @@ swr_status enqueue_frame(swr_renderer* r, const swr_scene* scene, const swr_came
         r->prof_pending[slot] = true;
         r->prof_resolve[slot] = deferred;
     }
-    launch_frame(a, stream, r->eng.num_sms, ev);
+    FrameArgs a{};
+    swr_status st = r->eng.run(scenes, views, cams, stream, &a, err, ev);
+    if (st != SWR_OK) return fail(st, err);
     if (deferred) {
         const size_t nt = (size_t)r->tiles_x * r->tiles_y;
         cudaMemcpyAsync(r->h_lum, r->tile_lum.p, nt * sizeof(float), cudaMemcpyDeviceToHost, stream);
@@ -431,7 +430,7 @@ swr_status swr_renderer_get_stats(swr_renderer* r, swr_frame_stats* o) {
     if (st != SWR_OK) return st;
     std::memset(o, 0, sizeof(*o));
     const DCounters& c = r->eng.last;
-    o->triangles_in = r->last_args.tri_total;
+    o->triangles_in = r->eng.dyn.tri_total;
     o->triangles_clipped = c.clip_queue;
     o->setup_triangles = c.setup_tris;
     o->bin_pairs = c.pairs;

@@ -191,18 +191,35 @@ struct alignas(16) DCounters {
     uint32_t pad[3];
 };
 
-// Everything a frame's kernels need, passed by value.
+// Per-frame counts, uploaded with the tables: kernels read them from device
+// memory so a launch sequence captured once (grids sized by capacity)
+// serves any batch that fits the capacities.
+struct alignas(16) DFrameDyn {
+    uint32_t n_views;
+    uint32_t n_chunks;
+    uint32_t tri_total;        // T: main record slots used this frame
+    uint32_t n_stiles;         // bins over all views
+    uint32_t total_quads;      // shading work over all views
+    uint32_t max_view_pixels;  // largest width * (height & ~1)
+    uint32_t pad[2];
+};
+
+// Everything a frame's kernels need, passed by value: pointers and
+// capacities only (they change only when buffers grow).
 struct FrameArgs {
+    const DFrameDyn* dyn;
     const DScene* scenes;
     const DView* views;
-    uint32_t n_views;
     const DDraw* draws;
     const DChunk* chunks;
-    uint32_t n_chunks;
-    uint32_t tri_total;        // T: main record slots
+    uint32_t chunk_cap;        // grid of k_frontend
+    uint32_t tri_cap;          // main record slots allocated
     uint32_t extra_cap;        // extra record slots
     uint32_t clip_cap;         // clip queue capacity
-    uint32_t n_stiles;         // bins over all views
+    uint32_t stile_cap;        // bins allocated
+    uint32_t quad_cap;         // shading quads allocated (grid bound)
+    uint32_t pixel_cap;        // largest view's pixels (resolve grid)
+    uint32_t view_cap;
     uint64_t bin_cap;
     uint32_t sched_tile;       // S
     uint32_t pad0;
@@ -218,9 +235,9 @@ struct FrameArgs {
     unsigned long long* keys;
     DCounters* counters;
     const uint8_t* rsqrt_table;// 512 entries, FRSQRTE estimates
-    uint32_t total_quads;      // shading work over all views
-    uint32_t max_view_pixels;  // largest width * (height & ~1) over views
     const float* exposure_dev; // exposure computed by the host step (dt > 0)
+    uint32_t raster_grid;      // persistent raster CTAs
+    uint32_t shade_grid;       // grid-stride shading CTAs
 };
 
 // Launch wrappers (kernels.cu). `ev`, when given, holds 8 events recorded
@@ -228,5 +245,9 @@ struct FrameArgs {
 void launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t* ev = nullptr);
 void launch_reset(const FrameArgs& a, void* stream);
 void launch_resolve(const FrameArgs& a, void* stream);
+// Per-device constant tables; call once per device outside stream capture.
+cudaError_t init_kernel_constants();
+// Persistent raster / grid-stride shading grid sizes for this device.
+void frame_grids(int num_sms, uint32_t sched_tile, uint32_t* raster_grid, uint32_t* shade_grid);
 
 }  // namespace swr

@@ -29,6 +29,16 @@
 #include "devmath.cuh"
 #include "internal.h"
 
+// Raster variants: persistent CTAs pulling tiles from a device counter
+// (needed for graph replay with a fixed grid) or one CTA per tile; early row
+// exit on monotone edges.
+#ifndef SWR_RASTER_PERSISTENT
+#define SWR_RASTER_PERSISTENT 1
+#endif
+#ifndef SWR_ROW_EXIT
+#define SWR_ROW_EXIT 0
+#endif
+
 namespace swr {
 
 // --------------------------------------------------------------------------
@@ -418,9 +428,10 @@ __device__ bool setup_triangle(const FrameArgs& a, const DView& view, const Vtx&
 }
 
 __global__ void k_reset(FrameArgs a) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < a.n_stiles) a.tile_count[i] = 0u;
-    if (i == 0) {
+    const uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = a.dyn->n_stiles;
+    for (uint32_t i = i0; i < n; i += gridDim.x * blockDim.x) a.tile_count[i] = 0u;
+    if (i0 == 0) {
         a.counters->status = 0u;
         a.counters->clip_queue = 0u;
         a.counters->extra_used = 0u;
@@ -438,6 +449,7 @@ __device__ __forceinline__ bool vtx_inside_all(const Vtx& v) {
 }
 
 __global__ void __launch_bounds__(kChunkTris) k_frontend(FrameArgs a) {
+    if (blockIdx.x >= a.dyn->n_chunks) return;
     const DChunk ch = a.chunks[blockIdx.x];
     const DDraw& d = a.draws[ch.draw];
     const uint32_t local = ch.tri_start + threadIdx.x;
@@ -494,6 +506,7 @@ __device__ __forceinline__ float plane_dist(const Vtx& v, int p) {
 
 __global__ void __launch_bounds__(128) k_clip(FrameArgs a) {
     const uint32_t nq = min(a.counters->clip_queue, a.clip_cap);
+    const uint32_t tri_total = a.dyn->tri_total;
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
         const uint2 e = a.clip_queue[q];
         const uint32_t g = e.x;
@@ -538,10 +551,10 @@ __global__ void __launch_bounds__(128) k_clip(FrameArgs a) {
                     a.tri_state[g] = 0;
                     continue;
                 }
-                a.fan_base[g] = a.tri_total + base;
+                a.fan_base[g] = tri_total + base;
             }
             for (int f = 0; f < fans; ++f) {
-                const uint32_t slot = f == 0 ? g : a.tri_total + base + (uint32_t)(f - 1);
+                const uint32_t slot = f == 0 ? g : tri_total + base + (uint32_t)(f - 1);
                 const bool ok = setup_triangle(a, view, poly[0], poly[f + 1], poly[f + 2], slot, (g << 3) | (uint32_t)f,
                                                d.static_base + local, mword, d.view);
                 if (ok) {
@@ -560,7 +573,7 @@ __global__ void __launch_bounds__(128) k_clip(FrameArgs a) {
 // Exclusive scan of tile counts (single CTA). Also seeds the scatter cursors.
 __global__ void __launch_bounds__(1024) k_scan(FrameArgs a) {
     __shared__ uint32_t part[1024];
-    const uint32_t n = a.n_stiles;
+    const uint32_t n = a.dyn->n_stiles;
     const uint32_t per = (n + 1023u) / 1024u;
     const uint32_t b = threadIdx.x * per;
     const uint32_t e = min(b + per, n);
@@ -590,12 +603,13 @@ __global__ void __launch_bounds__(1024) k_scan(FrameArgs a) {
 __global__ void k_scatter(FrameArgs a) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (a.counters->status & (ST_BIN_OVERFLOW | ST_CLIP_OVERFLOW | ST_QUEUE_OVERFLOW)) return;
+    const uint32_t tri_total = a.dyn->tri_total;
     uint32_t slot;
-    if (i < a.tri_total) {
+    if (i < tri_total) {
         if (a.tri_state[i] != 1) return;
         slot = i;
     } else {
-        const uint32_t x = i - a.tri_total;
+        const uint32_t x = i - tri_total;
         if (x >= min(a.counters->extra_used, a.extra_cap)) return;
         slot = i;
         if (a.rec_r[slot].view == 0xFFFFFFFFu) return;
@@ -619,7 +633,7 @@ __global__ void k_scatter(FrameArgs a) {
 // Raster
 // --------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t find_view_by_stile(const FrameArgs& a, uint32_t st) {
-    uint32_t lo = 0, hi = a.n_views - 1;
+    uint32_t lo = 0, hi = a.dyn->n_views - 1;
     while (lo < hi) {
         const uint32_t mid = (lo + hi + 1) >> 1;
         if (a.views[mid].stile_base <= st) lo = mid; else hi = mid - 1;
@@ -668,7 +682,7 @@ __device__ __forceinline__ void fine_region(unsigned long long* sk, const Edge& 
             const int32_t px = (ox >> 4) + 2 * i + kx;
             // Monotone rounding: an edge with x step <= 0 that is negative
             // stays negative for the rest of this lane's row.
-            if ((dec0 && w0 < 0.0f) || (dec1 && w1 < 0.0f) || (dec2 && w2 < 0.0f)) break;
+            if (SWR_ROW_EXIT && ((dec0 && w0 < 0.0f) || (dec1 && w1 < 0.0f) || (dec2 && w2 < 0.0f))) break;
             if ((S == kRefTile || (uint32_t)(px - sx0) < (uint32_t)S) && w0 >= 0.0f && w1 >= 0.0f && w2 >= 0.0f) {
                 const float b1 = w1 * r.ooa, b2 = w2 * r.ooa;
                 const float w = 1.0f / interp(r.oow, b1, b2);
@@ -722,11 +736,12 @@ __device__ __forceinline__ void fine_thread(unsigned long long* sk, const Edge& 
             }
             for (int32_t x = ox; x < xe; x += 32) {
                 const int32_t px0 = x >> 4;
+                bool cov[4];
                 bool any = false;
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    const bool cov = w0[k] >= 0.0f && w1[k] >= 0.0f && w2[k] >= 0.0f;
-                    any |= cov;
+                    cov[k] = w0[k] >= 0.0f && w1[k] >= 0.0f && w2[k] >= 0.0f;
+                    any |= cov[k];
                 }
                 if (any) {
 #pragma unroll
@@ -734,7 +749,7 @@ __device__ __forceinline__ void fine_thread(unsigned long long* sk, const Edge& 
                         const int32_t px = px0 + (k & 1), py = py0 + (k >> 1);
                         const bool in_tile = S == kRefTile || ((uint32_t)(px - sx0) < (uint32_t)S &&
                                                                (uint32_t)(py - sy0) < (uint32_t)S);
-                        if (w0[k] >= 0.0f && w1[k] >= 0.0f && w2[k] >= 0.0f && in_tile) {
+                        if (cov[k] && in_tile) {
                             const float b1 = w1[k] * r.ooa, b2 = w2[k] * r.ooa;
                             const float w = 1.0f / interp(r.oow, b1, b2);
                             const float z = interp(r.zow, b1, b2) * w;
@@ -747,7 +762,7 @@ __device__ __forceinline__ void fine_thread(unsigned long long* sk, const Edge& 
                             }
                         }
                     }
-                } else {
+                } else if (SWR_ROW_EXIT) {
                     const bool out0 = dec0 && w0[0] < 0.0f && w0[1] < 0.0f && w0[2] < 0.0f && w0[3] < 0.0f;
                     const bool out1 = dec1 && w1[0] < 0.0f && w1[1] < 0.0f && w1[2] < 0.0f && w1[3] < 0.0f;
                     const bool out2 = dec2 && w2[0] < 0.0f && w2[1] < 0.0f && w2[2] < 0.0f && w2[3] < 0.0f;
@@ -837,12 +852,25 @@ __device__ __forceinline__ void block_range(int32_t start, int32_t end, int32_t 
 
 constexpr int kUnitCap = 1024;  // queued (packet, block) units per tile pass
 
+// Persistent: each CTA pulls (view, scheduling tile) work items from a
+// device-side counter until every tile of every view is done.
 template <int S>
 __global__ void __launch_bounds__(256) k_raster(FrameArgs a) {
     __shared__ unsigned long long sk[S * S];
     __shared__ uint2 units[kUnitCap];
     __shared__ uint32_t n_units;
+    __shared__ uint32_t cur_tile;
+    const uint32_t n_tiles = a.dyn->n_stiles;
+    for (uint32_t iter = 0;; ++iter) {
+#if SWR_RASTER_PERSISTENT
+    if (threadIdx.x == 0) cur_tile = atomicAdd(&a.counters->work_next, 1u);
+    __syncthreads();
+    const uint32_t st = cur_tile;
+#else
+    if (iter > 0) break;
     const uint32_t st = blockIdx.x;
+#endif
+    if (st >= n_tiles) break;
     const uint32_t vi = find_view_by_stile(a, st);
     const DView& view = a.views[vi];
     const uint32_t local = st - view.stile_base;
@@ -912,13 +940,15 @@ __global__ void __launch_bounds__(256) k_raster(FrameArgs a) {
         const int32_t ly = i / S, lx = i % S;
         dst[(uint64_t)(sy0 + ly) * view.key_pitch + (uint64_t)(sx0 + lx)] = sk[i];
     }
+    __syncthreads();
+    }
 }
 
 // --------------------------------------------------------------------------
 // Shading
 // --------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t find_view_by_quad(const FrameArgs& a, uint32_t q) {
-    uint32_t lo = 0, hi = a.n_views - 1;
+    uint32_t lo = 0, hi = a.dyn->n_views - 1;
     while (lo < hi) {
         const uint32_t mid = (lo + hi + 1) >> 1;
         if (a.views[mid].quad_base <= q) lo = mid; else hi = mid - 1;
@@ -1128,15 +1158,12 @@ __device__ __forceinline__ uint32_t tonemap_pack(f3 c, float exposure) {
     return (r << 24) | (g << 16) | (b << 8) | 0xFFu;
 }
 
-__global__ void __launch_bounds__(256) k_shade(FrameArgs a) {
-    __shared__ uint8_t tab[512];
-    for (int i = threadIdx.x; i < 512; i += blockDim.x) tab[i] = a.rsqrt_table[i];
-    __syncthreads();
-    const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
+// One lane of the shading pass; all 32 lanes of a warp call it together
+// (quad barycentrics and luminance are exchanged with warp shuffles).
+__device__ __forceinline__ void shade_thread(const FrameArgs& a, const uint8_t* tab, uint32_t gt, uint32_t total) {
     const uint32_t gq = gt >> 2;
     const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t qmask = 0xFu << (lane & ~3u);
-    const bool live = gq < a.total_quads;
+    const bool live = gq < total;
     const uint32_t vi = find_view_by_quad(a, live ? gq : 0u);
     const DView& v = a.views[vi];
     const DScene& sc = a.scenes[v.scene];
@@ -1202,7 +1229,6 @@ __global__ void __launch_bounds__(256) k_shade(FrameArgs a) {
     const float l1 = __shfl_sync(0xFFFFFFFFu, lum, (int)((lane & ~3u) + 1u));
     const float l2 = __shfl_sync(0xFFFFFFFFu, lum, (int)((lane & ~3u) + 2u));
     const float l3 = __shfl_sync(0xFFFFFFFFu, lum, (int)((lane & ~3u) + 3u));
-    (void)qmask;
     if (needed && centre && k == 0) {
         const uint32_t tile = (uint32_t)(qy >> 5) * (uint32_t)v.tiles_x + (uint32_t)(qx >> 5);
         v.tile_lum[tile] = (((l0 + l1) + l2) + l3) * 0.25f;
@@ -1224,9 +1250,21 @@ __global__ void __launch_bounds__(256) k_shade(FrameArgs a) {
     }
 }
 
+__global__ void __launch_bounds__(256) k_shade(FrameArgs a) {
+    __shared__ uint8_t tab[512];
+    for (int i = threadIdx.x; i < 512; i += blockDim.x) tab[i] = a.rsqrt_table[i];
+    __syncthreads();
+    // Every view's quad count is a multiple of 32, so each warp's lanes are
+    // either all live or all past the end (warp-uniform loop).
+    const uint32_t total = a.dyn->total_quads;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < total * 4u; base += gridDim.x * blockDim.x)
+        shade_thread(a, tab, base + threadIdx.x, total);
+}
+
 // Exposure applied after the host's update_auto_exposure (dt > 0 path).
 __global__ void k_resolve(FrameArgs a) {
     const uint32_t vi = blockIdx.y;
+    if (vi >= a.dyn->n_views) return;
     const DView& v = a.views[vi];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t w = (uint32_t)v.width, h = (uint32_t)(v.height & ~1);
@@ -1240,20 +1278,39 @@ __global__ void k_resolve(FrameArgs a) {
 // --------------------------------------------------------------------------
 // Host launch wrappers
 // --------------------------------------------------------------------------
-static bool g_const_init = false;
-static void init_constants() {
-    if (g_const_init) return;
+static uint64_t g_const_init_mask = 0;  // one bit per device
+
+cudaError_t init_kernel_constants() {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 64 && (g_const_init_mask >> dev) & 1ull) return cudaSuccess;
     float t[256];
     for (int i = 0; i < 256; ++i) t[i] = (float)i / 255.0f;
-    cudaMemcpyToSymbol(c_unorm8, t, sizeof(t));
-    g_const_init = true;
+    e = cudaMemcpyToSymbol(c_unorm8, t, sizeof(t));
+    if (e == cudaSuccess && dev < 64) g_const_init_mask |= 1ull << dev;
+    return e;
+}
+
+void frame_grids(int num_sms, uint32_t S, uint32_t* raster_grid, uint32_t* shade_grid) {
+    int rb = 1, sb = 1;
+    const int threads = S <= 16 ? 128 : 256;
+    switch (S) {
+        case 8: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rb, k_raster<8>, threads, 0); break;
+        case 16: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rb, k_raster<16>, threads, 0); break;
+        case 32: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rb, k_raster<32>, threads, 0); break;
+        default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rb, k_raster<64>, threads, 0); break;
+    }
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sb, k_shade, 256, 0);
+    cudaGetLastError();
+    *raster_grid = (uint32_t)(num_sms * (rb > 0 ? rb : 1));
+    *shade_grid = (uint32_t)(num_sms * (sb > 0 ? sb : 1));
 }
 
 void launch_reset(const FrameArgs& a, void* stream) {
-    init_constants();
     cudaStream_t s = (cudaStream_t)stream;
-    const uint32_t n = a.n_stiles > 0 ? a.n_stiles : 1u;
-    k_reset<<<(n + 255) / 256, 256, 0, s>>>(a);
+    const uint32_t n = a.stile_cap > 0 ? a.stile_cap : 1u;
+    k_reset<<<min((n + 255) / 256, 512u), 256, 0, s>>>(a);
 }
 
 void launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t* ev) {
@@ -1264,32 +1321,34 @@ void launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t* ev
     mark(0);
     launch_reset(a, stream);
     mark(1);
-    if (a.n_chunks > 0) k_frontend<<<a.n_chunks, kChunkTris, 0, s>>>(a);
+    if (a.chunk_cap > 0) k_frontend<<<a.chunk_cap, kChunkTris, 0, s>>>(a);
     mark(2);
     k_clip<<<num_sms * 4, 128, 0, s>>>(a);
     mark(3);
     k_scan<<<1, 1024, 0, s>>>(a);
     mark(4);
     {
-        const uint64_t n = (uint64_t)a.tri_total + a.extra_cap;
+        const uint64_t n = (uint64_t)a.tri_cap + a.extra_cap;
         if (n > 0) k_scatter<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
     }
     mark(5);
+    const uint32_t rg = SWR_RASTER_PERSISTENT ? (a.raster_grid > 0 ? a.raster_grid : (uint32_t)num_sms)
+                                              : (a.stile_cap > 0 ? a.stile_cap : 1u);
     switch (a.sched_tile) {
-        case 8: k_raster<8><<<a.n_stiles, 128, 0, s>>>(a); break;
-        case 16: k_raster<16><<<a.n_stiles, 128, 0, s>>>(a); break;
-        case 32: k_raster<32><<<a.n_stiles, 256, 0, s>>>(a); break;
-        default: k_raster<64><<<a.n_stiles, 256, 0, s>>>(a); break;
+        case 8: k_raster<8><<<rg, 128, 0, s>>>(a); break;
+        case 16: k_raster<16><<<rg, 128, 0, s>>>(a); break;
+        case 32: k_raster<32><<<rg, 256, 0, s>>>(a); break;
+        default: k_raster<64><<<rg, 256, 0, s>>>(a); break;
     }
     mark(6);
-    if (a.total_quads > 0) k_shade<<<(a.total_quads * 4 + 255) / 256, 256, 0, s>>>(a);
+    k_shade<<<a.shade_grid > 0 ? a.shade_grid : (uint32_t)num_sms, 256, 0, s>>>(a);
     mark(7);
 }
 
 void launch_resolve(const FrameArgs& a, void* stream) {
     cudaStream_t s = (cudaStream_t)stream;
-    const uint32_t maxpx = a.max_view_pixels > 0 ? a.max_view_pixels : 1u;
-    dim3 grid((maxpx + 255) / 256, a.n_views);
+    const uint32_t maxpx = a.pixel_cap > 0 ? a.pixel_cap : 1u;
+    dim3 grid((maxpx + 255) / 256, a.view_cap > 0 ? a.view_cap : 1u);
     k_resolve<<<grid, 256, 0, s>>>(a);
 }
 

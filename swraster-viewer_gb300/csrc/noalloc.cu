@@ -48,7 +48,8 @@ constexpr uint32_t kNaTiles = (kNaMaxDim / kRefTile) * (kNaMaxDim / kRefTile);
 
 constexpr size_t al(size_t x) { return (x + 255) & ~size_t(255); }
 // Scratch layout (byte offsets).
-constexpr size_t oScene = 0;
+constexpr size_t oDyn = 0;
+constexpr size_t oScene = oDyn + al(sizeof(DFrameDyn));
 constexpr size_t oView = oScene + al(sizeof(DScene));
 constexpr size_t oDraws = oView + al(sizeof(DView));
 constexpr size_t oChunks = oDraws + al(sizeof(DDraw) * kNaMaxDraws);
@@ -75,8 +76,9 @@ int g_dev_sms[kMaxDevices] = {};
 std::mutex g_mu;
 
 // Host staging (static, no heap): scene, view, draws, chunks.
-unsigned char g_stage[al(sizeof(DScene)) + al(sizeof(DView)) + al(sizeof(DDraw) * kNaMaxDraws) +
+unsigned char g_stage[al(sizeof(DFrameDyn)) + al(sizeof(DScene)) + al(sizeof(DView)) + al(sizeof(DDraw) * kNaMaxDraws) +
                       al(sizeof(DChunk) * kNaMaxChunks)];
+uint32_t g_raster_grid[64] = {}, g_shade_grid[64] = {};
 uint32_t g_order[kNaMaxNodes], g_tmp[kNaMaxNodes];
 float g_key[kNaMaxNodes];
 
@@ -149,9 +151,14 @@ extern "C" swr_status swr_render_frame_noalloc(const swr_scene* scene, const swr
             cudaGetLastError();
             return na_fail(SWR_CUDA_ERROR, "scratch set-up copy failed");
         }
+        if (init_kernel_constants() != cudaSuccess) {
+            cudaGetLastError();
+            return na_fail(SWR_CUDA_ERROR, "kernel constant set-up failed");
+        }
         int sms = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         g_dev_sms[dev] = sms > 0 ? sms : 148;
+        frame_grids(g_dev_sms[dev], 64, &g_raster_grid[dev], &g_shade_grid[dev]);
         g_dev_ptr[dev] = static_cast<unsigned char*>(p);
     }
     unsigned char* base = g_dev_ptr[dev];
@@ -165,9 +172,8 @@ extern "C" swr_status swr_render_frame_noalloc(const swr_scene* scene, const swr
         g_key[i] = dot3(d, d);
     }
     stable_sort_nodes(nn);
-    DDraw* draws = reinterpret_cast<DDraw*>(g_stage + al(sizeof(DScene)) + al(sizeof(DView)));
-    DChunk* chunks = reinterpret_cast<DChunk*>(g_stage + al(sizeof(DScene)) + al(sizeof(DView)) +
-                                               al(sizeof(DDraw) * kNaMaxDraws));
+    DDraw* draws = reinterpret_cast<DDraw*>(g_stage + oDraws);
+    DChunk* chunks = reinterpret_cast<DChunk*>(g_stage + oDraws + al(sizeof(DDraw) * kNaMaxDraws));
     uint32_t nd = 0, nc = 0, tri = 0;
     const M4 vp = from_array(cam->view_project);
     const M4 view_m = from_array(cam->view);
@@ -217,7 +223,7 @@ extern "C" swr_status swr_render_frame_noalloc(const swr_scene* scene, const swr
             tri += tc;
         }
     }
-    DView* v = reinterpret_cast<DView*>(g_stage + al(sizeof(DScene)));
+    DView* v = reinterpret_cast<DView*>(g_stage + oView);
     std::memset(v, 0, sizeof(DView));
     init_view(*v, *cam, width, height, 64);
     v->scene = 0;
@@ -230,11 +236,18 @@ extern "C" swr_status swr_render_frame_noalloc(const swr_scene* scene, const swr
     v->stile_base = 0;
     v->quad_base = 0;
     v->key_offset = 0;
-    std::memcpy(g_stage, &s.dscene, sizeof(DScene));
+    std::memcpy(g_stage + oScene, &s.dscene, sizeof(DScene));
+    DFrameDyn* dyn = reinterpret_cast<DFrameDyn*>(g_stage + oDyn);
+    std::memset(dyn, 0, sizeof(DFrameDyn));
+    dyn->n_views = 1;
+    dyn->n_chunks = nc;
+    dyn->tri_total = tri;
+    dyn->n_stiles = (uint32_t)(v->stiles_x * v->stiles_y);
+    dyn->total_quads = v->quad_pitch * (uint32_t)v->tiles_y * 32u;
+    dyn->max_view_pixels = (uint32_t)width * (uint32_t)(height & ~1);
     // Tables to the scratch array (pageable source: the copy is staged
     // before cudaMemcpyAsync returns, so the static buffer can be reused).
-    cudaError_t e = cudaMemcpyAsync(base + oScene, g_stage, al(sizeof(DScene)) + al(sizeof(DView)) + sizeof(DDraw) * nd,
-                                    cudaMemcpyHostToDevice, stream);
+    cudaError_t e = cudaMemcpyAsync(base + oDyn, g_stage, oDraws + sizeof(DDraw) * nd, cudaMemcpyHostToDevice, stream);
     if (e == cudaSuccess && nc)
         e = cudaMemcpyAsync(base + oChunks, chunks, sizeof(DChunk) * nc, cudaMemcpyHostToDevice, stream);
     if (e != cudaSuccess) {
@@ -242,16 +255,19 @@ extern "C" swr_status swr_render_frame_noalloc(const swr_scene* scene, const swr
         return na_fail(SWR_CUDA_ERROR, "table upload failed");
     }
     FrameArgs a{};
+    a.dyn = reinterpret_cast<const DFrameDyn*>(base + oDyn);
     a.scenes = reinterpret_cast<const DScene*>(base + oScene);
     a.views = reinterpret_cast<const DView*>(base + oView);
-    a.n_views = 1;
     a.draws = reinterpret_cast<const DDraw*>(base + oDraws);
     a.chunks = reinterpret_cast<const DChunk*>(base + oChunks);
-    a.n_chunks = nc;
-    a.tri_total = tri;
+    a.chunk_cap = nc;
+    a.tri_cap = tri > 0 ? tri : 1u;
     a.extra_cap = kNaExtra;
     a.clip_cap = tri > 0 ? tri : 1u;
-    a.n_stiles = (uint32_t)(v->stiles_x * v->stiles_y);
+    a.stile_cap = dyn->n_stiles;
+    a.quad_cap = dyn->total_quads;
+    a.pixel_cap = dyn->max_view_pixels;
+    a.view_cap = 1;
     a.bin_cap = kNaBinCap;
     a.sched_tile = 64;
     a.tri_state = base + oState;
@@ -266,9 +282,9 @@ extern "C" swr_status swr_render_frame_noalloc(const swr_scene* scene, const swr
     a.keys = reinterpret_cast<unsigned long long*>(base + oKeys);
     a.counters = reinterpret_cast<DCounters*>(base + oCounters);
     a.rsqrt_table = base + oTab;
-    a.total_quads = v->quad_pitch * (uint32_t)v->tiles_y * 32u;
-    a.max_view_pixels = (uint32_t)width * (uint32_t)(height & ~1);
     a.exposure_dev = nullptr;
+    a.raster_grid = g_raster_grid[dev];
+    a.shade_grid = g_shade_grid[dev];
     launch_frame(a, stream, g_dev_sms[dev]);
     e = cudaGetLastError();
     if (e != cudaSuccess) return na_fail(SWR_CUDA_ERROR, "kernel launch failed");

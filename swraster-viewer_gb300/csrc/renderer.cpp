@@ -135,11 +135,28 @@ void ExposureState::update(const float* lum, size_t n, float dt) {
     exposure = std::exp2(ev);
 }
 
+TableLayout table_layout(uint32_t scene_cap, uint32_t view_cap, uint32_t draw_cap, uint32_t chunk_cap) {
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    TableLayout L;
+    L.o_dyn = 0;
+    L.o_scenes = al(sizeof(DFrameDyn));
+    L.o_views = L.o_scenes + al(sizeof(DScene) * scene_cap);
+    L.o_draws = L.o_views + al(sizeof(DView) * view_cap);
+    L.o_chunks = L.o_draws + al(sizeof(DDraw) * draw_cap);
+    L.total = L.o_chunks + al(sizeof(DChunk) * chunk_cap);
+    return L;
+}
+
 swr_status FrameEngine::init(std::string& err) {
     int dev = 0;
     cudaGetDevice(&dev);
     int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && sms > 0) num_sms = sms;
+    if (init_kernel_constants() != cudaSuccess) {
+        err = "kernel constant upload failed";
+        cudaGetLastError();
+        return SWR_CUDA_ERROR;
+    }
     if (rsqrt_tab.ensure(512) != cudaSuccess || counters.ensure(sizeof(DCounters)) != cudaSuccess) {
         err = "cudaMalloc failed";
         return SWR_NO_MEMORY;
@@ -158,18 +175,28 @@ swr_status FrameEngine::init(std::string& err) {
 }
 
 void FrameEngine::release() {
-    for (DBuf* b : {&scene_tab, &views, &draws, &chunks, &tri_state, &rec_r, &rec_s, &fan_base, &clip_queue, &tile_count,
-                    &tile_offset, &tile_cursor, &bins, &keys, &counters, &rsqrt_tab})
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    graph_exec = nullptr;
+    if (capture_stream) cudaStreamDestroy(capture_stream);
+    capture_stream = nullptr;
+    for (DBuf* b : {&tables, &tri_state, &rec_r, &rec_s, &fan_base, &clip_queue, &tile_count, &tile_offset,
+                    &tile_cursor, &bins, &keys, &counters, &rsqrt_tab})
         b->release();
     h_stage.release();
     if (stage_done) cudaEventDestroy(stage_done);
     stage_done = nullptr;
 }
 
-swr_status FrameEngine::run(const std::vector<const SceneImpl*>& scenes, std::vector<DView>& vws,
-                            const std::vector<const swr_camera*>& cams, cudaStream_t stream, FrameArgs* out,
-                            std::string& err) {
-    // Draw lists for every view, canonical order within a view.
+namespace {
+inline uint32_t grow(uint32_t cur, uint64_t need) {
+    if (need <= cur) return cur;
+    const uint64_t g = need + need / 4 + 16;
+    return (uint32_t)std::min<uint64_t>(g, 0xFFFFFFF0ull);
+}
+}  // namespace
+
+swr_status FrameEngine::prepare(const std::vector<const SceneImpl*>& scenes, std::vector<DView>& vws,
+                                const std::vector<const swr_camera*>& cams, std::string& err) {
     std::vector<DDraw> hdraws;
     std::vector<DChunk> hchunks;
     uint32_t tri_cursor = 0;
@@ -183,75 +210,86 @@ swr_status FrameEngine::run(const std::vector<const SceneImpl*>& scenes, std::ve
         v.quad_base = quad_cursor;
         quad_cursor += v.quad_pitch * (uint32_t)v.tiles_y * 32u;
         v.key_offset = key_cursor;
-        max_px = std::max<uint32_t>(max_px, (uint32_t)v.width * (uint32_t)(v.height & ~1));
         key_cursor += v.key_pitch * (uint64_t)v.tiles_y * kRefTile;
+        max_px = std::max<uint32_t>(max_px, (uint32_t)v.width * (uint32_t)(v.height & ~1));
     }
     const uint32_t T = tri_cursor;
-    if (extra_cap == 0) extra_cap = std::max<uint64_t>(4096, T / 4);
-    if (bin_cap == 0) bin_cap = std::max<uint64_t>(65536, (uint64_t)T * 2 + stile_cursor * 4ull);
-    // Capacities.
+    // Capacities (grow-only, with headroom so small changes keep a captured graph valid).
+    scene_cap = grow(scene_cap, scenes.size());
+    view_cap = grow(view_cap, vws.size());
+    draw_cap = grow(draw_cap, std::max<size_t>(1, hdraws.size()));
+    chunk_cap = grow(chunk_cap, std::max<size_t>(1, hchunks.size()));
+    tri_cap = grow(tri_cap, std::max<uint32_t>(1, T));
+    stile_cap = grow(stile_cap, stile_cursor + 1);
+    quad_cap = grow(quad_cap, quad_cursor);
+    pixel_cap = grow(pixel_cap, max_px);
+    if (key_cursor > key_cap) key_cap = key_cursor + key_cursor / 4;
+    if (extra_cap < std::max<uint64_t>(4096, tri_cap / 4)) extra_cap = std::max<uint64_t>(4096, tri_cap / 4);
+    if (bin_cap < std::max<uint64_t>(65536, (uint64_t)tri_cap * 2 + stile_cap * 4ull))
+        bin_cap = std::max<uint64_t>(65536, (uint64_t)tri_cap * 2 + stile_cap * 4ull);
+    lay = table_layout(scene_cap, view_cap, draw_cap, chunk_cap);
     cudaError_t e = cudaSuccess;
     auto chk = [&](cudaError_t x) {
         if (x != cudaSuccess && e == cudaSuccess) e = x;
     };
-    const size_t slots = (size_t)T + extra_cap;
-    chk(scene_tab.ensure(scenes.size() * sizeof(DScene)));
-    chk(views.ensure(vws.size() * sizeof(DView)));
-    chk(draws.ensure(std::max<size_t>(1, hdraws.size()) * sizeof(DDraw)));
-    chk(chunks.ensure(std::max<size_t>(1, hchunks.size()) * sizeof(DChunk)));
-    chk(tri_state.ensure(std::max<size_t>(1, T)));
-    chk(rec_r.ensure(std::max<size_t>(1, slots) * sizeof(RecRaster)));
-    chk(rec_s.ensure(std::max<size_t>(1, slots) * sizeof(RecShade)));
-    chk(fan_base.ensure(std::max<size_t>(1, T) * sizeof(uint32_t)));
-    chk(clip_queue.ensure(std::max<size_t>(1, T) * sizeof(uint2)));
-    chk(tile_count.ensure((stile_cursor + 1) * sizeof(uint32_t)));
-    chk(tile_offset.ensure((stile_cursor + 1) * sizeof(uint32_t)));
-    chk(tile_cursor.ensure((stile_cursor + 1) * sizeof(uint32_t)));
+    const size_t slots = (size_t)tri_cap + extra_cap;
+    chk(tables.ensure(lay.total));
+    chk(tri_state.ensure(tri_cap));
+    chk(rec_r.ensure(slots * sizeof(RecRaster)));
+    chk(rec_s.ensure(slots * sizeof(RecShade)));
+    chk(fan_base.ensure((size_t)tri_cap * sizeof(uint32_t)));
+    chk(clip_queue.ensure((size_t)tri_cap * sizeof(uint2)));
+    chk(tile_count.ensure((size_t)(stile_cap + 1) * sizeof(uint32_t)));
+    chk(tile_offset.ensure((size_t)(stile_cap + 1) * sizeof(uint32_t)));
+    chk(tile_cursor.ensure((size_t)(stile_cap + 1) * sizeof(uint32_t)));
     chk(bins.ensure(bin_cap * sizeof(uint32_t)));
-    chk(keys.ensure(std::max<uint64_t>(1, key_cursor) * sizeof(unsigned long long)));
+    chk(keys.ensure(std::max<uint64_t>(1, key_cap) * sizeof(unsigned long long)));
     if (e != cudaSuccess) {
         err = std::string("device allocation failed: ") + cudaGetErrorString(e);
         cudaGetLastError();
         return e == cudaErrorMemoryAllocation ? SWR_NO_MEMORY : SWR_CUDA_ERROR;
     }
-    // Stage tables through pinned memory (wait for the previous frame's copy).
     if (stage_pending) {
         cudaEventSynchronize(stage_done);
         stage_pending = false;
     }
-    const size_t sb = scenes.size() * sizeof(DScene);
-    const size_t vb = vws.size() * sizeof(DView), db = hdraws.size() * sizeof(DDraw), cb = hchunks.size() * sizeof(DChunk);
-    const size_t so = 0, vo = (sb + 255) & ~size_t(255), dof = (vo + vb + 255) & ~size_t(255),
-                 co = (dof + db + 255) & ~size_t(255);
-    if (h_stage.ensure(co + cb) != cudaSuccess) {
+    if (h_stage.ensure(lay.total) != cudaSuccess) {
         err = "pinned allocation failed";
         return SWR_NO_MEMORY;
     }
+    dyn = DFrameDyn{};
+    dyn.n_views = (uint32_t)vws.size();
+    dyn.n_chunks = (uint32_t)hchunks.size();
+    dyn.tri_total = T;
+    dyn.n_stiles = stile_cursor;
+    dyn.total_quads = quad_cursor;
+    dyn.max_view_pixels = max_px;
     uint8_t* hs = static_cast<uint8_t*>(h_stage.p);
-    for (size_t i = 0; i < scenes.size(); ++i) std::memcpy(hs + so + i * sizeof(DScene), &scenes[i]->dscene, sizeof(DScene));
-    std::memcpy(hs + vo, vws.data(), vb);
-    if (db) std::memcpy(hs + dof, hdraws.data(), db);
-    if (cb) std::memcpy(hs + co, hchunks.data(), cb);
-    chk(cudaMemcpyAsync(scene_tab.p, hs + so, sb, cudaMemcpyHostToDevice, stream));
-    chk(cudaMemcpyAsync(views.p, hs + vo, vb, cudaMemcpyHostToDevice, stream));
-    if (db) chk(cudaMemcpyAsync(draws.p, hs + dof, db, cudaMemcpyHostToDevice, stream));
-    if (cb) chk(cudaMemcpyAsync(chunks.p, hs + co, cb, cudaMemcpyHostToDevice, stream));
-    chk(cudaEventRecord(stage_done, stream));
-    stage_pending = true;
-    if (e != cudaSuccess) {
-        err = std::string("upload failed: ") + cudaGetErrorString(e);
-        return SWR_CUDA_ERROR;
+    std::memcpy(hs + lay.o_dyn, &dyn, sizeof(dyn));
+    for (size_t i = 0; i < scenes.size(); ++i)
+        std::memcpy(hs + lay.o_scenes + i * sizeof(DScene), &scenes[i]->dscene, sizeof(DScene));
+    std::memcpy(hs + lay.o_views, vws.data(), vws.size() * sizeof(DView));
+    if (!hdraws.empty()) std::memcpy(hs + lay.o_draws, hdraws.data(), hdraws.size() * sizeof(DDraw));
+    if (!hchunks.empty()) std::memcpy(hs + lay.o_chunks, hchunks.data(), hchunks.size() * sizeof(DChunk));
+    if (grid_tile != sched_tile) {
+        frame_grids(num_sms, sched_tile, &raster_grid, &shade_grid);
+        grid_tile = sched_tile;
     }
+    uint8_t* tb = static_cast<uint8_t*>(tables.p);
     FrameArgs a{};
-    a.views = views.as<DView>();
-    a.n_views = (uint32_t)vws.size();
-    a.draws = draws.as<DDraw>();
-    a.chunks = chunks.as<DChunk>();
-    a.n_chunks = (uint32_t)hchunks.size();
-    a.tri_total = T;
+    a.dyn = reinterpret_cast<const DFrameDyn*>(tb + lay.o_dyn);
+    a.scenes = reinterpret_cast<const DScene*>(tb + lay.o_scenes);
+    a.views = reinterpret_cast<const DView*>(tb + lay.o_views);
+    a.draws = reinterpret_cast<const DDraw*>(tb + lay.o_draws);
+    a.chunks = reinterpret_cast<const DChunk*>(tb + lay.o_chunks);
+    a.chunk_cap = chunk_cap;
+    a.tri_cap = tri_cap;
     a.extra_cap = (uint32_t)extra_cap;
-    a.clip_cap = std::max<uint32_t>(1, T);
-    a.n_stiles = stile_cursor;
+    a.clip_cap = tri_cap;
+    a.stile_cap = stile_cap;
+    a.quad_cap = quad_cap;
+    a.pixel_cap = pixel_cap;
+    a.view_cap = view_cap;
     a.bin_cap = bin_cap;
     a.sched_tile = sched_tile;
     a.tri_state = tri_state.as<uint8_t>();
@@ -266,12 +304,67 @@ swr_status FrameEngine::run(const std::vector<const SceneImpl*>& scenes, std::ve
     a.keys = keys.as<unsigned long long>();
     a.counters = counters.as<DCounters>();
     a.rsqrt_table = rsqrt_tab.as<uint8_t>();
-    a.total_quads = quad_cursor;
-    a.max_view_pixels = max_px;
     a.exposure_dev = nullptr;
-    a.scenes = scene_tab.as<DScene>();
-    *out = a;
+    a.raster_grid = raster_grid;
+    a.shade_grid = shade_grid;
+    args = a;
     return SWR_OK;
+}
+
+swr_status FrameEngine::launch(cudaStream_t stream, cudaEvent_t* ev, std::string& err) {
+    cudaError_t e = cudaSuccess;
+    if (use_graph && !ev) {
+        const bool same = graph_exec && graph_stage == h_stage.p && graph_bytes == lay.total &&
+                          std::memcmp(&graph_args, &args, sizeof(args)) == 0;
+        if (!same) {
+            if (graph_exec) cudaGraphExecDestroy(graph_exec);
+            graph_exec = nullptr;
+            if (!capture_stream) e = cudaStreamCreateWithFlags(&capture_stream, cudaStreamNonBlocking);
+            cudaGraph_t g = nullptr;
+            // Capture on the engine's own stream; the graph is then launched
+            // into the caller's stream (which may be the legacy default one).
+            if (e == cudaSuccess) e = cudaStreamBeginCapture(capture_stream, cudaStreamCaptureModeThreadLocal);
+            if (e == cudaSuccess) {
+                cudaMemcpyAsync(tables.p, h_stage.p, lay.total, cudaMemcpyHostToDevice, capture_stream);
+                launch_frame(args, capture_stream, num_sms, nullptr);
+                e = cudaStreamEndCapture(capture_stream, &g);
+            }
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&graph_exec, g, 0);
+            if (g) cudaGraphDestroy(g);
+            if (e != cudaSuccess) {
+                err = std::string("graph capture failed: ") + cudaGetErrorString(e);
+                cudaGetLastError();
+                graph_exec = nullptr;
+                return SWR_CUDA_ERROR;
+            }
+            graph_args = args;
+            graph_stream = stream;
+            graph_stage = h_stage.p;
+            graph_bytes = lay.total;
+        }
+        e = cudaGraphLaunch(graph_exec, stream);
+    } else {
+        e = cudaMemcpyAsync(tables.p, h_stage.p, lay.total, cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess) launch_frame(args, stream, num_sms, ev);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(stage_done, stream);
+    stage_pending = true;
+    if (e != cudaSuccess) {
+        err = std::string("frame launch failed: ") + cudaGetErrorString(e);
+        cudaGetLastError();
+        return SWR_CUDA_ERROR;
+    }
+    return SWR_OK;
+}
+
+swr_status FrameEngine::run(const std::vector<const SceneImpl*>& scenes, std::vector<DView>& vws,
+                            const std::vector<const swr_camera*>& cams, cudaStream_t stream, FrameArgs* out,
+                            std::string& err, cudaEvent_t* ev) {
+    swr_status st = prepare(scenes, vws, cams, err);
+    if (st != SWR_OK) return st;
+    st = launch(stream, ev, err);
+    if (out) *out = args;
+    return st;
 }
 
 }  // namespace swr

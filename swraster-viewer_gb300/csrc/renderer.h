@@ -58,26 +58,53 @@ struct HBuf {
     }
 };
 
+// Table region layout (host staging and device copy use the same offsets).
+struct TableLayout {
+    size_t o_dyn = 0, o_scenes = 0, o_views = 0, o_draws = 0, o_chunks = 0, total = 0;
+};
+TableLayout table_layout(uint32_t scene_cap, uint32_t view_cap, uint32_t draw_cap, uint32_t chunk_cap);
+
 // Reusable frame engine: everything a batch of views needs on the device.
+// prepare() builds the per-frame tables on the host and grows capacities;
+// launch() uploads the tables with one copy and runs the frame, either as
+// direct launches or by replaying a CUDA graph captured for the current
+// capacities (every per-frame count is read from the device table header).
 struct FrameEngine {
     int num_sms = 148;
     uint32_t sched_tile = 64;
     uint64_t bin_cap = 0, extra_cap = 0;
-    DBuf scene_tab, views, draws, chunks, tri_state, rec_r, rec_s, fan_base, clip_queue;
+    uint32_t scene_cap = 0, view_cap = 0, draw_cap = 0, chunk_cap = 0, tri_cap = 0, stile_cap = 0, quad_cap = 0;
+    uint32_t pixel_cap = 0;
+    uint64_t key_cap = 0;
+    uint32_t raster_grid = 0, shade_grid = 0, grid_tile = 0;
+    DBuf tables, tri_state, rec_r, rec_s, fan_base, clip_queue;
     DBuf tile_count, tile_offset, tile_cursor, bins, keys, counters, rsqrt_tab;
     HBuf h_stage;
+    TableLayout lay;
     cudaEvent_t stage_done = nullptr;
     bool stage_pending = false;
     uint32_t retries = 0;
     DCounters last{};
+    DFrameDyn dyn{};
+    FrameArgs args{};
+    // Graph replay.
+    bool use_graph = false;
+    cudaGraphExec_t graph_exec = nullptr;
+    FrameArgs graph_args{};
+    cudaStream_t graph_stream = nullptr;
+    cudaStream_t capture_stream = nullptr;  // legacy default streams cannot be captured
+    const void* graph_stage = nullptr;  // the capture bakes in the staging copy's source and size
+    size_t graph_bytes = 0;
 
     swr_status init(std::string& err);
     void release();
-    // Build, upload and launch one frame over `views` (views[i].scene indexes
-    // `scenes`). Returns after enqueueing.
+    swr_status prepare(const std::vector<const SceneImpl*>& scenes, std::vector<DView>& views,
+                       const std::vector<const swr_camera*>& cams, std::string& err);
+    swr_status launch(cudaStream_t stream, cudaEvent_t* ev, std::string& err);
+    // prepare + launch (the plain renderer's path).
     swr_status run(const std::vector<const SceneImpl*>& scenes, std::vector<DView>& views,
                    const std::vector<const swr_camera*>& cams, cudaStream_t stream, FrameArgs* out_args,
-                   std::string& err);
+                   std::string& err, cudaEvent_t* ev = nullptr);
 };
 
 // Per-frame draw list for one view (render_scene's front half,

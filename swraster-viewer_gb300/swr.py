@@ -133,12 +133,46 @@ class FrameStats(C.Structure):
                 ("overflow_retries", C.c_uint32), ("tile_luminance_mean", C.c_float), ("exposure", C.c_float)]
 
 
+class ViewDesc(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("camera", C.POINTER(Camera)), ("width", C.c_int32), ("height", C.c_int32),
+                ("exposure", C.c_float), ("rsqrt_mode", C.c_uint32), ("rgba8", C.c_void_p), ("vis", C.c_void_p)]
+
+
+class BatchOpts(C.Structure):
+    _fields_ = [("sched_tile", C.c_uint32), ("use_graph", C.c_uint32), ("bin_capacity", C.c_uint64)]
+
+
+class ServerOpts(C.Structure):
+    _fields_ = [("memory_budget", C.c_uint64), ("max_batch_views", C.c_uint32), ("max_queue", C.c_uint32),
+                ("inflight", C.c_uint32), ("sched_tile", C.c_uint32), ("rsqrt_mode", C.c_uint32),
+                ("use_graph", C.c_uint32)]
+
+
+class Request(C.Structure):
+    _fields_ = [("scene", C.c_int32), ("width", C.c_int32), ("height", C.c_int32), ("exposure", C.c_float),
+                ("camera", Camera), ("tag", C.c_uint64)]
+
+
+class Completion(C.Structure):
+    _fields_ = [("ticket", C.c_uint64), ("tag", C.c_uint64), ("status", C.c_int32), ("width", C.c_int32),
+                ("height", C.c_int32), ("batch_views", C.c_int32), ("rgba8", C.c_void_p), ("vis", C.c_void_p),
+                ("queue_ms", C.c_double), ("latency_ms", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("rejected", C.c_uint64),
+                ("batches", C.c_uint64), ("device_bytes", C.c_uint64), ("budget", C.c_uint64)]
+
+
 EXPORTS = [
     "swr_scene_create", "swr_scene_destroy", "swr_scene_get_info", "swr_scene_export", "swr_camera_init",
     "swr_camera_update", "swr_renderer_create", "swr_renderer_destroy", "swr_render_frame", "swr_renderer_sync",
     "swr_blit", "swr_read_visbuffer", "swr_renderer_device_outputs", "swr_renderer_get_exposure",
     "swr_renderer_set_exposure", "swr_renderer_get_stats", "swr_renderer_get_tile_luminance", "swr_last_error",
     "swr_abi_version", "swr_renderer_set_profiling", "swr_renderer_get_profile", "swr_render_frame_noalloc",
+    "swr_batch_create", "swr_batch_destroy", "swr_batch_render", "swr_batch_sync", "swr_batch_output",
+    "swr_batch_autotune", "swr_batch_last_ms", "swr_server_create", "swr_server_destroy", "swr_server_add_scene",
+    "swr_server_submit", "swr_server_poll", "swr_server_release", "swr_server_get_stats", "swr_copy_to_host",
 ]
 STAGES = ["reset", "frontend", "clip", "scan", "scatter", "raster", "shade", "resolve"]
 
@@ -176,6 +210,21 @@ def lib():
         "swr_renderer_get_profile": ([vp, f32p, C.c_int32, C.POINTER(C.c_uint32)], C.c_int),
         "swr_render_frame_noalloc": ([vp, C.POINTER(Camera), C.c_int32, C.c_int32, C.c_float, C.c_uint32, vp, vp, vp],
                                      C.c_int),
+        "swr_batch_create": ([C.POINTER(BatchOpts), C.POINTER(vp)], C.c_int),
+        "swr_batch_destroy": ([vp], None),
+        "swr_batch_render": ([vp, C.POINTER(ViewDesc), C.c_int32, vp], C.c_int),
+        "swr_batch_sync": ([vp], C.c_int),
+        "swr_batch_output": ([vp, C.c_int32, C.POINTER(vp), C.POINTER(vp)], C.c_int),
+        "swr_batch_autotune": ([vp, C.POINTER(ViewDesc), C.c_int32, vp, C.POINTER(C.c_uint32), f32p], C.c_int),
+        "swr_batch_last_ms": ([vp, f32p], C.c_int),
+        "swr_server_create": ([C.POINTER(ServerOpts), C.POINTER(vp)], C.c_int),
+        "swr_server_destroy": ([vp], None),
+        "swr_server_add_scene": ([vp, vp, C.POINTER(C.c_int32)], C.c_int),
+        "swr_server_submit": ([vp, C.POINTER(Request), C.POINTER(C.c_uint64)], C.c_int),
+        "swr_server_poll": ([vp, C.POINTER(Completion), C.c_int32, C.POINTER(C.c_int32), C.c_int32], C.c_int),
+        "swr_server_release": ([vp, C.c_uint64], C.c_int),
+        "swr_server_get_stats": ([vp, C.POINTER(ServerStats)], C.c_int),
+        "swr_copy_to_host": ([vp, vp, C.c_size_t, vp], C.c_int),
         "swr_last_error": ([], C.c_char_p),
         "swr_abi_version": ([], C.c_int32),
     }
@@ -377,6 +426,116 @@ class Renderer:
     def close(self):
         if getattr(self, "handle", None):
             lib().swr_renderer_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def copy_device_to_host(dev_ptr, nbytes, out, stream=None):
+    """Copies device memory (batch/server outputs) into a numpy array."""
+    check(lib().swr_copy_to_host(out.ctypes.data_as(C.c_void_p), C.c_void_p(dev_ptr), nbytes, stream))
+    return out
+
+
+class Batch:
+    """Many views per launch sequence (swr_batch_*)."""
+
+    def __init__(self, sched_tile=0, use_graph=False, bin_capacity=0):
+        h = C.c_void_p()
+        o = BatchOpts(sched_tile, 1 if use_graph else 0, bin_capacity)
+        check(lib().swr_batch_create(C.byref(o), C.byref(h)))
+        self.handle = h
+
+    @staticmethod
+    def views(items):
+        """items: [(scene, camera, width, height, exposure, rsqrt_mode)]"""
+        arr = (ViewDesc * len(items))()
+        for i, (scene, cam, w, h, e, m) in enumerate(items):
+            arr[i] = ViewDesc(scene.handle.value, C.pointer(cam), w, h, e, m, None, None)
+        return arr
+
+    def render(self, arr, stream=None):
+        check(lib().swr_batch_render(self.handle, arr, len(arr), stream))
+
+    def sync(self):
+        check(lib().swr_batch_sync(self.handle))
+
+    def output(self, i, w, h):
+        a, b = C.c_void_p(), C.c_void_p()
+        check(lib().swr_batch_output(self.handle, i, C.byref(a), C.byref(b)))
+        rgba = copy_device_to_host(a.value, w * h * 4, np.zeros((h, w), np.uint32))
+        vis = copy_device_to_host(b.value, w * h * 8, np.zeros((h, w), np.uint64))
+        return rgba, vis
+
+    def autotune(self, arr, stream=None):
+        t = C.c_uint32()
+        ms = C.c_float()
+        check(lib().swr_batch_autotune(self.handle, arr, len(arr), stream, C.byref(t), C.byref(ms)))
+        return t.value, ms.value
+
+    def last_ms(self):
+        ms = C.c_float()
+        check(lib().swr_batch_last_ms(self.handle, C.byref(ms)))
+        return ms.value
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().swr_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Request loop with continuous batching (swr_server_*)."""
+
+    def __init__(self, memory_budget=40 << 30, max_batch_views=64, max_queue=4096, inflight=2, sched_tile=64,
+                 rsqrt_mode=RSQRT_AARCH64, use_graph=False):
+        h = C.c_void_p()
+        o = ServerOpts(memory_budget, max_batch_views, max_queue, inflight, sched_tile, rsqrt_mode,
+                       1 if use_graph else 0)
+        check(lib().swr_server_create(C.byref(o), C.byref(h)))
+        self.handle = h
+
+    def add_scene(self, scene):
+        i = C.c_int32()
+        check(lib().swr_server_add_scene(self.handle, scene.handle, C.byref(i)))
+        return i.value
+
+    def submit(self, scene_id, cam, w, h, exposure=2.0, tag=0):
+        r = Request(scene_id, w, h, exposure, cam, tag)
+        t = C.c_uint64()
+        st = lib().swr_server_submit(self.handle, C.byref(r), C.byref(t))
+        if st == SWR_BUSY:
+            return None
+        check(st)
+        return t.value
+
+    def poll(self, max_n=256, wait_ms=10):
+        out = (Completion * max_n)()
+        n = C.c_int32()
+        check(lib().swr_server_poll(self.handle, out, max_n, C.byref(n), wait_ms))
+        return [out[i] for i in range(n.value)]
+
+    def release(self, ticket):
+        check(lib().swr_server_release(self.handle, ticket))
+
+    def stats(self):
+        s = ServerStats()
+        check(lib().swr_server_get_stats(self.handle, C.byref(s)))
+        return s
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().swr_server_destroy(self.handle)
             self.handle = None
 
     def __del__(self):
