@@ -43,6 +43,12 @@ def parse():
     ap.add_argument("--cpu-frames", type=int, default=3, help="frames in the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sched-tile", type=int, default=64, help="raster scheduling tile (8, 16, 32, 64)")
+    ap.add_argument("--mode", default="plain", choices=["plain", "batched", "hetero", "served"],
+                    help="plain: 4K per-frame path (the headline); batched: 64 views of the 81,920-triangle scene "
+                         "in one launch; hetero: 16 heterogeneous scenes in one launch; served: request loop")
+    ap.add_argument("--rates", default="100,500,1000,2000,5000", help="served arrival rates (requests/s)")
+    ap.add_argument("--seconds", type=float, default=2.0, help="served: arrival window per rate")
+    ap.add_argument("--max-tris", type=int, default=0, help="hetero/served: cap on triangles per scene")
     return ap.parse_args()
 
 
@@ -159,10 +165,178 @@ def run_reference(args):
     return 0
 
 
+def _timed(torch, fn, reps):
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(s)
+    for _ in range(reps):
+        fn()
+    e1.record(s)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def run_batched(args, hetero):
+    """One launch sequence for many views vs the same views rendered one per
+    frame by the plain path, on the same GPU."""
+    import numpy as np
+    import torch
+    import scenes
+    import swr
+    sh = torch.cuda.current_stream().cuda_stream
+    rng = np.random.default_rng(3)
+    if hetero:
+        items = []
+        for sd, cp in scenes.hetero_scenes(max_triangles=args.max_tris or None):
+            s = swr.Scene(sd)
+            items.append((s, swr.make_camera(*cp), cp[3], cp[4]))
+        cfg = {"workload": "16 heterogeneous scenes (10k-4M triangles log-uniform, 1-8 textures of 512-2048 px), "
+                           "one view each at 640x480-3840x2160, all in one launch",
+               "views": len(items), "triangles": int(sum(s.info().triangle_count for s, *_ in items))}
+    else:
+        s = swr.Scene(scenes.spheres_scene())
+        res = [(320, 240), (640, 480), (1280, 720), (1920, 1080)]
+        items = []
+        for i in range(64):
+            w, h = res[int(rng.integers(4))]
+            items.append((s, swr.make_camera(*scenes.sphere_camera(rng, s.info(), w, h)), w, h))
+        cfg = {"workload": "64 views of the 81,920-triangle sphere scene on a sphere of radius 15-40, resolutions "
+                           "from {320x240, 640x480, 1280x720, 1920x1080}, one launch", "views": 64,
+               "triangles": 81920 * 64}
+    px = sum(w * h for _, _, w, h in items)
+    b = swr.Batch(use_graph=True)
+    arr = swr.Batch.views([(sc, cam, w, h, 2.0, swr.RSQRT_AARCH64) for sc, cam, w, h in items])
+    tile, _ = b.autotune(arr, sh)
+    for _ in range(max(3, args.warmup)):
+        b.render(arr, sh)
+    b.sync()
+    def one():
+        b.render(arr, sh)
+    ms_batch = _timed(torch, one, args.steps)
+    b.sync()
+    # Plain path: one renderer per resolution, views one after another.
+    rends = {}
+    for sc, cam, w, h in items:
+        if (w, h) not in rends:
+            rends[(w, h)] = swr.Renderer(w, h)
+    def seq():
+        for sc, cam, w, h in items:
+            rends[(w, h)].render(sc, cam, 0.0, sh)
+    for _ in range(2):
+        seq()
+    ms_seq = _timed(torch, seq, max(3, args.steps // 4))
+    for r in rends.values():
+        r.close()
+    n = len(items)
+    line = {"metric": "batched views/s", "value": n / (ms_batch / 1000.0), "unit": "views/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms_batch,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": dict(cfg, sched_tile=tile, graph=True),
+            "plain_sequential": {"value": n / (ms_seq / 1000.0), "unit": "views/s", "ms_per_batch": ms_seq},
+            "speedup_vs_plain": ms_seq / ms_batch, "gpix_per_s": px / (ms_batch / 1000.0) / 1e9,
+            "gpu_launches": KERNELS_PER_FRAME * args.steps}
+    print(json.dumps(line), flush=True)
+    b.close()
+    return 0
+
+
+def run_served(args):
+    """Poisson request stream over 8 resident scenes: served form (continuous
+    batching) vs the plain per-frame path (one request at a time, FIFO)."""
+    import threading
+    import numpy as np
+    import torch
+    import scenes
+    import swr
+    sh = torch.cuda.current_stream().cuda_stream
+    scs = [swr.Scene(sd) for sd, _ in scenes.hetero_scenes(seed=31, count=8, max_triangles=args.max_tris or None)]
+    res = [(640, 480), (1280, 720), (1920, 1080), (3840, 2160)]
+    srv = swr.Server(memory_budget=40 << 30, max_batch_views=64, inflight=2, use_graph=False)
+    ids = [srv.add_scene(s) for s in scs]
+    rends = {r: swr.Renderer(r[0], r[1]) for r in res}
+    results = {}
+    for rate in [float(x) for x in args.rates.split(",")]:
+        rng = np.random.default_rng(int(rate))
+        n = max(20, min(int(rate * args.seconds), 4000))
+        gaps = rng.exponential(1.0 / rate, n)
+        reqs = []
+        for i in range(n):
+            k = int(rng.integers(len(scs)))
+            w, h = res[int(rng.integers(len(res)))]
+            cam = swr.make_camera(*scenes.sphere_camera(rng, scs[k].info(), w, h, 0.7 * scs[k].info().bounds_diagonal,
+                                                        1.5 * scs[k].info().bounds_diagonal))
+            reqs.append((k, cam, w, h))
+        # Served.
+        lat = []
+        done = [0]
+        def submit():
+            t0 = time.perf_counter()
+            t = t0
+            for i, (k, cam, w, h) in enumerate(reqs):
+                t += gaps[i]
+                d = t - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                while srv.submit(ids[k], cam, w, h, 2.0, tag=i) is None:
+                    time.sleep(0.0005)
+        th = threading.Thread(target=submit)
+        t_start = time.perf_counter()
+        th.start()
+        while done[0] < n:
+            for c in srv.poll(256, wait_ms=5):
+                lat.append(c.latency_ms)
+                srv.release(c.ticket)
+                done[0] += 1
+        t_end = time.perf_counter()
+        th.join()
+        served = {"completed": n, "frames_per_s": n / (t_end - t_start), "p50_ms": float(np.percentile(lat, 50)),
+                  "p99_ms": float(np.percentile(lat, 99))}
+        # Plain path: the same arrivals, served one at a time in order.
+        plat = []
+        t0 = time.perf_counter()
+        arr_t = t0 + np.cumsum(gaps)
+        for i, (k, cam, w, h) in enumerate(reqs):
+            d = arr_t[i] - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            r = rends[(w, h)]
+            r.render(scs[k], cam, 0.0, sh)
+            r.sync()
+            plat.append((time.perf_counter() - arr_t[i]) * 1000.0)
+        t1 = time.perf_counter()
+        plain = {"frames_per_s": n / (t1 - t0), "p50_ms": float(np.percentile(plat, 50)),
+                 "p99_ms": float(np.percentile(plat, 99))}
+        results[str(int(rate))] = {"served": served, "plain": plain}
+    st = srv.stats()
+    line = {"metric": "served frames/s + p99 latency vs plain GPU", "unit": "frames/s", "n_gpus": 1,
+            "config": {"workload": "8 resident scenes (10k-4M triangles), Poisson arrivals, random scene, camera on "
+                                   "a sphere, resolution from {640x480, 1280x720, 1920x1080, 3840x2160}, 40 GB "
+                                   "budget, continuous batching over 2 in-flight batches",
+                       "triangles": int(sum(s.info().triangle_count for s in scs))},
+            "rates": results, "batches": st.batches, "device_bytes": st.device_bytes, "data": "synthetic"}
+    best_served = max((v["served"]["frames_per_s"] for v in results.values()), default=0.0)
+    best_plain = max((v["plain"]["frames_per_s"] for v in results.values()), default=0.0)
+    line["value"] = best_served
+    line["plain_max_frames_per_s"] = best_plain
+    line["speedup_vs_plain"] = best_served / best_plain if best_plain else None
+    print(json.dumps(line), flush=True)
+    srv.close()
+    for r in rends.values():
+        r.close()
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.mode in ("batched", "hetero", "served"):
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        if args.mode == "served":
+            return run_served(args)
+        return run_batched(args, args.mode == "hetero")
     world, rank, local = dist_init()
     import torch
     torch.cuda.set_device(local)

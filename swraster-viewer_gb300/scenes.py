@@ -259,3 +259,38 @@ def stress_scene(seed=2, triangles=2_000_000, width=3840, height=2160, fov=math.
           "specular_samples": specular_samples, "brdf_lut_size": brdf_lut_size}
     cam = ((0.0, 0.0, 0.0), (0.0, 0.0, -1.0), fov, width, height, far)
     return sd, cam
+
+
+def hetero_scenes(seed=21, count=16, tri_range=(10_000, 4_000_000), res_range=((640, 480), (3840, 2160)),
+                  max_triangles=None):
+    """Batched heterogeneous scenes: `count` seeded scenes with triangle counts
+    log-uniform in `tri_range`, 1-8 textures of 512-2048 px each, one view per
+    scene at a resolution between 640x480 and 3840x2160. Returns a list of
+    (scene dict, camera params)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    widths = [640, 960, 1280, 1600, 1920, 2560, 3200, 3840]
+    for i in range(count):
+        t = int(math.exp(rng.uniform(math.log(tri_range[0]), math.log(tri_range[1]))))
+        if max_triangles:
+            t = min(t, max_triangles)
+        w = int(rng.choice(widths))
+        h = int(round(w * 9 / 16 / 2)) * 2 if w > 640 else 480
+        ntex = int(rng.integers(1, 9))
+        tsz = int(rng.choice([512, 1024, 2048]))
+        sd, cam = stress_scene(seed=seed * 100 + i, triangles=t, width=w, height=h, n_textures=ntex, tex_size=tsz,
+                               voxel=128)
+        out.append((sd, cam))
+    return out
+
+
+def sphere_camera(rng, info, width, height, rmin=15.0, rmax=40.0, fov=math.pi / 3.0):
+    """A camera on a sphere of radius in [rmin, rmax] around the scene centre,
+    looking at the centre (far plane beyond the scene)."""
+    c = np.array(info.bounds_center[:], np.float64)
+    u = rng.normal(size=3)
+    u /= np.linalg.norm(u)
+    r = rng.uniform(rmin, rmax)
+    pos = c + u * r
+    far = float(r + info.bounds_diagonal)
+    return (tuple(map(float, pos)), tuple(map(float, c)), fov, width, height, far)
