@@ -38,7 +38,8 @@ class Opts(C.Structure):
 
 class Result(C.Structure):
     _fields_ = [("ev", C.c_float), ("exposure", C.c_float), ("target", C.c_float), ("tiles", C.c_uint32),
-                ("packets", C.c_uint64), ("triangles_in", C.c_uint64)]
+                ("packets", C.c_uint64), ("triangles_in", C.c_uint64), ("quads_tested", C.c_uint64),
+                ("fragments", C.c_uint64), ("depth_passed", C.c_uint64)]
 
 
 _lib = None

@@ -502,6 +502,7 @@ struct Queue {
 
 struct Tile {
     IV2 smin, smax;
+    uint64_t quads_tested = 0, fragments = 0, depth_passed = 0;
     Queue opaque;
     std::vector<V3x4> color;
     std::vector<F4> depth;
@@ -689,9 +690,11 @@ static void fine_raster(const Frame& f, Tile& t, const Packet& pk, const Edges& 
         for (int32_t px = xs; px < xe; px += 32) {
             B4 mask;
             bool any = false;
+            t.quads_tested++;
             for (int i = 0; i < 4; ++i) {
                 mask[i] = w0.l[i] >= 0.0f && w1.l[i] >= 0.0f && w2.l[i] >= 0.0f;
                 any |= mask[i];
+                t.fragments += mask[i] ? 1 : 0;
             }
             if (any) {
                 const F4 b1 = w1 * ooa, b2 = w2 * ooa;
@@ -706,6 +709,7 @@ static void fine_raster(const Frame& f, Tile& t, const Packet& pk, const Edges& 
                 for (int i = 0; i < 4; ++i) {
                     fm[i] = mask[i] && (z.l[i] <= cur.l[i]);
                     anyp |= fm[i];
+                    t.depth_passed += fm[i] ? 1 : 0;
                 }
                 if (anyp) {
                     // VBufferOpaqueShader::shade (src/shader.rs:32-63).
@@ -981,6 +985,9 @@ typedef struct oracle_result {
     uint32_t tiles;
     uint64_t packets;     /* (triangle, tile) pairs queued */
     uint64_t triangles_in;
+    uint64_t quads_tested;   /* quad coverage tests in fine_raster */
+    uint64_t fragments;      /* lanes inside a triangle */
+    uint64_t depth_passed;   /* lanes passing the depth test in queue order */
 } oracle_result;
 
 // Renderer::render_scene + update_auto_exposure + blit_to_buffer for a fresh
@@ -1163,6 +1170,12 @@ int oracle_render(const swr_scene_host_view* s, const swr_camera* cam, int32_t w
         res->tiles = (uint32_t)f.tiles.size();
         res->packets = packets;
         res->triangles_in = tri_in;
+        res->quads_tested = res->fragments = res->depth_passed = 0;
+        for (Tile* t : f.tiles) {
+            res->quads_tested += t->quads_tested;
+            res->fragments += t->fragments;
+            res->depth_passed += t->depth_passed;
+        }
     }
     for (Tile* t : f.tiles) delete t;
     return 0;
