@@ -38,6 +38,17 @@
 #ifndef SWR_ROW_EXIT
 #define SWR_ROW_EXIT 0
 #endif
+// Early depth rejection with a conservative per-packet depth bound. Off: packets of one tile
+// run concurrently, so few meet a filled depth key, and the bound costs more than it saves
+// (4K frame, 2M triangles: raster 2.54 ms with it, 2.05 ms without).
+#ifndef SWR_EARLY_Z
+#define SWR_EARLY_Z 0
+#endif
+// Rasterize large (coarse) packets before small ones (measured neutral at 4K, slower on
+// small frames).
+#ifndef SWR_COARSE_FIRST
+#define SWR_COARSE_FIRST 0
+#endif
 
 namespace swr {
 
@@ -641,6 +652,66 @@ __device__ __forceinline__ uint32_t find_view_by_stile(const FrameArgs& a, uint3
     return lo;
 }
 
+// Conservative early depth rejection.
+//
+// Returns orderable(zlo) where zlo is a lower bound of the f32 depth that the
+// reference arithmetic (bary from the incrementally stepped edge values, then
+// z = interp(z/w) * (1 / interp(1/w))) can produce at ANY covered pixel of
+// the packet, or 0 (no rejection) when no bound can be given. A covered lane
+// whose current key holds a depth strictly below zlo would fail `z <= cur`
+// whatever its exact z, so its z math is skipped; equal depths are never
+// skipped, so the tie rule is untouched.
+//
+// Derivation: every edge value is evaluated from integers with at most ~20
+// roundings of magnitude <= M, so |w_float - E_exact| <= D = M * 2^-19.
+// Covered means all three w_float >= 0, hence E_exact >= -D; the exact edge
+// values sum to A = |signed area|, so b1, b2 >= 0 and b1 + b2 <= s =
+// (1 + 3D/A)(1 + 2^-20). The interpolants are affine in (b1, b2), so their
+// extremes over that triangle are at its corners; their f32 evaluation adds
+// at most 4 roundings. Intervals are evaluated with directed rounding.
+__device__ __forceinline__ float rd_add(float a, float b) { return __fadd_rd(a, b); }
+__device__ __forceinline__ float ru_add(float a, float b) { return __fadd_ru(a, b); }
+__device__ __forceinline__ float rd_mul(float a, float b) { return __fmul_rd(a, b); }
+__device__ __forceinline__ float ru_mul(float a, float b) { return __fmul_ru(a, b); }
+
+__device__ __forceinline__ uint32_t packet_zlo_ord(const RecRaster& r, int32_t x1, int32_t y1) {
+    const float px[3] = {fabsf(i2f(r.p[0])), fabsf(i2f(r.p[2])), fabsf(i2f(r.p[4]))};
+    const float py[3] = {fabsf(i2f(r.p[1])), fabsf(i2f(r.p[3])), fabsf(i2f(r.p[5]))};
+    // A >= 1 / ooa (1 - 2^-22): ooa = 1 / |area| with two roundings.
+    if (!(r.ooa > 0.0f) || !isfinite(r.ooa)) return 0u;
+    const float A = rd_mul(__fdiv_rd(1.0f, r.ooa), 0.99999976f);
+    const float X = (float)((x1 + 2) * 16), Y = (float)((y1 + 2) * 16);
+    float M = 0.0f;
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        const int i = e, j = (e + 1) % 3;
+        const float fa = ru_add(py[i], py[j]), fb = ru_add(px[i], px[j]);      // |a|, |b| bounds
+        const float fc = ru_add(ru_add(ru_mul(px[j], py[i]), ru_mul(px[i], py[j])), 1.0f);  // |c| bound
+        if (!(fc < 2.1474836e9f) || !(fa < 1.6e7f) || !(fb < 1.6e7f)) return 0u;  // i32 setup may wrap
+        float m = ru_add(ru_add(ru_mul(fa, X), ru_mul(fb, Y)), fc);
+        m = ru_add(m, ru_mul(512.0f, ru_add(fa, fb)));
+        M = fmaxf(M, m);
+    }
+    // The wrapped i32 signed area would make A meaningless.
+    if (!(ru_mul(ru_add(px[0], ru_add(px[1], px[2])), ru_add(py[0], ru_add(py[1], py[2]))) < 1.0e9f)) return 0u;
+    const float D = ru_mul(M, 1.9073486e-06f);  // 2^-19
+    const float s = ru_mul(ru_add(1.0f, __fdiv_ru(ru_mul(3.0f, D), A)), 1.00000095f);  // (1 + 3D/A)(1 + 2^-20)
+    const float z0 = r.zow[0], dz1 = r.zow[1], dz2 = r.zow[2];
+    const float o0 = r.oow[0], do1 = r.oow[1], do2 = r.oow[2];
+    const float ez = ru_mul(ru_add(fabsf(z0), ru_mul(s, ru_add(fabsf(dz1), fabsf(dz2)))), 2.3841858e-07f);  // 2^-22
+    const float eo = ru_mul(ru_add(fabsf(o0), ru_mul(s, ru_add(fabsf(do1), fabsf(do2)))), 2.3841858e-07f);
+    const float zi_lo = rd_add(rd_add(z0, rd_mul(s, fminf(0.0f, fminf(dz1, dz2)))), -ez);
+    const float zi_hi = ru_add(ru_add(z0, ru_mul(s, fmaxf(0.0f, fmaxf(dz1, dz2)))), ez);
+    const float oi_lo = rd_add(rd_add(o0, rd_mul(s, fminf(0.0f, fminf(do1, do2)))), -eo);
+    const float oi_hi = ru_add(ru_add(o0, ru_mul(s, fmaxf(0.0f, fmaxf(do1, do2)))), eo);
+    if (!(oi_lo > 0.0f) || !isfinite(oi_hi) || !isfinite(zi_lo) || !isfinite(zi_hi)) return 0u;
+    const float w_lo = __fdiv_rd(1.0f, oi_hi), w_hi = __fdiv_ru(1.0f, oi_lo);
+    float zl = fminf(fminf(rd_mul(zi_lo, w_lo), rd_mul(zi_lo, w_hi)), fminf(rd_mul(zi_hi, w_lo), rd_mul(zi_hi, w_hi)));
+    zl = rd_add(zl, -ru_mul(fabsf(zl), 9.5367432e-07f));  // slack 2^-20
+    if (!isfinite(zl)) return 0u;
+    return float_to_ordered(zl);
+}
+
 // Alpha test of one lane (get_alpha_test_mask, src/shader.rs:311-329): the
 // mip comes from the packet's du_dv without the per-lane w scale.
 __device__ __forceinline__ bool alpha_pass(const DScene& sc, const DMaterial& m, const RecShade& q, float b1, float b2,
@@ -659,7 +730,7 @@ template <int S>
 __device__ __forceinline__ void fine_region(unsigned long long* sk, const Edge& e12, const Edge& e20, const Edge& e01,
                                             const RecRaster& r, int32_t ox, int32_t oy, int32_t xe, int32_t ye,
                                             int32_t sx0, int32_t sy0, const DScene* sc, const DMaterial* mat,
-                                            const RecShade* qs, uint32_t amip) {
+                                            const RecShade* qs, uint32_t amip, uint32_t zlo) {
     const uint32_t lane = threadIdx.x & 31u;
     const int32_t k = (int32_t)(lane & 3u);
     const int32_t kx = k & 1, ky = k >> 1;
@@ -683,7 +754,8 @@ __device__ __forceinline__ void fine_region(unsigned long long* sk, const Edge& 
             // Monotone rounding: an edge with x step <= 0 that is negative
             // stays negative for the rest of this lane's row.
             if (SWR_ROW_EXIT && ((dec0 && w0 < 0.0f) || (dec1 && w1 < 0.0f) || (dec2 && w2 < 0.0f))) break;
-            if ((S == kRefTile || (uint32_t)(px - sx0) < (uint32_t)S) && w0 >= 0.0f && w1 >= 0.0f && w2 >= 0.0f) {
+            if ((S == kRefTile || (uint32_t)(px - sx0) < (uint32_t)S) && w0 >= 0.0f && w1 >= 0.0f && w2 >= 0.0f &&
+                (zlo == 0u || zlo <= (uint32_t)(sk[(py - sy0) * S + (px - sx0)] >> 32))) {
                 const float b1 = w1 * r.ooa, b2 = w2 * r.ooa;
                 const float w = 1.0f / interp(r.oow, b1, b2);
                 const float z = interp(r.zow, b1, b2) * w;
@@ -709,7 +781,7 @@ template <int S>
 __device__ __forceinline__ void fine_thread(unsigned long long* sk, const Edge& e12, const Edge& e20, const Edge& e01,
                                             const RecRaster& r, int32_t ox, int32_t oy, int32_t xe, int32_t ye,
                                             int32_t sx0, int32_t sy0, const DScene* sc, const DMaterial* mat,
-                                            const RecShade* qs, uint32_t amip) {
+                                            const RecShade* qs, uint32_t amip, uint32_t zlo) {
     float r0[4], r1[4], r2[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
@@ -749,7 +821,8 @@ __device__ __forceinline__ void fine_thread(unsigned long long* sk, const Edge& 
                         const int32_t px = px0 + (k & 1), py = py0 + (k >> 1);
                         const bool in_tile = S == kRefTile || ((uint32_t)(px - sx0) < (uint32_t)S &&
                                                                (uint32_t)(py - sy0) < (uint32_t)S);
-                        if (cov[k] && in_tile) {
+                        if (cov[k] && in_tile &&
+                            (zlo == 0u || zlo <= (uint32_t)(sk[(py - sy0) * S + (px - sx0)] >> 32))) {
                             const float b1 = w1[k] * r.ooa, b2 = w2[k] * r.ooa;
                             const float w = 1.0f / interp(r.oow, b1, b2);
                             const float z = interp(r.zow, b1, b2) * w;
@@ -808,7 +881,21 @@ struct PacketCtx {
     const DMaterial* mat;
     const RecShade* qs;
     uint32_t amip;
+    int32_t x1, y1;  // clipped rect max (pixels)
 };
+
+__device__ __forceinline__ uint32_t ctx_zlo(const PacketCtx& c) {
+    return SWR_EARLY_Z ? packet_zlo_ord(c.r, c.x1, c.y1) : 0u;
+}
+
+// Coarse/fine decision from the bbox words only (2 of the record's 5 loads).
+__device__ __forceinline__ bool packet_is_coarse(const RecRaster* rec, int32_t tx0, int32_t ty0) {
+    const int4 q1 = __ldg(reinterpret_cast<const int4*>(rec) + 1);  // p[4], p[5], bb[0], bb[1]
+    const int4 q2 = __ldg(reinterpret_cast<const int4*>(rec) + 2);  // bb[2], bb[3], ooa, zow[0]
+    const int32_t x0 = max(q1.z, tx0), y0 = max(q1.w, ty0);
+    const int32_t x1 = min(q2.x, tx0 + kRefTile), y1 = min(q2.y, ty0 + kRefTile);
+    return (x1 - x0 > 16) || (y1 - y0 > 16);
+}
 
 __device__ __forceinline__ void load_packet(const FrameArgs& a, const DScene& sc, uint32_t slot, int32_t tx0,
                                             int32_t ty0, PacketCtx& c) {
@@ -822,6 +909,8 @@ __device__ __forceinline__ void load_packet(const FrameArgs& a, const DScene& sc
     int32_t x0, y0, x1, y1;
     clipped_rect(c.r, tx0, ty0, x0, y0, x1, y1);
     c.coarse = (x1 - x0 > 16) || (y1 - y0 > 16);
+    c.x1 = x1;
+    c.y1 = y1;
     c.xs = (x0 & ~1) * kSubpixelScale;
     c.ys = (y0 & ~1) * kSubpixelScale;
     c.xe = x1 * kSubpixelScale;
@@ -884,15 +973,18 @@ __global__ void __launch_bounds__(256) k_raster(FrameArgs a) {
     if (!bad) {
         const uint32_t b0 = a.tile_offset[st], b1 = a.tile_offset[st + 1];
         const DScene& sc = a.scenes[view.scene];
-        // Pass 1: one thread per packet. Small packets are rasterized here;
-        // large ones are split into 16-px block units for pass 2.
+        // Pass 1: one thread per packet. Large packets are split into 16-px
+        // block units for pass 2; small ones are rasterized here unless they
+        // wait for pass 3 (after the large ones, which occlude the most).
         for (uint32_t p = b0 + threadIdx.x; p < b1; p += blockDim.x) {
             const uint32_t slot = a.bins[p];
+            if (SWR_COARSE_FIRST && !packet_is_coarse(a.rec_r + slot, tx0, ty0)) continue;
             PacketCtx c;
             load_packet(a, sc, slot, tx0, ty0, c);
             if (!c.coarse) {
-                fine_thread<S>(sk, c.e12, c.e20, c.e01, c.r, c.xs, c.ys, c.xe, c.ye, sx0, sy0, &sc, c.mat, c.qs,
-                               c.amip);
+                if (!SWR_COARSE_FIRST)
+                    fine_thread<S>(sk, c.e12, c.e20, c.e01, c.r, c.xs, c.ys, c.xe, c.ye, sx0, sy0, &sc, c.mat, c.qs,
+                                   c.amip, ctx_zlo(c));
                 continue;
             }
             int32_t bxl, bxh, byl, byh;
@@ -914,7 +1006,7 @@ __global__ void __launch_bounds__(256) k_raster(FrameArgs a) {
                         const int32_t ox = c.xs + 256 * bx, oy = c.ys + 256 * by;
                         if (block_rejected(c.e12, c.e20, c.e01, ox, oy)) continue;
                         fine_thread<S>(sk, c.e12, c.e20, c.e01, c.r, ox, oy, min(ox + 256, c.xe), min(oy + 256, c.ye),
-                                       sx0, sy0, &sc, c.mat, c.qs, c.amip);
+                                       sx0, sy0, &sc, c.mat, c.qs, c.amip, ctx_zlo(c));
                     }
             }
         }
@@ -931,7 +1023,19 @@ __global__ void __launch_bounds__(256) k_raster(FrameArgs a) {
             const int32_t ox = c.xs + 256 * bx, oy = c.ys + 256 * by;
             if (block_rejected(c.e12, c.e20, c.e01, ox, oy)) continue;
             fine_region<S>(sk, c.e12, c.e20, c.e01, c.r, ox, oy, min(ox + 256, c.xe), min(oy + 256, c.ye), sx0, sy0,
-                           &sc, c.mat, c.qs, c.amip);
+                           &sc, c.mat, c.qs, c.amip, ctx_zlo(c));
+        }
+        // Pass 3: the small packets.
+        if (SWR_COARSE_FIRST) {
+            __syncthreads();
+            for (uint32_t p = b0 + threadIdx.x; p < b1; p += blockDim.x) {
+                const uint32_t slot = a.bins[p];
+                if (packet_is_coarse(a.rec_r + slot, tx0, ty0)) continue;
+                PacketCtx c;
+                load_packet(a, sc, slot, tx0, ty0, c);
+                fine_thread<S>(sk, c.e12, c.e20, c.e01, c.r, c.xs, c.ys, c.xe, c.ye, sx0, sy0, &sc, c.mat, c.qs,
+                               c.amip, ctx_zlo(c));
+            }
         }
     }
     __syncthreads();

@@ -10,6 +10,7 @@
 // different engines overlap on the device. A host callback on each batch's
 // stream wakes the worker, which checks the batch's status word (re-running
 // it on bin overflow) and publishes completions.
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
@@ -77,13 +78,7 @@ struct swr_server {
 
     uint64_t engine_bytes() {
         uint64_t t = 0;
-        for (auto& e : engines) {
-            const FrameEngine& f = e->b->eng;
-            for (const DBuf* d : {&f.tables, &f.tri_state, &f.rec_r, &f.rec_s, &f.fan_base, &f.clip_queue,
-                                  &f.tile_count, &f.tile_offset, &f.tile_cursor, &f.bins, &f.keys})
-                t += d->bytes;
-            t += e->b->tile_lum.bytes;
-        }
+        for (auto& e : engines) t += one_engine_bytes(*e);
         return t;
     }
 
@@ -108,6 +103,28 @@ struct swr_server {
         fb_bytes += f->rgba8.bytes + f->vis.bytes;
         all_fbs.push_back(std::move(f));
         return all_fbs.back().get();
+    }
+
+    // Device bytes an engine needs for a batch, upper estimate: keys of the
+    // padded tile grids, triangle records (raster + shade + clip headroom) and
+    // bins for every triangle of every view's scene.
+    static uint64_t batch_need(const std::vector<std::pair<int32_t, int32_t>>& dims,
+                               const std::vector<uint64_t>& tris) {
+        uint64_t t = 0;
+        for (size_t i = 0; i < dims.size(); ++i) {
+            const uint64_t tx = (uint64_t)(dims[i].first + 63) / 64, ty = (uint64_t)(dims[i].second + 63) / 64;
+            t += tx * ty * 64 * 64 * 8;
+            t += tris[i] * (80 + 176 + 4 + 8 + 1) * 5 / 4 + tris[i] * 2 * 4;
+        }
+        return t + (1u << 20);
+    }
+    static uint64_t one_engine_bytes(const Engine& e) {
+        const FrameEngine& f = e.b->eng;
+        uint64_t t = e.b->tile_lum.bytes;
+        for (const DBuf* d : {&f.tables, &f.tri_state, &f.rec_r, &f.rec_s, &f.fan_base, &f.clip_queue,
+                              &f.tile_count, &f.tile_offset, &f.tile_cursor, &f.bins, &f.keys})
+            t += d->bytes;
+        return t;
     }
 
     void put_fb(FB* f) { free_fbs[((uint64_t)(uint32_t)f->w << 32) | (uint32_t)f->h].push_back(f); }
@@ -169,10 +186,29 @@ struct swr_server {
                 if (e.busy) continue;
                 std::vector<Req> reqs;
                 std::vector<FB*> fbs;
+                std::vector<std::pair<int32_t, int32_t>> dims;
+                std::vector<uint64_t> tris;
+                const uint64_t others = engine_bytes() - one_engine_bytes(e);
                 while (!pending.empty() && reqs.size() < opts.max_batch_views) {
                     const Req& q = pending.front();
+                    // Admission: this engine's buffers for the grown batch must
+                    // fit the budget next to the scenes, framebuffers and the
+                    // other engines (a lone request is always tried).
+                    dims.push_back({q.r.width, q.r.height});
+                    tris.push_back(scenes[q.r.scene]->impl.tri_total);
+                    const uint64_t need = std::max(one_engine_bytes(e), batch_need(dims, tris));
+                    if (!reqs.empty() && scene_bytes + fb_bytes + others + need +
+                                                 (uint64_t)q.r.width * q.r.height * 12 > opts.memory_budget) {
+                        dims.pop_back();
+                        tris.pop_back();
+                        break;
+                    }
                     FB* f = get_fb(q.r.width, q.r.height);
-                    if (!f) break;  // wait for framebuffers to be released
+                    if (!f) {  // wait for framebuffers to be released
+                        dims.pop_back();
+                        tris.pop_back();
+                        break;
+                    }
                     reqs.push_back(q);
                     fbs.push_back(f);
                     pending.pop_front();
