@@ -29,25 +29,10 @@
 #include "devmath.cuh"
 #include "internal.h"
 
-// Raster variants: persistent CTAs pulling tiles from a device counter
-// (needed for graph replay with a fixed grid) or one CTA per tile; early row
-// exit on monotone edges.
+// Raster variant: persistent CTAs pulling tiles from a device counter (needed
+// for graph replay with a fixed grid) or one CTA per tile.
 #ifndef SWR_RASTER_PERSISTENT
 #define SWR_RASTER_PERSISTENT 1
-#endif
-#ifndef SWR_ROW_EXIT
-#define SWR_ROW_EXIT 0
-#endif
-// Early depth rejection with a conservative per-packet depth bound. Off: packets of one tile
-// run concurrently, so few meet a filled depth key, and the bound costs more than it saves
-// (4K frame, 2M triangles: raster 2.54 ms with it, 2.05 ms without).
-#ifndef SWR_EARLY_Z
-#define SWR_EARLY_Z 0
-#endif
-// Rasterize large (coarse) packets before small ones (measured neutral at 4K, slower on
-// small frames).
-#ifndef SWR_COARSE_FIRST
-#define SWR_COARSE_FIRST 0
 #endif
 
 namespace swr {
@@ -652,66 +637,6 @@ __device__ __forceinline__ uint32_t find_view_by_stile(const FrameArgs& a, uint3
     return lo;
 }
 
-// Conservative early depth rejection.
-//
-// Returns orderable(zlo) where zlo is a lower bound of the f32 depth that the
-// reference arithmetic (bary from the incrementally stepped edge values, then
-// z = interp(z/w) * (1 / interp(1/w))) can produce at ANY covered pixel of
-// the packet, or 0 (no rejection) when no bound can be given. A covered lane
-// whose current key holds a depth strictly below zlo would fail `z <= cur`
-// whatever its exact z, so its z math is skipped; equal depths are never
-// skipped, so the tie rule is untouched.
-//
-// Derivation: every edge value is evaluated from integers with at most ~20
-// roundings of magnitude <= M, so |w_float - E_exact| <= D = M * 2^-19.
-// Covered means all three w_float >= 0, hence E_exact >= -D; the exact edge
-// values sum to A = |signed area|, so b1, b2 >= 0 and b1 + b2 <= s =
-// (1 + 3D/A)(1 + 2^-20). The interpolants are affine in (b1, b2), so their
-// extremes over that triangle are at its corners; their f32 evaluation adds
-// at most 4 roundings. Intervals are evaluated with directed rounding.
-__device__ __forceinline__ float rd_add(float a, float b) { return __fadd_rd(a, b); }
-__device__ __forceinline__ float ru_add(float a, float b) { return __fadd_ru(a, b); }
-__device__ __forceinline__ float rd_mul(float a, float b) { return __fmul_rd(a, b); }
-__device__ __forceinline__ float ru_mul(float a, float b) { return __fmul_ru(a, b); }
-
-__device__ __forceinline__ uint32_t packet_zlo_ord(const RecRaster& r, int32_t x1, int32_t y1) {
-    const float px[3] = {fabsf(i2f(r.p[0])), fabsf(i2f(r.p[2])), fabsf(i2f(r.p[4]))};
-    const float py[3] = {fabsf(i2f(r.p[1])), fabsf(i2f(r.p[3])), fabsf(i2f(r.p[5]))};
-    // A >= 1 / ooa (1 - 2^-22): ooa = 1 / |area| with two roundings.
-    if (!(r.ooa > 0.0f) || !isfinite(r.ooa)) return 0u;
-    const float A = rd_mul(__fdiv_rd(1.0f, r.ooa), 0.99999976f);
-    const float X = (float)((x1 + 2) * 16), Y = (float)((y1 + 2) * 16);
-    float M = 0.0f;
-#pragma unroll
-    for (int e = 0; e < 3; ++e) {
-        const int i = e, j = (e + 1) % 3;
-        const float fa = ru_add(py[i], py[j]), fb = ru_add(px[i], px[j]);      // |a|, |b| bounds
-        const float fc = ru_add(ru_add(ru_mul(px[j], py[i]), ru_mul(px[i], py[j])), 1.0f);  // |c| bound
-        if (!(fc < 2.1474836e9f) || !(fa < 1.6e7f) || !(fb < 1.6e7f)) return 0u;  // i32 setup may wrap
-        float m = ru_add(ru_add(ru_mul(fa, X), ru_mul(fb, Y)), fc);
-        m = ru_add(m, ru_mul(512.0f, ru_add(fa, fb)));
-        M = fmaxf(M, m);
-    }
-    // The wrapped i32 signed area would make A meaningless.
-    if (!(ru_mul(ru_add(px[0], ru_add(px[1], px[2])), ru_add(py[0], ru_add(py[1], py[2]))) < 1.0e9f)) return 0u;
-    const float D = ru_mul(M, 1.9073486e-06f);  // 2^-19
-    const float s = ru_mul(ru_add(1.0f, __fdiv_ru(ru_mul(3.0f, D), A)), 1.00000095f);  // (1 + 3D/A)(1 + 2^-20)
-    const float z0 = r.zow[0], dz1 = r.zow[1], dz2 = r.zow[2];
-    const float o0 = r.oow[0], do1 = r.oow[1], do2 = r.oow[2];
-    const float ez = ru_mul(ru_add(fabsf(z0), ru_mul(s, ru_add(fabsf(dz1), fabsf(dz2)))), 2.3841858e-07f);  // 2^-22
-    const float eo = ru_mul(ru_add(fabsf(o0), ru_mul(s, ru_add(fabsf(do1), fabsf(do2)))), 2.3841858e-07f);
-    const float zi_lo = rd_add(rd_add(z0, rd_mul(s, fminf(0.0f, fminf(dz1, dz2)))), -ez);
-    const float zi_hi = ru_add(ru_add(z0, ru_mul(s, fmaxf(0.0f, fmaxf(dz1, dz2)))), ez);
-    const float oi_lo = rd_add(rd_add(o0, rd_mul(s, fminf(0.0f, fminf(do1, do2)))), -eo);
-    const float oi_hi = ru_add(ru_add(o0, ru_mul(s, fmaxf(0.0f, fmaxf(do1, do2)))), eo);
-    if (!(oi_lo > 0.0f) || !isfinite(oi_hi) || !isfinite(zi_lo) || !isfinite(zi_hi)) return 0u;
-    const float w_lo = __fdiv_rd(1.0f, oi_hi), w_hi = __fdiv_ru(1.0f, oi_lo);
-    float zl = fminf(fminf(rd_mul(zi_lo, w_lo), rd_mul(zi_lo, w_hi)), fminf(rd_mul(zi_hi, w_lo), rd_mul(zi_hi, w_hi)));
-    zl = rd_add(zl, -ru_mul(fabsf(zl), 9.5367432e-07f));  // slack 2^-20
-    if (!isfinite(zl)) return 0u;
-    return float_to_ordered(zl);
-}
-
 // Alpha test of one lane (get_alpha_test_mask, src/shader.rs:311-329): the
 // mip comes from the packet's du_dv without the per-lane w scale.
 __device__ __forceinline__ bool alpha_pass(const DScene& sc, const DMaterial& m, const RecShade& q, float b1, float b2,
@@ -721,141 +646,6 @@ __device__ __forceinline__ bool alpha_pass(const DScene& sc, const DMaterial& m,
     const float v = interp(q.vow, b1, b2) * w;
     const uint32_t tx = sample_texel(t, u, v, mip, m.wrap_s[TS_BASE], m.wrap_t[TS_BASE]);
     return c_unorm8[tx & 0xFFu] >= m.alpha_cutoff;
-}
-
-// One warp rasterizes one fine region (a whole small packet, or one 16-px
-// block of a coarse packet). Lane = (quad row j, lane-in-quad k); each lane
-// walks its row along x with the reference's sequential f32 additions.
-template <int S>
-__device__ __forceinline__ void fine_region(unsigned long long* sk, const Edge& e12, const Edge& e20, const Edge& e01,
-                                            const RecRaster& r, int32_t ox, int32_t oy, int32_t xe, int32_t ye,
-                                            int32_t sx0, int32_t sy0, const DScene* sc, const DMaterial* mat,
-                                            const RecShade* qs, uint32_t amip, uint32_t zlo) {
-    const uint32_t lane = threadIdx.x & 31u;
-    const int32_t k = (int32_t)(lane & 3u);
-    const int32_t kx = k & 1, ky = k >> 1;
-    const float lx = i2f(ox + (kx ? 24 : 8));
-    const float ly = i2f(oy + (ky ? 24 : 8));
-    const int32_t nrow = (ye - oy + 31) >> 5;
-    const int32_t ncol = (xe - ox + 31) >> 5;
-    for (int32_t j = (int32_t)(lane >> 2); j < nrow; j += 8) {
-        const int32_t py = (oy >> 4) + 2 * j + ky;
-        float w0 = edge_eval(e12, lx, ly), w1 = edge_eval(e20, lx, ly), w2 = edge_eval(e01, lx, ly);
-        for (int32_t s = 0; s < j; ++s) {
-            w0 += e12.sy;
-            w1 += e20.sy;
-            w2 += e01.sy;
-        }
-        const bool row_in = S == kRefTile || (uint32_t)(py - sy0) < (uint32_t)S;
-        if (!row_in) continue;
-        const bool dec0 = !(e12.sx > 0.0f), dec1 = !(e20.sx > 0.0f), dec2 = !(e01.sx > 0.0f);
-        for (int32_t i = 0; i < ncol; ++i) {
-            const int32_t px = (ox >> 4) + 2 * i + kx;
-            // Monotone rounding: an edge with x step <= 0 that is negative
-            // stays negative for the rest of this lane's row.
-            if (SWR_ROW_EXIT && ((dec0 && w0 < 0.0f) || (dec1 && w1 < 0.0f) || (dec2 && w2 < 0.0f))) break;
-            if ((S == kRefTile || (uint32_t)(px - sx0) < (uint32_t)S) && w0 >= 0.0f && w1 >= 0.0f && w2 >= 0.0f &&
-                (zlo == 0u || zlo <= (uint32_t)(sk[(py - sy0) * S + (px - sx0)] >> 32))) {
-                const float b1 = w1 * r.ooa, b2 = w2 * r.ooa;
-                const float w = 1.0f / interp(r.oow, b1, b2);
-                const float z = interp(r.zow, b1, b2) * w;
-                bool pass = (z == z);
-                if (pass && mat) pass = alpha_pass(*sc, *mat, *qs, b1, b2, w, amip);
-                if (pass) {
-                    const unsigned long long key = make_key(z, r.seq8);
-                    unsigned long long* slot = sk + (py - sy0) * S + (px - sx0);
-                    if (key < *slot) atomicMin(slot, key);
-                }
-            }
-            w0 += e12.sx;
-            w1 += e20.sx;
-            w2 += e01.sx;
-        }
-    }
-}
-
-// One thread rasterizes a whole fine region (a small packet, or one 16-px
-// block), stepping its four quad lanes with the reference's sequential f32
-// additions: row starts accumulate step_y, quads accumulate step_x.
-template <int S>
-__device__ __forceinline__ void fine_thread(unsigned long long* sk, const Edge& e12, const Edge& e20, const Edge& e01,
-                                            const RecRaster& r, int32_t ox, int32_t oy, int32_t xe, int32_t ye,
-                                            int32_t sx0, int32_t sy0, const DScene* sc, const DMaterial* mat,
-                                            const RecShade* qs, uint32_t amip, uint32_t zlo) {
-    float r0[4], r1[4], r2[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const float lx = i2f(ox + ((k & 1) ? 24 : 8));
-        const float ly = i2f(oy + ((k >> 1) ? 24 : 8));
-        r0[k] = edge_eval(e12, lx, ly);
-        r1[k] = edge_eval(e20, lx, ly);
-        r2[k] = edge_eval(e01, lx, ly);
-    }
-    // Rounding is monotone, so along a row an edge whose x step is <= 0 never
-    // grows: once it is negative in all four lanes the rest of the row is
-    // outside the triangle and the walk stops (the values it would have
-    // computed are never used).
-    const bool dec0 = !(e12.sx > 0.0f), dec1 = !(e20.sx > 0.0f), dec2 = !(e01.sx > 0.0f);
-    for (int32_t y = oy; y < ye; y += 32) {
-        const int32_t py0 = y >> 4;
-        if (S == kRefTile || (py0 + 1 >= sy0 && py0 < sy0 + S)) {
-            float w0[4], w1[4], w2[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                w0[k] = r0[k];
-                w1[k] = r1[k];
-                w2[k] = r2[k];
-            }
-            for (int32_t x = ox; x < xe; x += 32) {
-                const int32_t px0 = x >> 4;
-                bool cov[4];
-                bool any = false;
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    cov[k] = w0[k] >= 0.0f && w1[k] >= 0.0f && w2[k] >= 0.0f;
-                    any |= cov[k];
-                }
-                if (any) {
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        const int32_t px = px0 + (k & 1), py = py0 + (k >> 1);
-                        const bool in_tile = S == kRefTile || ((uint32_t)(px - sx0) < (uint32_t)S &&
-                                                               (uint32_t)(py - sy0) < (uint32_t)S);
-                        if (cov[k] && in_tile &&
-                            (zlo == 0u || zlo <= (uint32_t)(sk[(py - sy0) * S + (px - sx0)] >> 32))) {
-                            const float b1 = w1[k] * r.ooa, b2 = w2[k] * r.ooa;
-                            const float w = 1.0f / interp(r.oow, b1, b2);
-                            const float z = interp(r.zow, b1, b2) * w;
-                            bool pass = (z == z);
-                            if (pass && mat) pass = alpha_pass(*sc, *mat, *qs, b1, b2, w, amip);
-                            if (pass) {
-                                const unsigned long long key = make_key(z, r.seq8);
-                                unsigned long long* slot = sk + (py - sy0) * S + (px - sx0);
-                                if (key < *slot) atomicMin(slot, key);
-                            }
-                        }
-                    }
-                } else if (SWR_ROW_EXIT) {
-                    const bool out0 = dec0 && w0[0] < 0.0f && w0[1] < 0.0f && w0[2] < 0.0f && w0[3] < 0.0f;
-                    const bool out1 = dec1 && w1[0] < 0.0f && w1[1] < 0.0f && w1[2] < 0.0f && w1[3] < 0.0f;
-                    const bool out2 = dec2 && w2[0] < 0.0f && w2[1] < 0.0f && w2[2] < 0.0f && w2[3] < 0.0f;
-                    if (out0 || out1 || out2) break;
-                }
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    w0[k] += e12.sx;
-                    w1[k] += e20.sx;
-                    w2[k] += e01.sx;
-                }
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            r0[k] += e12.sy;
-            r1[k] += e20.sy;
-            r2[k] += e01.sy;
-        }
-    }
 }
 
 // coarse_raster's block reject (src/tilerasterizer.rs:238-269): the block is
@@ -878,24 +668,8 @@ struct PacketCtx {
     Edge e01, e12, e20;
     int32_t xs, ys, xe, ye;
     bool coarse;
-    const DMaterial* mat;
-    const RecShade* qs;
     uint32_t amip;
-    int32_t x1, y1;  // clipped rect max (pixels)
 };
-
-__device__ __forceinline__ uint32_t ctx_zlo(const PacketCtx& c) {
-    return SWR_EARLY_Z ? packet_zlo_ord(c.r, c.x1, c.y1) : 0u;
-}
-
-// Coarse/fine decision from the bbox words only (2 of the record's 5 loads).
-__device__ __forceinline__ bool packet_is_coarse(const RecRaster* rec, int32_t tx0, int32_t ty0) {
-    const int4 q1 = __ldg(reinterpret_cast<const int4*>(rec) + 1);  // p[4], p[5], bb[0], bb[1]
-    const int4 q2 = __ldg(reinterpret_cast<const int4*>(rec) + 2);  // bb[2], bb[3], ooa, zow[0]
-    const int32_t x0 = max(q1.z, tx0), y0 = max(q1.w, ty0);
-    const int32_t x1 = min(q2.x, tx0 + kRefTile), y1 = min(q2.y, ty0 + kRefTile);
-    return (x1 - x0 > 16) || (y1 - y0 > 16);
-}
 
 __device__ __forceinline__ void load_packet(const FrameArgs& a, const DScene& sc, uint32_t slot, int32_t tx0,
                                             int32_t ty0, PacketCtx& c) {
@@ -909,21 +683,15 @@ __device__ __forceinline__ void load_packet(const FrameArgs& a, const DScene& sc
     int32_t x0, y0, x1, y1;
     clipped_rect(c.r, tx0, ty0, x0, y0, x1, y1);
     c.coarse = (x1 - x0 > 16) || (y1 - y0 > 16);
-    c.x1 = x1;
-    c.y1 = y1;
     c.xs = (x0 & ~1) * kSubpixelScale;
     c.ys = (y0 & ~1) * kSubpixelScale;
     c.xe = x1 * kSubpixelScale;
     c.ye = y1 * kSubpixelScale;
-    c.mat = nullptr;
-    c.qs = nullptr;
     c.amip = 0;
     if (c.r.material & kRecAlphaBit) {
         const DMaterial& m = sc.materials[c.r.material & ~kRecAlphaBit];
-        c.mat = &m;
-        c.qs = a.rec_s + slot;
-        c.amip = mip_level(sc.textures[m.tex[TS_BASE]], c.qs->du_dv[0], c.qs->du_dv[1], c.qs->du_dv[2],
-                           c.qs->du_dv[3]);
+        const RecShade& q = a.rec_s[slot];
+        c.amip = mip_level(sc.textures[m.tex[TS_BASE]], q.du_dv[0], q.du_dv[1], q.du_dv[2], q.du_dv[3]);
     }
 }
 
@@ -939,112 +707,352 @@ __device__ __forceinline__ void block_range(int32_t start, int32_t end, int32_t 
     while (hi > lo && start + 256 * (hi - 1) >= t1) --hi;
 }
 
-constexpr int kUnitCap = 1024;  // queued (packet, block) units per tile pass
+// ---- Regions -------------------------------------------------------------
+//
+// A region is what one fine_raster call walks (src/tilerasterizer.rs:293-384):
+// a whole packet when its rect clipped to the 64-px reference tile is at most
+// 16 px both ways, else one unrejected 16-px block of it. Its quads are
+// (i, j) = (column, row) from the region origin; the reference reaches quad
+// (i, j)'s edge values by adding step_y j times to the origin's values, then
+// step_x i times. Origin values and steps are integers held in f32 (products
+// and sums of integer-valued floats), so when |origin| + j_max |step_y| +
+// i_max |step_x| <= 2^24 every partial sum is an exactly representable
+// integer, and the value equals origin + j step_y + i step_x evaluated in any
+// grouping. Such regions are "exact": any quad is evaluated directly, one
+// quad per lane over all exact regions of a round. The others replay the
+// sequential additions, one warp per region.
+
+__device__ __forceinline__ float ru_add(float a, float b) { return __fadd_ru(a, b); }
+__device__ __forceinline__ float ru_mul(float a, float b) { return __fmul_ru(a, b); }
+
+// Quad range of a region clipped to the scheduling tile; returns the quad
+// count (0: nothing of the region is in the tile). Region origins and tile
+// origins are even pixels, so a quad is either wholly in the tile or out.
+__device__ __forceinline__ uint32_t clip_quads(int32_t ox, int32_t oy, int32_t ex, int32_t ey, int32_t sx0,
+                                               int32_t sy0, int32_t S, uint32_t& ij) {
+    const int32_t ncol = (ex - ox + 31) >> 5, nrow = (ey - oy + 31) >> 5;
+    const int32_t px = ox >> kSubpixelShift, py = oy >> kSubpixelShift;
+    const int32_t ilo = max(0, (sx0 - px) / 2), ihi = min(ncol, (sx0 + S - px) / 2);
+    const int32_t jlo = max(0, (sy0 - py) / 2), jhi = min(nrow, (sy0 + S - py) / 2);
+    if (ihi <= ilo || jhi <= jlo) return 0u;
+    ij = (uint32_t)ilo | ((uint32_t)jlo << 8) | ((uint32_t)ihi << 16) | ((uint32_t)jhi << 24);
+    return (uint32_t)((ihi - ilo) * (jhi - jlo));
+}
+
+// Edge values of the four quad lanes at a region origin, [edge * 4 + lane],
+// edges in the order e12, e20, e01 (w0, w1, w2).
+__device__ __forceinline__ void origin_values(const PacketCtx& c, int32_t ox, int32_t oy, float w[12]) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float lx = i2f(ox + ((k & 1) ? 24 : 8));
+        const float ly = i2f(oy + ((k >> 1) ? 24 : 8));
+        w[k] = edge_eval(c.e12, lx, ly);
+        w[4 + k] = edge_eval(c.e20, lx, ly);
+        w[8 + k] = edge_eval(c.e01, lx, ly);
+    }
+}
+
+__device__ __forceinline__ bool region_exact(const PacketCtx& c, const float w[12], uint32_t ij) {
+    const float im = (float)((int32_t)((ij >> 16) & 0xFFu) - 1), jm = (float)((int32_t)(ij >> 24) - 1);
+    const float sx[3] = {c.e12.sx, c.e20.sx, c.e01.sx}, sy[3] = {c.e12.sy, c.e20.sy, c.e01.sy};
+    bool ok = true;
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        const float m = fmaxf(fmaxf(fabsf(w[4 * e]), fabsf(w[4 * e + 1])), fmaxf(fabsf(w[4 * e + 2]), fabsf(w[4 * e + 3])));
+        const float b = ru_add(ru_add(m, ru_mul(jm, fabsf(sy[e]))), ru_mul(im, fabsf(sx[e])));
+        ok = ok && (b <= 16777216.0f);
+    }
+    return ok;
+}
+
+template <int S>
+struct RasterShared {
+    static constexpr int kThreads = S <= 16 ? 128 : 256;
+    static constexpr int kRegions = 2 * kThreads;  // regions staged per round
+    unsigned long long sk[S * S];                  // depth keys of the scheduling tile
+    // Regions: exact ones from the front, sequential ones from the back.
+    float r_w[12][kRegions];   // origin edge values
+    uint32_t r_pkt[kRegions];  // packet index in the round
+    uint32_t r_ij[kRegions];   // ilo | jlo << 8 | ihi << 16 | jhi << 24
+    uint32_t r_org[kRegions];  // origin pixel relative to the tile: x | y << 16 (int16 each)
+    float r_inv_ni[kRegions];  // 1 / (ihi - ilo)
+    uint32_t r_qbeg[kRegions + 40];  // first flattened quad of each exact region, then end markers
+    // Packets of the round, one per thread.
+    float p_sx[3][kThreads], p_sy[3][kThreads];
+    float p_ooa[kThreads], p_oow[3][kThreads], p_zow[3][kThreads];
+    uint32_t p_seq8[kThreads], p_mat[kThreads], p_amip[kThreads], p_slot[kThreads];
+    uint32_t scan[kThreads / 32][3];
+    uint32_t n_exact, n_quads, n_slow, cur_tile;
+};
+
+// Depth test of one covered lane: bary, w, z as fine_raster computes them,
+// then the canonical-order key (atomicMin keeps the lowest z, ties broken by
+// submission order).
+template <int S>
+__device__ __forceinline__ void raster_lane(RasterShared<S>& s, const FrameArgs& a, const DScene& sc, uint32_t pk,
+                                            float w1, float w2, int32_t lx, int32_t ly) {
+    const float ooa = s.p_ooa[pk];
+    const float b1 = w1 * ooa, b2 = w2 * ooa;
+    const float oow[3] = {s.p_oow[0][pk], s.p_oow[1][pk], s.p_oow[2][pk]};
+    const float zow[3] = {s.p_zow[0][pk], s.p_zow[1][pk], s.p_zow[2][pk]};
+    const float w = 1.0f / interp(oow, b1, b2);
+    const float z = interp(zow, b1, b2) * w;
+    bool pass = (z == z);
+    const uint32_t m = s.p_mat[pk];
+    if (pass && (m & kRecAlphaBit))
+        pass = alpha_pass(sc, sc.materials[m & ~kRecAlphaBit], a.rec_s[s.p_slot[pk]], b1, b2, w, s.p_amip[pk]);
+    if (pass) {
+        const unsigned long long key = make_key(z, s.p_seq8[pk]);
+        unsigned long long* slot = s.sk + ly * S + lx;
+        if (key < *slot) atomicMin(slot, key);
+    }
+}
+
+// Exact region quad: lane = one quad, evaluated in closed form.
+template <int S>
+__device__ __forceinline__ void raster_exact_quad(RasterShared<S>& s, const FrameArgs& a, const DScene& sc,
+                                                  uint32_t r, uint32_t q) {
+    const uint32_t pk = s.r_pkt[r], ij = s.r_ij[r], org = s.r_org[r];
+    const int32_t ilo = (int32_t)(ij & 0xFFu), jlo = (int32_t)((ij >> 8) & 0xFFu);
+    const int32_t ni = (int32_t)((ij >> 16) & 0xFFu) - ilo;
+    const int32_t jj = (int32_t)(((float)q + 0.5f) * s.r_inv_ni[r]);  // q / ni, exact for q < 2^16
+    const int32_t i = ilo + ((int32_t)q - jj * ni), j = jlo + jj;
+    const float fi = (float)i, fj = (float)j;
+    float w[12];
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        const float d = s.p_sy[e][pk] * fj + s.p_sx[e][pk] * fi;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) w[4 * e + k] = s.r_w[4 * e + k][r] + d;
+    }
+    const int32_t lx0 = (int32_t)(int16_t)(org & 0xFFFFu) + 2 * i;
+    const int32_t ly0 = (int32_t)(int16_t)(org >> 16) + 2 * j;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (w[k] >= 0.0f && w[4 + k] >= 0.0f && w[8 + k] >= 0.0f)
+            raster_lane<S>(s, a, sc, pk, w[4 + k], w[8 + k], lx0 + (k & 1), ly0 + (k >> 1));
+    }
+}
+
+// Sequential region: one warp, lane = (quad row, quad lane); each lane walks
+// its row along x with the reference's additions.
+template <int S>
+__device__ __forceinline__ void raster_slow_region(RasterShared<S>& s, const FrameArgs& a, const DScene& sc,
+                                                   uint32_t r) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const int32_t k = (int32_t)(lane & 3u);
+    const uint32_t pk = s.r_pkt[r], ij = s.r_ij[r], org = s.r_org[r];
+    const int32_t ilo = (int32_t)(ij & 0xFFu), jlo = (int32_t)((ij >> 8) & 0xFFu);
+    const int32_t ihi = (int32_t)((ij >> 16) & 0xFFu), jhi = (int32_t)(ij >> 24);
+    const int32_t lx0 = (int32_t)(int16_t)(org & 0xFFFFu) + (k & 1);
+    const int32_t ly0 = (int32_t)(int16_t)(org >> 16) + (k >> 1);
+    const float sx0 = s.p_sx[0][pk], sx1 = s.p_sx[1][pk], sx2 = s.p_sx[2][pk];
+    const float sy0 = s.p_sy[0][pk], sy1 = s.p_sy[1][pk], sy2 = s.p_sy[2][pk];
+    for (int32_t j = jlo + (int32_t)(lane >> 2); j < jhi; j += 8) {
+        float w0 = s.r_w[k][r], w1 = s.r_w[4 + k][r], w2 = s.r_w[8 + k][r];
+        for (int32_t t = 0; t < j; ++t) {
+            w0 += sy0;
+            w1 += sy1;
+            w2 += sy2;
+        }
+        for (int32_t i = 0; i < ihi; ++i) {
+            if (i >= ilo && w0 >= 0.0f && w1 >= 0.0f && w2 >= 0.0f)
+                raster_lane<S>(s, a, sc, pk, w1, w2, lx0 + 2 * i, ly0 + 2 * j);
+            w0 += sx0;
+            w1 += sx1;
+            w2 += sx2;
+        }
+    }
+}
+
+// Pass 1 of a round for one packet: classify, split into regions and count
+// (or, with write set, stage them at the given positions).
+template <int S>
+__device__ __forceinline__ void packet_regions(RasterShared<S>& s, const PacketCtx& c, int32_t sx0, int32_t sy0,
+                                               bool write, uint32_t pk, uint32_t& n_ex, uint32_t& n_q,
+                                               uint32_t& n_sl) {
+    constexpr int R = RasterShared<S>::kRegions;
+    auto region = [&](int32_t ox, int32_t oy, int32_t ex, int32_t ey) {
+        uint32_t ij = 0;
+        const uint32_t nq = clip_quads(ox, oy, ex, ey, sx0, sy0, S, ij);
+        if (nq == 0) return;
+        float w[12];
+        origin_values(c, ox, oy, w);
+        const bool exact = region_exact(c, w, ij);
+        uint32_t r;
+        if (exact) {
+            r = n_ex;
+            if (write) s.r_qbeg[r] = n_q;
+            ++n_ex;
+            n_q += nq;
+        } else {
+            r = (uint32_t)R - 1u - n_sl;
+            ++n_sl;
+        }
+        if (!write) return;
+#pragma unroll
+        for (int t = 0; t < 12; ++t) s.r_w[t][r] = w[t];
+        s.r_pkt[r] = pk;
+        s.r_ij[r] = ij;
+        const int32_t ox_rel = (ox >> kSubpixelShift) - sx0, oy_rel = (oy >> kSubpixelShift) - sy0;
+        s.r_org[r] = ((uint32_t)ox_rel & 0xFFFFu) | ((uint32_t)oy_rel << 16);
+        s.r_inv_ni[r] = 1.0f / (float)((int32_t)((ij >> 16) & 0xFFu) - (int32_t)(ij & 0xFFu));
+    };
+    if (!c.coarse) {
+        region(c.xs, c.ys, c.xe, c.ye);
+        return;
+    }
+    int32_t bxl, bxh, byl, byh;
+    block_range(c.xs, c.xe, sx0, S, bxl, bxh);
+    block_range(c.ys, c.ye, sy0, S, byl, byh);
+    for (int32_t by = byl; by < byh; ++by)
+        for (int32_t bx = bxl; bx < bxh; ++bx) {
+            const int32_t ox = c.xs + 256 * bx, oy = c.ys + 256 * by;
+            if (block_rejected(c.e12, c.e20, c.e01, ox, oy)) continue;
+            region(ox, oy, min(ox + 256, c.xe), min(oy + 256, c.ye));
+        }
+}
 
 // Persistent: each CTA pulls (view, scheduling tile) work items from a
-// device-side counter until every tile of every view is done.
+// device-side counter until every tile of every view is done. Per tile, the
+// bin's packets go through rounds of one packet per thread: pass 1 stages
+// regions (a block-wide scan places them), pass 2 rasterizes the exact
+// regions' quads flattened over all lanes, pass 3 the sequential regions.
 template <int S>
-__global__ void __launch_bounds__(256) k_raster(FrameArgs a) {
-    __shared__ unsigned long long sk[S * S];
-    __shared__ uint2 units[kUnitCap];
-    __shared__ uint32_t n_units;
-    __shared__ uint32_t cur_tile;
+__global__ void __launch_bounds__(RasterShared<S>::kThreads) k_raster(FrameArgs a) {
+    using Sh = RasterShared<S>;
+    constexpr int NT = Sh::kThreads, R = Sh::kRegions, NW = NT / 32;
+    extern __shared__ __align__(16) unsigned char raster_smem[];
+    Sh& s = *reinterpret_cast<Sh*>(raster_smem);
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t n_tiles = a.dyn->n_stiles;
     for (uint32_t iter = 0;; ++iter) {
 #if SWR_RASTER_PERSISTENT
-    if (threadIdx.x == 0) cur_tile = atomicAdd(&a.counters->work_next, 1u);
-    __syncthreads();
-    const uint32_t st = cur_tile;
+        if (threadIdx.x == 0) s.cur_tile = atomicAdd(&a.counters->work_next, 1u);
+        __syncthreads();
+        const uint32_t st = s.cur_tile;
 #else
-    if (iter > 0) break;
-    const uint32_t st = blockIdx.x;
+        if (iter > 0) break;
+        const uint32_t st = blockIdx.x;
 #endif
-    if (st >= n_tiles) break;
-    const uint32_t vi = find_view_by_stile(a, st);
-    const DView& view = a.views[vi];
-    const uint32_t local = st - view.stile_base;
-    const int32_t sx0 = (int32_t)(local % (uint32_t)view.stiles_x) * S;
-    const int32_t sy0 = (int32_t)(local / (uint32_t)view.stiles_x) * S;
-    const int32_t tx0 = (sx0 / kRefTile) * kRefTile, ty0 = (sy0 / kRefTile) * kRefTile;
-    for (int i = threadIdx.x; i < S * S; i += blockDim.x) sk[i] = kEmptyKey;
-    if (threadIdx.x == 0) n_units = 0;
-    __syncthreads();
-    const bool bad = (a.counters->status & (ST_BIN_OVERFLOW | ST_CLIP_OVERFLOW | ST_QUEUE_OVERFLOW)) != 0u;
-    if (!bad) {
-        const uint32_t b0 = a.tile_offset[st], b1 = a.tile_offset[st + 1];
+        if (st >= n_tiles) break;
+        const uint32_t vi = find_view_by_stile(a, st);
+        const DView& view = a.views[vi];
+        const uint32_t local = st - view.stile_base;
+        const int32_t sx0 = (int32_t)(local % (uint32_t)view.stiles_x) * S;
+        const int32_t sy0 = (int32_t)(local / (uint32_t)view.stiles_x) * S;
+        const int32_t tx0 = (sx0 / kRefTile) * kRefTile, ty0 = (sy0 / kRefTile) * kRefTile;
+        for (int i = threadIdx.x; i < S * S; i += NT) s.sk[i] = kEmptyKey;
+        const bool bad = (a.counters->status & (ST_BIN_OVERFLOW | ST_CLIP_OVERFLOW | ST_QUEUE_OVERFLOW)) != 0u;
+        const uint32_t b0 = a.tile_offset[st], b1 = bad ? b0 : a.tile_offset[st + 1];
         const DScene& sc = a.scenes[view.scene];
-        // Pass 1: one thread per packet. Large packets are split into 16-px
-        // block units for pass 2; small ones are rasterized here unless they
-        // wait for pass 3 (after the large ones, which occlude the most).
-        for (uint32_t p = b0 + threadIdx.x; p < b1; p += blockDim.x) {
-            const uint32_t slot = a.bins[p];
-            if (SWR_COARSE_FIRST && !packet_is_coarse(a.rec_r + slot, tx0, ty0)) continue;
+        for (uint32_t cursor = b0; cursor < b1;) {
+            // Pass 1: count this thread's regions and quads.
+            const uint32_t pidx = cursor + threadIdx.x;
             PacketCtx c;
-            load_packet(a, sc, slot, tx0, ty0, c);
-            if (!c.coarse) {
-                if (!SWR_COARSE_FIRST)
-                    fine_thread<S>(sk, c.e12, c.e20, c.e01, c.r, c.xs, c.ys, c.xe, c.ye, sx0, sy0, &sc, c.mat, c.qs,
-                                   c.amip, ctx_zlo(c));
-                continue;
+            uint32_t slot = 0, n_ex = 0, n_q = 0, n_sl = 0;
+            if (pidx < b1) {
+                slot = a.bins[pidx];
+                load_packet(a, sc, slot, tx0, ty0, c);
+                packet_regions<S>(s, c, sx0, sy0, false, threadIdx.x, n_ex, n_q, n_sl);
             }
-            int32_t bxl, bxh, byl, byh;
-            block_range(c.xs, c.xe, sx0, S, bxl, bxh);
-            block_range(c.ys, c.ye, sy0, S, byl, byh);
-            const int32_t nb = (bxh - bxl) * (byh - byl);
-            if (nb <= 0) continue;
-            const uint32_t base = atomicAdd(&n_units, (uint32_t)nb);
-            if (base + (uint32_t)nb <= (uint32_t)kUnitCap) {
-                uint32_t u = base;
-                for (int32_t by = byl; by < byh; ++by)
-                    for (int32_t bx = bxl; bx < bxh; ++bx) units[u++] = make_uint2(slot, (uint32_t)((by << 8) | bx));
-            } else {
-                // Queue full: mark the part of the reservation that fits as
-                // empty, then walk the packet's blocks in this thread.
-                for (uint32_t u = base; u < (uint32_t)kUnitCap; ++u) units[u] = make_uint2(0xFFFFFFFFu, 0u);
-                for (int32_t by = byl; by < byh; ++by)
-                    for (int32_t bx = bxl; bx < bxh; ++bx) {
-                        const int32_t ox = c.xs + 256 * bx, oy = c.ys + 256 * by;
-                        if (block_rejected(c.e12, c.e20, c.e01, ox, oy)) continue;
-                        fine_thread<S>(sk, c.e12, c.e20, c.e01, c.r, ox, oy, min(ox + 256, c.xe), min(oy + 256, c.ye),
-                                       sx0, sy0, &sc, c.mat, c.qs, c.amip, ctx_zlo(c));
+            // Block-wide exclusive scan of (exact regions, quads, sequential regions).
+            uint32_t ie = n_ex, iq = n_q, is = n_sl;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t xe = __shfl_up_sync(0xFFFFFFFFu, ie, o);
+                const uint32_t xq = __shfl_up_sync(0xFFFFFFFFu, iq, o);
+                const uint32_t xs = __shfl_up_sync(0xFFFFFFFFu, is, o);
+                if (lane >= (uint32_t)o) {
+                    ie += xe;
+                    iq += xq;
+                    is += xs;
+                }
+            }
+            if (lane == 31u) {
+                s.scan[warp][0] = ie;
+                s.scan[warp][1] = iq;
+                s.scan[warp][2] = is;
+            }
+            __syncthreads();
+            uint32_t pe = 0, pq = 0, ps = 0;
+            for (uint32_t w = 0; w < warp; ++w) {
+                pe += s.scan[w][0];
+                pq += s.scan[w][1];
+                ps += s.scan[w][2];
+            }
+            pe += ie - n_ex;
+            pq += iq - n_q;
+            ps += is - n_sl;
+            // Packets are taken in order while their regions fit.
+            const bool taken = pe + n_ex + ps + n_sl <= (uint32_t)R;
+            const uint32_t n_taken = (uint32_t)__syncthreads_count(taken);
+            if (taken && threadIdx.x + 1u == n_taken) {
+                s.n_exact = pe + n_ex;
+                s.n_quads = pq + n_q;
+                s.n_slow = ps + n_sl;
+                s.r_qbeg[pe + n_ex] = pq + n_q;
+                for (int t = 1; t <= 33; ++t) s.r_qbeg[pe + n_ex + t] = 0xFFFFFFFFu;
+            }
+            if (taken && (n_ex + n_sl) > 0u) {
+                const uint32_t pk = threadIdx.x;
+                s.p_sx[0][pk] = c.e12.sx;
+                s.p_sx[1][pk] = c.e20.sx;
+                s.p_sx[2][pk] = c.e01.sx;
+                s.p_sy[0][pk] = c.e12.sy;
+                s.p_sy[1][pk] = c.e20.sy;
+                s.p_sy[2][pk] = c.e01.sy;
+                s.p_ooa[pk] = c.r.ooa;
+#pragma unroll
+                for (int t = 0; t < 3; ++t) {
+                    s.p_oow[t][pk] = c.r.oow[t];
+                    s.p_zow[t][pk] = c.r.zow[t];
+                }
+                s.p_seq8[pk] = c.r.seq8;
+                s.p_mat[pk] = c.r.material;
+                s.p_amip[pk] = c.amip;
+                s.p_slot[pk] = slot;
+                packet_regions<S>(s, c, sx0, sy0, true, pk, pe, pq, ps);
+            }
+            cursor += n_taken;
+            __syncthreads();
+            // Pass 2: exact quads, numbered 0..n_quads-1 region after region;
+            // each warp takes one contiguous range, 32 quads per step.
+            const uint32_t nq = s.n_quads, ne = s.n_exact;
+            if (nq > 0u) {
+                const uint32_t chunk = (nq + NW - 1u) / NW;
+                const uint32_t f0 = warp * chunk, f1 = min(f0 + chunk, nq);
+                if (f0 < f1) {
+                    uint32_t lo = 0, hi = ne - 1u;  // last region starting at or before f0
+                    while (lo < hi) {
+                        const uint32_t mid = (lo + hi + 1u) >> 1;
+                        if (s.r_qbeg[mid] <= f0) lo = mid; else hi = mid - 1u;
                     }
+                    uint32_t rb = lo;
+                    for (uint32_t f = f0; f < f1; f += 32u) {
+                        // Region ends are strictly increasing (no empty region):
+                        // lane l's region is rb + #{ends <= f + l}.
+                        const uint32_t d = s.r_qbeg[rb + 1u + lane] - f;
+                        const uint32_t mask = __reduce_or_sync(0xFFFFFFFFu, d <= 31u ? (1u << d) : 0u);
+                        const uint32_t adv = __popc(__ballot_sync(0xFFFFFFFFu, d <= 32u));
+                        const uint32_t r = rb + __popc(mask & ((2u << lane) - 1u));
+                        const uint32_t g = f + lane;
+                        if (g < f1) raster_exact_quad<S>(s, a, sc, r, g - s.r_qbeg[r]);
+                        rb += adv;
+                    }
+                }
             }
+            // Pass 3: sequential regions, one warp each.
+            const uint32_t nsl = s.n_slow;
+            for (uint32_t m = warp; m < nsl; m += NW) raster_slow_region<S>(s, a, sc, (uint32_t)R - 1u - m);
+            __syncthreads();
+        }
+        unsigned long long* dst = a.keys + view.key_offset;
+        for (int i = threadIdx.x; i < S * S; i += NT) {
+            const int32_t ly = i / S, lx = i % S;
+            dst[(uint64_t)(sy0 + ly) * view.key_pitch + (uint64_t)(sx0 + lx)] = s.sk[i];
         }
         __syncthreads();
-        // Pass 2: one warp per queued 16-px block of a large packet.
-        const uint32_t nu = min(n_units, (uint32_t)kUnitCap);
-        const uint32_t warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-        for (uint32_t u = warp; u < nu; u += nwarps) {
-            const uint2 un = units[u];
-            if (un.x == 0xFFFFFFFFu) continue;
-            PacketCtx c;
-            load_packet(a, sc, un.x, tx0, ty0, c);
-            const int32_t bx = (int32_t)(un.y & 0xFFu), by = (int32_t)(un.y >> 8);
-            const int32_t ox = c.xs + 256 * bx, oy = c.ys + 256 * by;
-            if (block_rejected(c.e12, c.e20, c.e01, ox, oy)) continue;
-            fine_region<S>(sk, c.e12, c.e20, c.e01, c.r, ox, oy, min(ox + 256, c.xe), min(oy + 256, c.ye), sx0, sy0,
-                           &sc, c.mat, c.qs, c.amip, ctx_zlo(c));
-        }
-        // Pass 3: the small packets.
-        if (SWR_COARSE_FIRST) {
-            __syncthreads();
-            for (uint32_t p = b0 + threadIdx.x; p < b1; p += blockDim.x) {
-                const uint32_t slot = a.bins[p];
-                if (packet_is_coarse(a.rec_r + slot, tx0, ty0)) continue;
-                PacketCtx c;
-                load_packet(a, sc, slot, tx0, ty0, c);
-                fine_thread<S>(sk, c.e12, c.e20, c.e01, c.r, c.xs, c.ys, c.xe, c.ye, sx0, sy0, &sc, c.mat, c.qs,
-                               c.amip, ctx_zlo(c));
-            }
-        }
-    }
-    __syncthreads();
-    unsigned long long* dst = a.keys + view.key_offset;
-    for (int i = threadIdx.x; i < S * S; i += blockDim.x) {
-        const int32_t ly = i / S, lx = i % S;
-        dst[(uint64_t)(sy0 + ly) * view.key_pitch + (uint64_t)(sx0 + lx)] = sk[i];
-    }
-    __syncthreads();
     }
 }
 
@@ -1384,6 +1392,12 @@ __global__ void k_resolve(FrameArgs a) {
 // --------------------------------------------------------------------------
 static uint64_t g_const_init_mask = 0;  // one bit per device
 
+template <int S>
+static cudaError_t raster_smem_attr() {
+    return cudaFuncSetAttribute(k_raster<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)sizeof(RasterShared<S>));
+}
+
 cudaError_t init_kernel_constants() {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -1392,18 +1406,29 @@ cudaError_t init_kernel_constants() {
     float t[256];
     for (int i = 0; i < 256; ++i) t[i] = (float)i / 255.0f;
     e = cudaMemcpyToSymbol(c_unorm8, t, sizeof(t));
+    if (e == cudaSuccess) e = raster_smem_attr<8>();
+    if (e == cudaSuccess) e = raster_smem_attr<16>();
+    if (e == cudaSuccess) e = raster_smem_attr<32>();
+    if (e == cudaSuccess) e = raster_smem_attr<64>();
     if (e == cudaSuccess && dev < 64) g_const_init_mask |= 1ull << dev;
     return e;
 }
 
+template <int S>
+static int raster_blocks_per_sm() {
+    int rb = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rb, k_raster<S>, RasterShared<S>::kThreads,
+                                                  sizeof(RasterShared<S>));
+    return rb;
+}
+
 void frame_grids(int num_sms, uint32_t S, uint32_t* raster_grid, uint32_t* shade_grid) {
     int rb = 1, sb = 1;
-    const int threads = S <= 16 ? 128 : 256;
     switch (S) {
-        case 8: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rb, k_raster<8>, threads, 0); break;
-        case 16: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rb, k_raster<16>, threads, 0); break;
-        case 32: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rb, k_raster<32>, threads, 0); break;
-        default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rb, k_raster<64>, threads, 0); break;
+        case 8: rb = raster_blocks_per_sm<8>(); break;
+        case 16: rb = raster_blocks_per_sm<16>(); break;
+        case 32: rb = raster_blocks_per_sm<32>(); break;
+        default: rb = raster_blocks_per_sm<64>(); break;
     }
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sb, k_shade, 256, 0);
     cudaGetLastError();
@@ -1439,10 +1464,10 @@ void launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t* ev
     const uint32_t rg = SWR_RASTER_PERSISTENT ? (a.raster_grid > 0 ? a.raster_grid : (uint32_t)num_sms)
                                               : (a.stile_cap > 0 ? a.stile_cap : 1u);
     switch (a.sched_tile) {
-        case 8: k_raster<8><<<rg, 128, 0, s>>>(a); break;
-        case 16: k_raster<16><<<rg, 128, 0, s>>>(a); break;
-        case 32: k_raster<32><<<rg, 256, 0, s>>>(a); break;
-        default: k_raster<64><<<rg, 256, 0, s>>>(a); break;
+        case 8: k_raster<8><<<rg, RasterShared<8>::kThreads, sizeof(RasterShared<8>), s>>>(a); break;
+        case 16: k_raster<16><<<rg, RasterShared<16>::kThreads, sizeof(RasterShared<16>), s>>>(a); break;
+        case 32: k_raster<32><<<rg, RasterShared<32>::kThreads, sizeof(RasterShared<32>), s>>>(a); break;
+        default: k_raster<64><<<rg, RasterShared<64>::kThreads, sizeof(RasterShared<64>), s>>>(a); break;
     }
     mark(6);
     k_shade<<<a.shade_grid > 0 ? a.shade_grid : (uint32_t)num_sms, 256, 0, s>>>(a);
