@@ -42,7 +42,8 @@ def parse():
     ap.add_argument("--workload", default="4k", choices=["4k", "small"])
     ap.add_argument("--cpu-frames", type=int, default=3, help="frames in the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--sched-tile", type=int, default=64, help="raster scheduling tile (8, 16, 32, 64)")
+    ap.add_argument("--sched-tile", type=int, default=0,
+                    help="raster scheduling tile (8, 16, 32, 64; 0 = the library's choice for the frame size)")
     ap.add_argument("--mode", default="plain", choices=["plain", "batched", "hetero", "served"],
                     help="plain: 4K per-frame path (the headline); batched: 64 views of the 81,920-triangle scene "
                          "in one launch; hetero: 16 heterogeneous scenes in one launch; served: request loop")
@@ -429,7 +430,7 @@ def main():
             "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded scene of the configured shape; inputs larger than L2)",
-            "config": dict(cfg, parallelism="replicas" if world > 1 else "single", sched_tile=args.sched_tile),
+            "config": dict(cfg, parallelism="replicas" if world > 1 else "single", sched_tile=st.sched_tile),
             "gtri_per_s": fps * cfg["triangles"] / 1e9, "gpix_per_s": fps * W * H / 1e9,
             "stage_ms": {k: round(v, 4) for k, v in prof.items()},
             "frame_stats": {"triangles_in": st.triangles_in, "clipped": st.triangles_clipped,

@@ -327,7 +327,7 @@ swr_status swr_camera_update(swr_camera* cam);
 
 typedef struct swr_renderer_opts {
     uint32_t rsqrt_mode;        /* SWR_RSQRT_*, default AARCH64 */
-    uint32_t sched_tile;        /* raster scheduling tile: 8, 16, 32 or 64 (0 = 64) */
+    uint32_t sched_tile;        /* raster scheduling tile: 8, 16, 32 or 64; 0 = chosen from the frame size */
     uint64_t bin_capacity;      /* initial (triangle, tile) pair capacity, 0 = auto */
     uint32_t raster_warps;      /* warps per raster CTA, 0 = default */
     uint32_t flags;             /* reserved, 0 */
@@ -380,6 +380,7 @@ typedef struct swr_frame_stats {
     uint32_t overflow_retries;
     float tile_luminance_mean;
     float exposure;
+    uint32_t sched_tile;        /* scheduling tile the renderer uses */
 } swr_frame_stats;
 
 swr_status swr_renderer_get_stats(swr_renderer* r, swr_frame_stats* out);
@@ -415,7 +416,7 @@ typedef struct swr_view_desc {
 } swr_view_desc;
 
 typedef struct swr_batch_opts {
-    uint32_t sched_tile;        /* 8, 16, 32, 64; 0 = autotuned choice for the batch's class */
+    uint32_t sched_tile;        /* 8, 16, 32, 64; 0 = autotuned choice for the batch's class, else chosen from the view sizes */
     uint32_t use_graph;         /* replay the frame as a CUDA graph */
     uint64_t bin_capacity;      /* initial pair capacity, 0 = auto */
 } swr_batch_opts;
@@ -449,7 +450,7 @@ typedef struct swr_server_opts {
     uint32_t max_batch_views;   /* views per batch (default 64) */
     uint32_t max_queue;         /* pending requests before submit returns SWR_BUSY (default 4096) */
     uint32_t inflight;          /* batches in flight on separate streams (default 2) */
-    uint32_t sched_tile;        /* 0 = autotuned choice */
+    uint32_t sched_tile;        /* 0 = autotuned, else chosen from the view sizes */
     uint32_t rsqrt_mode;
     uint32_t use_graph;
 } swr_server_opts;

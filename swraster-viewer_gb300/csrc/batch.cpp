@@ -138,7 +138,13 @@ swr_status BatchImpl::render(const swr_view_desc* vd, int32_t n, cudaStream_t st
 
 uint32_t BatchImpl::tuned_tile(const swr_view_desc* vd, int32_t n) const {
     auto it = tuned.find(batch_class(vd, n));
-    return it == tuned.end() ? 64u : it->second;
+    if (it != tuned.end()) return it->second;
+    std::vector<int32_t> w((size_t)n), h((size_t)n);
+    for (int32_t i = 0; i < n; ++i) {
+        w[(size_t)i] = vd[i].width;
+        h[(size_t)i] = vd[i].height;
+    }
+    return auto_sched_tile(w.data(), h.data(), n, eng.num_sms);
 }
 
 }  // namespace swr

@@ -173,15 +173,13 @@ swr_status swr_renderer_create(int32_t width, int32_t height, const swr_renderer
     o.rsqrt_mode = SWR_RSQRT_AARCH64;
     if (opts) o = *opts;
     if (o.rsqrt_mode > SWR_RSQRT_AARCH64) return fail(SWR_INVALID_ARG, "bad rsqrt_mode");
-    if (o.sched_tile == 0) o.sched_tile = 64;
-    if (o.sched_tile != 8 && o.sched_tile != 16 && o.sched_tile != 32 && o.sched_tile != 64)
-        return fail(SWR_INVALID_ARG, "sched_tile must be 8, 16, 32 or 64");
+    if (o.sched_tile != 0 && o.sched_tile != 8 && o.sched_tile != 16 && o.sched_tile != 32 && o.sched_tile != 64)
+        return fail(SWR_INVALID_ARG, "sched_tile must be 0, 8, 16, 32 or 64");
     swr_renderer* r = new (std::nothrow) swr_renderer();
     if (!r) return fail(SWR_NO_MEMORY, "out of host memory");
     r->width = width;
     r->height = height;
     r->opts = o;
-    r->eng.sched_tile = o.sched_tile;
     r->eng.bin_cap = o.bin_capacity;
     std::string err;
     swr_status st = r->eng.init(err);
@@ -190,6 +188,8 @@ swr_status swr_renderer_create(int32_t width, int32_t height, const swr_renderer
         delete r;
         return fail(st, err);
     }
+    if (r->opts.sched_tile == 0) r->opts.sched_tile = auto_sched_tile(&width, &height, 1, r->eng.num_sms);
+    r->eng.sched_tile = r->opts.sched_tile;
     r->tiles_x = (uint32_t)((width + 63) / 64);
     r->tiles_y = (uint32_t)((height + 63) / 64);
     cudaError_t e = cudaSuccess;
@@ -438,6 +438,7 @@ swr_status swr_renderer_get_stats(swr_renderer* r, swr_frame_stats* o) {
     o->tiles = r->tiles_x * r->tiles_y;
     o->overflow_retries = r->eng.retries;
     o->exposure = r->expo.exposure;
+    o->sched_tile = r->opts.sched_tile;
     return SWR_OK;
 }
 

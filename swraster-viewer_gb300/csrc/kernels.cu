@@ -725,9 +725,10 @@ __device__ __forceinline__ void block_range(int32_t start, int32_t end, int32_t 
 __device__ __forceinline__ float ru_add(float a, float b) { return __fadd_ru(a, b); }
 __device__ __forceinline__ float ru_mul(float a, float b) { return __fmul_ru(a, b); }
 
-// Quad range of a region clipped to the scheduling tile; returns the quad
-// count (0: nothing of the region is in the tile). Region origins and tile
-// origins are even pixels, so a quad is either wholly in the tile or out.
+// Quad range of a region clipped to the scheduling tile, packed as
+// ilo | jlo << 4 | ihi << 8 | jhi << 12 (at most 9 quads a side); returns the
+// quad count (0: nothing of the region is in the tile). Region origins and
+// tile origins are even pixels, so a quad is either wholly in the tile or out.
 __device__ __forceinline__ uint32_t clip_quads(int32_t ox, int32_t oy, int32_t ex, int32_t ey, int32_t sx0,
                                                int32_t sy0, int32_t S, uint32_t& ij) {
     const int32_t ncol = (ex - ox + 31) >> 5, nrow = (ey - oy + 31) >> 5;
@@ -735,7 +736,7 @@ __device__ __forceinline__ uint32_t clip_quads(int32_t ox, int32_t oy, int32_t e
     const int32_t ilo = max(0, (sx0 - px) / 2), ihi = min(ncol, (sx0 + S - px) / 2);
     const int32_t jlo = max(0, (sy0 - py) / 2), jhi = min(nrow, (sy0 + S - py) / 2);
     if (ihi <= ilo || jhi <= jlo) return 0u;
-    ij = (uint32_t)ilo | ((uint32_t)jlo << 8) | ((uint32_t)ihi << 16) | ((uint32_t)jhi << 24);
+    ij = (uint32_t)ilo | ((uint32_t)jlo << 4) | ((uint32_t)ihi << 8) | ((uint32_t)jhi << 12);
     return (uint32_t)((ihi - ilo) * (jhi - jlo));
 }
 
@@ -753,7 +754,7 @@ __device__ __forceinline__ void origin_values(const PacketCtx& c, int32_t ox, in
 }
 
 __device__ __forceinline__ bool region_exact(const PacketCtx& c, const float w[12], uint32_t ij) {
-    const float im = (float)((int32_t)((ij >> 16) & 0xFFu) - 1), jm = (float)((int32_t)(ij >> 24) - 1);
+    const float im = (float)((int32_t)((ij >> 8) & 0xFu) - 1), jm = (float)((int32_t)((ij >> 12) & 0xFu) - 1);
     const float sx[3] = {c.e12.sx, c.e20.sx, c.e01.sx}, sy[3] = {c.e12.sy, c.e20.sy, c.e01.sy};
     bool ok = true;
 #pragma unroll
@@ -768,54 +769,77 @@ __device__ __forceinline__ bool region_exact(const PacketCtx& c, const float w[1
 template <int S>
 struct RasterShared {
     static constexpr int kThreads = S <= 16 ? 128 : 256;
-    static constexpr int kRegions = 2 * kThreads;  // regions staged per round
-    unsigned long long sk[S * S];                  // depth keys of the scheduling tile
-    // Regions: exact ones from the front, sequential ones from the back.
+    static constexpr int kRegions = kThreads + kThreads / 2;  // regions staged per round
+    unsigned long long sk[S * S];                             // depth keys of the scheduling tile
+    // Regions of the round, in packet order.
     float r_w[12][kRegions];   // origin edge values
-    uint32_t r_pkt[kRegions];  // packet index in the round
-    uint32_t r_ij[kRegions];   // ilo | jlo << 8 | ihi << 16 | jhi << 24
-    uint32_t r_org[kRegions];  // origin pixel relative to the tile: x | y << 16 (int16 each)
-    float r_inv_ni[kRegions];  // 1 / (ihi - ilo)
-    uint32_t r_qbeg[kRegions + 40];  // first flattened quad of each exact region, then end markers
+    uint32_t r_geom[kRegions];  // quad range (16 b) | exact << 15 | origin x, y relative to the tile (int8 each)
+    uint32_t r_pi[kRegions];    // packet index | kSlowRegion | ceil(2^15 / ni) << 16
+    uint32_t r_qbeg[kRegions + 40];  // first flattened quad of each region, then end markers
+    uint16_t slow[kRegions];    // regions that replay the sequential additions
     // Packets of the round, one per thread.
     float p_sx[3][kThreads], p_sy[3][kThreads];
     float p_ooa[kThreads], p_oow[3][kThreads], p_zow[3][kThreads];
     uint32_t p_seq8[kThreads], p_mat[kThreads], p_amip[kThreads], p_slot[kThreads];
-    uint32_t scan[kThreads / 32][3];
-    uint32_t n_exact, n_quads, n_slow, cur_tile;
+    uint32_t scan[kThreads / 32][2];
+    uint32_t n_regions, n_quads, n_slow, cur_tile;
 };
+
+constexpr uint32_t kSlowRegion = 0x8000u;  // region replays the sequential additions
+
+// Interpolation constants of one packet.
+struct PacketLanes {
+    float ooa, oow[3], zow[3];
+    uint32_t seq8, mat;
+};
+
+template <int S>
+__device__ __forceinline__ PacketLanes packet_lanes(const RasterShared<S>& s, uint32_t pk) {
+    PacketLanes L;
+    L.ooa = s.p_ooa[pk];
+#pragma unroll
+    for (int t = 0; t < 3; ++t) {
+        L.oow[t] = s.p_oow[t][pk];
+        L.zow[t] = s.p_zow[t][pk];
+    }
+    L.seq8 = s.p_seq8[pk];
+    L.mat = s.p_mat[pk];
+    return L;
+}
 
 // Depth test of one covered lane: bary, w, z as fine_raster computes them,
 // then the canonical-order key (atomicMin keeps the lowest z, ties broken by
 // submission order).
 template <int S>
-__device__ __forceinline__ void raster_lane(RasterShared<S>& s, const FrameArgs& a, const DScene& sc, uint32_t pk,
-                                            float w1, float w2, int32_t lx, int32_t ly) {
-    const float ooa = s.p_ooa[pk];
-    const float b1 = w1 * ooa, b2 = w2 * ooa;
-    const float oow[3] = {s.p_oow[0][pk], s.p_oow[1][pk], s.p_oow[2][pk]};
-    const float zow[3] = {s.p_zow[0][pk], s.p_zow[1][pk], s.p_zow[2][pk]};
-    const float w = 1.0f / interp(oow, b1, b2);
-    const float z = interp(zow, b1, b2) * w;
+__device__ __forceinline__ void raster_lane(RasterShared<S>& s, const FrameArgs& a, const DScene& sc,
+                                            const PacketLanes& L, uint32_t pk, float w1, float w2, int32_t lx,
+                                            int32_t ly) {
+    const float b1 = w1 * L.ooa, b2 = w2 * L.ooa;
+    const float w = 1.0f / interp(L.oow, b1, b2);
+    const float z = interp(L.zow, b1, b2) * w;
     bool pass = (z == z);
-    const uint32_t m = s.p_mat[pk];
-    if (pass && (m & kRecAlphaBit))
-        pass = alpha_pass(sc, sc.materials[m & ~kRecAlphaBit], a.rec_s[s.p_slot[pk]], b1, b2, w, s.p_amip[pk]);
+    if (pass && (L.mat & kRecAlphaBit))
+        pass = alpha_pass(sc, sc.materials[L.mat & ~kRecAlphaBit], a.rec_s[s.p_slot[pk]], b1, b2, w, s.p_amip[pk]);
     if (pass) {
-        const unsigned long long key = make_key(z, s.p_seq8[pk]);
+        const unsigned long long key = make_key(z, L.seq8);
         unsigned long long* slot = s.sk + ly * S + lx;
         if (key < *slot) atomicMin(slot, key);
     }
 }
 
+__device__ __forceinline__ int32_t geom_ox(uint32_t g) { return (int32_t)(int8_t)((g >> 16) & 0xFFu); }
+__device__ __forceinline__ int32_t geom_oy(uint32_t g) { return (int32_t)(int8_t)(g >> 24); }
+
 // Exact region quad: lane = one quad, evaluated in closed form.
 template <int S>
 __device__ __forceinline__ void raster_exact_quad(RasterShared<S>& s, const FrameArgs& a, const DScene& sc,
-                                                  uint32_t r, uint32_t q) {
-    const uint32_t pk = s.r_pkt[r], ij = s.r_ij[r], org = s.r_org[r];
-    const int32_t ilo = (int32_t)(ij & 0xFFu), jlo = (int32_t)((ij >> 8) & 0xFFu);
-    const int32_t ni = (int32_t)((ij >> 16) & 0xFFu) - ilo;
-    const int32_t jj = (int32_t)(((float)q + 0.5f) * s.r_inv_ni[r]);  // q / ni, exact for q < 2^16
+                                                  uint32_t r, uint32_t q, uint32_t g) {
+    const uint32_t pi = s.r_pi[r];
+    if (pi & kSlowRegion) return;
+    const uint32_t pk = pi & 0x7FFFu;
+    const int32_t ilo = (int32_t)(g & 0xFu), jlo = (int32_t)((g >> 4) & 0xFu);
+    const int32_t ni = (int32_t)((g >> 8) & 0xFu) - ilo;
+    const int32_t jj = (int32_t)((q * (pi >> 16)) >> 15);  // q / ni for q < 2^12
     const int32_t i = ilo + ((int32_t)q - jj * ni), j = jlo + jj;
     const float fi = (float)i, fj = (float)j;
     float w[12];
@@ -825,12 +849,15 @@ __device__ __forceinline__ void raster_exact_quad(RasterShared<S>& s, const Fram
 #pragma unroll
         for (int k = 0; k < 4; ++k) w[4 * e + k] = s.r_w[4 * e + k][r] + d;
     }
-    const int32_t lx0 = (int32_t)(int16_t)(org & 0xFFFFu) + 2 * i;
-    const int32_t ly0 = (int32_t)(int16_t)(org >> 16) + 2 * j;
+    uint32_t cov = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) cov |= (w[k] >= 0.0f && w[4 + k] >= 0.0f && w[8 + k] >= 0.0f) ? (1u << k) : 0u;
+    if (cov == 0u) return;
+    const PacketLanes L = packet_lanes(s, pk);
+    const int32_t lx0 = geom_ox(g) + 2 * i, ly0 = geom_oy(g) + 2 * j;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        if (w[k] >= 0.0f && w[4 + k] >= 0.0f && w[8 + k] >= 0.0f)
-            raster_lane<S>(s, a, sc, pk, w[4 + k], w[8 + k], lx0 + (k & 1), ly0 + (k >> 1));
+        if (cov & (1u << k)) raster_lane<S>(s, a, sc, L, pk, w[4 + k], w[8 + k], lx0 + (k & 1), ly0 + (k >> 1));
     }
 }
 
@@ -841,13 +868,13 @@ __device__ __forceinline__ void raster_slow_region(RasterShared<S>& s, const Fra
                                                    uint32_t r) {
     const uint32_t lane = threadIdx.x & 31u;
     const int32_t k = (int32_t)(lane & 3u);
-    const uint32_t pk = s.r_pkt[r], ij = s.r_ij[r], org = s.r_org[r];
-    const int32_t ilo = (int32_t)(ij & 0xFFu), jlo = (int32_t)((ij >> 8) & 0xFFu);
-    const int32_t ihi = (int32_t)((ij >> 16) & 0xFFu), jhi = (int32_t)(ij >> 24);
-    const int32_t lx0 = (int32_t)(int16_t)(org & 0xFFFFu) + (k & 1);
-    const int32_t ly0 = (int32_t)(int16_t)(org >> 16) + (k >> 1);
+    const uint32_t pk = s.r_pi[r] & 0x7FFFu, g = s.r_geom[r];
+    const int32_t ilo = (int32_t)(g & 0xFu), jlo = (int32_t)((g >> 4) & 0xFu);
+    const int32_t ihi = (int32_t)((g >> 8) & 0xFu), jhi = (int32_t)((g >> 12) & 0xFu);
+    const int32_t lx0 = geom_ox(g) + (k & 1), ly0 = geom_oy(g) + (k >> 1);
     const float sx0 = s.p_sx[0][pk], sx1 = s.p_sx[1][pk], sx2 = s.p_sx[2][pk];
     const float sy0 = s.p_sy[0][pk], sy1 = s.p_sy[1][pk], sy2 = s.p_sy[2][pk];
+    const PacketLanes L = packet_lanes(s, pk);
     for (int32_t j = jlo + (int32_t)(lane >> 2); j < jhi; j += 8) {
         float w0 = s.r_w[k][r], w1 = s.r_w[4 + k][r], w2 = s.r_w[8 + k][r];
         for (int32_t t = 0; t < j; ++t) {
@@ -857,7 +884,7 @@ __device__ __forceinline__ void raster_slow_region(RasterShared<S>& s, const Fra
         }
         for (int32_t i = 0; i < ihi; ++i) {
             if (i >= ilo && w0 >= 0.0f && w1 >= 0.0f && w2 >= 0.0f)
-                raster_lane<S>(s, a, sc, pk, w1, w2, lx0 + 2 * i, ly0 + 2 * j);
+                raster_lane<S>(s, a, sc, L, pk, w1, w2, lx0 + 2 * i, ly0 + 2 * j);
             w0 += sx0;
             w1 += sx1;
             w2 += sx2;
@@ -865,38 +892,31 @@ __device__ __forceinline__ void raster_slow_region(RasterShared<S>& s, const Fra
     }
 }
 
-// Pass 1 of a round for one packet: classify, split into regions and count
-// (or, with write set, stage them at the given positions).
+// Pass 1 of a round for one packet: classify and split into regions, and
+// either count them (regions, quads) or stage them from the given positions.
 template <int S>
 __device__ __forceinline__ void packet_regions(RasterShared<S>& s, const PacketCtx& c, int32_t sx0, int32_t sy0,
-                                               bool write, uint32_t pk, uint32_t& n_ex, uint32_t& n_q,
-                                               uint32_t& n_sl) {
-    constexpr int R = RasterShared<S>::kRegions;
+                                               bool write, uint32_t pk, uint32_t& n_r, uint32_t& n_q) {
     auto region = [&](int32_t ox, int32_t oy, int32_t ex, int32_t ey) {
         uint32_t ij = 0;
         const uint32_t nq = clip_quads(ox, oy, ex, ey, sx0, sy0, S, ij);
         if (nq == 0) return;
-        float w[12];
-        origin_values(c, ox, oy, w);
-        const bool exact = region_exact(c, w, ij);
-        uint32_t r;
-        if (exact) {
-            r = n_ex;
-            if (write) s.r_qbeg[r] = n_q;
-            ++n_ex;
-            n_q += nq;
-        } else {
-            r = (uint32_t)R - 1u - n_sl;
-            ++n_sl;
-        }
-        if (!write) return;
+        if (write) {
+            const uint32_t r = n_r;
+            float w[12];
+            origin_values(c, ox, oy, w);
+            const bool exact = region_exact(c, w, ij);
 #pragma unroll
-        for (int t = 0; t < 12; ++t) s.r_w[t][r] = w[t];
-        s.r_pkt[r] = pk;
-        s.r_ij[r] = ij;
-        const int32_t ox_rel = (ox >> kSubpixelShift) - sx0, oy_rel = (oy >> kSubpixelShift) - sy0;
-        s.r_org[r] = ((uint32_t)ox_rel & 0xFFFFu) | ((uint32_t)oy_rel << 16);
-        s.r_inv_ni[r] = 1.0f / (float)((int32_t)((ij >> 16) & 0xFFu) - (int32_t)(ij & 0xFFu));
+            for (int t = 0; t < 12; ++t) s.r_w[t][r] = w[t];
+            const int32_t ox_rel = (ox >> kSubpixelShift) - sx0, oy_rel = (oy >> kSubpixelShift) - sy0;
+            s.r_geom[r] = ij | ((uint32_t)(ox_rel & 0xFF) << 16) | ((uint32_t)(oy_rel & 0xFF) << 24);
+            const uint32_t ni = ((ij >> 8) & 0xFu) - (ij & 0xFu);
+            s.r_pi[r] = pk | (exact ? 0u : kSlowRegion) | (((32768u + ni - 1u) / ni) << 16);
+            s.r_qbeg[r] = n_q;
+            if (!exact) s.slow[atomicAdd(&s.n_slow, 1u)] = (uint16_t)r;
+        }
+        ++n_r;
+        n_q += nq;
     };
     if (!c.coarse) {
         region(c.xs, c.ys, c.xe, c.ye);
@@ -912,7 +932,6 @@ __device__ __forceinline__ void packet_regions(RasterShared<S>& s, const PacketC
             region(ox, oy, min(ox + 256, c.xe), min(oy + 256, c.ye));
         }
 }
-
 // Persistent: each CTA pulls (view, scheduling tile) work items from a
 // device-side counter until every tile of every view is done. Per tile, the
 // bin's packets go through rounds of one packet per thread: pass 1 stages
@@ -950,51 +969,44 @@ __global__ void __launch_bounds__(RasterShared<S>::kThreads) k_raster(FrameArgs 
             // Pass 1: count this thread's regions and quads.
             const uint32_t pidx = cursor + threadIdx.x;
             PacketCtx c;
-            uint32_t slot = 0, n_ex = 0, n_q = 0, n_sl = 0;
+            uint32_t slot = 0, n_r = 0, n_q = 0;
             if (pidx < b1) {
                 slot = a.bins[pidx];
                 load_packet(a, sc, slot, tx0, ty0, c);
-                packet_regions<S>(s, c, sx0, sy0, false, threadIdx.x, n_ex, n_q, n_sl);
+                packet_regions<S>(s, c, sx0, sy0, false, threadIdx.x, n_r, n_q);
             }
-            // Block-wide exclusive scan of (exact regions, quads, sequential regions).
-            uint32_t ie = n_ex, iq = n_q, is = n_sl;
+            if (threadIdx.x == 0) s.n_slow = 0;
+            // Block-wide exclusive scan of (regions, quads).
+            uint32_t ir = n_r, iq = n_q;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t xe = __shfl_up_sync(0xFFFFFFFFu, ie, o);
+                const uint32_t xr = __shfl_up_sync(0xFFFFFFFFu, ir, o);
                 const uint32_t xq = __shfl_up_sync(0xFFFFFFFFu, iq, o);
-                const uint32_t xs = __shfl_up_sync(0xFFFFFFFFu, is, o);
                 if (lane >= (uint32_t)o) {
-                    ie += xe;
+                    ir += xr;
                     iq += xq;
-                    is += xs;
                 }
             }
             if (lane == 31u) {
-                s.scan[warp][0] = ie;
+                s.scan[warp][0] = ir;
                 s.scan[warp][1] = iq;
-                s.scan[warp][2] = is;
             }
             __syncthreads();
-            uint32_t pe = 0, pq = 0, ps = 0;
+            uint32_t pr = ir - n_r, pq = iq - n_q;
             for (uint32_t w = 0; w < warp; ++w) {
-                pe += s.scan[w][0];
+                pr += s.scan[w][0];
                 pq += s.scan[w][1];
-                ps += s.scan[w][2];
             }
-            pe += ie - n_ex;
-            pq += iq - n_q;
-            ps += is - n_sl;
             // Packets are taken in order while their regions fit.
-            const bool taken = pe + n_ex + ps + n_sl <= (uint32_t)R;
+            const bool taken = pr + n_r <= (uint32_t)R;
             const uint32_t n_taken = (uint32_t)__syncthreads_count(taken);
             if (taken && threadIdx.x + 1u == n_taken) {
-                s.n_exact = pe + n_ex;
+                s.n_regions = pr + n_r;
                 s.n_quads = pq + n_q;
-                s.n_slow = ps + n_sl;
-                s.r_qbeg[pe + n_ex] = pq + n_q;
-                for (int t = 1; t <= 33; ++t) s.r_qbeg[pe + n_ex + t] = 0xFFFFFFFFu;
+                s.r_qbeg[pr + n_r] = pq + n_q;
+                for (int t = 1; t <= 33; ++t) s.r_qbeg[pr + n_r + t] = 0xFFFFFFFFu;
             }
-            if (taken && (n_ex + n_sl) > 0u) {
+            if (taken && n_r > 0u) {
                 const uint32_t pk = threadIdx.x;
                 s.p_sx[0][pk] = c.e12.sx;
                 s.p_sx[1][pk] = c.e20.sx;
@@ -1012,18 +1024,18 @@ __global__ void __launch_bounds__(RasterShared<S>::kThreads) k_raster(FrameArgs 
                 s.p_mat[pk] = c.r.material;
                 s.p_amip[pk] = c.amip;
                 s.p_slot[pk] = slot;
-                packet_regions<S>(s, c, sx0, sy0, true, pk, pe, pq, ps);
+                packet_regions<S>(s, c, sx0, sy0, true, pk, pr, pq);
             }
             cursor += n_taken;
             __syncthreads();
-            // Pass 2: exact quads, numbered 0..n_quads-1 region after region;
-            // each warp takes one contiguous range, 32 quads per step.
-            const uint32_t nq = s.n_quads, ne = s.n_exact;
+            // Pass 2: quads numbered 0..n_quads-1 region after region; each
+            // warp takes one contiguous range, 32 quads per step.
+            const uint32_t nq = s.n_quads, nr = s.n_regions;
             if (nq > 0u) {
                 const uint32_t chunk = (nq + NW - 1u) / NW;
                 const uint32_t f0 = warp * chunk, f1 = min(f0 + chunk, nq);
                 if (f0 < f1) {
-                    uint32_t lo = 0, hi = ne - 1u;  // last region starting at or before f0
+                    uint32_t lo = 0, hi = nr - 1u;  // last region starting at or before f0
                     while (lo < hi) {
                         const uint32_t mid = (lo + hi + 1u) >> 1;
                         if (s.r_qbeg[mid] <= f0) lo = mid; else hi = mid - 1u;
@@ -1037,14 +1049,14 @@ __global__ void __launch_bounds__(RasterShared<S>::kThreads) k_raster(FrameArgs 
                         const uint32_t adv = __popc(__ballot_sync(0xFFFFFFFFu, d <= 32u));
                         const uint32_t r = rb + __popc(mask & ((2u << lane) - 1u));
                         const uint32_t g = f + lane;
-                        if (g < f1) raster_exact_quad<S>(s, a, sc, r, g - s.r_qbeg[r]);
+                        if (g < f1) raster_exact_quad<S>(s, a, sc, r, g - s.r_qbeg[r], s.r_geom[r]);
                         rb += adv;
                     }
                 }
             }
             // Pass 3: sequential regions, one warp each.
             const uint32_t nsl = s.n_slow;
-            for (uint32_t m = warp; m < nsl; m += NW) raster_slow_region<S>(s, a, sc, (uint32_t)R - 1u - m);
+            for (uint32_t m = warp; m < nsl; m += NW) raster_slow_region<S>(s, a, sc, s.slow[m]);
             __syncthreads();
         }
         unsigned long long* dst = a.keys + view.key_offset;

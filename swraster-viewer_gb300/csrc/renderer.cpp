@@ -110,6 +110,17 @@ void init_view(DView& v, const swr_camera& cam, int32_t width, int32_t height, u
     v.key_pitch = (uint64_t)v.tiles_x * kRefTile;
 }
 
+uint32_t auto_sched_tile(const int32_t* widths, const int32_t* heights, int32_t n, int num_sms) {
+    const uint64_t want = 8ull * (uint64_t)(num_sms > 0 ? num_sms : 1);
+    for (uint32_t S : {64u, 32u}) {
+        uint64_t tiles = 0;
+        for (int32_t i = 0; i < n; ++i)
+            tiles += (uint64_t)((widths[i] + S - 1) / S) * (uint64_t)((heights[i] + S - 1) / S);
+        if (tiles >= want) return S;
+    }
+    return 16u;
+}
+
 void ExposureState::update(const float* lum, size_t n, float dt) {
     if (n == 0) return;
     std::vector<float> s(n);

@@ -115,6 +115,11 @@ void build_view_draws(const SceneImpl& s, const swr_camera& cam, uint32_t view_i
 // Fill the view-geometry fields of a DView (tiles, pitches, camera).
 void init_view(DView& v, const swr_camera& cam, int32_t width, int32_t height, uint32_t sched_tile);
 
+// Scheduling tile for views of the given sizes when the caller leaves it to
+// the library: the largest of 64, 32, 16 that still gives the raster kernel
+// at least 8 tiles per SM (16 when none does).
+uint32_t auto_sched_tile(const int32_t* widths, const int32_t* heights, int32_t n, int num_sms);
+
 // Sets the calling thread's swr_last_error() message.
 void set_last_error(const char* msg);
 

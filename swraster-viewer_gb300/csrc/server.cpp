@@ -277,7 +277,10 @@ swr_status swr_server_create(const swr_server_opts* opts, swr_server** out) {
     if (o.max_queue == 0) o.max_queue = 4096;
     if (o.inflight == 0) o.inflight = 2;
     if (o.inflight > 8) o.inflight = 8;
-    if (o.sched_tile == 0) o.sched_tile = 64;
+    if (o.sched_tile != 0 && o.sched_tile != 8 && o.sched_tile != 16 && o.sched_tile != 32 && o.sched_tile != 64) {
+        set_last_error("sched_tile must be 0, 8, 16, 32 or 64");
+        return SWR_INVALID_ARG;
+    }
     swr_server* s = new (std::nothrow) swr_server();
     if (!s) {
         set_last_error("out of host memory");

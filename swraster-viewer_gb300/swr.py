@@ -130,7 +130,8 @@ class RendererOpts(C.Structure):
 class FrameStats(C.Structure):
     _fields_ = [("triangles_in", C.c_uint64), ("triangles_clipped", C.c_uint64), ("setup_triangles", C.c_uint64),
                 ("bin_pairs", C.c_uint64), ("bin_capacity", C.c_uint64), ("tiles", C.c_uint32),
-                ("overflow_retries", C.c_uint32), ("tile_luminance_mean", C.c_float), ("exposure", C.c_float)]
+                ("overflow_retries", C.c_uint32), ("tile_luminance_mean", C.c_float), ("exposure", C.c_float),
+                ("sched_tile", C.c_uint32)]
 
 
 class ViewDesc(C.Structure):
@@ -363,7 +364,7 @@ def make_camera(position, look_at, fov, width, height, far_plane):
 
 
 class Renderer:
-    def __init__(self, width, height, rsqrt_mode=RSQRT_AARCH64, sched_tile=64, bin_capacity=0):
+    def __init__(self, width, height, rsqrt_mode=RSQRT_AARCH64, sched_tile=0, bin_capacity=0):
         o = RendererOpts(rsqrt_mode, sched_tile, bin_capacity, 0, 0)
         h = C.c_void_p()
         check(lib().swr_renderer_create(width, height, C.byref(o), C.byref(h)))
@@ -497,7 +498,7 @@ class Batch:
 class Server:
     """Request loop with continuous batching (swr_server_*)."""
 
-    def __init__(self, memory_budget=40 << 30, max_batch_views=64, max_queue=4096, inflight=2, sched_tile=64,
+    def __init__(self, memory_budget=40 << 30, max_batch_views=64, max_queue=4096, inflight=2, sched_tile=0,
                  rsqrt_mode=RSQRT_AARCH64, use_graph=False):
         h = C.c_void_p()
         o = ServerOpts(memory_budget, max_batch_views, max_queue, inflight, sched_tile, rsqrt_mode,

@@ -60,6 +60,41 @@ def test_sched_tiles_match(small, tile):
     compare(small, cam, 256, 160, sched_tile=tile)
 
 
+@pytest.fixture(scope="module")
+def big_tris():
+    s = swr.Scene(scenes.spheres_scene(seed=5, count=3, subdiv=0, box=3.0, radius=(1.5, 2.5), tex_size=64,
+                                       cube_size=16, voxel=32, specular_samples=16, brdf_lut_size=32))
+    yield s
+    s.close()
+
+
+@pytest.mark.parametrize("tile", [16, 64])
+@pytest.mark.parametrize("dist", [4.0, 6.0])
+def test_large_triangles_sequential_regions(big_tris, tile, dist):
+    # Icosahedra seen from close by: triangles hundreds of pixels across, so
+    # edge values leave the exact-integer range (2^24) inside many 16-px
+    # blocks and those regions replay the reference's sequential additions
+    # (about half of the quads at distance 4, a fifth at 6).
+    c = np.array(big_tris.info().bounds_center[:])
+    cam = swr.make_camera((float(c[0]), float(c[1]) + 0.5, float(c[2]) + dist), (float(c[0]), float(c[1]), float(c[2])),
+                          1.0, 1024, 768, 100.0)
+    compare(big_tris, cam, 1024, 768, sched_tile=tile)
+
+
+def test_auto_sched_tile(small):
+    # sched_tile 0: the largest tile that still gives >= 8 tiles per SM.
+    cam = swr.make_camera(*scenes.default_camera_params(small.info(), 320, 200))
+    for (w, h) in [(3840, 2160), (320, 200)]:
+        r = swr.Renderer(w, h)
+        r.render(small, cam, 0.0)
+        r.sync()
+        st = r.stats().sched_tile
+        r.close()
+        assert st in (16, 32, 64)
+        if (w, h) == (320, 200):
+            assert st == 16
+
+
 def test_camera_inside_scene_clips(small):
     # Camera among the spheres: primitives straddle the near and side planes.
     info = small.info()
