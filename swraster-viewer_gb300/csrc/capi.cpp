@@ -204,6 +204,8 @@ swr_status swr_renderer_create(int32_t width, int32_t height, const swr_renderer
     chk(cudaHostAlloc((void**)&r->h_status, sizeof(uint32_t), cudaHostAllocDefault));
     if (e == cudaSuccess) chk(cudaHostGetDevicePointer((void**)&r->d_expo, r->h_expo, 0));
     chk(cudaEventCreateWithFlags(&r->expo_done, cudaEventDisableTiming));
+    chk(cudaHostAlloc((void**)&r->h_counters, sizeof(DCounters), cudaHostAllocDefault));
+    chk(cudaEventCreateWithFlags(&r->status_ev, cudaEventDisableTiming));
     if (e != cudaSuccess) {
         swr_renderer_destroy(r);
         return cuda_fail(e, "renderer allocation");
@@ -225,6 +227,8 @@ void swr_renderer_destroy(swr_renderer* r) {
     if (r->h_expo) cudaFreeHost(r->h_expo);
     if (r->h_status) cudaFreeHost(r->h_status);
     if (r->expo_done) cudaEventDestroy(r->expo_done);
+    if (r->h_counters) cudaFreeHost(r->h_counters);
+    if (r->status_ev) cudaEventDestroy(r->status_ev);
     for (auto& set : r->prof_ev)
         for (cudaEvent_t& e : set)
             if (e) cudaEventDestroy(e);
@@ -317,9 +321,38 @@ swr_status enqueue_frame(swr_renderer* r, const swr_scene* scene, const swr_came
         cudaEventRecord(r->expo_done, stream);
         r->expo_pending = true;
     }
+    cudaMemcpyAsync(r->h_counters, r->eng.counters.p, sizeof(DCounters), cudaMemcpyDeviceToHost, stream);
+    cudaEventRecord(r->status_ev, stream);
+    r->status_pending = true;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
     r->last_args = a;
+    return SWR_OK;
+}
+
+void grow_for_overflow(swr_renderer* r, const DCounters& c) {
+    if (c.status & ST_BIN_OVERFLOW) r->eng.bin_cap = std::max<uint64_t>(r->eng.bin_cap * 2, c.pairs + c.pairs / 4);
+    if (c.status & ST_CLIP_OVERFLOW)
+        r->eng.extra_cap = std::max<uint64_t>(r->eng.extra_cap * 2, (uint64_t)c.extra_used + c.extra_used / 4);
+}
+
+// Before a new frame replaces the last one: if the last frame's counters are
+// already back, grow what overflowed; never waits.
+swr_status poll_frame(swr_renderer* r) {
+    if (r->checked || !r->status_pending) return SWR_OK;
+    const cudaError_t e = cudaEventQuery(r->status_ev);
+    if (e == cudaErrorNotReady) {
+        cudaGetLastError();
+        return SWR_OK;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "frame execution");
+    r->status_pending = false;
+    const DCounters c = *r->h_counters;
+    r->eng.last = c;
+    if (c.status & (ST_BIN_OVERFLOW | ST_CLIP_OVERFLOW | ST_QUEUE_OVERFLOW)) {
+        grow_for_overflow(r, c);
+        r->eng.retries++;
+    }
     return SWR_OK;
 }
 
@@ -337,9 +370,7 @@ swr_status check_frame(swr_renderer* r) {
             r->checked = true;
             return SWR_OK;
         }
-        if (c.status & ST_BIN_OVERFLOW) r->eng.bin_cap = std::max<uint64_t>(r->eng.bin_cap * 2, c.pairs + c.pairs / 4);
-        if (c.status & ST_CLIP_OVERFLOW)
-            r->eng.extra_cap = std::max<uint64_t>(r->eng.extra_cap * 2, (uint64_t)c.extra_used + c.extra_used / 4);
+        grow_for_overflow(r, c);
         r->eng.retries++;
         // The overflowed frame's exposure step was skipped by the callback.
         swr_status st = enqueue_frame(r, r->last_scene, &r->last_cam, r->last_dt, r->last_stream);
@@ -354,7 +385,9 @@ swr_status swr_render_frame(swr_renderer* r, const swr_scene* scene, const swr_c
     if (!r || !scene || !cam) return fail(SWR_INVALID_ARG, "null argument");
     if (!scene->impl.d_scene) return fail(SWR_INVALID_ARG, "scene was created host-only");
     if (!(dt >= 0.0f) && !(dt < 0.0f)) return fail(SWR_INVALID_ARG, "dt is NaN");
-    swr_status st = check_frame(r);
+    // The previous frame is replaced, so it is not waited for: a frame is
+    // checked (and re-rendered after an overflow) when its result is read.
+    swr_status st = poll_frame(r);
     if (st != SWR_OK) return st;
     r->last_scene = scene;
     r->last_cam = *cam;

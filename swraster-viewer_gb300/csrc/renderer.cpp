@@ -323,10 +323,14 @@ swr_status FrameEngine::prepare(const std::vector<const SceneImpl*>& scenes, std
 }
 
 swr_status FrameEngine::launch(cudaStream_t stream, cudaEvent_t* ev, std::string& err) {
-    cudaError_t e = cudaSuccess;
-    if (use_graph && !ev) {
-        const bool same = graph_exec && graph_stage == h_stage.p && graph_bytes == lay.total &&
-                          std::memcmp(&graph_args, &args, sizeof(args)) == 0;
+    // The staging copy runs ahead of the kernels (graph or not) and is the
+    // only reader of h_stage: once it is done the host may stage the next
+    // frame while this one renders.
+    cudaError_t e = cudaMemcpyAsync(tables.p, h_stage.p, lay.total, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaEventRecord(stage_done, stream);
+    if (e == cudaSuccess) stage_pending = true;
+    if (e == cudaSuccess && use_graph && !ev) {
+        const bool same = graph_exec && std::memcmp(&graph_args, &args, sizeof(args)) == 0;
         if (!same) {
             if (graph_exec) cudaGraphExecDestroy(graph_exec);
             graph_exec = nullptr;
@@ -336,7 +340,6 @@ swr_status FrameEngine::launch(cudaStream_t stream, cudaEvent_t* ev, std::string
             // into the caller's stream (which may be the legacy default one).
             if (e == cudaSuccess) e = cudaStreamBeginCapture(capture_stream, cudaStreamCaptureModeThreadLocal);
             if (e == cudaSuccess) {
-                cudaMemcpyAsync(tables.p, h_stage.p, lay.total, cudaMemcpyHostToDevice, capture_stream);
                 launch_frame(args, capture_stream, num_sms, nullptr);
                 e = cudaStreamEndCapture(capture_stream, &g);
             }
@@ -350,16 +353,12 @@ swr_status FrameEngine::launch(cudaStream_t stream, cudaEvent_t* ev, std::string
             }
             graph_args = args;
             graph_stream = stream;
-            graph_stage = h_stage.p;
-            graph_bytes = lay.total;
         }
         e = cudaGraphLaunch(graph_exec, stream);
-    } else {
-        e = cudaMemcpyAsync(tables.p, h_stage.p, lay.total, cudaMemcpyHostToDevice, stream);
-        if (e == cudaSuccess) launch_frame(args, stream, num_sms, ev);
+    } else if (e == cudaSuccess) {
+        launch_frame(args, stream, num_sms, ev);
+        e = cudaGetLastError();
     }
-    if (e == cudaSuccess) e = cudaEventRecord(stage_done, stream);
-    stage_pending = true;
     if (e != cudaSuccess) {
         err = std::string("frame launch failed: ") + cudaGetErrorString(e);
         cudaGetLastError();

@@ -93,8 +93,6 @@ struct FrameEngine {
     FrameArgs graph_args{};
     cudaStream_t graph_stream = nullptr;
     cudaStream_t capture_stream = nullptr;  // legacy default streams cannot be captured
-    const void* graph_stage = nullptr;  // the capture bakes in the staging copy's source and size
-    size_t graph_bytes = 0;
 
     swr_status init(std::string& err);
     void release();
@@ -154,6 +152,11 @@ struct swr_renderer {
     cudaStream_t last_stream = nullptr;
     bool have_frame = false;
     bool checked = true;
+    // Counters of the last frame, copied back asynchronously so the next
+    // frame can adapt capacities without waiting for this one.
+    swr::DCounters* h_counters = nullptr;
+    cudaEvent_t status_ev = nullptr;
+    bool status_pending = false;
     swr::FrameArgs last_args{};
     uint32_t tiles_x = 0, tiles_y = 0;
     // Stage profiling: a ring of event sets, one per in-flight frame.
