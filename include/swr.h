@@ -501,6 +501,11 @@ swr_status swr_server_get_stats(swr_server* s, swr_server_stats* out);
  * memory `dst`, ordered on `stream`; returns when the copy is done. */
 swr_status swr_copy_to_host(void* dst, const void* src_device, size_t bytes, void* stream);
 
+/* Numerics self-test: the device reciprocal square root of `n` host values
+ * in the given SWR_RSQRT_* mode (the arithmetic every normalize of the
+ * shading pass uses, src/math.rs:17-49), written to host `out`. */
+swr_status swr_selftest_rsqrt(const float* in, float* out, uint64_t n, uint32_t rsqrt_mode);
+
 /* Allocation-free frame. No counterpart in the reference: an addition for
  * callers that cannot allocate device memory while they render (code running
  * under CUDA stream capture, processes whose device memory belongs to another

@@ -509,4 +509,27 @@ swr_status swr_renderer_get_tile_luminance(swr_renderer* r, float* out, uint32_t
     return SWR_OK;
 }
 
+
+swr_status swr_selftest_rsqrt(const float* in, float* out, uint64_t n, uint32_t rsqrt_mode) {
+    if ((!in || !out) && n > 0) return fail(SWR_INVALID_ARG, "null argument");
+    if (rsqrt_mode > SWR_RSQRT_AARCH64) return fail(SWR_INVALID_ARG, "bad rsqrt_mode");
+    if (n == 0) return SWR_OK;
+    uint8_t tab[512];
+    build_rsqrt_table(tab);
+    void* d = nullptr;
+    const size_t bytes = (size_t)n * sizeof(float);
+    cudaError_t e = cudaMalloc(&d, 2 * bytes + 512);
+    if (e != cudaSuccess) return cuda_fail(e, "self-test allocation");
+    float* din = static_cast<float*>(d);
+    float* dout = din + n;
+    uint8_t* dtab = reinterpret_cast<uint8_t*>(dout + n);
+    e = cudaMemcpy(din, in, bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dtab, tab, 512, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = launch_rsqrt_selftest(din, dout, n, rsqrt_mode, dtab);
+    if (e == cudaSuccess) e = cudaMemcpy(out, dout, bytes, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_fail(e, "self-test");
+    return SWR_OK;
+}
+
 }  // extern "C"

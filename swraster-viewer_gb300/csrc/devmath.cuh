@@ -66,7 +66,7 @@ __device__ __forceinline__ float rsqrt_ieee(float x) { return __fdiv_rn(1.0f, __
 // FRSQRTE (single precision, FPCR.AH = 0): 8-bit estimate from the Arm
 // architecture's RecipSqrtEstimate, table-driven. `tab` holds estimate<7:0>
 // for the 9-bit scaled operand (128..511).
-__device__ __forceinline__ float frsqrte(float x, const uint8_t* tab) {
+__device__ __noinline__ float frsqrte_special(float x, const uint8_t* tab) {
     const uint32_t b = __float_as_uint(x);
     if (x != x) return __uint_as_float(b | 0x00400000u);
     if (x == 0.0f) return __uint_as_float((b & 0x80000000u) | 0x7F800000u);
@@ -90,8 +90,20 @@ __device__ __forceinline__ float frsqrte(float x, const uint8_t* tab) {
     const uint32_t est = tab[scaled];
     return __uint_as_float(((uint32_t)(rexp & 0xFF) << 23) | (est << 15));
 }
+__device__ __forceinline__ float frsqrte(float x, const uint8_t* tab) {
+    const uint32_t b = __float_as_uint(x);
+    const uint32_t e = b >> 23;  // sign bit included: negative inputs leave the fast path
+    if (e - 1u < 254u) {         // positive normal: fraction<51:44> / <51:45> are mantissa bits
+        const uint32_t m = b & 0x7FFFFFu;
+        const uint32_t scaled = (e & 1u) ? (128u | (m >> 16)) : (256u | (m >> 15));
+        const uint32_t rexp = (380u - e) >> 1;
+        return __uint_as_float((rexp << 23) | ((uint32_t)tab[scaled] << 15));
+    }
+    return frsqrte_special(x, tab);
+}
 // FRSQRTS: (3 - a*b) / 2 with a single rounding.
 __device__ __forceinline__ float frsqrts(float a, float b) {
+    if (isfinite(a) && isfinite(b)) return __fmul_rn(__fmaf_rn(-a, b, 3.0f), 0.5f);
     if (a != a) return a;
     if (b != b) return b;
     const bool ia = isinf(a), ib = isinf(b);

@@ -56,6 +56,10 @@ struct alignas(16) DTexture {
     uint32_t array_stride[16];
     float mip_wf[16];
     float mip_hf[16];
+    // 1 / mip_wf (1 / mip_hf) when that size is a power of two, else 0: a
+    // division by 2^k and a multiplication by 2^-k round the same exact value.
+    float mip_rwf[16];
+    float mip_rhf[16];
 };
 
 enum : uint32_t {
@@ -245,6 +249,8 @@ struct FrameArgs {
 void launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t* ev = nullptr);
 void launch_reset(const FrameArgs& a, void* stream);
 void launch_resolve(const FrameArgs& a, void* stream);
+// rsqrt of n device values in the given mode (table: the 512-byte FRSQRTE table).
+cudaError_t launch_rsqrt_selftest(const float* in, float* out, uint64_t n, uint32_t mode, const uint8_t* table);
 // Per-device constant tables; call once per device outside stream capture.
 cudaError_t init_kernel_constants();
 // Persistent raster / grid-stride shading grid sizes for this device.

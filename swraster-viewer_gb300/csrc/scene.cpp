@@ -994,6 +994,9 @@ DTexture to_dtex(const HTexture& t, uintptr_t addr) {
         d.array_stride[m] = t.array_stride[m];
         d.mip_wf[m] = t.mip_widths_f[m];
         d.mip_hf[m] = t.mip_heights_f[m];
+        const uint32_t w = t.mip_widths[m], h = t.mip_heights[m];
+        d.mip_rwf[m] = (w > 0 && (w & (w - 1)) == 0 && (float)w == d.mip_wf[m]) ? 1.0f / (float)w : 0.0f;
+        d.mip_rhf[m] = (h > 0 && (h & (h - 1)) == 0 && (float)h == d.mip_hf[m]) ? 1.0f / (float)h : 0.0f;
     }
     return d;
 }

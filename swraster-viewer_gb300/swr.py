@@ -174,6 +174,7 @@ EXPORTS = [
     "swr_batch_create", "swr_batch_destroy", "swr_batch_render", "swr_batch_sync", "swr_batch_output",
     "swr_batch_autotune", "swr_batch_last_ms", "swr_server_create", "swr_server_destroy", "swr_server_add_scene",
     "swr_server_submit", "swr_server_poll", "swr_server_release", "swr_server_get_stats", "swr_copy_to_host",
+    "swr_selftest_rsqrt",
 ]
 STAGES = ["reset", "frontend", "clip", "scan", "scatter", "raster", "shade", "resolve"]
 
@@ -209,6 +210,7 @@ def lib():
         "swr_renderer_get_tile_luminance": ([vp, f32p, C.c_uint32], C.c_int),
         "swr_renderer_set_profiling": ([vp, C.c_int32], C.c_int),
         "swr_renderer_get_profile": ([vp, f32p, C.c_int32, C.POINTER(C.c_uint32)], C.c_int),
+        "swr_selftest_rsqrt": ([f32p, f32p, C.c_uint64, C.c_uint32], C.c_int),
         "swr_render_frame_noalloc": ([vp, C.POINTER(Camera), C.c_int32, C.c_int32, C.c_float, C.c_uint32, vp, vp, vp],
                                      C.c_int),
         "swr_batch_create": ([C.POINTER(BatchOpts), C.POINTER(vp)], C.c_int),
@@ -434,6 +436,14 @@ class Renderer:
             self.close()
         except Exception:
             pass
+
+
+def selftest_rsqrt(values, mode=RSQRT_AARCH64):
+    """Device reciprocal square root of `values` (float32) in the given mode."""
+    x = np.ascontiguousarray(values, np.float32)
+    out = np.empty_like(x)
+    check(lib().swr_selftest_rsqrt(x.ctypes.data_as(f32p), out.ctypes.data_as(f32p), x.size, mode))
+    return out
 
 
 def copy_device_to_host(dev_ptr, nbytes, out, stream=None):

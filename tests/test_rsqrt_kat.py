@@ -72,3 +72,21 @@ def test_emulation_matches_arm_hardware():
             if bad < 5:
                 print("mismatch x=%r emu=(%r, %r) hw=(%r, %r)" % (x, e, r, he, hr))
     assert bad == 0, "%d of %d inputs differ from the hardware" % (bad, len(xs))
+
+
+@pytest.mark.gpu
+def test_device_rsqrt_matches_oracle():
+    # The shading pass's normalize arithmetic on the device, bit for bit
+    # against the oracle's restatement (Arm mode) and IEEE 1/sqrt (IEEE mode).
+    import swr
+    L = oracle.lib()
+    xs = _inputs()
+    dev = swr.selftest_rsqrt(xs, swr.RSQRT_AARCH64)
+    ref = np.array([L.oracle_rsqrt_aarch64(float(x)) for x in xs], np.float32)
+    same = (dev.view(np.uint32) == ref.view(np.uint32)) | (np.isnan(dev) & np.isnan(ref))
+    assert same.all(), "%d of %d differ, first x=%r" % ((~same).sum(), xs.size, xs[~same][:3])
+    dev = swr.selftest_rsqrt(xs, swr.RSQRT_IEEE)
+    with np.errstate(all="ignore"):
+        ref = np.float32(1.0) / np.sqrt(xs)
+    same = (dev.view(np.uint32) == ref.view(np.uint32)) | (np.isnan(dev) & np.isnan(ref))
+    assert same.all(), "%d of %d differ (IEEE)" % ((~same).sum(), xs.size)
