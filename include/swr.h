@@ -381,6 +381,7 @@ typedef struct swr_frame_stats {
     float tile_luminance_mean;
     float exposure;
     uint32_t sched_tile;        /* scheduling tile the renderer uses */
+    uint64_t staged_bytes;      /* host-to-device bytes per frame (draw and chunk tables) */
 } swr_frame_stats;
 
 swr_status swr_renderer_get_stats(swr_renderer* r, swr_frame_stats* out);

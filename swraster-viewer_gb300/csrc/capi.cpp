@@ -472,6 +472,7 @@ swr_status swr_renderer_get_stats(swr_renderer* r, swr_frame_stats* o) {
     o->overflow_retries = r->eng.retries;
     o->exposure = r->expo.exposure;
     o->sched_tile = r->opts.sched_tile;
+    o->staged_bytes = r->eng.lay.total;
     return SWR_OK;
 }
 
