@@ -517,7 +517,8 @@ swr_status swr_selftest_rsqrt(const float* in, float* out, uint64_t n, uint32_t 
  * renderer's) and without allocating anything: all per-frame work buffers
  * live in one fixed __device__ array of about 9 MB. Limits: width, height
  * <= 512, at most 16384 triangles passing the frustum test, 4096 nodes, 4096
- * draws, 65536 (triangle, tile) pairs; larger inputs return SWR_INVALID_ARG,
+ * draws, 65536 (triangle, tile) pairs, no translucent primitives; larger
+ * inputs return SWR_INVALID_ARG,
  * capacity overflow on the device returns SWR_OVERFLOW. Returns after the
  * frame has finished. The first call on each device looks up the array's
  * address and must come before any stream capture; all calls share the array,

@@ -19,9 +19,11 @@
 // multiply and an add; this file must be compiled with -ffp-contract=off),
 // tiles of 64x64 pixels hold 2x2-quad buffers (color, depth, packet index,
 // barycentrics), packets are queued per tile in the canonical sequential order
-// (node rank after the stable distance sort, opaque primitive, triangle, fan)
-// when run single-threaded, and in rayon-like nondeterministic order when run
-// multi-threaded (the timed CPU baseline).
+// (node rank after the stable distance sort, primitive — a mesh's opaque
+// primitives before its translucent ones — triangle, fan) when run
+// single-threaded, and in rayon-like nondeterministic order when run
+// multi-threaded (the timed CPU baseline). Translucent packets are sorted back
+// to front per tile by average clip z, equal keys in queue order.
 #include <algorithm>
 #include <atomic>
 #include <cmath>
@@ -473,6 +475,7 @@ struct Packet {
     uint32_t material;
     float du_dv[4];
     uint32_t static_id, fan;
+    float avg_z;  // translucent packets: mean clip-space z of the three vertices
 };
 
 constexpr int TILE = 64;
@@ -503,7 +506,7 @@ struct Queue {
 struct Tile {
     IV2 smin, smax;
     uint64_t quads_tested = 0, fragments = 0, depth_passed = 0;
-    Queue opaque;
+    Queue opaque, translucent;
     std::vector<V3x4> color;
     std::vector<F4> depth;
     std::vector<uint32_t> pidx;  // 4 per quad
@@ -532,8 +535,8 @@ static IV2 to_screen(const Frame& f, const float* v) {
     return {as_i32(std::round(sx * 16.0f)), as_i32(std::round(sy * 16.0f))};
 }
 
-// bin_triangle (src/renderer.rs:668-831), opaque mode.
-static void bin_triangle(Frame& f, const Vertex* v, uint32_t material, uint32_t static_id, uint32_t fan) {
+// bin_triangle (src/renderer.rs:668-831); MODE_OPAQUE selects the queue.
+static void bin_triangle(Frame& f, const Vertex* v, uint32_t material, uint32_t static_id, uint32_t fan, bool opaque) {
     const IV2 p0 = to_screen(f, v[0].pos_clip), p1 = to_screen(f, v[1].pos_clip), p2 = to_screen(f, v[2].pos_clip);
     const int32_t area = wsub(wmul(wsub(p1.x, p0.x), wsub(p2.y, p0.y)), wmul(wsub(p2.x, p0.x), wsub(p1.y, p0.y)));
     if (area > 0) return;
@@ -577,6 +580,8 @@ static void bin_triangle(Frame& f, const Vertex* v, uint32_t material, uint32_t 
     pk.material = material;
     pk.static_id = static_id;
     pk.fan = fan;
+    // Average z for the per-tile translucency sort (src/renderer.rs:765-774).
+    pk.avg_z = opaque ? 0.0f : ((v[0].pos_clip[2] + v[1].pos_clip[2]) + v[2].pos_clip[2]) / 3.0f;
     const int32_t bx0 = mnp.x / TILE, by0 = mnp.y / TILE;
     const int32_t bx1 = (mxp.x + TILE - 1) / TILE, by1 = (mxp.y + TILE - 1) / TILE;
     const int32_t ntiles = (int32_t)f.tiles.size();
@@ -590,13 +595,16 @@ static void bin_triangle(Frame& f, const Vertex* v, uint32_t material, uint32_t 
             if (cmax.x - cmin.x < 1 || cmax.y - cmin.y < 1) continue;
             pk.min = cmin;
             pk.max = cmax;
-            t->opaque.push(pk);
+            if (opaque)
+                t->opaque.push(pk);
+            else
+                t->translucent.push(pk);
         }
     }
 }
 
 // clip_against_frustum (src/renderer.rs:579-665).
-static void clip_triangle(Frame& f, const Vertex* tri, uint32_t material, uint32_t static_id) {
+static void clip_triangle(Frame& f, const Vertex* tri, uint32_t material, uint32_t static_id, bool opaque) {
     static const float planes[6][4] = {{0, 0, 1, 1}, {0, 0, -1, 1}, {1, 0, 0, 1},
                                        {-1, 0, 0, 1}, {0, 1, 0, 1}, {0, -1, 0, 1}};
     Vertex poly[16], np[16];
@@ -633,13 +641,13 @@ static void clip_triangle(Frame& f, const Vertex* tri, uint32_t material, uint32
     if (len < 3) return;
     for (int i = 1; i < len - 1; ++i) {
         const Vertex t3[3] = {poly[0], poly[i], poly[i + 1]};
-        bin_triangle(f, t3, material, static_id, (uint32_t)(i - 1));
+        bin_triangle(f, t3, material, static_id, (uint32_t)(i - 1), opaque);
     }
 }
 
 // render_primitive_inner (src/renderer.rs:470-574) for one triangle.
 static void process_triangle(Frame& f, const swr_primitive_view& p, const float* model, const float* mvp, bool clip,
-                             uint32_t t, uint32_t static_base) {
+                             uint32_t t, uint32_t static_base, bool opaque) {
     Vertex v[3];
     for (int k = 0; k < 3; ++k) {
         const uint32_t i = p.indices[3 * t + k];
@@ -659,9 +667,9 @@ static void process_triangle(Frame& f, const swr_primitive_view& p, const float*
         v[k].uv[1] = p.texcoords[2 * (size_t)i + 1];
     }
     if (clip)
-        clip_triangle(f, v, p.material, static_base + t);
+        clip_triangle(f, v, p.material, static_base + t, opaque);
     else
-        bin_triangle(f, v, p.material, static_base + t, 0);
+        bin_triangle(f, v, p.material, static_base + t, 0, opaque);
 }
 
 // ---------------------------------------------------------------- tilerasterizer.rs
@@ -676,8 +684,13 @@ struct Edges {
     F4 sx01, sx12, sx20, sy01, sy12, sy20;
 };
 
+static V3x4 pbr_shader(const Frame& f, const Packet& pk, F4 b1, F4 b2, bool translucent, const V3x4* cur);
+
+// fine_raster (src/tilerasterizer.rs:293-383) with VBufferOpaqueShader
+// (src/shader.rs:32-63) or, for translucent packets, TranslucentForwardShader
+// (src/shader.rs:66-76).
 static void fine_raster(const Frame& f, Tile& t, const Packet& pk, const Edges& e, size_t packet_index, int32_t xs,
-                        int32_t ys, int32_t xe, int32_t ye) {
+                        int32_t ys, int32_t xe, int32_t ye, bool translucent) {
     const swr_material_view& mat = f.s->materials[pk.material];
     const F4 x = mk((float)(xs + 8), (float)(xs + 24), (float)(xs + 8), (float)(xs + 24));
     const F4 y = mk((float)(ys + 8), (float)(ys + 8), (float)(ys + 24), (float)(ys + 24));
@@ -711,7 +724,13 @@ static void fine_raster(const Frame& f, Tile& t, const Packet& pk, const Edges& 
                     anyp |= fm[i];
                     t.depth_passed += fm[i] ? 1 : 0;
                 }
-                if (anyp) {
+                if (anyp && translucent) {
+                    // TranslucentForwardShader::shade: blend over the tile colour,
+                    // no depth write.
+                    const V3x4 cur = t.color[qi];
+                    const V3x4 c = pbr_shader(f, pk, b1, b2, true, &cur);
+                    t.color[qi] = v3select(fm, c, cur);
+                } else if (anyp) {
                     // VBufferOpaqueShader::shade (src/shader.rs:32-63).
                     if (mat.is_alpha_tested) {
                         const Tex tx = texof(f, mat, 0);
@@ -739,7 +758,7 @@ static void fine_raster(const Frame& f, Tile& t, const Packet& pk, const Edges& 
 }
 
 // rasterize_packet + coarse_raster (src/tilerasterizer.rs:114-291).
-static void rasterize_packet(const Frame& f, Tile& t, const Packet& pk, size_t packet_index) {
+static void rasterize_packet(const Frame& f, Tile& t, const Packet& pk, size_t packet_index, bool translucent) {
     const IV2 p0 = pk.p[0], p1 = pk.p[1], p2 = pk.p[2];
     auto bias = [](int32_t a, int32_t b) { return (a < 0 || (a == 0 && b > 0)) ? 0 : -1; };
     const int32_t a01 = wsub(p1.y, p0.y), b01 = wsub(p0.x, p1.x);
@@ -767,16 +786,18 @@ static void rasterize_packet(const Frame& f, Tile& t, const Packet& pk, size_t p
                 const F4 w2c = (e.a01 * cx + e.b01 * cy) + e.c01;
                 auto maxel = [](F4 v) { return std::fmax(std::fmax(v.l[0], v.l[1]), std::fmax(v.l[2], v.l[3])); };
                 if (maxel(w0c) < 0.0f || maxel(w1c) < 0.0f || maxel(w2c) < 0.0f) continue;
-                fine_raster(f, t, pk, e, packet_index, bx, by, std::min(bx + 256, xe), std::min(by + 256, ye));
+                fine_raster(f, t, pk, e, packet_index, bx, by, std::min(bx + 256, xe), std::min(by + 256, ye),
+                            translucent);
             }
         }
     } else {
-        fine_raster(f, t, pk, e, packet_index, xs, ys, xe, ye);
+        fine_raster(f, t, pk, e, packet_index, xs, ys, xe, ye, translucent);
     }
 }
 
-// pbr_shader<false> (src/shader.rs:110-309).
-static V3x4 pbr_shader(const Frame& f, const Packet& pk, F4 b1, F4 b2) {
+// pbr_shader<TRANSLUCENT> (src/shader.rs:110-309); cur is the tile colour
+// under a translucent fragment.
+static V3x4 pbr_shader(const Frame& f, const Packet& pk, F4 b1, F4 b2, bool translucent, const V3x4* cur) {
     const swr_material_view& m = f.s->materials[pk.material];
     const float PI = 3.14159265358979f;
     const F4 EPS = splat(1e-6f);
@@ -865,7 +886,16 @@ static V3x4 pbr_shader(const Frame& f, const Packet& pk, F4 b1, F4 b2) {
     V3x4 cis = env * bsf;
     const F4 ao_spec = 1.0f + (ao - 1.0f) * 0.5f;
     cis = cis * (ao_spec * skyv);
-    V3x4 color = ((cdd + cds) + cid) + cis;
+    V3x4 color;
+    if (translucent) {
+        F4 tr = splat(m.transmission);
+        if (m.tex[5] >= 0) tr = tr * sample4_rgb(texof(f, m, 5), uvx, uvy, du_dv).x;
+        tr = vclamp(tr, splat(0.0f), splat(1.0f));
+        const F4 inv = 1.0f - tr;
+        color = ((((*cur) * bc) * tr + (cdd + cid) * inv) + cds) + cis;
+    } else {
+        color = ((cdd + cds) + cid) + cis;
+    }
     V3x4 em = v3splat(1.0f);
     if (m.tex[3] >= 0) em = srgb_fast(sample4_rgb(texof(f, m, 3), uvx, uvy, du_dv));
     color = color + em * v3f(m.emissive_factor[0], m.emissive_factor[1], m.emissive_factor[2]);
@@ -925,7 +955,7 @@ static void shade_vbuffer(const Frame& f, Tile& t, bool skybox_only) {
                     B4 mask;
                     for (int i = 0; i < 4; ++i) mask[i] = pi[i] == p;
                     const Packet& pk = t.opaque.get(p);
-                    const V3x4 c = pbr_shader(f, pk, t.bary1[qi], t.bary2[qi]);
+                    const V3x4 c = pbr_shader(f, pk, t.bary1[qi], t.bary2[qi], false, nullptr);
                     out = v3select(mask, c, out);
                     for (int i = 0; i < 4; ++i) rem[i] = rem[i] && !mask[i];
                 }
@@ -936,12 +966,31 @@ static void shade_vbuffer(const Frame& f, Tile& t, bool skybox_only) {
     }
 }
 
-// render_tile (src/tilerasterizer.rs:72-111), opaque path.
+// The translucency sort's order (src/tilerasterizer.rs:92-95): OrderedFloat
+// avg_z, back to front (NaN is the largest value, -0 equals +0). The
+// reference's in-place quicksort is unstable over a rayon-ordered queue, so
+// equal keys have no defined order there; here they keep submission order.
+static bool translucent_before(float a, float b) {
+    if (a != a) return !(b != b);
+    if (b != b) return false;
+    return a > b;
+}
+
+// render_tile (src/tilerasterizer.rs:72-111).
 static void render_tile(const Frame& f, Tile& t) {
     for (F4& d : t.depth) d = splat(INFINITY);
     const size_t n = t.opaque.size();
-    for (size_t i = 0; i < n; ++i) rasterize_packet(f, t, t.opaque.get(i), i);
+    for (size_t i = 0; i < n; ++i) rasterize_packet(f, t, t.opaque.get(i), i, false);
     shade_vbuffer(f, t, n == 0);
+    const size_t nt = t.translucent.size();
+    if (nt > 0) {
+        std::vector<size_t> order(nt);
+        std::iota(order.begin(), order.end(), (size_t)0);
+        std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+            return translucent_before(t.translucent.get(a).avg_z, t.translucent.get(b).avg_z);
+        });
+        for (size_t k = 0; k < nt; ++k) rasterize_packet(f, t, t.translucent.get(order[k]), order[k], true);
+    }
     const V3x4 cq = t.color[t.color.size() / 2];
     const F4 lx = (cq.x * 0.2126f + cq.y * 0.7152f) + cq.z * 0.0722f;
     t.center_luminance = (((lx.l[0] + lx.l[1]) + lx.l[2]) + lx.l[3]) * 0.25f;
@@ -1051,6 +1100,7 @@ int oracle_render(const swr_scene_host_view* s, const swr_camera* cam, int32_t w
         const float* model;
         bool clip;
         uint32_t t0, t1, static_base;
+        bool opaque;
     };
     std::vector<Item> items;
     uint64_t tri_in = 0;
@@ -1060,8 +1110,11 @@ int oracle_render(const swr_scene_host_view* s, const swr_camera* cam, int32_t w
         // render_node: mvp = VP * model (src/renderer.rs:369-384).
         const M4 mvp = mat_mul(cam->view_project, n.transform);
         const swr_mesh_view& mesh = s->meshes[n.mesh];
-        for (uint32_t k = 0; k < mesh.opaque_count; ++k) {
-            const swr_primitive_view& p = s->primitives[mesh.primitives[mesh.opaque[k]]];
+        // render_mesh (src/renderer.rs:386-420): opaque primitives, then translucent.
+        for (uint32_t k = 0; k < mesh.opaque_count + mesh.translucent_count; ++k) {
+            const bool opaque = k < mesh.opaque_count;
+            const uint32_t local = opaque ? mesh.opaque[k] : mesh.translucent[k - mesh.opaque_count];
+            const swr_primitive_view& p = s->primitives[mesh.primitives[local]];
             // Mat4 * &BoundingSphere (src/scene.rs:53-63) and
             // test_sphere_frustum (src/renderer.rs:130-142).
             const float* M = n.transform;
@@ -1087,15 +1140,16 @@ int oracle_render(const swr_scene_host_view* s, const swr_camera* cam, int32_t w
             tri_in += nt;
             for (uint32_t t0 = 0; t0 < nt; t0 += 128)
                 items.push_back({&p, mvp, n.transform, result == 1, t0, std::min(nt, t0 + 128),
-                                 n.triangle_id_base + p.triangle_id_base});
+                                 n.triangle_id_base + p.triangle_id_base, opaque});
         }
     }
     par_for(items.size(), threads, [&](size_t i) {
         const Item& it = items[i];
-        for (uint32_t t = it.t0; t < it.t1; ++t) process_triangle(f, *it.p, it.model, it.mvp.m, it.clip, t, it.static_base);
+        for (uint32_t t = it.t0; t < it.t1; ++t)
+            process_triangle(f, *it.p, it.model, it.mvp.m, it.clip, t, it.static_base, it.opaque);
     });
     uint64_t packets = 0;
-    for (Tile* t : f.tiles) packets += t->opaque.size();
+    for (Tile* t : f.tiles) packets += t->opaque.size() + t->translucent.size();
     par_for(f.tiles.size(), threads, [&](size_t i) { render_tile(f, *f.tiles[i]); });
     // update_auto_exposure (src/renderer.rs:258-290).
     float ev = o->ev;

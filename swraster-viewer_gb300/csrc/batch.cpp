@@ -106,14 +106,15 @@ swr_status BatchImpl::sync(std::string& err) {
             return SWR_CUDA_ERROR;
         }
         eng.last = c;
-        if (!(c.status & (ST_BIN_OVERFLOW | ST_CLIP_OVERFLOW | ST_QUEUE_OVERFLOW))) {
+        if (!(c.status & kStRetry)) {
             pending = false;
             return SWR_OK;
         }
-        if (c.status & ST_BIN_OVERFLOW) eng.bin_cap = std::max<uint64_t>(eng.bin_cap * 2, c.pairs + c.pairs / 4);
-        if (c.status & ST_CLIP_OVERFLOW)
-            eng.extra_cap = std::max<uint64_t>(eng.extra_cap * 2, (uint64_t)c.extra_used + c.extra_used / 4);
-        eng.retries++;
+        swr_status gs = eng.grow_for(c, err);
+        if (gs != SWR_OK) {
+            pending = false;
+            return gs;
+        }
         std::vector<swr_view_desc> vd = saved;
         for (size_t i = 0; i < vd.size(); ++i) vd[i].camera = &saved_cams[i];
         swr_status st = enqueue(vd.data(), (int32_t)vd.size(), last_stream, err);

@@ -221,7 +221,6 @@ void swr_renderer_destroy(swr_renderer* r) {
     r->eng.release();
     r->rgba8.release();
     r->vis.release();
-    r->color.release();
     r->tile_lum.release();
     if (r->h_lum) cudaFreeHost(r->h_lum);
     if (r->h_expo) cudaFreeHost(r->h_expo);
@@ -259,7 +258,7 @@ void CUDART_CB exposure_callback(void* p) {
     swr_renderer* r = static_cast<swr_renderer*>(p);
     // A frame that overflowed its bins is re-rendered; it must not advance
     // the exposure state.
-    if (*r->h_status & (ST_BIN_OVERFLOW | ST_CLIP_OVERFLOW | ST_QUEUE_OVERFLOW)) return;
+    if (*r->h_status & kStRetry) return;
     r->expo.update(r->h_lum, (size_t)r->tiles_x * r->tiles_y, r->pending_dt);
     *r->h_expo = r->expo.exposure;
 }
@@ -275,7 +274,7 @@ swr_status enqueue_frame(swr_renderer* r, const swr_scene* scene, const swr_came
     std::vector<DView> views(1);
     DView& v = views[0];
     std::memset(&v, 0, sizeof(v));
-    init_view(v, *cam, r->width, r->height, r->opts.sched_tile);
+    init_view(v, *cam, r->width, r->height, r->eng.sched_tile);
     v.scene = 0;
     v.rsqrt_mode = r->opts.rsqrt_mode;
     v.rgba8 = r->rgba8.as<uint32_t>();
@@ -283,11 +282,9 @@ swr_status enqueue_frame(swr_renderer* r, const swr_scene* scene, const swr_came
     v.tile_lum = r->tile_lum.as<float>();
     v.out_pitch = (uint32_t)r->width;
     const bool deferred = dt > 0.0f;
+    r->eng.defer_resolve = deferred;
     if (deferred) {
-        if (r->color.ensure((size_t)r->width * r->height * 3 * sizeof(float)) != cudaSuccess)
-            return cuda_fail(cudaErrorMemoryAllocation, "colour buffer");
-        v.color = r->color.as<float>();
-        v.flags = 1u;
+        v.flags = kViewLinear;  // the engine provides the colour buffer
         v.exposure = 0.0f;
     } else {
         // update_auto_exposure with dt == 0 leaves ev unchanged: exposure = 2^ev.
@@ -330,10 +327,12 @@ swr_status enqueue_frame(swr_renderer* r, const swr_scene* scene, const swr_came
     return SWR_OK;
 }
 
-void grow_for_overflow(swr_renderer* r, const DCounters& c) {
-    if (c.status & ST_BIN_OVERFLOW) r->eng.bin_cap = std::max<uint64_t>(r->eng.bin_cap * 2, c.pairs + c.pairs / 4);
-    if (c.status & ST_CLIP_OVERFLOW)
-        r->eng.extra_cap = std::max<uint64_t>(r->eng.extra_cap * 2, (uint64_t)c.extra_used + c.extra_used / 4);
+swr_status grow_for_overflow(swr_renderer* r, const DCounters& c) {
+    std::string err;
+    const swr_status st = r->eng.grow_for(c, err);
+    r->opts.sched_tile = r->eng.sched_tile;
+    if (st != SWR_OK) return fail(st, err);
+    return SWR_OK;
 }
 
 // Before a new frame replaces the last one: if the last frame's counters are
@@ -349,10 +348,7 @@ swr_status poll_frame(swr_renderer* r) {
     r->status_pending = false;
     const DCounters c = *r->h_counters;
     r->eng.last = c;
-    if (c.status & (ST_BIN_OVERFLOW | ST_CLIP_OVERFLOW | ST_QUEUE_OVERFLOW)) {
-        grow_for_overflow(r, c);
-        r->eng.retries++;
-    }
+    if (c.status & kStRetry) return grow_for_overflow(r, c);
     return SWR_OK;
 }
 
@@ -365,13 +361,12 @@ swr_status check_frame(swr_renderer* r) {
         e = cudaMemcpy(&c, r->eng.counters.p, sizeof(c), cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) return cuda_fail(e, "counter readback");
         r->eng.last = c;
-        const uint32_t bad = c.status & (ST_BIN_OVERFLOW | ST_CLIP_OVERFLOW | ST_QUEUE_OVERFLOW);
-        if (!bad) {
+        if (!(c.status & kStRetry)) {
             r->checked = true;
             return SWR_OK;
         }
-        grow_for_overflow(r, c);
-        r->eng.retries++;
+        swr_status gs = grow_for_overflow(r, c);
+        if (gs != SWR_OK) return gs;
         // The overflowed frame's exposure step was skipped by the callback.
         swr_status st = enqueue_frame(r, r->last_scene, &r->last_cam, r->last_dt, r->last_stream);
         if (st != SWR_OK) return st;

@@ -118,16 +118,20 @@ struct alignas(16) DView {
     uint32_t quad_base;        // first shading quad of this view
     uint32_t quad_pitch;       // tiles_x * 32
     uint32_t rsqrt_mode;
-    uint32_t flags;            // 1: write linear colour instead of RGBA8
+    uint32_t flags;            // kViewLinear / kViewTranslucent: linear colour instead of RGBA8
     uint64_t key_offset;       // into the key buffer (u64 elements)
     uint64_t key_pitch;        // tiles_x * 64
     uint32_t* rgba8;           // width*height, row pitch out_pitch
     uint64_t* vis;             // width*height
-    float* color;              // width*height*3 when flags&1
+    float* color;              // key_pitch * tiles_y * 64 * 3 (padded tile grid) when flags != 0
     float* tile_lum;           // tiles_x*tiles_y
     uint32_t out_pitch;
     uint32_t pad2[3];
 };
+
+// DView.flags
+constexpr uint32_t kViewLinear = 1u;       // caller wants linear colour (exposure applied later)
+constexpr uint32_t kViewTranslucent = 2u;  // view has translucent draws: shade, blend, then resolve
 
 struct alignas(16) DDraw {
     float mvp[16];
@@ -139,6 +143,8 @@ struct alignas(16) DDraw {
     uint32_t tri_count;
     uint32_t static_base;      // static triangle ID of triangle 0
     uint32_t scene;
+    uint32_t translucent;      // primitive of a translucent material (mesh.primitives_translucent)
+    uint32_t pad[3];
 };
 
 struct DChunk {
@@ -146,8 +152,12 @@ struct DChunk {
     uint32_t tri_start;        // local to the draw
 };
 
-// RecRaster.material carries the alpha-test flag in its top bit.
+// RecRaster.material carries the alpha-test flag in its top bit and the
+// translucent flag below it; RecShade.pad[0] holds a translucent record's
+// average clip-space z (the sort key).
 constexpr uint32_t kRecAlphaBit = 0x80000000u;
+constexpr uint32_t kRecTransBit = 0x40000000u;
+constexpr uint32_t kRecMaterialMask = 0x3FFFFFFFu;
 
 // Raster-side triangle record (one per emitted, non-culled triangle).
 struct alignas(16) RecRaster {
@@ -182,7 +192,10 @@ enum : uint32_t {
     ST_CLIP_OVERFLOW = 2u,
     ST_QUEUE_OVERFLOW = 4u,
     ST_TIMEOUT = 8u,
+    ST_TRANS_OVERFLOW = 16u,   // a scheduling tile has more translucent packets than one sort holds
 };
+// Status bits after which a frame is incomplete and is rendered again.
+constexpr uint32_t kStRetry = ST_BIN_OVERFLOW | ST_CLIP_OVERFLOW | ST_QUEUE_OVERFLOW | ST_TRANS_OVERFLOW;
 
 // Frame-level counters (device).
 struct alignas(16) DCounters {
@@ -192,7 +205,9 @@ struct alignas(16) DCounters {
     uint32_t setup_tris;       // records written
     unsigned long long pairs;  // (triangle, tile) pairs counted
     uint32_t work_next;        // persistent raster work cursor
-    uint32_t pad[3];
+    uint32_t trans_next;       // translucent pass work cursor
+    uint32_t trans_packets;    // translucent (packet, tile) pairs
+    uint32_t pad;
 };
 
 // Per-frame counts, uploaded with the tables: kernels read them from device
@@ -205,7 +220,8 @@ struct alignas(16) DFrameDyn {
     uint32_t n_stiles;         // bins over all views
     uint32_t total_quads;      // shading work over all views
     uint32_t max_view_pixels;  // largest width * (height & ~1)
-    uint32_t pad[2];
+    uint32_t n_bins;           // n_stiles, or 2 * n_stiles with translucent bins after the opaque ones
+    uint32_t pad;
 };
 
 // Everything a frame's kernels need, passed by value: pointers and
@@ -232,9 +248,9 @@ struct FrameArgs {
     RecShade* rec_s;
     uint32_t* fan_base;
     uint2* clip_queue;         // (g, draw)
-    uint32_t* tile_count;      // n_stiles
-    uint32_t* tile_offset;     // n_stiles + 1
-    uint32_t* tile_cursor;     // n_stiles
+    uint32_t* tile_count;      // n_bins
+    uint32_t* tile_offset;     // n_bins + 1
+    uint32_t* tile_cursor;     // n_bins
     uint32_t* bins;
     unsigned long long* keys;
     DCounters* counters;
@@ -242,6 +258,8 @@ struct FrameArgs {
     const float* exposure_dev; // exposure computed by the host step (dt > 0)
     uint32_t raster_grid;      // persistent raster CTAs
     uint32_t shade_grid;       // grid-stride shading CTAs
+    uint32_t has_translucent;  // some view has translucent draws: run the translucent pass
+    uint32_t defer_resolve;    // the caller launches the resolve (exposure from the host step)
 };
 
 // Launch wrappers (kernels.cu). `ev`, when given, holds 8 events recorded

@@ -410,7 +410,10 @@ __device__ bool setup_triangle(const FrameArgs& a, const DView& view, const Vtx&
     q.pww[6] = px2 - px0; q.pww[7] = py2 - py0; q.pww[8] = pz2 - pz0;
     q.du_dv[0] = du_dx * s; q.du_dv[1] = du_dy * s; q.du_dv[2] = dv_dx * s; q.du_dv[3] = dv_dy * s;
     q.static_id = static_id;
-    q.pad[0] = q.pad[1] = q.pad[2] = 0;
+    // Average z for the per-tile translucency sort (src/renderer.rs:765-774).
+    const bool translucent = (material & kRecTransBit) != 0u;
+    q.pad[0] = translucent ? __float_as_uint(((v0.cz + v1.cz) + v2.cz) / 3.0f) : 0u;
+    q.pad[1] = q.pad[2] = 0;
 
     {
         const float4* src = reinterpret_cast<const float4*>(&r);
@@ -424,13 +427,14 @@ __device__ bool setup_triangle(const FrameArgs& a, const DView& view, const Vtx&
 #pragma unroll
         for (int i = 0; i < 11; ++i) dst[i] = src[i];
     }
-    for_each_stile(view, S, mnx, mny, mxx, mxy, [&](uint32_t st) { agg_inc(a.tile_count, st); });
+    const uint32_t bin_off = translucent ? a.dyn->n_stiles : 0u;
+    for_each_stile(view, S, mnx, mny, mxx, mxy, [&](uint32_t st) { agg_inc(a.tile_count, bin_off + st); });
     return true;
 }
 
 __global__ void k_reset(FrameArgs a) {
     const uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t n = a.dyn->n_stiles;
+    const uint32_t n = a.dyn->n_bins;
     for (uint32_t i = i0; i < n; i += gridDim.x * blockDim.x) a.tile_count[i] = 0u;
     if (i0 == 0) {
         a.counters->status = 0u;
@@ -439,7 +443,16 @@ __global__ void k_reset(FrameArgs a) {
         a.counters->setup_tris = 0u;
         a.counters->pairs = 0ull;
         a.counters->work_next = 0u;
+        a.counters->trans_next = 0u;
+        a.counters->trans_packets = 0u;
     }
+}
+
+// Record material word: translucent primitives (no alpha test on their path,
+// src/shader.rs:66-76) or opaque ones with the alpha-test flag.
+__device__ __forceinline__ uint32_t record_material(const DScene& sc, const DDraw& d, uint32_t material) {
+    if (d.translucent) return material | kRecTransBit;
+    return material | ((sc.materials[material].flags & MAT_ALPHA_TESTED) ? kRecAlphaBit : 0u);
 }
 
 __device__ __forceinline__ bool vtx_inside_all(const Vtx& v) {
@@ -476,7 +489,7 @@ __global__ void __launch_bounds__(kChunkTris) k_frontend(FrameArgs a) {
         return;
     }
     // All three vertices inside: the clipper would return the triangle unchanged.
-    const uint32_t mword = pr.material | ((sc.materials[pr.material].flags & MAT_ALPHA_TESTED) ? kRecAlphaBit : 0u);
+    const uint32_t mword = record_material(sc, d, pr.material);
     const bool ok = setup_triangle(a, view, v0, v1, v2, g, g << 3, d.static_base + local, mword, d.view);
     a.tri_state[g] = ok ? 1 : 0;
     warp_count(&a.counters->setup_tris, ok);
@@ -516,7 +529,7 @@ __global__ void __launch_bounds__(128) k_clip(FrameArgs a) {
         const DScene& sc = a.scenes[d.scene];
         const DView& view = a.views[d.view];
         const DPrimitive pr = sc.prims[d.prim];
-        const uint32_t mword = pr.material | ((sc.materials[pr.material].flags & MAT_ALPHA_TESTED) ? kRecAlphaBit : 0u);
+        const uint32_t mword = record_material(sc, d, pr.material);
         const float* model = sc.node_xform + 16u * d.node;
         const uint32_t* ib = sc.indices + pr.idx_base + 3u * local;
         Vtx poly[16], np[16];
@@ -574,7 +587,7 @@ __global__ void __launch_bounds__(128) k_clip(FrameArgs a) {
 // Exclusive scan of tile counts (single CTA). Also seeds the scatter cursors.
 __global__ void __launch_bounds__(1024) k_scan(FrameArgs a) {
     __shared__ uint32_t part[1024];
-    const uint32_t n = a.dyn->n_stiles;
+    const uint32_t n = a.dyn->n_bins;
     const uint32_t per = (n + 1023u) / 1024u;
     const uint32_t b = threadIdx.x * per;
     const uint32_t e = min(b + per, n);
@@ -617,7 +630,9 @@ __global__ void k_scatter(FrameArgs a) {
     }
     const RecRaster& r = a.rec_r[slot];
     const DView& view = a.views[r.view];
-    for_each_stile(view, (int32_t)a.sched_tile, r.bb[0], r.bb[1], r.bb[2], r.bb[3], [&](uint32_t st) {
+    const uint32_t bin_off = (r.material & kRecTransBit) ? a.dyn->n_stiles : 0u;
+    for_each_stile(view, (int32_t)a.sched_tile, r.bb[0], r.bb[1], r.bb[2], r.bb[3], [&](uint32_t b) {
+        const uint32_t st = bin_off + b;
         const uint32_t active = __activemask();
         const uint32_t peers = __match_any_sync(active, st);
         const int leader = __ffs(peers) - 1;
@@ -694,7 +709,7 @@ __device__ __forceinline__ void load_packet(const FrameArgs& a, const DScene& sc
     c.ye = y1 * kSubpixelScale;
     c.amip = 0;
     if (c.r.material & kRecAlphaBit) {
-        const DMaterial& m = sc.materials[c.r.material & ~kRecAlphaBit];
+        const DMaterial& m = sc.materials[c.r.material & kRecMaterialMask];
         const RecShade& q = a.rec_s[slot];
         c.amip = mip_level(sc.textures[m.tex[TS_BASE]], q.du_dv[0], q.du_dv[1], q.du_dv[2], q.du_dv[3]);
     }
@@ -824,7 +839,7 @@ __device__ __forceinline__ void raster_lane(RasterShared<S>& s, const FrameArgs&
     const float z = interp(L.zow, b1, b2) * w;
     bool pass = (z == z);
     if (pass && (L.mat & kRecAlphaBit))
-        pass = alpha_pass(sc, sc.materials[L.mat & ~kRecAlphaBit], a.rec_s[s.p_slot[pk]], b1, b2, w, s.p_amip[pk]);
+        pass = alpha_pass(sc, sc.materials[L.mat & kRecMaterialMask], a.rec_s[s.p_slot[pk]], b1, b2, w, s.p_amip[pk]);
     if (pass) {
         const unsigned long long key = make_key(z, L.seq8);
         unsigned long long* slot = s.sk + ly * S + lx;
@@ -1149,10 +1164,12 @@ __device__ void voxel_gi(const DScene& sc, f3 pos, f3 sh[4], float& w0, float& w
     }
 }
 
-// pbr_shader<false> for one lane (src/shader.rs:110-309). du_dv already holds
-// packet.du_dv * w with component i scaled by lane i's w (Q6 quirk).
+// pbr_shader<TRANS> for one lane (src/shader.rs:110-309). du_dv already holds
+// packet.du_dv * w with component i scaled by lane i's w (Q6 quirk). `cur` is
+// the colour under a translucent fragment.
+template <bool TRANS>
 __device__ f3 pbr_lane(const DScene& sc, const DView& v, const DMaterial& m, const RecShade& q, float w, float b1,
-                       float b2, const float du_dv[4], const uint8_t* tab) {
+                       float b2, const float du_dv[4], const uint8_t* tab, f3 cur) {
     const uint32_t md = v.rsqrt_mode;
     const float PI = 3.14159265358979f;
     const float EPS = 1e-6f;
@@ -1265,7 +1282,21 @@ __device__ f3 pbr_lane(const DScene& sc, const DView& v, const DMaterial& m, con
     f3 cis = env * bsf;
     const float ao_spec = 1.0f + (ao - 1.0f) * 0.5f;
     cis = cis * (ao_spec * skyv);
-    f3 col = ((cdd + cds) + cid) + cis;
+    f3 col;
+    if (TRANS) {
+        float tr = m.transmission;
+        if (m.tex[TS_TRANSMISSION] >= 0) {
+            const DTexture& t = sc.textures[m.tex[TS_TRANSMISSION]];
+            const uint32_t mip = mip_level(t, du_dv[0], du_dv[1], du_dv[2], du_dv[3]);
+            tr = tr * unpack_rgb(sample_texel(t, uvx, uvy, mip, m.wrap_s[TS_TRANSMISSION],
+                                              m.wrap_t[TS_TRANSMISSION])).x;
+        }
+        tr = clampf(tr, 0.0f, 1.0f);
+        const float inv = 1.0f - tr;
+        col = (((cur * bc) * tr + (cdd + cid) * inv) + cds) + cis;
+    } else {
+        col = ((cdd + cds) + cid) + cis;
+    }
     f3 em = one;
     if (m.tex[TS_EMISSIVE] >= 0) {
         const DTexture& t = sc.textures[m.tex[TS_EMISSIVE]];
@@ -1349,8 +1380,8 @@ __device__ __forceinline__ void shade_thread(const FrameArgs& a, const uint8_t* 
                 dd[i] = q.du_dv[i] * wq[i];
             }
             const float w_own = k == 0 ? wq[0] : (k == 1 ? wq[1] : (k == 2 ? wq[2] : wq[3]));
-            const DMaterial& m = sc.materials[r.material & ~kRecAlphaBit];
-            col = pbr_lane(sc, v, m, q, w_own, b1, b2, dd, tab);
+            const DMaterial& m = sc.materials[r.material & kRecMaterialMask];
+            col = pbr_lane<false>(sc, v, m, q, w_own, b1, b2, dd, tab, col);
             vis_hi = q.static_id;
             vis_fan = r.seq8 & 7u;
         } else {
@@ -1372,15 +1403,15 @@ __device__ __forceinline__ void shade_thread(const FrameArgs& a, const uint8_t* 
         v.vis[(uint64_t)py * (uint64_t)v.width + (uint64_t)px] =
             covered ? (((unsigned long long)vis_hi << 3) | vis_fan) : ~0ull;
     }
-    if (px < v.width && py < (v.height & ~1)) {
-        if (v.flags & 1u) {
-            float* c = v.color + ((uint64_t)py * (uint64_t)v.width + (uint64_t)px) * 3u;
-            c[0] = col.x;
-            c[1] = col.y;
-            c[2] = col.z;
-        } else {
-            v.rgba8[(uint64_t)py * v.out_pitch + (uint64_t)px] = tonemap_pack(col, v.exposure);
-        }
+    if (v.flags) {
+        // Linear colour over the padded tile grid (the translucent pass may
+        // blend into the off-screen centre quad the luminance meter reads).
+        float* c = v.color + ((uint64_t)py * v.key_pitch + (uint64_t)px) * 3u;
+        c[0] = col.x;
+        c[1] = col.y;
+        c[2] = col.z;
+    } else if (px < v.width && py < (v.height & ~1)) {
+        v.rgba8[(uint64_t)py * v.out_pitch + (uint64_t)px] = tonemap_pack(col, v.exposure);
     }
 }
 
@@ -1408,6 +1439,188 @@ __global__ void k_rsqrt_selftest(const float* in, float* out, uint64_t n, uint32
         out[i] = rsqrt_mode(in[i], mode, tab);
 }
 
+// --------------------------------------------------------------------------
+// Translucent forward pass (render_tile, src/tilerasterizer.rs:92-101)
+// --------------------------------------------------------------------------
+constexpr int kTransCap = 2048;  // translucent packets one scheduling tile can sort
+constexpr int kTransThreads = 256;
+
+// Sort key of a translucent packet: OrderedFloat avg_z back to front (NaN is
+// the largest value, -0 equals +0), then submission order. The reference's
+// in-place quicksort (src/bumpqueue.rs:155-233) is unstable over a
+// rayon-ordered queue, so it defines no order for equal keys; submission
+// order is the one chosen here.
+__device__ __forceinline__ unsigned long long trans_key(float avg_z, uint32_t seq8) {
+    const uint32_t o = (avg_z != avg_z) ? 0xFFFFFFFFu : float_to_ordered(avg_z);
+    return ((unsigned long long)(0xFFFFFFFFu - o) << 32) | (unsigned long long)seq8;
+}
+
+// Edge values of a quad's four lanes at quad (i, j) of a region with origin
+// (ox, oy), as fine_raster reaches them: step_y added j times to the origin
+// value, then step_x i times. Closed form where every partial sum is an
+// integer below 2^24 (then exact), else the additions themselves.
+__device__ __forceinline__ void quad_edge_values(const Edge& e, int32_t ox, int32_t oy, int32_t i, int32_t j,
+                                                 float out[4]) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        float v = edge_eval(e, i2f(ox + ((k & 1) ? 24 : 8)), i2f(oy + ((k >> 1) ? 24 : 8)));
+        const float b = ru_add(ru_add(fabsf(v), ru_mul((float)j, fabsf(e.sy))), ru_mul((float)i, fabsf(e.sx)));
+        if (b <= 16777216.0f) {
+            v = v + (e.sy * (float)j + e.sx * (float)i);
+        } else {
+            for (int32_t t = 0; t < j; ++t) v += e.sy;
+            for (int32_t t = 0; t < i; ++t) v += e.sx;
+        }
+        out[k] = v;
+    }
+}
+
+// Per scheduling tile, after opaque shading: sort the tile's translucent
+// packets back to front, then every thread walks its own quads through the
+// sorted packets (fine_raster coverage, depth test against the opaque depth,
+// TranslucentForwardShader blend over the current colour; no depth write).
+// Quads are disjoint, so the per-pixel order is the sorted order.
+template <int S>
+__global__ void __launch_bounds__(kTransThreads) k_translucent(FrameArgs a) {
+    __shared__ unsigned long long tkey[kTransCap];
+    __shared__ uint32_t tslot[kTransCap];
+    __shared__ uint32_t tsorted[kTransCap];
+    __shared__ uint32_t tblk[kTransCap];
+    __shared__ uint8_t tab[512];
+    __shared__ uint32_t cur_tile;
+    for (int i = threadIdx.x; i < 512; i += blockDim.x) tab[i] = a.rsqrt_table[i];
+    const uint32_t n_st = a.dyn->n_stiles;
+    const bool bad = (a.counters->status & (ST_BIN_OVERFLOW | ST_CLIP_OVERFLOW | ST_QUEUE_OVERFLOW)) != 0u;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) cur_tile = atomicAdd(&a.counters->trans_next, 1u);
+        __syncthreads();
+        const uint32_t st = cur_tile;
+        if (st >= n_st || bad) break;
+        const uint32_t b0 = a.tile_offset[n_st + st], n = a.tile_offset[n_st + st + 1] - b0;
+        if (n == 0u) continue;
+        if (n > (uint32_t)kTransCap) {
+            if (threadIdx.x == 0) atomicOr(&a.counters->status, ST_TRANS_OVERFLOW);
+            continue;
+        }
+        const uint32_t vi = find_view_by_stile(a, st);
+        const DView& view = a.views[vi];
+        const DScene& sc = a.scenes[view.scene];
+        const uint32_t local = st - view.stile_base;
+        const int32_t sx0 = (int32_t)(local % (uint32_t)view.stiles_x) * S;
+        const int32_t sy0 = (int32_t)(local / (uint32_t)view.stiles_x) * S;
+        const int32_t tx0 = (sx0 / kRefTile) * kRefTile, ty0 = (sy0 / kRefTile) * kRefTile;
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+            const uint32_t slot = a.bins[b0 + i];
+            tslot[i] = slot;
+            tkey[i] = trans_key(__uint_as_float(a.rec_s[slot].pad[0]), a.rec_r[slot].seq8);
+        }
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {  // keys are unique: rank = position
+            const unsigned long long k = tkey[i];
+            uint32_t rank = 0;
+            for (uint32_t j = 0; j < n; ++j) rank += tkey[j] < k ? 1u : 0u;
+            tsorted[rank] = tslot[i];
+        }
+        __syncthreads();
+        // Coarse flag and accepted 16-px blocks (coarse_raster's reject) per packet.
+        for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+            PacketCtx c;
+            load_packet(a, sc, tsorted[k], tx0, ty0, c);
+            uint32_t m = 0;
+            if (c.coarse) {
+                m = 0x80000000u;
+                for (int32_t by = 0; by * 256 < c.ye - c.ys; ++by)
+                    for (int32_t bx = 0; bx * 256 < c.xe - c.xs; ++bx)
+                        if (!block_rejected(c.e12, c.e20, c.e01, c.xs + 256 * bx, c.ys + 256 * by))
+                            m |= 1u << (by * 5 + bx);
+            }
+            tblk[k] = m;
+        }
+        __syncthreads();
+        for (int32_t q = threadIdx.x; q < (S / 2) * (S / 2); q += blockDim.x) {
+            const int32_t px0 = sx0 + 2 * (q % (S / 2)), py0 = sy0 + 2 * (q / (S / 2));
+            float zop[4];
+            f3 col[4];
+#pragma unroll
+            for (int l = 0; l < 4; ++l) {
+                const uint64_t pi = (uint64_t)(py0 + (l >> 1)) * view.key_pitch + (uint64_t)(px0 + (l & 1));
+                zop[l] = ordered_to_float((uint32_t)(a.keys[view.key_offset + pi] >> 32));
+                const float* cp = view.color + pi * 3u;
+                col[l] = mk3(cp[0], cp[1], cp[2]);
+            }
+            const int32_t X = px0 * kSubpixelScale, Y = py0 * kSubpixelScale;
+            bool touched = false;
+            for (uint32_t k = 0; k < n; ++k) {
+                const uint32_t slot = tsorted[k];
+                const RecRaster& rr = a.rec_r[slot];
+                int32_t x0, y0, x1, y1;
+                clipped_rect(rr, tx0, ty0, x0, y0, x1, y1);
+                const int32_t xs = (x0 & ~1) * kSubpixelScale, ys = (y0 & ~1) * kSubpixelScale;
+                if (X < xs || X >= x1 * kSubpixelScale || Y < ys || Y >= y1 * kSubpixelScale) continue;
+                int32_t ox = xs, oy = ys;
+                const uint32_t blk = tblk[k];
+                if (blk >> 31) {
+                    const int32_t bx = (X - xs) >> 8, by = (Y - ys) >> 8;
+                    if (!((blk >> (by * 5 + bx)) & 1u)) continue;
+                    ox = xs + 256 * bx;
+                    oy = ys + 256 * by;
+                }
+                const int32_t i = (X - ox) >> 5, j = (Y - oy) >> 5;
+                PacketCtx c;
+                load_packet(a, sc, slot, tx0, ty0, c);
+                float w0[4], w1[4], w2[4];
+                quad_edge_values(c.e12, ox, oy, i, j, w0);
+                quad_edge_values(c.e20, ox, oy, i, j, w1);
+                quad_edge_values(c.e01, ox, oy, i, j, w2);
+                float b1[4], b2[4], wl[4];
+                uint32_t mask = 0;
+#pragma unroll
+                for (int l = 0; l < 4; ++l) {
+                    b1[l] = w1[l] * c.r.ooa;
+                    b2[l] = w2[l] * c.r.ooa;
+                    wl[l] = 1.0f / interp(c.r.oow, b1[l], b2[l]);
+                    const float z = interp(c.r.zow, b1[l], b2[l]) * wl[l];
+                    if (w0[l] >= 0.0f && w1[l] >= 0.0f && w2[l] >= 0.0f && z <= zop[l]) mask |= 1u << l;
+                }
+                if (mask == 0u) continue;
+                RecShade qs;
+                {
+                    const float4* src = reinterpret_cast<const float4*>(a.rec_s + slot);
+                    float4* dst = reinterpret_cast<float4*>(&qs);
+#pragma unroll
+                    for (int t = 0; t < 11; ++t) dst[t] = __ldg(src + t);
+                }
+                float dd[4];
+#pragma unroll
+                for (int l = 0; l < 4; ++l) dd[l] = qs.du_dv[l] * wl[l];
+                const DMaterial& m = sc.materials[c.r.material & kRecMaterialMask];
+#pragma unroll
+                for (int l = 0; l < 4; ++l)
+                    if (mask & (1u << l)) col[l] = pbr_lane<true>(sc, view, m, qs, wl[l], b1[l], b2[l], dd, tab, col[l]);
+                touched = true;
+            }
+            if (!touched) continue;
+#pragma unroll
+            for (int l = 0; l < 4; ++l) {
+                const uint64_t pi = (uint64_t)(py0 + (l >> 1)) * view.key_pitch + (uint64_t)(px0 + (l & 1));
+                float* cp = view.color + pi * 3u;
+                cp[0] = col[l].x;
+                cp[1] = col[l].y;
+                cp[2] = col[l].z;
+            }
+            // Centre luminance of the reference tile (src/tilerasterizer.rs:103-106): quad (0, 16).
+            if ((px0 & (kRefTile - 1)) == 0 && (py0 & (kRefTile - 1)) == kRefTile / 2) {
+                float l4[4];
+#pragma unroll
+                for (int l = 0; l < 4; ++l) l4[l] = (col[l].x * 0.2126f + col[l].y * 0.7152f) + col[l].z * 0.0722f;
+                const uint32_t tile = (uint32_t)(py0 / kRefTile) * (uint32_t)view.tiles_x + (uint32_t)(px0 / kRefTile);
+                view.tile_lum[tile] = (((l4[0] + l4[1]) + l4[2]) + l4[3]) * 0.25f;
+            }
+        }
+    }
+}
+
 // Exposure applied after the host's update_auto_exposure (dt > 0 path).
 __global__ void k_resolve(FrameArgs a) {
     const uint32_t vi = blockIdx.y;
@@ -1415,9 +1628,9 @@ __global__ void k_resolve(FrameArgs a) {
     const DView& v = a.views[vi];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t w = (uint32_t)v.width, h = (uint32_t)(v.height & ~1);
-    if (i >= w * h || !(v.flags & 1u)) return;
+    if (i >= w * h || !v.flags) return;
     const uint32_t x = i % w, y = i / w;
-    const float* c = v.color + (uint64_t)i * 3u;
+    const float* c = v.color + ((uint64_t)y * v.key_pitch + x) * 3u;
     const float e = a.exposure_dev ? *a.exposure_dev : v.exposure;
     v.rgba8[(uint64_t)y * v.out_pitch + x] = tonemap_pack(mk3(c[0], c[1], c[2]), e);
 }
@@ -1507,6 +1720,16 @@ void launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t* ev
     mark(6);
     k_shade<<<a.shade_grid > 0 ? a.shade_grid : (uint32_t)num_sms, 256, 0, s>>>(a);
     mark(7);
+    if (a.has_translucent) {
+        const uint32_t tg = (uint32_t)num_sms * 2u;
+        switch (a.sched_tile) {
+            case 8: k_translucent<8><<<tg, kTransThreads, 0, s>>>(a); break;
+            case 16: k_translucent<16><<<tg, kTransThreads, 0, s>>>(a); break;
+            case 32: k_translucent<32><<<tg, kTransThreads, 0, s>>>(a); break;
+            default: k_translucent<64><<<tg, kTransThreads, 0, s>>>(a); break;
+        }
+        if (!a.defer_resolve) launch_resolve(a, stream);
+    }
 }
 
 cudaError_t launch_rsqrt_selftest(const float* in, float* out, uint64_t n, uint32_t mode, const uint8_t* table) {

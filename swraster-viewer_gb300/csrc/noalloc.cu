@@ -183,6 +183,8 @@ extern "C" swr_status swr_render_frame_noalloc(const swr_scene* scene, const swr
         if (n.mesh < 0) continue;
         const M4 mvp = mulmm(vp, n.transform);
         const HMesh& m = s.meshes[n.mesh];
+        if (!m.translucent.empty())
+            return na_fail(SWR_INVALID_ARG, "translucent primitives need a colour buffer: use swr_render_frame");
         for (uint32_t lp : m.opaque) {
             const uint32_t gp = m.prims[lp];
             const HPrimitive& p = s.prims[gp];
@@ -243,6 +245,7 @@ extern "C" swr_status swr_render_frame_noalloc(const swr_scene* scene, const swr
     dyn->n_chunks = nc;
     dyn->tri_total = tri;
     dyn->n_stiles = (uint32_t)(v->stiles_x * v->stiles_y);
+    dyn->n_bins = dyn->n_stiles;
     dyn->total_quads = v->quad_pitch * (uint32_t)v->tiles_y * 32u;
     dyn->max_view_pixels = (uint32_t)width * (uint32_t)(height & ~1);
     // Tables to the scratch array (pageable source: the copy is staged
@@ -297,7 +300,7 @@ extern "C" swr_status swr_render_frame_noalloc(const swr_scene* scene, const swr
         cudaGetLastError();
         return na_fail(SWR_CUDA_ERROR, "frame execution failed");
     }
-    if (status & (ST_BIN_OVERFLOW | ST_CLIP_OVERFLOW | ST_QUEUE_OVERFLOW))
+    if (status & kStRetry)
         return na_fail(SWR_OVERFLOW, "swr_render_frame_noalloc: fixed scratch capacity exceeded (bins or clip output)");
     return SWR_OK;
 }

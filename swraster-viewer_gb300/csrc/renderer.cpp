@@ -56,7 +56,11 @@ void build_view_draws(const SceneImpl& s, const swr_camera& cam, uint32_t view_i
         if (n.mesh < 0) continue;
         const M4 mvp = mulmm(vp, n.transform);
         const HMesh& m = s.meshes[n.mesh];
-        for (uint32_t lp : m.opaque) {
+        // render_mesh (src/renderer.rs:386-420): opaque primitives, then translucent.
+        const size_t n_op = m.opaque.size();
+        for (size_t k = 0; k < n_op + m.translucent.size(); ++k) {
+            const bool translucent = k >= n_op;
+            const uint32_t lp = translucent ? m.translucent[k - n_op] : m.opaque[k];
             const uint32_t gp = m.prims[lp];
             const HPrimitive& p = s.prims[gp];
             float ws[4];
@@ -83,6 +87,7 @@ void build_view_draws(const SceneImpl& s, const swr_camera& cam, uint32_t view_i
             d.tri_count = tc;
             d.static_base = n.tri_id_base + p.tri_id_base;
             d.scene = scene_idx;
+            d.translucent = translucent ? 1u : 0u;
             const uint32_t di = (uint32_t)draws.size();
             draws.push_back(d);
             for (uint32_t t = 0; t < tc; t += kChunkTris) chunks.push_back({di, t});
@@ -191,7 +196,7 @@ void FrameEngine::release() {
     if (capture_stream) cudaStreamDestroy(capture_stream);
     capture_stream = nullptr;
     for (DBuf* b : {&tables, &tri_state, &rec_r, &rec_s, &fan_base, &clip_queue, &tile_count, &tile_offset,
-                    &tile_cursor, &bins, &keys, &counters, &rsqrt_tab})
+                    &tile_cursor, &bins, &keys, &counters, &rsqrt_tab, &color})
         b->release();
     h_stage.release();
     if (stage_done) cudaEventDestroy(stage_done);
@@ -212,10 +217,23 @@ swr_status FrameEngine::prepare(const std::vector<const SceneImpl*>& scenes, std
     std::vector<DChunk> hchunks;
     uint32_t tri_cursor = 0;
     uint32_t stile_cursor = 0, quad_cursor = 0, max_px = 0;
-    uint64_t key_cursor = 0;
+    uint64_t key_cursor = 0, color_floats = 0;
+    bool any_translucent = false;
     for (size_t i = 0; i < vws.size(); ++i) {
         DView& v = vws[i];
+        const size_t d0 = hdraws.size();
         build_view_draws(*scenes[v.scene], *cams[i], (uint32_t)i, v.scene, tri_cursor, hdraws, hchunks);
+        bool view_translucent = false;
+        for (size_t k = d0; k < hdraws.size(); ++k) view_translucent |= hdraws[k].translucent != 0u;
+        v.flags = (v.flags & kViewLinear) | (view_translucent ? kViewTranslucent : 0u);
+        any_translucent |= view_translucent;
+        // Linear colour over the padded tile grid (engine-owned), offset kept
+        // in the pointer field until the buffer exists.
+        v.color = nullptr;
+        if (v.flags) {
+            v.color = reinterpret_cast<float*>((uintptr_t)(color_floats + 1));
+            color_floats += v.key_pitch * (uint64_t)v.tiles_y * kRefTile * 3u;
+        }
         v.stile_base = stile_cursor;
         stile_cursor += (uint32_t)(v.stiles_x * v.stiles_y);
         v.quad_base = quad_cursor;
@@ -231,7 +249,9 @@ swr_status FrameEngine::prepare(const std::vector<const SceneImpl*>& scenes, std
     draw_cap = grow(draw_cap, std::max<size_t>(1, hdraws.size()));
     chunk_cap = grow(chunk_cap, std::max<size_t>(1, hchunks.size()));
     tri_cap = grow(tri_cap, std::max<uint32_t>(1, T));
-    stile_cap = grow(stile_cap, stile_cursor + 1);
+    // Bins: opaque per scheduling tile, then (frames with translucent draws)
+    // translucent per scheduling tile.
+    stile_cap = grow(stile_cap, 2ull * stile_cursor + 1);
     quad_cap = grow(quad_cap, quad_cursor);
     pixel_cap = grow(pixel_cap, max_px);
     if (key_cursor > key_cap) key_cap = key_cursor + key_cursor / 4;
@@ -255,6 +275,7 @@ swr_status FrameEngine::prepare(const std::vector<const SceneImpl*>& scenes, std
     chk(tile_cursor.ensure((size_t)(stile_cap + 1) * sizeof(uint32_t)));
     chk(bins.ensure(bin_cap * sizeof(uint32_t)));
     chk(keys.ensure(std::max<uint64_t>(1, key_cap) * sizeof(unsigned long long)));
+    if (color_floats > 0) chk(color.ensure(color_floats * sizeof(float)));
     if (e != cudaSuccess) {
         err = std::string("device allocation failed: ") + cudaGetErrorString(e);
         cudaGetLastError();
@@ -275,6 +296,9 @@ swr_status FrameEngine::prepare(const std::vector<const SceneImpl*>& scenes, std
     dyn.n_stiles = stile_cursor;
     dyn.total_quads = quad_cursor;
     dyn.max_view_pixels = max_px;
+    dyn.n_bins = any_translucent ? 2u * stile_cursor : stile_cursor;
+    for (DView& v : vws)
+        if (v.color) v.color = color.as<float>() + ((uintptr_t)v.color - 1u);
     uint8_t* hs = static_cast<uint8_t*>(h_stage.p);
     std::memcpy(hs + lay.o_dyn, &dyn, sizeof(dyn));
     for (size_t i = 0; i < scenes.size(); ++i)
@@ -318,6 +342,8 @@ swr_status FrameEngine::prepare(const std::vector<const SceneImpl*>& scenes, std
     a.exposure_dev = nullptr;
     a.raster_grid = raster_grid;
     a.shade_grid = shade_grid;
+    a.has_translucent = any_translucent ? 1u : 0u;
+    a.defer_resolve = defer_resolve ? 1u : 0u;
     args = a;
     return SWR_OK;
 }
@@ -364,6 +390,21 @@ swr_status FrameEngine::launch(cudaStream_t stream, cudaEvent_t* ev, std::string
         cudaGetLastError();
         return SWR_CUDA_ERROR;
     }
+    return SWR_OK;
+}
+
+swr_status FrameEngine::grow_for(const DCounters& c, std::string& err) {
+    if (c.status & ST_BIN_OVERFLOW) bin_cap = std::max<uint64_t>(bin_cap * 2, c.pairs + c.pairs / 4);
+    if (c.status & ST_CLIP_OVERFLOW)
+        extra_cap = std::max<uint64_t>(extra_cap * 2, (uint64_t)c.extra_used + c.extra_used / 4);
+    if (c.status & ST_TRANS_OVERFLOW) {
+        if (sched_tile <= 8) {
+            err = "more translucent packets overlap one 8-pixel tile than the translucent sort holds";
+            return SWR_OVERFLOW;
+        }
+        sched_tile /= 2;
+    }
+    retries++;
     return SWR_OK;
 }
 

@@ -79,6 +79,8 @@ struct FrameEngine {
     uint32_t raster_grid = 0, shade_grid = 0, grid_tile = 0;
     DBuf tables, tri_state, rec_r, rec_s, fan_base, clip_queue;
     DBuf tile_count, tile_offset, tile_cursor, bins, keys, counters, rsqrt_tab;
+    DBuf color;                // linear colour of views that need it (padded tile grids)
+    bool defer_resolve = false;// the caller resolves (renderer frames with dt > 0)
     HBuf h_stage;
     TableLayout lay;
     cudaEvent_t stage_done = nullptr;
@@ -95,6 +97,10 @@ struct FrameEngine {
     cudaStream_t capture_stream = nullptr;  // legacy default streams cannot be captured
 
     swr_status init(std::string& err);
+    // Grows what a frame's counters report as overflowed (bins, clip slots)
+    // or, when a tile held too many translucent packets, halves the
+    // scheduling tile; SWR_OVERFLOW when nothing is left to grow.
+    swr_status grow_for(const DCounters& c, std::string& err);
     void release();
     swr_status prepare(const std::vector<const SceneImpl*>& scenes, std::vector<DView>& views,
                        const std::vector<const swr_camera*>& cams, std::string& err);
@@ -135,7 +141,7 @@ struct swr_renderer {
     int32_t width = 0, height = 0;
     swr_renderer_opts opts{};
     swr::FrameEngine eng;
-    swr::DBuf rgba8, vis, color, tile_lum;
+    swr::DBuf rgba8, vis, tile_lum;
     swr::ExposureState expo;
     // Mapped pinned memory for the dt > 0 exposure step.
     float* h_lum = nullptr;

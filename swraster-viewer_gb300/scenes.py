@@ -18,7 +18,7 @@ import math
 import numpy as np
 
 TEX_SRGB, TEX_NORMAL, TEX_METALLIC_ROUGHNESS, TEX_CUBEMAP, TEX_LINEAR = 0, 1, 2, 3, 4
-WRAP_REPEAT = 0
+WRAP_REPEAT, WRAP_MIRRORED = 0, 1
 
 
 def icosphere(subdiv):
@@ -138,6 +138,62 @@ def spheres_scene(seed=1, count=64, subdiv=3, box=10.0, radius=(0.5, 2.0), tex_s
     return {"meshes": meshes, "nodes": nodes, "materials": mats, "textures": [tex],
             "cubemap": cubemap_faces(rng, cube_size), "cubemap_face_size": cube_size, "voxel_grid_size": voxel,
             "specular_samples": specular_samples, "brdf_lut_size": brdf_lut_size}
+
+
+def translucent_scene(seed=11, count=8, subdiv=2, box=4.0, tex_size=64, cube_size=16, voxel=32):
+    """Opaque and translucent (KHR_materials_transmission) spheres, one mesh
+    with an opaque and a translucent primitive, a large translucent plane
+    through the scene and a translucent sphere instanced twice at the same
+    place (equal sort keys)."""
+    rng = np.random.default_rng(seed)
+    P, F = icosphere(subdiv)
+    UV = spherical_uv(P)
+    tex = noise_texture(rng, tex_size)
+    meshes, nodes, mats = [], [], []
+
+    def mat(translucent, textured_transmission=False):
+        m = {"base_color_factor": tuple(float(x) for x in rng.uniform(0.3, 1.0, 3)) + (1.0,),
+             "metallic": float(rng.random()), "roughness": float(rng.uniform(0.1, 1.0)),
+             "base_color": (0, WRAP_REPEAT, WRAP_REPEAT)}
+        if translucent:
+            m["has_transmission"] = 1
+            m["transmission"] = float(rng.uniform(0.2, 0.95))
+            if textured_transmission:
+                m["transmission_texture"] = (0, WRAP_MIRRORED, WRAP_REPEAT)
+        mats.append(m)
+        return len(mats) - 1
+
+    centers = rng.uniform(-box, box, (count, 3)).astype(np.float32)
+    radii = rng.uniform(0.8, 2.0, count).astype(np.float32)
+    for i in range(count):
+        mi = mat(translucent=(i % 2 == 1), textured_transmission=(i % 4 == 3))
+        meshes.append([{"positions": P, "normals": P.copy(), "texcoords": UV, "indices": F, "material": mi}])
+        w = translate_scale(centers[i], radii[i])
+        nodes.append({"world": w, "local": w, "mesh": len(meshes) - 1})
+    # One mesh, two primitives: translucent outer shell listed first, opaque core second.
+    shell, core = mat(True), mat(False)
+    meshes.append([{"positions": P * np.float32(1.6), "normals": P.copy(), "texcoords": UV, "indices": F,
+                    "material": shell},
+                   {"positions": P * np.float32(0.7), "normals": P.copy(), "texcoords": UV, "indices": F,
+                    "material": core}])
+    w = translate_scale(np.zeros(3, np.float32), 1.0)
+    nodes.append({"world": w, "local": w, "mesh": len(meshes) - 1})
+    # Large translucent plane facing the camera (+z), through the scene.
+    GP, GUV, GF = grid(6, 6)
+    gm = mat(True, textured_transmission=True)
+    meshes.append([{"positions": GP, "normals": np.tile(np.array([[0, 0, 1]], np.float32), (len(GP), 1)),
+                    "texcoords": GUV, "indices": GF, "material": gm}])
+    w = translate_scale(np.array([0.0, 0.0, 1.0], np.float32), 3.0 * box)
+    nodes.append({"world": w, "local": w, "mesh": len(meshes) - 1})
+    # The same translucent sphere twice at one place.
+    tm = mat(True)
+    meshes.append([{"positions": P, "normals": P.copy(), "texcoords": UV, "indices": F, "material": tm}])
+    w = translate_scale(np.array([1.0, -0.5, 2.0], np.float32), 1.2)
+    nodes.append({"world": w, "local": w, "mesh": len(meshes) - 1})
+    nodes.append({"world": w, "local": w, "mesh": len(meshes) - 1})
+    return {"meshes": meshes, "nodes": nodes, "materials": mats, "textures": [tex],
+            "cubemap": cubemap_faces(rng, cube_size), "cubemap_face_size": cube_size, "voxel_grid_size": voxel,
+            "specular_samples": 16, "brdf_lut_size": 32}
 
 
 def default_camera_params(info, width, height, fov=math.pi / 3.0):
