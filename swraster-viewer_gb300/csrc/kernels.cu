@@ -35,6 +35,10 @@
 #ifndef SWR_RASTER_PERSISTENT
 #define SWR_RASTER_PERSISTENT 1
 #endif
+// Raster: prefetch into L2 the record each thread will likely load in the next round.
+#ifndef SWR_RASTER_PREFETCH
+#define SWR_RASTER_PREFETCH 1
+#endif
 
 namespace swr {
 
@@ -343,11 +347,11 @@ __device__ __forceinline__ void for_each_stile(const DView& v, int32_t S, int32_
     }
 }
 
-// bin_triangle (src/renderer.rs:668-831): setup + count. Returns true when a
-// record was written to `slot`.
+// bin_triangle (src/renderer.rs:668-831): setup + count. Returns true when
+// the triangle covers at least one tile; its records are then in r and q.
 __device__ bool setup_triangle(const FrameArgs& a, const DView& view, const Vtx& v0, const Vtx& v1, const Vtx& v2,
-                               uint32_t slot, uint32_t seq8, uint32_t static_id, uint32_t material,
-                               uint32_t view_idx) {
+                               uint32_t seq8, uint32_t static_id, uint32_t material, uint32_t view_idx,
+                               RecRaster& r, RecShade& q) {
     int32_t p0x, p0y, p1x, p1y, p2x, p2y;
     to_screen(v0, view.width_f, view.height_f, p0x, p0y);
     to_screen(v1, view.width_f, view.height_f, p1x, p1y);
@@ -383,7 +387,6 @@ __device__ bool setup_triangle(const FrameArgs& a, const DView& view, const Vtx&
     const float dv_dy = dv2 * dx1 - dv1 * dx2;
     const float s = ooa * 16.0f;
 
-    RecRaster r;
     r.p[0] = p0x; r.p[1] = p0y; r.p[2] = p1x; r.p[3] = p1y; r.p[4] = p2x; r.p[5] = p2y;
     r.bb[0] = mnx; r.bb[1] = mny; r.bb[2] = mxx; r.bb[3] = mxy;
     r.ooa = ooa;
@@ -392,7 +395,6 @@ __device__ bool setup_triangle(const FrameArgs& a, const DView& view, const Vtx&
     r.seq8 = seq8;
     r.material = material;
     r.view = view_idx;
-    RecShade q;
     q.nrm[0] = v0.nx; q.nrm[1] = v0.ny; q.nrm[2] = v0.nz;
     q.nrm[3] = v1.nx - v0.nx; q.nrm[4] = v1.ny - v0.ny; q.nrm[5] = v1.nz - v0.nz;
     q.nrm[6] = v2.nx - v0.nx; q.nrm[7] = v2.ny - v0.ny; q.nrm[8] = v2.nz - v0.nz;
@@ -414,22 +416,21 @@ __device__ bool setup_triangle(const FrameArgs& a, const DView& view, const Vtx&
     const bool translucent = (material & kRecTransBit) != 0u;
     q.pad[0] = translucent ? __float_as_uint(((v0.cz + v1.cz) + v2.cz) / 3.0f) : 0u;
     q.pad[1] = q.pad[2] = 0;
-
-    {
-        const float4* src = reinterpret_cast<const float4*>(&r);
-        float4* dst = reinterpret_cast<float4*>(a.rec_r + slot);
-#pragma unroll
-        for (int i = 0; i < 5; ++i) dst[i] = src[i];
-    }
-    {
-        const float4* src = reinterpret_cast<const float4*>(&q);
-        float4* dst = reinterpret_cast<float4*>(a.rec_s + slot);
-#pragma unroll
-        for (int i = 0; i < 11; ++i) dst[i] = src[i];
-    }
     const uint32_t bin_off = translucent ? a.dyn->n_stiles : 0u;
     for_each_stile(view, S, mnx, mny, mxx, mxy, [&](uint32_t st) { agg_inc(a.tile_count, bin_off + st); });
     return true;
+}
+
+__device__ __forceinline__ void store_records(const FrameArgs& a, uint32_t slot, const RecRaster& r,
+                                              const RecShade& q) {
+    const float4* sr = reinterpret_cast<const float4*>(&r);
+    float4* dr = reinterpret_cast<float4*>(a.rec_r + slot);
+#pragma unroll
+    for (int i = 0; i < 5; ++i) dr[i] = sr[i];
+    const float4* sq = reinterpret_cast<const float4*>(&q);
+    float4* dq = reinterpret_cast<float4*>(a.rec_s + slot);
+#pragma unroll
+    for (int i = 0; i < 11; ++i) dq[i] = sq[i];
 }
 
 __global__ void k_reset(FrameArgs a) {
@@ -462,6 +463,7 @@ __device__ __forceinline__ bool vtx_inside_all(const Vtx& v) {
            (v.cy + v.cw >= 0.0f) && (-v.cy + v.cw >= 0.0f);
 }
 
+// Thread per triangle of a 256-triangle chunk of one draw.
 __global__ void __launch_bounds__(kChunkTris) k_frontend(FrameArgs a) {
     if (blockIdx.x >= a.dyn->n_chunks) return;
     const DChunk ch = a.chunks[blockIdx.x];
@@ -490,7 +492,10 @@ __global__ void __launch_bounds__(kChunkTris) k_frontend(FrameArgs a) {
     }
     // All three vertices inside: the clipper would return the triangle unchanged.
     const uint32_t mword = record_material(sc, d, pr.material);
-    const bool ok = setup_triangle(a, view, v0, v1, v2, g, g << 3, d.static_base + local, mword, d.view);
+    RecRaster r;
+    RecShade q;
+    const bool ok = setup_triangle(a, view, v0, v1, v2, g << 3, d.static_base + local, mword, d.view, r, q);
+    if (ok) store_records(a, g, r, q);
     a.tri_state[g] = ok ? 1 : 0;
     warp_count(&a.counters->setup_tris, ok);
 }
@@ -569,8 +574,11 @@ __global__ void __launch_bounds__(128) k_clip(FrameArgs a) {
             }
             for (int f = 0; f < fans; ++f) {
                 const uint32_t slot = f == 0 ? g : tri_total + base + (uint32_t)(f - 1);
-                const bool ok = setup_triangle(a, view, poly[0], poly[f + 1], poly[f + 2], slot, (g << 3) | (uint32_t)f,
-                                               d.static_base + local, mword, d.view);
+                RecRaster r;
+                RecShade q;
+                const bool ok = setup_triangle(a, view, poly[0], poly[f + 1], poly[f + 2], (g << 3) | (uint32_t)f,
+                                               d.static_base + local, mword, d.view, r, q);
+                if (ok) store_records(a, slot, r, q);
                 if (ok) {
                     atomicAdd(&a.counters->setup_tris, 1u);
                     if (f == 0) any = 1;
@@ -835,15 +843,17 @@ __device__ __forceinline__ void raster_lane(RasterShared<S>& s, const FrameArgs&
                                             const PacketLanes& L, uint32_t pk, float w1, float w2, int32_t lx,
                                             int32_t ly) {
     const float b1 = w1 * L.ooa, b2 = w2 * L.ooa;
-    const float w = 1.0f / interp(L.oow, b1, b2);
-    const float z = interp(L.zow, b1, b2) * w;
+    const float oi = interp(L.oow, b1, b2), zi = interp(L.zow, b1, b2);
+    unsigned long long* slot = s.sk + ly * S + lx;
+    const unsigned long long cur = *slot;
+    const float w = 1.0f / oi;
+    const float z = zi * w;
     bool pass = (z == z);
     if (pass && (L.mat & kRecAlphaBit))
         pass = alpha_pass(sc, sc.materials[L.mat & kRecMaterialMask], a.rec_s[s.p_slot[pk]], b1, b2, w, s.p_amip[pk]);
     if (pass) {
         const unsigned long long key = make_key(z, L.seq8);
-        unsigned long long* slot = s.sk + ly * S + lx;
-        if (key < *slot) atomicMin(slot, key);
+        if (key < cur) atomicMin(slot, key);
     }
 }
 
@@ -913,14 +923,17 @@ __device__ __forceinline__ void raster_slow_region(RasterShared<S>& s, const Fra
 }
 
 // Pass 1 of a round for one packet: classify and split into regions, and
-// either count them (regions, quads) or stage them from the given positions.
+// either count them (regions, quads; the accepted 16-px blocks of a coarse
+// packet go to bmask) or stage them from the given positions (bmask as the
+// count left it).
 template <int S>
 __device__ __forceinline__ void packet_regions(RasterShared<S>& s, const PacketCtx& c, int32_t sx0, int32_t sy0,
-                                               bool write, uint32_t pk, uint32_t& n_r, uint32_t& n_q) {
+                                               bool write, uint32_t pk, uint32_t& n_r, uint32_t& n_q,
+                                               uint32_t& bmask) {
     auto region = [&](int32_t ox, int32_t oy, int32_t ex, int32_t ey) {
         uint32_t ij = 0;
         const uint32_t nq = clip_quads(ox, oy, ex, ey, sx0, sy0, S, ij);
-        if (nq == 0) return;
+        if (nq == 0) return false;
         if (write) {
             const uint32_t r = n_r;
             float w[12];
@@ -937,6 +950,7 @@ __device__ __forceinline__ void packet_regions(RasterShared<S>& s, const PacketC
         }
         ++n_r;
         n_q += nq;
+        return true;
     };
     if (!c.coarse) {
         region(c.xs, c.ys, c.xe, c.ye);
@@ -945,13 +959,20 @@ __device__ __forceinline__ void packet_regions(RasterShared<S>& s, const PacketC
     int32_t bxl, bxh, byl, byh;
     block_range(c.xs, c.xe, sx0, S, bxl, bxh);
     block_range(c.ys, c.ye, sy0, S, byl, byh);
+    if (!write) bmask = 0;
+    uint32_t bit = 1;  // at most 5 x 5 blocks of a 64-px reference tile
     for (int32_t by = byl; by < byh; ++by)
-        for (int32_t bx = bxl; bx < bxh; ++bx) {
+        for (int32_t bx = bxl; bx < bxh; ++bx, bit <<= 1) {
             const int32_t ox = c.xs + 256 * bx, oy = c.ys + 256 * by;
-            if (block_rejected(c.e12, c.e20, c.e01, ox, oy)) continue;
-            region(ox, oy, min(ox + 256, c.xe), min(oy + 256, c.ye));
+            if (write) {
+                if (bmask & bit) region(ox, oy, min(ox + 256, c.xe), min(oy + 256, c.ye));
+            } else if (!block_rejected(c.e12, c.e20, c.e01, ox, oy) &&
+                       region(ox, oy, min(ox + 256, c.xe), min(oy + 256, c.ye))) {
+                bmask |= bit;
+            }
         }
 }
+
 // Persistent: each CTA pulls (view, scheduling tile) work items from a
 // device-side counter until every tile of every view is done. Per tile, the
 // bin's packets go through rounds of one packet per thread: pass 1 stages
@@ -989,11 +1010,20 @@ __global__ void __launch_bounds__(RasterShared<S>::kThreads) k_raster(FrameArgs 
             // Pass 1: count this thread's regions and quads.
             const uint32_t pidx = cursor + threadIdx.x;
             PacketCtx c;
-            uint32_t slot = 0, n_r = 0, n_q = 0;
+            uint32_t slot = 0, n_r = 0, n_q = 0, bmask = 0;
             if (pidx < b1) {
                 slot = a.bins[pidx];
+                const uint32_t nidx = pidx + NT;  // this thread's likely packet next round
+                const uint32_t nslot = nidx < b1 ? __ldg(a.bins + nidx) : 0xFFFFFFFFu;
                 load_packet(a, sc, slot, tx0, ty0, c);
-                packet_regions<S>(s, c, sx0, sy0, false, threadIdx.x, n_r, n_q);
+#if SWR_RASTER_PREFETCH
+                if (nslot != 0xFFFFFFFFu) {
+                    const char* np = reinterpret_cast<const char*>(a.rec_r + nslot);
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(np));
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(np + sizeof(RecRaster) - 1));
+                }
+#endif
+                packet_regions<S>(s, c, sx0, sy0, false, threadIdx.x, n_r, n_q, bmask);
             }
             if (threadIdx.x == 0) s.n_slow = 0;
             // Block-wide exclusive scan of (regions, quads).
@@ -1044,7 +1074,7 @@ __global__ void __launch_bounds__(RasterShared<S>::kThreads) k_raster(FrameArgs 
                 s.p_mat[pk] = c.r.material;
                 s.p_amip[pk] = c.amip;
                 s.p_slot[pk] = slot;
-                packet_regions<S>(s, c, sx0, sy0, true, pk, pr, pq);
+                packet_regions<S>(s, c, sx0, sy0, true, pk, pr, pq, bmask);
             }
             cursor += n_taken;
             __syncthreads();
