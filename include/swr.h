@@ -186,6 +186,31 @@ typedef struct swr_scene_desc {
 typedef struct swr_scene swr_scene;
 
 swr_status swr_scene_create(const swr_scene_desc* desc, swr_scene** out);
+
+/* glTF 2.0 file loading: replaces load_gltf + Scene::from_gltf
+ * (src/main.rs:86-98, src/scene.rs:145-354) followed by the voxel-grid setup
+ * of load_scene (src/main.rs:226-287, non-GI path). Reads .gltf (external or
+ * base64 data: buffers) and .glb files; every document node is kept
+ * (compute_final_transform_recursive), primitives need positions and
+ * indices, texture images are loaded from their URI relative to the file's
+ * directory (PNG, or baseline JPEG) and images embedded in buffer views are
+ * skipped, as the reference does. The environment cubemap is given as raw
+ * faces or as the path of a cross-layout image (the reference's
+ * assets/cubemap.jpg). Errors: SWR_IO_ERROR (file, buffer or image),
+ * SWR_BAD_SCENE (missing positions/indices, out-of-range references),
+ * SWR_INVALID_ARG (no cubemap). */
+typedef struct swr_gltf_opts {
+    const uint32_t* cubemap_faces;  /* 6 faces +X,-X,+Y,-Y,+Z,-Z of face_size^2 RGBA8 (R in MSB), or NULL */
+    uint32_t cubemap_face_size;
+    uint32_t voxel_grid_size;       /* 0 = 128 (src/main.rs:228) */
+    const char* cubemap_path;       /* used when cubemap_faces is NULL */
+    uint32_t specular_samples;      /* 0 = 64 */
+    uint32_t brdf_lut_size;         /* 0 = 128 */
+    uint32_t host_threads;          /* precompute threads, 0 = all cores */
+    uint32_t flags;                 /* SWR_SCENE_* */
+} swr_gltf_opts;
+
+swr_status swr_scene_load_gltf(const char* path, const swr_gltf_opts* opts, swr_scene** out);
 void swr_scene_destroy(swr_scene* scene);
 
 typedef struct swr_scene_info {

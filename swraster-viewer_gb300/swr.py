@@ -65,6 +65,12 @@ class SceneDesc(C.Structure):
                 ("sky_visibility", C.c_float), ("host_threads", C.c_uint32), ("flags", C.c_uint32)]
 
 
+class GltfOpts(C.Structure):
+    _fields_ = [("cubemap_faces", u32p), ("cubemap_face_size", C.c_uint32), ("voxel_grid_size", C.c_uint32),
+                ("cubemap_path", C.c_char_p), ("specular_samples", C.c_uint32), ("brdf_lut_size", C.c_uint32),
+                ("host_threads", C.c_uint32), ("flags", C.c_uint32)]
+
+
 class SceneInfo(C.Structure):
     _fields_ = [("triangle_count", C.c_uint64), ("vertex_count", C.c_uint64), ("device_bytes", C.c_uint64),
                 ("node_count", C.c_uint32), ("draw_count", C.c_uint32), ("bounds_min", C.c_float * 3),
@@ -174,7 +180,7 @@ EXPORTS = [
     "swr_batch_create", "swr_batch_destroy", "swr_batch_render", "swr_batch_sync", "swr_batch_output",
     "swr_batch_autotune", "swr_batch_last_ms", "swr_server_create", "swr_server_destroy", "swr_server_add_scene",
     "swr_server_submit", "swr_server_poll", "swr_server_release", "swr_server_get_stats", "swr_copy_to_host",
-    "swr_selftest_rsqrt",
+    "swr_selftest_rsqrt", "swr_scene_load_gltf",
 ]
 STAGES = ["reset", "frontend", "clip", "scan", "scatter", "raster", "shade", "resolve"]
 
@@ -211,6 +217,7 @@ def lib():
         "swr_renderer_set_profiling": ([vp, C.c_int32], C.c_int),
         "swr_renderer_get_profile": ([vp, f32p, C.c_int32, C.POINTER(C.c_uint32)], C.c_int),
         "swr_selftest_rsqrt": ([f32p, f32p, C.c_uint64, C.c_uint32], C.c_int),
+        "swr_scene_load_gltf": ([C.c_char_p, C.POINTER(GltfOpts), C.POINTER(vp)], C.c_int),
         "swr_render_frame_noalloc": ([vp, C.POINTER(Camera), C.c_int32, C.c_int32, C.c_float, C.c_uint32, vp, vp, vp],
                                      C.c_int),
         "swr_batch_create": ([C.POINTER(BatchOpts), C.POINTER(vp)], C.c_int),
@@ -333,6 +340,30 @@ class Scene:
         check(lib().swr_scene_create(C.byref(desc), C.byref(h)))
         self.handle = h
         self._keep = None  # the library copied everything it needs
+
+    @classmethod
+    def load_gltf(cls, path, cubemap_faces=None, cubemap_face_size=0, cubemap_path=None, voxel_grid_size=0,
+                  specular_samples=0, brdf_lut_size=0, host_only=False, host_threads=0):
+        """swr_scene_load_gltf: a .gltf/.glb file; the cubemap as raw faces or a cross image path."""
+        o = GltfOpts()
+        faces = None
+        if cubemap_faces is not None:
+            faces = np.ascontiguousarray(cubemap_faces, np.uint32)
+            o.cubemap_faces = _up(faces)
+            o.cubemap_face_size = cubemap_face_size
+        if cubemap_path is not None:
+            o.cubemap_path = os.fsencode(cubemap_path)
+        o.voxel_grid_size = voxel_grid_size
+        o.specular_samples = specular_samples
+        o.brdf_lut_size = brdf_lut_size
+        o.host_threads = host_threads
+        o.flags = SCENE_HOST_ONLY if host_only else 0
+        h = C.c_void_p()
+        check(lib().swr_scene_load_gltf(os.fsencode(path), C.byref(o), C.byref(h)))
+        self = cls.__new__(cls)
+        self._keep = None
+        self.handle = h
+        return self
 
     def info(self):
         i = SceneInfo()
