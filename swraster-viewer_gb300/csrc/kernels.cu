@@ -449,6 +449,24 @@ __global__ void k_reset(FrameArgs a) {
     }
 }
 
+// True when clip_against_frustum (src/renderer.rs:579-665) returns nothing
+// for this triangle without producing any intersection: at the first plane
+// (near, far, right, left, top, bottom) that some vertex is outside of, all
+// three are outside. Earlier planes then left the triangle untouched, so the
+// clipper's polygon becomes empty at exactly that plane.
+__device__ __forceinline__ bool clip_rejects_all(const Vtx& a, const Vtx& b, const Vtx& c) {
+    const float da[6] = {a.cz + a.cw, -a.cz + a.cw, a.cx + a.cw, -a.cx + a.cw, a.cy + a.cw, -a.cy + a.cw};
+    const float db[6] = {b.cz + b.cw, -b.cz + b.cw, b.cx + b.cw, -b.cx + b.cw, b.cy + b.cw, -b.cy + b.cw};
+    const float dc[6] = {c.cz + c.cw, -c.cz + c.cw, c.cx + c.cw, -c.cx + c.cw, c.cy + c.cw, -c.cy + c.cw};
+#pragma unroll
+    for (int p = 0; p < 6; ++p) {
+        const bool ia = da[p] >= 0.0f, ib = db[p] >= 0.0f, ic = dc[p] >= 0.0f;
+        if (ia && ib && ic) continue;
+        return !ia && !ib && !ic;
+    }
+    return false;
+}
+
 // Record material word: translucent primitives (no alpha test on their path,
 // src/shader.rs:66-76) or opaque ones with the alpha-test flag.
 __device__ __forceinline__ uint32_t record_material(const DScene& sc, const DDraw& d, uint32_t material) {
@@ -481,6 +499,10 @@ __global__ void __launch_bounds__(kChunkTris) k_frontend(FrameArgs a) {
     const Vtx v1 = transform_vertex(sc.vertices, pr.vtx_base + i1, model, d.mvp);
     const Vtx v2 = transform_vertex(sc.vertices, pr.vtx_base + i2, model, d.mvp);
     if (d.clip && !(vtx_inside_all(v0) && vtx_inside_all(v1) && vtx_inside_all(v2))) {
+        if (clip_rejects_all(v0, v1, v2)) {  // the clipper would return an empty polygon
+            a.tri_state[g] = 3;
+            return;
+        }
         const uint32_t q = warp_append(&a.counters->clip_queue);
         if (q < a.clip_cap) {
             a.clip_queue[q] = make_uint2(g, ch.draw);
@@ -1194,6 +1216,14 @@ __device__ void voxel_gi(const DScene& sc, f3 pos, f3 sh[4], float& w0, float& w
     }
 }
 
+// One material texture of a lane: quad mip (compute_mip_level) and point
+// sample (sample4_rgb / sample4_alpha lane, src/texture.rs:680-727).
+__device__ __forceinline__ uint32_t sample_slot(const DScene& sc, const DMaterial& m, int slot, float u, float v, const float* du_dv) {
+    const DTexture& t = sc.textures[m.tex[slot]];
+    const uint32_t mip = mip_level(t, du_dv[0], du_dv[1], du_dv[2], du_dv[3]);
+    return sample_texel(t, u, v, mip, m.wrap_s[slot], m.wrap_t[slot]);
+}
+
 // pbr_shader<TRANS> for one lane (src/shader.rs:110-309). du_dv already holds
 // packet.du_dv * w with component i scaled by lane i's w (Q6 quirk). `cur` is
 // the colour under a translucent fragment.
@@ -1215,9 +1245,7 @@ __device__ f3 pbr_lane(const DScene& sc, const DView& v, const DMaterial& m, con
     const f3 bw = cross(in_n, tw) * hand;
     f3 nw = normalize(in_n, md, tab);
     if (m.tex[TS_NORMAL] >= 0) {
-        const DTexture& t = sc.textures[m.tex[TS_NORMAL]];
-        const uint32_t mip = mip_level(t, du_dv[0], du_dv[1], du_dv[2], du_dv[3]);
-        const f3 s = unpack_rgb(sample_texel(t, uvx, uvy, mip, m.wrap_s[TS_NORMAL], m.wrap_t[TS_NORMAL]));
+        const f3 s = unpack_rgb(sample_slot(sc, m, TS_NORMAL, uvx, uvy, du_dv));
         const f3 tsn = mk3(s.x * 2.0f - 1.0f, s.y * 2.0f - 1.0f, s.z * 2.0f - 1.0f);
         nw = (tw * tsn.x + bw * tsn.y) + in_n * tsn.z;
         nw = normalize(nw, md, tab);
@@ -1237,16 +1265,10 @@ __device__ f3 pbr_lane(const DScene& sc, const DView& v, const DMaterial& m, con
     const float vli = clampf(gw0, 0.0f, 1.0f);
     const float skyv = clampf(gw1, 0.0f, 1.0f);
     f3 bc = mk3(m.base_color[0], m.base_color[1], m.base_color[2]);
-    if (m.tex[TS_BASE] >= 0) {
-        const DTexture& t = sc.textures[m.tex[TS_BASE]];
-        const uint32_t mip = mip_level(t, du_dv[0], du_dv[1], du_dv[2], du_dv[3]);
-        bc = bc * srgb_fast3(unpack_rgb(sample_texel(t, uvx, uvy, mip, m.wrap_s[TS_BASE], m.wrap_t[TS_BASE])));
-    }
+    if (m.tex[TS_BASE] >= 0) bc = bc * srgb_fast3(unpack_rgb(sample_slot(sc, m, TS_BASE, uvx, uvy, du_dv)));
     float rough = m.roughness, metal = m.metallic;
     if (m.tex[TS_MR] >= 0) {
-        const DTexture& t = sc.textures[m.tex[TS_MR]];
-        const uint32_t mip = mip_level(t, du_dv[0], du_dv[1], du_dv[2], du_dv[3]);
-        const f3 s = unpack_rgb(sample_texel(t, uvx, uvy, mip, m.wrap_s[TS_MR], m.wrap_t[TS_MR]));
+        const f3 s = unpack_rgb(sample_slot(sc, m, TS_MR, uvx, uvy, du_dv));
         rough = rough * s.y;
         metal = metal * s.z;
     }
@@ -1254,9 +1276,7 @@ __device__ f3 pbr_lane(const DScene& sc, const DView& v, const DMaterial& m, con
     metal = clampf(metal, 0.0f, 1.0f);
     float ao = 1.0f;
     if (m.tex[TS_OCCLUSION] >= 0) {
-        const DTexture& t = sc.textures[m.tex[TS_OCCLUSION]];
-        const uint32_t mip = mip_level(t, du_dv[0], du_dv[1], du_dv[2], du_dv[3]);
-        ao = unpack_rgb(sample_texel(t, uvx, uvy, mip, m.wrap_s[TS_OCCLUSION], m.wrap_t[TS_OCCLUSION])).x;
+        ao = unpack_rgb(sample_slot(sc, m, TS_OCCLUSION, uvx, uvy, du_dv)).x;
         ao = 1.0f + (ao - 1.0f) * m.occlusion_strength;
     }
     const f3 f0 = mk3(0.04f + (bc.x - 0.04f) * metal, 0.04f + (bc.y - 0.04f) * metal, 0.04f + (bc.z - 0.04f) * metal);
@@ -1315,12 +1335,7 @@ __device__ f3 pbr_lane(const DScene& sc, const DView& v, const DMaterial& m, con
     f3 col;
     if (TRANS) {
         float tr = m.transmission;
-        if (m.tex[TS_TRANSMISSION] >= 0) {
-            const DTexture& t = sc.textures[m.tex[TS_TRANSMISSION]];
-            const uint32_t mip = mip_level(t, du_dv[0], du_dv[1], du_dv[2], du_dv[3]);
-            tr = tr * unpack_rgb(sample_texel(t, uvx, uvy, mip, m.wrap_s[TS_TRANSMISSION],
-                                              m.wrap_t[TS_TRANSMISSION])).x;
-        }
+        if (m.tex[TS_TRANSMISSION] >= 0) tr = tr * unpack_rgb(sample_slot(sc, m, TS_TRANSMISSION, uvx, uvy, du_dv)).x;
         tr = clampf(tr, 0.0f, 1.0f);
         const float inv = 1.0f - tr;
         col = (((cur * bc) * tr + (cdd + cid) * inv) + cds) + cis;
@@ -1328,11 +1343,7 @@ __device__ f3 pbr_lane(const DScene& sc, const DView& v, const DMaterial& m, con
         col = ((cdd + cds) + cid) + cis;
     }
     f3 em = one;
-    if (m.tex[TS_EMISSIVE] >= 0) {
-        const DTexture& t = sc.textures[m.tex[TS_EMISSIVE]];
-        const uint32_t mip = mip_level(t, du_dv[0], du_dv[1], du_dv[2], du_dv[3]);
-        em = srgb_fast3(unpack_rgb(sample_texel(t, uvx, uvy, mip, m.wrap_s[TS_EMISSIVE], m.wrap_t[TS_EMISSIVE])));
-    }
+    if (m.tex[TS_EMISSIVE] >= 0) em = srgb_fast3(unpack_rgb(sample_slot(sc, m, TS_EMISSIVE, uvx, uvy, du_dv)));
     col = col + em * mk3(m.emissive[0], m.emissive[1], m.emissive[2]);
     return col;
 }
