@@ -73,6 +73,23 @@ def dist_init():
     return world, rank, local
 
 
+def max_over_ranks(value, world, device="cuda"):
+    """The largest of a per-rank float over all ranks (itself for one rank)."""
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_rate(world, units_per_rank, ms_max):
+    """Whole-job rate over replicas: the units every rank processed divided by
+    the slowest rank's time."""
+    return world * units_per_rank / (ms_max / 1000.0)
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -382,11 +399,8 @@ def main():
     prof, nprof = r.profile()
     r.set_profiling(False)
     clk = clocks.stop()
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    fps = world * args.steps / (ms / 1000.0)
+    ms = max_over_ranks(ms, world)
+    fps = aggregate_rate(world, args.steps, ms)
     # End to end through the C ABI with host buffers (pinned): each step is
     # the reference's frame, render_scene + update_auto_exposure +
     # blit_to_buffer, with the RGBA8 framebuffer copied into host memory.
@@ -406,11 +420,8 @@ def main():
     torch.cuda.synchronize()
     barrier()
     e2e_ms = e2.elapsed_time(e3)
-    if world > 1:
-        t = torch.tensor([e2e_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_fps = world * e2e_steps / (e2e_ms / 1000.0)
+    e2e_ms = max_over_ranks(e2e_ms, world)
+    e2e_fps = aggregate_rate(world, e2e_steps, e2e_ms)
     h2d = st.staged_bytes  # per-frame tables: scene/view headers, draws, chunks
     d2h = W * (H & ~1) * 4
     # Roofline for the dominant kernel (HBM: shading reads the 8-B depth key
