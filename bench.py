@@ -48,6 +48,10 @@ def parse():
                     help="plain: 4K per-frame path (the headline); batched: 64 views of the 81,920-triangle scene "
                          "in one launch; hetero: 16 heterogeneous scenes in one launch; served: request loop")
     ap.add_argument("--rates", default="100,500,1000,2000,5000", help="served arrival rates (requests/s)")
+    ap.add_argument("--inflight", type=int, default=3, help="served: batches in flight (one engine and stream each)")
+    ap.add_argument("--max-batch", type=int, default=64, help="served: views per batch")
+    ap.add_argument("--no-graph", dest="graph", action="store_false",
+                    help="served: launch each batch's kernels directly instead of replaying a captured graph")
     ap.add_argument("--seconds", type=float, default=2.0, help="served: arrival window per rate")
     ap.add_argument("--max-tris", type=int, default=0, help="hetero/served: cap on triangles per scene")
     return ap.parse_args()
@@ -270,7 +274,8 @@ def run_served(args):
     sh = torch.cuda.current_stream().cuda_stream
     scs = [swr.Scene(sd) for sd, _ in scenes.hetero_scenes(seed=31, count=8, max_triangles=args.max_tris or None)]
     res = [(640, 480), (1280, 720), (1920, 1080), (3840, 2160)]
-    srv = swr.Server(memory_budget=40 << 30, max_batch_views=64, inflight=2, use_graph=False)
+    srv = swr.Server(memory_budget=40 << 30, max_batch_views=args.max_batch, inflight=args.inflight,
+                     use_graph=args.graph)
     ids = [srv.add_scene(s) for s in scs]
     rends = {r: swr.Renderer(r[0], r[1]) for r in res}
     results = {}
@@ -330,8 +335,9 @@ def run_served(args):
     line = {"metric": "served frames/s + p99 latency vs plain GPU", "unit": "frames/s", "n_gpus": 1,
             "config": {"workload": "8 resident scenes (10k-4M triangles), Poisson arrivals, random scene, camera on "
                                    "a sphere, resolution from {640x480, 1280x720, 1920x1080, 3840x2160}, 40 GB "
-                                   "budget, continuous batching over 2 in-flight batches",
-                       "triangles": int(sum(s.info().triangle_count for s in scs))},
+                                   "budget, continuous batching",
+                       "triangles": int(sum(s.info().triangle_count for s in scs)), "inflight": args.inflight,
+                       "max_batch_views": args.max_batch, "graph": bool(args.graph)},
             "rates": results, "batches": st.batches, "device_bytes": st.device_bytes, "data": "synthetic"}
     best_served = max((v["served"]["frames_per_s"] for v in results.values()), default=0.0)
     best_plain = max((v["plain"]["frames_per_s"] for v in results.values()), default=0.0)

@@ -46,6 +46,7 @@ struct Engine {
     std::unique_ptr<BatchImpl> b;
     cudaStream_t stream = nullptr;
     bool busy = false;
+    uint64_t bytes = 0;  // device bytes of the engine's buffers, refreshed by the worker under the lock
     std::atomic<bool> done{false};
     std::vector<Req> reqs;
     std::vector<FB*> fbs;
@@ -62,6 +63,7 @@ struct Done {
 struct swr_server {
     swr_server_opts opts{};
     std::vector<const swr_scene*> scenes;
+    std::vector<bool> scene_translucent;  // the scene has translucent primitives (colour buffer per view)
     uint64_t scene_bytes = 0, fb_bytes = 0;
     std::vector<std::unique_ptr<Engine>> engines;
     std::map<uint64_t, std::vector<FB*>> free_fbs;  // key: w << 32 | h
@@ -76,9 +78,11 @@ struct swr_server {
     uint64_t next_ticket = 1;
     swr_server_stats stats{};
 
+    // Read under the lock; the worker refreshes Engine::bytes after an
+    // engine's buffers may have grown (never while another thread reads).
     uint64_t engine_bytes() {
         uint64_t t = 0;
-        for (auto& e : engines) t += one_engine_bytes(*e);
+        for (auto& e : engines) t += e->bytes;
         return t;
     }
 
@@ -106,24 +110,28 @@ struct swr_server {
     }
 
     // Device bytes an engine needs for a batch, upper estimate: keys of the
-    // padded tile grids, triangle records (raster + shade + clip headroom) and
-    // bins for every triangle of every view's scene.
+    // padded tile grids (and linear colour for views of scenes with
+    // translucent primitives), triangle records (raster + shade + clip
+    // headroom) and bins for every triangle of every view's scene.
     static uint64_t batch_need(const std::vector<std::pair<int32_t, int32_t>>& dims,
-                               const std::vector<uint64_t>& tris) {
+                               const std::vector<uint64_t>& tris, const std::vector<bool>& trans) {
         uint64_t t = 0;
         for (size_t i = 0; i < dims.size(); ++i) {
             const uint64_t tx = (uint64_t)(dims[i].first + 63) / 64, ty = (uint64_t)(dims[i].second + 63) / 64;
-            t += tx * ty * 64 * 64 * 8;
+            t += tx * ty * 64 * 64 * (trans[i] ? 8 + 12 : 8);
             t += tris[i] * (80 + 176 + 4 + 8 + 1) * 5 / 4 + tris[i] * 2 * 4;
         }
         return t + (1u << 20);
     }
+    // Worker thread only (the engine's buffers are not being grown).
     static uint64_t one_engine_bytes(const Engine& e) {
         const FrameEngine& f = e.b->eng;
         uint64_t t = e.b->tile_lum.bytes;
         for (const DBuf* d : {&f.tables, &f.tri_state, &f.rec_r, &f.rec_s, &f.fan_base, &f.clip_queue,
-                              &f.tile_count, &f.tile_offset, &f.tile_cursor, &f.bins, &f.keys})
+                              &f.tile_count, &f.tile_offset, &f.tile_cursor, &f.bins, &f.keys, &f.counters,
+                              &f.rsqrt_tab, &f.color})
             t += d->bytes;
+        for (const OwnedOutput& o : e.b->owned) t += o.rgba8.bytes + o.vis.bytes;
         return t;
     }
 
@@ -155,9 +163,11 @@ struct swr_server {
                 if (!e->busy || !e->done.load()) continue;
                 lk.unlock();
                 std::string err;
-                const swr_status st = e->b->sync(err);
+                const swr_status st = e->b->sync(err);  // may re-render with grown buffers
                 const double t = now_ms();
+                const uint64_t eb = one_engine_bytes(*e);
                 lk.lock();
+                e->bytes = eb;
                 for (size_t i = 0; i < e->reqs.size(); ++i) {
                     Done d{};
                     d.c.ticket = e->reqs[i].ticket;
@@ -188,7 +198,8 @@ struct swr_server {
                 std::vector<FB*> fbs;
                 std::vector<std::pair<int32_t, int32_t>> dims;
                 std::vector<uint64_t> tris;
-                const uint64_t others = engine_bytes() - one_engine_bytes(e);
+                std::vector<bool> trans;
+                const uint64_t others = engine_bytes() - e.bytes;
                 while (!pending.empty() && reqs.size() < opts.max_batch_views) {
                     const Req& q = pending.front();
                     // Admission: this engine's buffers for the grown batch must
@@ -196,19 +207,14 @@ struct swr_server {
                     // other engines (a lone request is always tried).
                     dims.push_back({q.r.width, q.r.height});
                     tris.push_back(scenes[q.r.scene]->impl.tri_total);
-                    const uint64_t need = std::max(one_engine_bytes(e), batch_need(dims, tris));
+                    trans.push_back(scene_translucent[q.r.scene]);
+                    const uint64_t need = std::max(e.bytes, batch_need(dims, tris, trans));
                     if (!reqs.empty() && scene_bytes + fb_bytes + others + need +
                                                  (uint64_t)q.r.width * q.r.height * 12 > opts.memory_budget) {
-                        dims.pop_back();
-                        tris.pop_back();
                         break;
                     }
                     FB* f = get_fb(q.r.width, q.r.height);
-                    if (!f) {  // wait for framebuffers to be released
-                        dims.pop_back();
-                        tris.pop_back();
-                        break;
-                    }
+                    if (!f) break;  // wait for framebuffers to be released
                     reqs.push_back(q);
                     fbs.push_back(f);
                     pending.pop_front();
@@ -239,7 +245,9 @@ struct swr_server {
                 if (st == SWR_OK) {
                     if (cudaLaunchHostFunc(e.stream, on_done, &cb_args[ei]) != cudaSuccess) st = SWR_CUDA_ERROR;
                 }
+                const uint64_t eb = one_engine_bytes(e);
                 lk.lock();
+                e.bytes = eb;
                 if (st != SWR_OK) {
                     // Report the failure for every request of the batch.
                     const double t = now_ms();
@@ -309,6 +317,7 @@ swr_status swr_server_create(const swr_server_opts* opts, swr_server** out) {
             return st;
         }
         s->cb_args[i] = {s, e.get()};
+        e->bytes = swr_server::one_engine_bytes(*e);
         s->engines.push_back(std::move(e));
     }
     s->worker = std::thread([s] { s->run(); });
@@ -359,6 +368,9 @@ swr_status swr_server_add_scene(swr_server* s, const swr_scene* scene, int32_t* 
     }
     s->scene_bytes += scene->impl.d_bytes;
     s->scenes.push_back(scene);
+    bool trans = false;
+    for (const HMesh& m : scene->impl.meshes) trans |= !m.translucent.empty();
+    s->scene_translucent.push_back(trans);
     *id = (int32_t)s->scenes.size() - 1;
     return SWR_OK;
 }
