@@ -819,6 +819,7 @@ __device__ __forceinline__ bool region_exact(const PacketCtx& c, const float w[1
 template <int S>
 struct RasterShared {
     static constexpr int kThreads = S <= 16 ? 128 : 256;
+    static constexpr int kMinBlocks = S <= 16 ? 6 : 3;         // CTAs per SM the register budget allows
     static constexpr int kRegions = kThreads + kThreads / 2;  // regions staged per round
     unsigned long long sk[S * S];                             // depth keys of the scheduling tile
     // Regions of the round, in packet order.
@@ -1001,7 +1002,7 @@ __device__ __forceinline__ void packet_regions(RasterShared<S>& s, const PacketC
 // regions (a block-wide scan places them), pass 2 rasterizes the exact
 // regions' quads flattened over all lanes, pass 3 the sequential regions.
 template <int S>
-__global__ void __launch_bounds__(RasterShared<S>::kThreads) k_raster(FrameArgs a) {
+__global__ void __launch_bounds__(RasterShared<S>::kThreads, RasterShared<S>::kMinBlocks) k_raster(FrameArgs a) {
     using Sh = RasterShared<S>;
     constexpr int NT = Sh::kThreads, R = Sh::kRegions, NW = NT / 32;
     extern __shared__ __align__(16) unsigned char raster_smem[];
