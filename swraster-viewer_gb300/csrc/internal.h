@@ -248,7 +248,7 @@ struct FrameArgs {
     RecShade* rec_s;
     uint32_t* fan_base;
     uint2* clip_queue;         // (g, draw)
-    uint32_t* tile_count;      // n_bins
+    uint32_t* tile_count;      // n_bins; after k_scan, the raster tile order
     uint32_t* tile_offset;     // n_bins + 1
     uint32_t* tile_cursor;     // n_bins
     uint32_t* bins;

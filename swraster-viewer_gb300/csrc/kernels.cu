@@ -614,7 +614,20 @@ __global__ void __launch_bounds__(128) k_clip(FrameArgs a) {
     }
 }
 
-// Exclusive scan of tile counts (single CTA). Also seeds the scatter cursors.
+// Bucket of a bin of c packets for the raster visiting order: 0 for an empty
+// bin, else two buckets per octave of c. Scheduling tiles below kOrderMinTile
+// px are cheap enough that the raster visits them in screen order.
+constexpr int kOrderBuckets = 66;
+constexpr uint32_t kOrderMinTile = 32;
+__device__ __forceinline__ uint32_t order_bucket(uint32_t c) {
+    if (c == 0u) return 0u;
+    const uint32_t bits = 32u - (uint32_t)__clz(c);
+    const uint32_t half = bits >= 2u ? (c >> (bits - 2u)) & 1u : 0u;
+    return 2u * bits - 1u + half;
+}
+
+// Exclusive scan of tile counts (single CTA). Also seeds the scatter cursors
+// and writes the raster's tile visiting order.
 __global__ void __launch_bounds__(1024) k_scan(FrameArgs a) {
     __shared__ uint32_t part[1024];
     const uint32_t n = a.dyn->n_bins;
@@ -641,6 +654,44 @@ __global__ void __launch_bounds__(1024) k_scan(FrameArgs a) {
         a.tile_offset[n] = part[1023];
         a.counters->pairs = part[1023];
         if ((uint64_t)part[1023] > a.bin_cap) atomicOr(&a.counters->status, ST_BIN_OVERFLOW);
+    }
+    // Raster visiting order: opaque scheduling tiles, heaviest bins first
+    // (longest job first over the persistent CTAs, so the kernel does not end
+    // on a late heavy tile). Bins are bucketed by half-octave of their size;
+    // order within a bucket is arbitrary, since tiles are independent. The
+    // counts are no longer needed, so the order is written over them.
+    if (a.sched_tile < kOrderMinTile) return;
+    __shared__ uint32_t bucket[kOrderBuckets];
+    if (threadIdx.x < kOrderBuckets) bucket[threadIdx.x] = 0u;
+    __syncthreads();
+    // Lanes of a warp that share a bucket add to it once (most bins of a
+    // frame fall in a few buckets).
+    const uint32_t n_st = a.dyn->n_stiles;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t n_st_pad = (n_st + 1023u) & ~1023u;
+    for (uint32_t i = threadIdx.x; i < n_st_pad; i += 1024u) {
+        const uint32_t k = i < n_st ? order_bucket(a.tile_offset[i + 1] - a.tile_offset[i]) : kOrderBuckets;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, k);
+        if (k < kOrderBuckets && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&bucket[k], (uint32_t)__popc(peers));
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t acc = 0;
+        for (int k = kOrderBuckets - 1; k >= 0; --k) {
+            const uint32_t c = bucket[k];
+            bucket[k] = acc;
+            acc += c;
+        }
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n_st_pad; i += 1024u) {
+        const uint32_t k = i < n_st ? order_bucket(a.tile_offset[i + 1] - a.tile_offset[i]) : kOrderBuckets;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, k);
+        const uint32_t leader = (uint32_t)(__ffs(peers) - 1);
+        uint32_t base = 0;
+        if (k < kOrderBuckets && lane == leader) base = atomicAdd(&bucket[k], (uint32_t)__popc(peers));
+        base = __shfl_sync(0xFFFFFFFFu, base, leader);
+        if (k < kOrderBuckets) a.tile_count[base + __popc(peers & ((1u << lane) - 1u))] = i;
     }
 }
 
@@ -1011,7 +1062,10 @@ __global__ void __launch_bounds__(RasterShared<S>::kThreads, RasterShared<S>::kM
     const uint32_t n_tiles = a.dyn->n_stiles;
     for (uint32_t iter = 0;; ++iter) {
 #if SWR_RASTER_PERSISTENT
-        if (threadIdx.x == 0) s.cur_tile = atomicAdd(&a.counters->work_next, 1u);
+        if (threadIdx.x == 0) {
+            const uint32_t w = atomicAdd(&a.counters->work_next, 1u);
+            s.cur_tile = w >= n_tiles ? n_tiles : a.sched_tile >= kOrderMinTile ? a.tile_count[w] : w;
+        }
         __syncthreads();
         const uint32_t st = s.cur_tile;
 #else
