@@ -17,6 +17,8 @@
  *   swr_render_frame       Renderer::render_scene             src/renderer.rs:201-256
  *                        + Renderer::update_auto_exposure     src/renderer.rs:258-290
  *   swr_blit               Renderer::blit_to_buffer           src/renderer.rs:293-355
+ *   swr_renderer_set_blit_target  (blit_to_buffer's destination, given once
+ *                           so the shading pass writes it directly)
  *   swr_read_visbuffer     (no reference counterpart: the reference keeps a
  *                           per-tile packet index, src/tilerasterizer.rs:33-36;
  *                           this exports primitive + triangle ID per pixel)
@@ -380,6 +382,20 @@ swr_status swr_renderer_sync(swr_renderer* r);
  * row_stride in pixels (0 = width). For an odd height the last row is left
  * untouched, as blit_to_buffer's chunks_exact drops it (src/renderer.rs:298). */
 swr_status swr_blit(swr_renderer* r, uint32_t* pixels, size_t row_stride, void* stream);
+
+/* Host framebuffer that every following frame's shading pass writes its
+ * RGBA8 pixels into directly, over the host link, while it shades (the
+ * renderer's device copy is written as well). A swr_blit to the same
+ * pointer and row_stride then only waits for the frame; a blit anywhere
+ * else copies as before. `pixels` must be device-writable: pinned or
+ * registered host memory, device or managed memory, or any host memory on
+ * systems whose GPU reads the host page tables (Grace); SWR_INVALID_ARG
+ * otherwise. It must hold (height & ~1) rows of row_stride pixels (0 =
+ * width) and stay valid while frames render into it. NULL detaches. The
+ * reference blits into one of two backbuffers that alternate per frame
+ * (src/main.rs:522-543): set the frame's backbuffer before its
+ * swr_render_frame (a cheap call), then swr_blit into it. */
+swr_status swr_renderer_set_blit_target(swr_renderer* r, uint32_t* pixels, size_t row_stride);
 
 /* Visibility buffer, width*height entries: (static triangle ID << 3) | fan
  * index for covered pixels, UINT64_MAX where depth stayed +inf. Static

@@ -281,6 +281,10 @@ swr_status enqueue_frame(swr_renderer* r, const swr_scene* scene, const swr_came
     v.vis = r->vis.as<uint64_t>();
     v.tile_lum = r->tile_lum.as<float>();
     v.out_pitch = (uint32_t)r->width;
+    v.rgba8_host = r->blit_target_dev;
+    v.host_pitch = (uint32_t)r->blit_stride;
+    r->frame_target = r->blit_target;
+    r->frame_stride = r->blit_stride;
     const bool deferred = dt > 0.0f;
     r->eng.defer_resolve = deferred;
     if (deferred) {
@@ -407,11 +411,52 @@ swr_status swr_blit(swr_renderer* r, uint32_t* pixels, size_t row_stride, void* 
     if (st != SWR_OK) return st;
     if (row_stride == 0) row_stride = (size_t)r->width;
     if (row_stride < (size_t)r->width) return fail(SWR_INVALID_ARG, "row_stride smaller than width");
+    if (pixels == r->frame_target && row_stride == r->frame_stride) {
+        // The shading pass already wrote this frame into `pixels`.
+        const cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+        if (e != cudaSuccess) return cuda_fail(e, "blit wait");
+        return SWR_OK;
+    }
     const size_t rows = (size_t)(r->height & ~1);
     cudaError_t e = cudaMemcpy2DAsync(pixels, row_stride * sizeof(uint32_t), r->rgba8.p, (size_t)r->width * 4,
                                       (size_t)r->width * 4, rows, cudaMemcpyDefault, (cudaStream_t)stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_fail(e, "blit copy");
+    return SWR_OK;
+}
+
+swr_status swr_renderer_set_blit_target(swr_renderer* r, uint32_t* pixels, size_t row_stride) {
+    if (!r) return fail(SWR_INVALID_ARG, "null argument");
+    if (!pixels) {
+        r->blit_target = r->blit_target_dev = nullptr;
+        r->blit_stride = 0;
+        return SWR_OK;
+    }
+    if (row_stride == 0) row_stride = (size_t)r->width;
+    if (row_stride < (size_t)r->width || row_stride > 0xFFFFFFFFull)
+        return fail(SWR_INVALID_ARG, "row_stride smaller than width or above 2^32-1");
+    // The device must be able to store to the memory: pinned or registered
+    // host memory (through its device address), device or managed memory,
+    // or pageable host memory where the device reads the host page tables.
+    cudaPointerAttributes at{};
+    cudaError_t e = cudaPointerGetAttributes(&at, pixels);
+    cudaGetLastError();
+    uint32_t* dev = nullptr;
+    if (e == cudaSuccess && (at.type == cudaMemoryTypeHost || at.type == cudaMemoryTypeDevice ||
+                             at.type == cudaMemoryTypeManaged)) {
+        dev = static_cast<uint32_t*>(at.devicePointer);
+    } else if (e == cudaSuccess && at.type == cudaMemoryTypeUnregistered) {
+        int d = 0, pageable = 0;
+        cudaGetDevice(&d);
+        if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, d) == cudaSuccess && pageable)
+            dev = pixels;
+    }
+    if (!dev)
+        return fail(SWR_INVALID_ARG,
+                    "blit target is not device-writable (use pinned or registered host memory)");
+    r->blit_target = pixels;
+    r->blit_target_dev = dev;
+    r->blit_stride = row_stride;
     return SWR_OK;
 }
 

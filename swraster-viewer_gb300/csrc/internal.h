@@ -126,7 +126,8 @@ struct alignas(16) DView {
     float* color;              // key_pitch * tiles_y * 64 * 3 (padded tile grid) when flags != 0
     float* tile_lum;           // tiles_x*tiles_y
     uint32_t out_pitch;
-    uint32_t pad2[3];
+    uint32_t host_pitch;       // row pitch of rgba8_host
+    uint32_t* rgba8_host;      // device-writable host copy of rgba8 (rows below height & ~1), or null
 };
 
 // DView.flags

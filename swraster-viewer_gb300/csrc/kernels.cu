@@ -1507,7 +1507,9 @@ __device__ __forceinline__ void shade_thread(const FrameArgs& a, const uint8_t* 
         c[1] = col.y;
         c[2] = col.z;
     } else if (px < v.width && py < (v.height & ~1)) {
-        v.rgba8[(uint64_t)py * v.out_pitch + (uint64_t)px] = tonemap_pack(col, v.exposure);
+        const uint32_t c = tonemap_pack(col, v.exposure);
+        v.rgba8[(uint64_t)py * v.out_pitch + (uint64_t)px] = c;
+        if (v.rgba8_host) v.rgba8_host[(uint64_t)py * v.host_pitch + (uint64_t)px] = c;
     }
 }
 
@@ -1728,7 +1730,9 @@ __global__ void k_resolve(FrameArgs a) {
     const uint32_t x = i % w, y = i / w;
     const float* c = v.color + ((uint64_t)y * v.key_pitch + x) * 3u;
     const float e = a.exposure_dev ? *a.exposure_dev : v.exposure;
-    v.rgba8[(uint64_t)y * v.out_pitch + x] = tonemap_pack(mk3(c[0], c[1], c[2]), e);
+    const uint32_t p = tonemap_pack(mk3(c[0], c[1], c[2]), e);
+    v.rgba8[(uint64_t)y * v.out_pitch + x] = p;
+    if (v.rgba8_host) v.rgba8_host[(uint64_t)y * v.host_pitch + x] = p;
 }
 
 // --------------------------------------------------------------------------

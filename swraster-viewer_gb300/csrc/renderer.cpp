@@ -5,7 +5,6 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
-#include <numeric>
 
 namespace swr {
 
@@ -28,30 +27,35 @@ Frustum test_sphere_frustum(const float sphere[4], const swr_camera& cam) {
     return r;
 }
 
-// OrderedFloat ordering: NaN sorts after everything.
-inline bool ordered_less(float a, float b) {
-    if (a != a) return false;
-    if (b != b) return true;
-    return a < b;
+// OrderedFloat ordering as an unsigned key: monotonic in the float value,
+// every NaN above +inf and equal to the others, -0 and +0 equal (they
+// compare equal, so a stable sort keeps them in index order).
+inline uint32_t ordered_bits(float f) {
+    if (f != f) return 0xFFFFFFFFu;
+    if (f == 0.0f) f = 0.0f;
+    uint32_t b;
+    std::memcpy(&b, &f, sizeof(b));
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
 }
 
 }  // namespace
 
 void build_view_draws(const SceneImpl& s, const swr_camera& cam, uint32_t view_idx, uint32_t scene_idx,
                       uint32_t& tri_cursor, std::vector<DDraw>& draws, std::vector<DChunk>& chunks) {
-    // compute_nodes_by_distance: stable sort by squared distance.
+    // compute_nodes_by_distance: stable sort by squared distance, as one
+    // sort of (distance key, node index) words.
     const size_t nn = s.nodes.size();
-    std::vector<uint32_t> order(nn);
-    std::iota(order.begin(), order.end(), 0u);
-    std::vector<float> key(nn);
+    thread_local std::vector<uint64_t> order;
+    order.resize(nn);
     const V3 cp = {cam.position[0], cam.position[1], cam.position[2]};
     for (size_t i = 0; i < nn; ++i) {
         const V3 d = sub(cp, {s.nodes[i].sphere[0], s.nodes[i].sphere[1], s.nodes[i].sphere[2]});
-        key[i] = dot3(d, d);
+        order[i] = ((uint64_t)ordered_bits(dot3(d, d)) << 32) | (uint64_t)i;
     }
-    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return ordered_less(key[a], key[b]); });
+    std::sort(order.begin(), order.end());
     const M4 vp = from_array(cam.view_project);
-    for (uint32_t ni : order) {
+    for (const uint64_t o : order) {
+        const uint32_t ni = (uint32_t)o;
         const HNode& n = s.nodes[ni];
         if (n.mesh < 0) continue;
         const M4 mvp = mulmm(vp, n.transform);
@@ -213,8 +217,10 @@ inline uint32_t grow(uint32_t cur, uint64_t need) {
 
 swr_status FrameEngine::prepare(const std::vector<const SceneImpl*>& scenes, std::vector<DView>& vws,
                                 const std::vector<const swr_camera*>& cams, std::string& err) {
-    std::vector<DDraw> hdraws;
-    std::vector<DChunk> hchunks;
+    std::vector<DDraw>& hdraws = h_draws;
+    std::vector<DChunk>& hchunks = h_chunks;
+    hdraws.clear();
+    hchunks.clear();
     uint32_t tri_cursor = 0;
     uint32_t stile_cursor = 0, quad_cursor = 0, max_px = 0;
     uint64_t key_cursor = 0, color_floats = 0;

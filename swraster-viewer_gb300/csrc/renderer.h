@@ -82,6 +82,8 @@ struct FrameEngine {
     DBuf color;                // linear colour of views that need it (padded tile grids)
     bool defer_resolve = false;// the caller resolves (renderer frames with dt > 0)
     HBuf h_stage;
+    std::vector<DDraw> h_draws;  // per-frame draw and chunk lists (capacity kept)
+    std::vector<DChunk> h_chunks;
     TableLayout lay;
     cudaEvent_t stage_done = nullptr;
     bool stage_pending = false;
@@ -142,6 +144,15 @@ struct swr_renderer {
     swr_renderer_opts opts{};
     swr::FrameEngine eng;
     swr::DBuf rgba8, vis, tile_lum;
+    // Host memory the shading pass also writes RGBA8 into
+    // (swr_renderer_set_blit_target): the caller's pointer, the address the
+    // device uses for it, its row pitch in pixels; and the target the last
+    // enqueued frame was rendered into.
+    uint32_t* blit_target = nullptr;
+    uint32_t* blit_target_dev = nullptr;
+    size_t blit_stride = 0;
+    uint32_t* frame_target = nullptr;
+    size_t frame_stride = 0;
     swr::ExposureState expo;
     // Mapped pinned memory for the dt > 0 exposure step.
     float* h_lum = nullptr;

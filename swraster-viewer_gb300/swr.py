@@ -174,7 +174,7 @@ class ServerStats(C.Structure):
 EXPORTS = [
     "swr_scene_create", "swr_scene_destroy", "swr_scene_get_info", "swr_scene_export", "swr_camera_init",
     "swr_camera_update", "swr_renderer_create", "swr_renderer_destroy", "swr_render_frame", "swr_renderer_sync",
-    "swr_blit", "swr_read_visbuffer", "swr_renderer_device_outputs", "swr_renderer_get_exposure",
+    "swr_blit", "swr_renderer_set_blit_target", "swr_read_visbuffer", "swr_renderer_device_outputs", "swr_renderer_get_exposure",
     "swr_renderer_set_exposure", "swr_renderer_get_stats", "swr_renderer_get_tile_luminance", "swr_last_error",
     "swr_abi_version", "swr_renderer_set_profiling", "swr_renderer_get_profile", "swr_render_frame_noalloc",
     "swr_batch_create", "swr_batch_destroy", "swr_batch_render", "swr_batch_sync", "swr_batch_output",
@@ -208,6 +208,7 @@ def lib():
         "swr_render_frame": ([vp, vp, C.POINTER(Camera), C.c_float, vp], C.c_int),
         "swr_renderer_sync": ([vp], C.c_int),
         "swr_blit": ([vp, vp, C.c_size_t, vp], C.c_int),
+        "swr_renderer_set_blit_target": ([vp, vp, C.c_size_t], C.c_int),
         "swr_read_visbuffer": ([vp, vp, vp], C.c_int),
         "swr_renderer_device_outputs": ([vp, C.POINTER(vp), C.POINTER(vp)], C.c_int),
         "swr_renderer_get_exposure": ([vp, f32p], C.c_int),
@@ -415,6 +416,13 @@ class Renderer:
             out = np.zeros((self.height, self.width), np.uint32)
         check(lib().swr_blit(self.handle, out.ctypes.data_as(C.c_void_p), out.shape[1], stream))
         return out
+
+    def set_blit_target(self, ptr, row_stride=0, keep=None):
+        """Host framebuffer (address as int, or None to detach) that each
+        following frame's shading pass writes directly; `keep` holds the
+        object that owns the memory alive while it is the target."""
+        check(lib().swr_renderer_set_blit_target(self.handle, C.c_void_p(ptr) if ptr else None, row_stride))
+        self._blit_keep = keep if ptr else None
 
     def visbuffer(self, out=None, stream=None):
         if out is None:
