@@ -422,7 +422,7 @@ typedef struct swr_frame_stats {
     float tile_luminance_mean;
     float exposure;
     uint32_t sched_tile;        /* scheduling tile the renderer uses */
-    uint64_t staged_bytes;      /* host-to-device bytes per frame (draw and chunk tables) */
+    uint64_t staged_bytes;      /* host-to-device bytes per frame (frame, scene and view headers, node order) */
 } swr_frame_stats;
 
 swr_status swr_renderer_get_stats(swr_renderer* r, swr_frame_stats* out);
@@ -433,7 +433,8 @@ swr_status swr_renderer_get_stats(swr_renderer* r, swr_frame_stats* out);
 swr_status swr_renderer_get_tile_luminance(swr_renderer* r, float* out, uint32_t count);
 
 /* Stage timing with CUDA events recorded on the frame's stream between the
- * kernels: reset, frontend, clip, scan, scatter, raster, shade, resolve.
+ * kernels: draws (counter reset and the draw-list build), frontend, clip,
+ * scan, scatter, raster, shade, resolve.
  * swr_renderer_get_profile waits for outstanding frames and returns the mean
  * milliseconds per stage over the frames since profiling was enabled. */
 #define SWR_STAGES 8

@@ -365,6 +365,7 @@ swr_status check_frame(swr_renderer* r) {
         e = cudaMemcpy(&c, r->eng.counters.p, sizeof(c), cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) return cuda_fail(e, "counter readback");
         r->eng.last = c;
+        if (c.status & ST_DRAW_OVERFLOW) return fail(SWR_OVERFLOW, "draw list above its capacity");
         if (!(c.status & kStRetry)) {
             r->checked = true;
             return SWR_OK;
@@ -503,7 +504,7 @@ swr_status swr_renderer_get_stats(swr_renderer* r, swr_frame_stats* o) {
     if (st != SWR_OK) return st;
     std::memset(o, 0, sizeof(*o));
     const DCounters& c = r->eng.last;
-    o->triangles_in = r->eng.dyn.tri_total;
+    o->triangles_in = c.draw_tris;
     o->triangles_clipped = c.clip_queue;
     o->setup_triangles = c.setup_tris;
     o->bin_pairs = c.pairs;
@@ -512,7 +513,7 @@ swr_status swr_renderer_get_stats(swr_renderer* r, swr_frame_stats* o) {
     o->overflow_retries = r->eng.retries;
     o->exposure = r->expo.exposure;
     o->sched_tile = r->opts.sched_tile;
-    o->staged_bytes = r->eng.lay.total;
+    o->staged_bytes = r->eng.lay.staged;
     return SWR_OK;
 }
 

@@ -82,6 +82,26 @@ struct alignas(16) DMaterial {
     uint32_t pad[1];
 };
 
+// Draw-list inputs (render_node / render_mesh, src/renderer.rs:357-420),
+// laid out so one node needs two dependent reads: per node its world
+// transform, static triangle base and its mesh's entry range; per mesh entry
+// (opaque primitives, then translucent ones) the primitive, its local
+// bounding sphere, triangle count and static triangle base within the mesh.
+struct alignas(16) DNodeInfo {
+    float xform[16];
+    uint32_t tri_id_base;
+    uint32_t entry_begin;      // into DScene.mesh_entries
+    uint32_t n_opaque;
+    uint32_t n_total;          // 0 for a node without a mesh
+};
+struct alignas(16) DMeshEntry {
+    float sphere[4];
+    uint32_t prim;             // global primitive index
+    uint32_t tri_count;
+    uint32_t tri_id_base;
+    uint32_t pad;
+};
+
 // Scene-wide device constants. The per-voxel SH4 of the non-GI path is
 // the same for every voxel (src/gi.rs:123-149): rgb = irradiance_sh * scale,
 // w0 = light intensity (per voxel), w1 = sky visibility, w2 = w3 = 0.
@@ -93,6 +113,8 @@ struct alignas(16) DScene {
     const DMaterial* materials;
     const DTexture* textures;  // scene textures, then cubemap, specular, brdf lut
     const float* voxel_light;  // voxel_n^3
+    const DNodeInfo* node_info;
+    const DMeshEntry* mesh_entries;
     uint32_t tex_cubemap, tex_specular, tex_brdf_lut, voxel_n;
     float voxel_min[3];
     float voxel_size_f[3];     // (max - min) / n per axis
@@ -128,11 +150,19 @@ struct alignas(16) DView {
     uint32_t out_pitch;
     uint32_t host_pitch;       // row pitch of rgba8_host
     uint32_t* rgba8_host;      // device-writable host copy of rgba8 (rows below height & ~1), or null
+    // Camera of the device draw-list build (RenderCamera, src/rendercamera.rs).
+    float cam_view[16];
+    float cam_view_project[16];
+    float cam_planes[24];      // view_clip_planes, view space
+    uint32_t order_base;       // this view's sorted nodes in FrameArgs.node_order
+    uint32_t n_order;
+    uint32_t pad3[2];
 };
 
 // DView.flags
 constexpr uint32_t kViewLinear = 1u;       // caller wants linear colour (exposure applied later)
 constexpr uint32_t kViewTranslucent = 2u;  // view has translucent draws: shade, blend, then resolve
+                                           // (set on the device by the draw-list build)
 
 struct alignas(16) DDraw {
     float mvp[16];
@@ -194,6 +224,7 @@ enum : uint32_t {
     ST_QUEUE_OVERFLOW = 4u,
     ST_TIMEOUT = 8u,
     ST_TRANS_OVERFLOW = 16u,   // a scheduling tile has more translucent packets than one sort holds
+    ST_DRAW_OVERFLOW = 32u,    // draw list above its capacity (the host sizes it from scene bounds)
 };
 // Status bits after which a frame is incomplete and is rendered again.
 constexpr uint32_t kStRetry = ST_BIN_OVERFLOW | ST_CLIP_OVERFLOW | ST_QUEUE_OVERFLOW | ST_TRANS_OVERFLOW;
@@ -208,7 +239,8 @@ struct alignas(16) DCounters {
     uint32_t work_next;        // persistent raster work cursor
     uint32_t trans_next;       // translucent pass work cursor
     uint32_t trans_packets;    // translucent (packet, tile) pairs
-    uint32_t pad;
+    uint32_t draw_tris;        // triangles of the frame's draws (the draw-list build's T)
+    uint32_t draw_done;        // CTAs done counting draws (zero between frames)
 };
 
 // Per-frame counts, uploaded with the tables: kernels read them from device
@@ -222,17 +254,17 @@ struct alignas(16) DFrameDyn {
     uint32_t total_quads;      // shading work over all views
     uint32_t max_view_pixels;  // largest width * (height & ~1)
     uint32_t n_bins;           // n_stiles, or 2 * n_stiles with translucent bins after the opaque ones
-    uint32_t pad;
+    uint32_t n_slots;          // node slots of all views (device draw-list build)
 };
 
 // Everything a frame's kernels need, passed by value: pointers and
 // capacities only (they change only when buffers grow).
 struct FrameArgs {
-    const DFrameDyn* dyn;
+    DFrameDyn* dyn;            // n_chunks and tri_total written by the draw-list build
     const DScene* scenes;
-    const DView* views;
-    const DDraw* draws;
-    const DChunk* chunks;
+    DView* views;              // flags gain kViewTranslucent in the draw-list build
+    DDraw* draws;
+    DChunk* chunks;
     uint32_t chunk_cap;        // grid of k_frontend
     uint32_t tri_cap;          // main record slots allocated
     uint32_t extra_cap;        // extra record slots
@@ -259,8 +291,13 @@ struct FrameArgs {
     const float* exposure_dev; // exposure computed by the host step (dt > 0)
     uint32_t raster_grid;      // persistent raster CTAs
     uint32_t shade_grid;       // grid-stride shading CTAs
-    uint32_t has_translucent;  // some view has translucent draws: run the translucent pass
+    uint32_t has_translucent;  // some view's scene has translucent primitives: run the translucent pass
     uint32_t defer_resolve;    // the caller launches the resolve (exposure from the host step)
+    const uint32_t* node_order;// node slots: per view, node indices nearest first (device draw-list build)
+    uint4* slot_blocks;        // per 256 node slots: draws, triangles, chunks; then their exclusive offsets
+    uint32_t draw_cap;
+    uint32_t slot_cap;
+    uint32_t gpu_draws;        // build draws and chunks on the device (else the host staged them)
 };
 
 // Launch wrappers (kernels.cu). `ev`, when given, holds 8 events recorded

@@ -1,8 +1,14 @@
 // GB300 (sm_103a) kernels for the per-frame rasterization path.
 //
-// Frame = reset -> frontend -> clip -> scan -> scatter -> raster -> shade.
-// All kernels are batched over views: the plain path is a batch of one.
+// Frame = reset -> draw_emit -> frontend -> clip -> scan -> scatter -> raster
+// -> shade (-> translucent -> resolve). All kernels are batched over views:
+// the plain path is a batch of one.
 //
+//   k_reset     counters and bin counts cleared; per node slot (nodes sorted
+//   k_draw_emit by the host) MVP, sphere/frustum test and draw counts
+//               (render_node / render_mesh, src/renderer.rs:357-420), then
+//               the draws and their 256-triangle chunks in the host loop's
+//               order.
 //   k_frontend  one thread per input triangle (256-triangle chunks of a draw):
 //               vertex transform (src/renderer.rs:470-574), trivial clip
 //               classification, triangle setup (bin_triangle,
@@ -433,7 +439,275 @@ __device__ __forceinline__ void store_records(const FrameArgs& a, uint32_t slot,
     for (int i = 0; i < 11; ++i) dq[i] = sq[i];
 }
 
-__global__ void k_reset(FrameArgs a) {
+// --------------------------------------------------------------------------
+// Draw list: render_scene's front half (src/renderer.rs:201-210, 357-420).
+// The host sorts each view's nodes nearest first (compute_nodes_by_distance)
+// into node slots, view after view. Per slot the device forms the node's MVP,
+// tests every primitive's world bounding sphere against the view frustum and
+// emits a draw, with its 256-triangle chunks, for each primitive not
+// outside. k_reset's CTAs count per block of 256 slots and the last of them
+// turns the block totals into offsets (so draws keep the host loop's order);
+// k_draw_emit scans within each block and writes the draws.
+// --------------------------------------------------------------------------
+struct DrawCount {
+    uint32_t draws, tris, chunks;
+};
+
+// Vec4::length with the pairwise dot (x*x + y*y) + (z*z + w*w).
+__device__ __forceinline__ float len4(const float* c) {
+    return __fsqrt_rn((c[0] * c[0] + c[1] * c[1]) + (c[2] * c[2] + c[3] * c[3]));
+}
+
+// Frustum class of a world-space sphere (test_sphere_frustum,
+// src/renderer.rs:130-142): 0 outside, 1 inside, 2 intersecting.
+__device__ __forceinline__ uint32_t sphere_class(const DView& v, const float ws[4]) {
+    const float* m = v.cam_view;
+    float cv[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) cv[r] = ((m[r] * ws[0] + m[4 + r] * ws[1]) + m[8 + r] * ws[2]) + m[12 + r] * 1.0f;
+    uint32_t res = 1u;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        const float* pl = v.cam_planes + 4 * i;
+        const float d = (pl[0] * cv[0] + pl[1] * cv[1]) + (pl[2] * cv[2] + pl[3] * cv[3]);
+        if (d < -ws[3]) return 0u;
+        if (d < ws[3]) res = 2u;
+    }
+    return res;
+}
+
+__device__ __forceinline__ uint32_t find_view_by_slot(const FrameArgs& a, uint32_t i) {
+    uint32_t lo = 0, hi = a.dyn->n_views - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (a.views[mid].order_base <= i) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Draws of one node (render_node + render_mesh): counted, and with EMIT
+// written from the given bases; `trans` is set when a translucent draw is
+// written.
+template <bool EMIT>
+__device__ DrawCount node_draws(const FrameArgs& a, uint32_t vi, const DView& v, const DScene& sc, uint32_t node,
+                                DrawCount base, bool& trans) {
+    DrawCount c{0u, 0u, 0u};
+    const DNodeInfo* np = sc.node_info + node;
+    const uint32_t n_total = np->n_total;
+    if (n_total == 0u) return c;
+    float t[16];
+    {
+        const float4* x = reinterpret_cast<const float4*>(np->xform);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const float4 q = __ldg(x + i);
+            t[4 * i] = q.x;
+            t[4 * i + 1] = q.y;
+            t[4 * i + 2] = q.z;
+            t[4 * i + 3] = q.w;
+        }
+    }
+    const uint32_t entry_begin = np->entry_begin, n_opaque = np->n_opaque, node_tri_base = np->tri_id_base;
+    const float max_scale = ((len4(t) + len4(t + 4)) + len4(t + 8)) / 3.0f;
+    float mvp[16];
+    if (EMIT) {
+        const float* p = v.cam_view_project;
+#pragma unroll
+        for (int col = 0; col < 4; ++col) {
+            const float* b = t + 4 * col;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) mvp[4 * col + r] = ((p[r] * b[0] + p[4 + r] * b[1]) + p[8 + r] * b[2]) + p[12 + r] * b[3];
+        }
+    }
+    for (uint32_t k = 0; k < n_total; ++k) {
+        const DMeshEntry me = sc.mesh_entries[entry_begin + k];
+        float ws[4];
+        // transform_point3: ((c0*x + c1*y) + c2*z) + c3.
+#pragma unroll
+        for (int r = 0; r < 3; ++r) ws[r] = ((t[r] * me.sphere[0] + t[4 + r] * me.sphere[1]) + t[8 + r] * me.sphere[2]) + t[12 + r];
+        ws[3] = me.sphere[3] * max_scale;
+        const uint32_t cls = sphere_class(v, ws);
+        if (cls == 0u) continue;
+        const uint32_t tc = me.tri_count;
+        if (tc == 0u) continue;
+        const uint32_t nch = (tc + (uint32_t)kChunkTris - 1u) / (uint32_t)kChunkTris;
+        if (EMIT) {
+            const uint32_t di = base.draws + c.draws, ci = base.chunks + c.chunks;
+            const bool translucent = k >= n_opaque;
+            if (di < a.draw_cap && (uint64_t)ci + nch <= a.chunk_cap &&
+                (uint64_t)base.tris + c.tris + tc <= a.tri_cap) {
+                DDraw d;
+#pragma unroll
+                for (int i = 0; i < 16; ++i) d.mvp[i] = mvp[i];
+                d.node = node;
+                d.prim = me.prim;
+                d.view = vi;
+                d.clip = cls == 2u ? 1u : 0u;
+                d.tri_begin = base.tris + c.tris;
+                d.tri_count = tc;
+                d.static_base = node_tri_base + me.tri_id_base;
+                d.scene = v.scene;
+                d.translucent = translucent ? 1u : 0u;
+                d.pad[0] = d.pad[1] = d.pad[2] = 0u;
+                a.draws[di] = d;
+                for (uint32_t j = 0; j < nch; ++j) a.chunks[ci + j] = DChunk{di, j * (uint32_t)kChunkTris};
+                trans |= translucent;
+            } else {
+                atomicOr(&a.counters->status, ST_DRAW_OVERFLOW);
+            }
+        }
+        c.draws += 1u;
+        c.tris += tc;
+        c.chunks += nch;
+    }
+    return c;
+}
+
+// Block-wide sum (SUM) or exclusive scan of three counters over NT threads;
+// `total` gets the block's sums.
+template <int NT>
+__device__ DrawCount block_scan3(DrawCount x, DrawCount& total, uint32_t* sm) {
+    constexpr int NW = NT / 32;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    DrawCount inc = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t d = __shfl_up_sync(0xFFFFFFFFu, inc.draws, o);
+        const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc.tris, o);
+        const uint32_t c = __shfl_up_sync(0xFFFFFFFFu, inc.chunks, o);
+        if (lane >= (uint32_t)o) {
+            inc.draws += d;
+            inc.tris += t;
+            inc.chunks += c;
+        }
+    }
+    __syncthreads();
+    if (lane == 31u) {
+        sm[warp] = inc.draws;
+        sm[NW + warp] = inc.tris;
+        sm[2 * NW + warp] = inc.chunks;
+    }
+    __syncthreads();
+    DrawCount before{0u, 0u, 0u};
+    total = DrawCount{0u, 0u, 0u};
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+        if ((uint32_t)w < warp) {
+            before.draws += sm[w];
+            before.tris += sm[NW + w];
+            before.chunks += sm[2 * NW + w];
+        }
+        total.draws += sm[w];
+        total.tris += sm[NW + w];
+        total.chunks += sm[2 * NW + w];
+    }
+    return DrawCount{before.draws + inc.draws - x.draws, before.tris + inc.tris - x.tris,
+                     before.chunks + inc.chunks - x.chunks};
+}
+
+constexpr int kSlotBlock = 256;  // node slots per draw-list block
+
+__device__ __forceinline__ DrawCount slot_count(const FrameArgs& a, uint32_t i, uint32_t n) {
+    if (i >= n) return DrawCount{0u, 0u, 0u};
+    const uint32_t vi = find_view_by_slot(a, i);
+    const DView& v = a.views[vi];
+    bool unused = false;
+    return node_draws<false>(a, vi, v, a.scenes[v.scene], a.node_order[i], DrawCount{0u, 0u, 0u}, unused);
+}
+
+// Frame totals from the draw-list sums; a frame past the capacities (sized
+// from the scenes' bounds, so only through a defect) draws nothing and
+// reports it.
+__device__ __forceinline__ void set_draw_totals(const FrameArgs& a, const DrawCount& total) {
+    if (total.tris > a.tri_cap || total.chunks > a.chunk_cap || total.draws > a.draw_cap) {
+        atomicOr(&a.counters->status, ST_DRAW_OVERFLOW);
+        a.dyn->n_chunks = 0u;
+        a.dyn->tri_total = 0u;
+    } else {
+        a.dyn->n_chunks = total.chunks;
+        a.dyn->tri_total = total.tris;
+    }
+    a.counters->draw_tris = total.tris;
+}
+
+// Counts per block of 256 node slots (run by k_reset's CTAs); the last CTA
+// to finish turns the block totals into exclusive offsets and sets the
+// frame totals. No CTA waits for another. A frame of at most 256 slots is
+// counted, scanned and emitted by CTA 0 alone (k_draw_emit then has nothing
+// to do).
+__device__ void draw_count_blocks(const FrameArgs& a) {
+    __shared__ uint32_t sm[3 * (kSlotBlock / 32)];
+    __shared__ bool last;
+    const uint32_t n = a.dyn->n_slots;
+    const uint32_t nb = (n + kSlotBlock - 1) / kSlotBlock;
+    if (nb <= 1u) {
+        if (blockIdx.x != 0) return;
+        const uint32_t i = threadIdx.x;
+        const DrawCount mine = slot_count(a, i, n);
+        DrawCount total;
+        const DrawCount ex = block_scan3<kSlotBlock>(mine, total, sm);
+        if (threadIdx.x == 0) set_draw_totals(a, total);
+        if (mine.draws == 0u || total.tris > a.tri_cap || total.chunks > a.chunk_cap || total.draws > a.draw_cap)
+            return;
+        const uint32_t vi = find_view_by_slot(a, i);
+        const DView& v = a.views[vi];
+        bool trans = false;
+        node_draws<true>(a, vi, v, a.scenes[v.scene], a.node_order[i], ex, trans);
+        if (trans) atomicOr(&a.views[vi].flags, kViewTranslucent);
+        return;
+    }
+    for (uint32_t b = blockIdx.x; b < nb; b += gridDim.x) {
+        DrawCount t;
+        block_scan3<kSlotBlock>(slot_count(a, b * kSlotBlock + threadIdx.x, n), t, sm);
+        if (threadIdx.x == 0) a.slot_blocks[b] = make_uint4(t.draws, t.tris, t.chunks, 0u);
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(&a.counters->draw_done, 1u) == gridDim.x - 1u;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const uint32_t per = (nb + kSlotBlock - 1) / kSlotBlock;
+    const uint32_t b0 = threadIdx.x * per, b1 = min(b0 + per, nb);
+    DrawCount mine{0u, 0u, 0u};
+    for (uint32_t b = b0; b < b1; ++b) {
+        const uint4 t = __ldcg(a.slot_blocks + b);
+        mine.draws += t.x;
+        mine.tris += t.y;
+        mine.chunks += t.z;
+    }
+    DrawCount total;
+    DrawCount run = block_scan3<kSlotBlock>(mine, total, sm);
+    for (uint32_t b = b0; b < b1; ++b) {
+        const uint4 t = __ldcg(a.slot_blocks + b);
+        a.slot_blocks[b] = make_uint4(run.draws, run.tris, run.chunks, 0u);
+        run.draws += t.x;
+        run.tris += t.y;
+        run.chunks += t.z;
+    }
+    if (threadIdx.x == 0) set_draw_totals(a, total);
+}
+
+__global__ void __launch_bounds__(kSlotBlock) k_draw_emit(FrameArgs a) {
+    __shared__ uint32_t sm[3 * (kSlotBlock / 32)];
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.counters->draw_done = 0u;  // for the next frame
+    const uint32_t n = a.dyn->n_slots;
+    const uint32_t i = blockIdx.x * kSlotBlock + threadIdx.x;
+    if (n <= (uint32_t)kSlotBlock || blockIdx.x * kSlotBlock >= n || a.dyn->n_chunks == 0u) return;
+    const DrawCount mine = slot_count(a, i, n);
+    DrawCount t;
+    const DrawCount ex = block_scan3<kSlotBlock>(mine, t, sm);
+    if (mine.draws == 0u) return;
+    const uint4 base = a.slot_blocks[blockIdx.x];
+    const uint32_t vi = find_view_by_slot(a, i);
+    const DView& v = a.views[vi];
+    bool trans = false;
+    node_draws<true>(a, vi, v, a.scenes[v.scene], a.node_order[i],
+                     DrawCount{base.x + ex.draws, base.y + ex.tris, base.z + ex.chunks}, trans);
+    if (trans) atomicOr(&a.views[vi].flags, kViewTranslucent);
+}
+
+__global__ void __launch_bounds__(256) k_reset(FrameArgs a) {
     const uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t n = a.dyn->n_bins;
     for (uint32_t i = i0; i < n; i += gridDim.x * blockDim.x) a.tile_count[i] = 0u;
@@ -446,7 +720,9 @@ __global__ void k_reset(FrameArgs a) {
         a.counters->work_next = 0u;
         a.counters->trans_next = 0u;
         a.counters->trans_packets = 0u;
+        a.counters->draw_tris = a.gpu_draws ? 0u : a.dyn->tri_total;
     }
+    if (a.gpu_draws) draw_count_blocks(a);
 }
 
 // True when clip_against_frustum (src/renderer.rs:579-665) returns nothing
@@ -1787,7 +2063,9 @@ void frame_grids(int num_sms, uint32_t S, uint32_t* raster_grid, uint32_t* shade
 void launch_reset(const FrameArgs& a, void* stream) {
     cudaStream_t s = (cudaStream_t)stream;
     const uint32_t n = a.stile_cap > 0 ? a.stile_cap : 1u;
-    k_reset<<<min((n + 255) / 256, 512u), 256, 0, s>>>(a);
+    // Enough CTAs for the bins and for the draw-list blocks (one per 256 node slots).
+    const uint32_t slot_blocks = a.gpu_draws ? (a.slot_cap + kSlotBlock - 1u) / kSlotBlock : 0u;
+    k_reset<<<min(max((n + 255) / 256, slot_blocks), 1024u), 256, 0, s>>>(a);
 }
 
 void launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t* ev) {
@@ -1797,6 +2075,13 @@ void launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t* ev
     };
     mark(0);
     launch_reset(a, stream);
+    // Frames of at most 256 node slots are emitted inside k_reset
+    // (k_draw_emit returns at once); with a slot capacity of at most 256 it
+    // is not launched.
+    if (a.gpu_draws) {
+        const uint32_t sg = (a.slot_cap + kSlotBlock - 1u) / kSlotBlock;
+        if (sg > 1u) k_draw_emit<<<sg, kSlotBlock, 0, s>>>(a);
+    }
     mark(1);
     if (a.chunk_cap > 0) k_frontend<<<a.chunk_cap, kChunkTris, 0, s>>>(a);
     mark(2);

@@ -258,11 +258,11 @@ extern "C" swr_status swr_render_frame_noalloc(const swr_scene* scene, const swr
         return na_fail(SWR_CUDA_ERROR, "table upload failed");
     }
     FrameArgs a{};
-    a.dyn = reinterpret_cast<const DFrameDyn*>(base + oDyn);
+    a.dyn = reinterpret_cast<DFrameDyn*>(base + oDyn);
     a.scenes = reinterpret_cast<const DScene*>(base + oScene);
-    a.views = reinterpret_cast<const DView*>(base + oView);
-    a.draws = reinterpret_cast<const DDraw*>(base + oDraws);
-    a.chunks = reinterpret_cast<const DChunk*>(base + oChunks);
+    a.views = reinterpret_cast<DView*>(base + oView);
+    a.draws = reinterpret_cast<DDraw*>(base + oDraws);
+    a.chunks = reinterpret_cast<DChunk*>(base + oChunks);
     a.chunk_cap = nc;
     a.tri_cap = tri > 0 ? tri : 1u;
     a.extra_cap = kNaExtra;

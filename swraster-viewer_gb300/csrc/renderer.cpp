@@ -1,5 +1,6 @@
-// Per-frame host runtime: node sort, sphere/frustum classification, draw
-// and chunk tables, device capacities, kernel launch, exposure.
+// Per-frame host runtime: node sort, view tables, device capacities,
+// kernel launch, exposure. The draw list itself (MVPs, sphere/frustum
+// classification, draws and chunks) is built on the device.
 #include "renderer.h"
 
 #include <algorithm>
@@ -9,23 +10,6 @@
 namespace swr {
 
 namespace {
-
-enum class Frustum { Inside, Outside, Intersecting };
-
-// test_sphere_frustum (src/renderer.rs:130-142).
-Frustum test_sphere_frustum(const float sphere[4], const swr_camera& cam) {
-    const M4 view = from_array(cam.view);
-    const V4 cv = mulmv(view, {sphere[0], sphere[1], sphere[2], 1.0f});
-    Frustum r = Frustum::Inside;
-    for (int i = 0; i < 6; ++i) {
-        const V4 pl = {cam.view_clip_planes[i][0], cam.view_clip_planes[i][1], cam.view_clip_planes[i][2],
-                       cam.view_clip_planes[i][3]};
-        const float d = dot4(pl, cv);
-        if (d < -sphere[3]) return Frustum::Outside;
-        if (d < sphere[3]) r = Frustum::Intersecting;
-    }
-    return r;
-}
 
 // OrderedFloat ordering as an unsigned key: monotonic in the float value,
 // every NaN above +inf and equal to the others, -0 and +0 equal (they
@@ -40,10 +24,9 @@ inline uint32_t ordered_bits(float f) {
 
 }  // namespace
 
-void build_view_draws(const SceneImpl& s, const swr_camera& cam, uint32_t view_idx, uint32_t scene_idx,
-                      uint32_t& tri_cursor, std::vector<DDraw>& draws, std::vector<DChunk>& chunks) {
-    // compute_nodes_by_distance: stable sort by squared distance, as one
-    // sort of (distance key, node index) words.
+void sort_nodes_by_distance(const SceneImpl& s, const swr_camera& cam, std::vector<uint32_t>& out) {
+    // compute_nodes_by_distance: stable sort by squared distance, as one sort
+    // of (distance key, node index) words.
     const size_t nn = s.nodes.size();
     thread_local std::vector<uint64_t> order;
     order.resize(nn);
@@ -53,51 +36,7 @@ void build_view_draws(const SceneImpl& s, const swr_camera& cam, uint32_t view_i
         order[i] = ((uint64_t)ordered_bits(dot3(d, d)) << 32) | (uint64_t)i;
     }
     std::sort(order.begin(), order.end());
-    const M4 vp = from_array(cam.view_project);
-    for (const uint64_t o : order) {
-        const uint32_t ni = (uint32_t)o;
-        const HNode& n = s.nodes[ni];
-        if (n.mesh < 0) continue;
-        const M4 mvp = mulmm(vp, n.transform);
-        const HMesh& m = s.meshes[n.mesh];
-        // render_mesh (src/renderer.rs:386-420): opaque primitives, then translucent.
-        const size_t n_op = m.opaque.size();
-        for (size_t k = 0; k < n_op + m.translucent.size(); ++k) {
-            const bool translucent = k >= n_op;
-            const uint32_t lp = translucent ? m.translucent[k - n_op] : m.opaque[k];
-            const uint32_t gp = m.prims[lp];
-            const HPrimitive& p = s.prims[gp];
-            float ws[4];
-            {
-                const float max_scale =
-                    ((length4(n.transform.c[0]) + length4(n.transform.c[1])) + length4(n.transform.c[2])) / 3.0f;
-                const V3 c = transform_point3(n.transform, {p.sphere[0], p.sphere[1], p.sphere[2]});
-                ws[0] = c.x;
-                ws[1] = c.y;
-                ws[2] = c.z;
-                ws[3] = p.sphere[3] * max_scale;
-            }
-            const Frustum f = test_sphere_frustum(ws, cam);
-            if (f == Frustum::Outside) continue;
-            const uint32_t tc = (uint32_t)(p.idx.size() / 3);
-            if (tc == 0) continue;
-            DDraw d{};
-            to_array(mvp, d.mvp);
-            d.node = ni;
-            d.prim = gp;
-            d.view = view_idx;
-            d.clip = f == Frustum::Intersecting ? 1u : 0u;
-            d.tri_begin = tri_cursor;
-            d.tri_count = tc;
-            d.static_base = n.tri_id_base + p.tri_id_base;
-            d.scene = scene_idx;
-            d.translucent = translucent ? 1u : 0u;
-            const uint32_t di = (uint32_t)draws.size();
-            draws.push_back(d);
-            for (uint32_t t = 0; t < tc; t += kChunkTris) chunks.push_back({di, t});
-            tri_cursor += tc;
-        }
-    }
+    for (const uint64_t o : order) out.push_back((uint32_t)o);
 }
 
 void init_view(DView& v, const swr_camera& cam, int32_t width, int32_t height, uint32_t S) {
@@ -155,13 +94,17 @@ void ExposureState::update(const float* lum, size_t n, float dt) {
     exposure = std::exp2(ev);
 }
 
-TableLayout table_layout(uint32_t scene_cap, uint32_t view_cap, uint32_t draw_cap, uint32_t chunk_cap) {
+TableLayout table_layout(uint32_t scene_cap, uint32_t view_cap, uint32_t order_cap, uint32_t draw_cap,
+                         uint32_t chunk_cap) {
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
     TableLayout L;
     L.o_dyn = 0;
     L.o_scenes = al(sizeof(DFrameDyn));
     L.o_views = L.o_scenes + al(sizeof(DScene) * scene_cap);
-    L.o_draws = L.o_views + al(sizeof(DView) * view_cap);
+    L.o_order = L.o_views + al(sizeof(DView) * view_cap);
+    L.staged = L.o_order + al(sizeof(uint32_t) * order_cap);
+    L.o_slots = L.staged;
+    L.o_draws = L.o_slots + al(sizeof(uint4) * ((order_cap + 255) / 256));
     L.o_chunks = L.o_draws + al(sizeof(DDraw) * draw_cap);
     L.total = L.o_chunks + al(sizeof(DChunk) * chunk_cap);
     return L;
@@ -181,16 +124,21 @@ swr_status FrameEngine::init(std::string& err) {
         err = "cudaMalloc failed";
         return SWR_NO_MEMORY;
     }
+    if (cudaMemset(counters.p, 0, sizeof(DCounters)) != cudaSuccess) {
+        err = "cudaMemset failed";
+        return SWR_CUDA_ERROR;
+    }
     uint8_t tab[512];
     build_rsqrt_table(tab);
     if (cudaMemcpy(rsqrt_tab.p, tab, 512, cudaMemcpyHostToDevice) != cudaSuccess) {
         err = "cudaMemcpy failed";
         return SWR_CUDA_ERROR;
     }
-    if (cudaEventCreateWithFlags(&stage_done, cudaEventDisableTiming) != cudaSuccess) {
-        err = "cudaEventCreate failed";
-        return SWR_CUDA_ERROR;
-    }
+    for (cudaEvent_t& ev : stage_done)
+        if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+            err = "cudaEventCreate failed";
+            return SWR_CUDA_ERROR;
+        }
     return SWR_OK;
 }
 
@@ -202,9 +150,12 @@ void FrameEngine::release() {
     for (DBuf* b : {&tables, &tri_state, &rec_r, &rec_s, &fan_base, &clip_queue, &tile_count, &tile_offset,
                     &tile_cursor, &bins, &keys, &counters, &rsqrt_tab, &color})
         b->release();
-    h_stage.release();
-    if (stage_done) cudaEventDestroy(stage_done);
-    stage_done = nullptr;
+    for (int i = 0; i < kStageRing; ++i) {
+        h_stage[i].release();
+        if (stage_done[i]) cudaEventDestroy(stage_done[i]);
+        stage_done[i] = nullptr;
+        stage_pending[i] = false;
+    }
 }
 
 namespace {
@@ -217,26 +168,37 @@ inline uint32_t grow(uint32_t cur, uint64_t need) {
 
 swr_status FrameEngine::prepare(const std::vector<const SceneImpl*>& scenes, std::vector<DView>& vws,
                                 const std::vector<const swr_camera*>& cams, std::string& err) {
-    std::vector<DDraw>& hdraws = h_draws;
-    std::vector<DChunk>& hchunks = h_chunks;
-    hdraws.clear();
-    hchunks.clear();
-    uint32_t tri_cursor = 0;
+    // Per view: the node order (the host's part of the draw list) and the
+    // camera the device builds the draws with; capacities from the scenes'
+    // bounds (every primitive in the frustum), since the draw list itself is
+    // only known on the device.
+    h_order.clear();
+    uint64_t tri_bound = 0, draw_bound = 0, chunk_bound = 0;
     uint32_t stile_cursor = 0, quad_cursor = 0, max_px = 0;
     uint64_t key_cursor = 0, color_floats = 0;
     bool any_translucent = false;
     for (size_t i = 0; i < vws.size(); ++i) {
         DView& v = vws[i];
-        const size_t d0 = hdraws.size();
-        build_view_draws(*scenes[v.scene], *cams[i], (uint32_t)i, v.scene, tri_cursor, hdraws, hchunks);
-        bool view_translucent = false;
-        for (size_t k = d0; k < hdraws.size(); ++k) view_translucent |= hdraws[k].translucent != 0u;
-        v.flags = (v.flags & kViewLinear) | (view_translucent ? kViewTranslucent : 0u);
-        any_translucent |= view_translucent;
+        const SceneImpl& sc = *scenes[v.scene];
+        const swr_camera& cam = *cams[i];
+        std::memcpy(v.cam_view, cam.view, sizeof(v.cam_view));
+        std::memcpy(v.cam_view_project, cam.view_project, sizeof(v.cam_view_project));
+        std::memcpy(v.cam_planes, cam.view_clip_planes, sizeof(v.cam_planes));
+        v.order_base = (uint32_t)h_order.size();
+        v.n_order = (uint32_t)sc.nodes.size();
+        sort_nodes_by_distance(sc, cam, h_order);
+        tri_bound += sc.tri_total;
+        draw_bound += sc.max_draws;
+        chunk_bound += sc.max_chunks;
+        // kViewTranslucent is set on the device when a translucent draw is
+        // emitted; a view whose scene has translucent primitives gets the
+        // colour buffer the translucent pass blends into.
+        v.flags &= kViewLinear;
+        any_translucent |= sc.any_translucent;
         // Linear colour over the padded tile grid (engine-owned), offset kept
         // in the pointer field until the buffer exists.
         v.color = nullptr;
-        if (v.flags) {
+        if (v.flags || sc.any_translucent) {
             v.color = reinterpret_cast<float*>((uintptr_t)(color_floats + 1));
             color_floats += v.key_pitch * (uint64_t)v.tiles_y * kRefTile * 3u;
         }
@@ -248,13 +210,17 @@ swr_status FrameEngine::prepare(const std::vector<const SceneImpl*>& scenes, std
         key_cursor += v.key_pitch * (uint64_t)v.tiles_y * kRefTile;
         max_px = std::max<uint32_t>(max_px, (uint32_t)v.width * (uint32_t)(v.height & ~1));
     }
-    const uint32_t T = tri_cursor;
+    if (tri_bound > 0xFFFFFFF0ull || chunk_bound > 0xFFFFFFF0ull || h_order.size() > 0xFFFFFFF0ull) {
+        err = "frame above 2^32 triangles, chunks or nodes";
+        return SWR_INVALID_ARG;
+    }
     // Capacities (grow-only, with headroom so small changes keep a captured graph valid).
     scene_cap = grow(scene_cap, scenes.size());
     view_cap = grow(view_cap, vws.size());
-    draw_cap = grow(draw_cap, std::max<size_t>(1, hdraws.size()));
-    chunk_cap = grow(chunk_cap, std::max<size_t>(1, hchunks.size()));
-    tri_cap = grow(tri_cap, std::max<uint32_t>(1, T));
+    order_cap = grow(order_cap, std::max<size_t>(1, h_order.size()));
+    draw_cap = grow(draw_cap, std::max<uint64_t>(1, draw_bound));
+    chunk_cap = grow(chunk_cap, std::max<uint64_t>(1, chunk_bound));
+    tri_cap = grow(tri_cap, std::max<uint64_t>(1, tri_bound));
     // Bins: opaque per scheduling tile, then (frames with translucent draws)
     // translucent per scheduling tile.
     stile_cap = grow(stile_cap, 2ull * stile_cursor + 1);
@@ -264,7 +230,7 @@ swr_status FrameEngine::prepare(const std::vector<const SceneImpl*>& scenes, std
     if (extra_cap < std::max<uint64_t>(4096, tri_cap / 4)) extra_cap = std::max<uint64_t>(4096, tri_cap / 4);
     if (bin_cap < std::max<uint64_t>(65536, (uint64_t)tri_cap * 2 + stile_cap * 4ull))
         bin_cap = std::max<uint64_t>(65536, (uint64_t)tri_cap * 2 + stile_cap * 4ull);
-    lay = table_layout(scene_cap, view_cap, draw_cap, chunk_cap);
+    lay = table_layout(scene_cap, view_cap, order_cap, draw_cap, chunk_cap);
     cudaError_t e = cudaSuccess;
     auto chk = [&](cudaError_t x) {
         if (x != cudaSuccess && e == cudaSuccess) e = x;
@@ -287,42 +253,50 @@ swr_status FrameEngine::prepare(const std::vector<const SceneImpl*>& scenes, std
         cudaGetLastError();
         return e == cudaErrorMemoryAllocation ? SWR_NO_MEMORY : SWR_CUDA_ERROR;
     }
-    if (stage_pending) {
-        cudaEventSynchronize(stage_done);
-        stage_pending = false;
+    // The staging buffer of this frame was last read by the copy of the
+    // frame kStageRing frames back.
+    if (stage_pending[stage_slot]) {
+        cudaEventSynchronize(stage_done[stage_slot]);
+        stage_pending[stage_slot] = false;
     }
-    if (h_stage.ensure(lay.total) != cudaSuccess) {
+    HBuf& h_stage_cur = h_stage[stage_slot];
+    if (h_stage_cur.ensure(lay.staged) != cudaSuccess) {
         err = "pinned allocation failed";
         return SWR_NO_MEMORY;
     }
     dyn = DFrameDyn{};
     dyn.n_views = (uint32_t)vws.size();
-    dyn.n_chunks = (uint32_t)hchunks.size();
-    dyn.tri_total = T;
+    dyn.n_chunks = 0;    // written by the draw-list build
+    dyn.tri_total = 0;
     dyn.n_stiles = stile_cursor;
     dyn.total_quads = quad_cursor;
     dyn.max_view_pixels = max_px;
     dyn.n_bins = any_translucent ? 2u * stile_cursor : stile_cursor;
+    dyn.n_slots = (uint32_t)h_order.size();
     for (DView& v : vws)
         if (v.color) v.color = color.as<float>() + ((uintptr_t)v.color - 1u);
-    uint8_t* hs = static_cast<uint8_t*>(h_stage.p);
+    uint8_t* hs = static_cast<uint8_t*>(h_stage_cur.p);
     std::memcpy(hs + lay.o_dyn, &dyn, sizeof(dyn));
     for (size_t i = 0; i < scenes.size(); ++i)
         std::memcpy(hs + lay.o_scenes + i * sizeof(DScene), &scenes[i]->dscene, sizeof(DScene));
     std::memcpy(hs + lay.o_views, vws.data(), vws.size() * sizeof(DView));
-    if (!hdraws.empty()) std::memcpy(hs + lay.o_draws, hdraws.data(), hdraws.size() * sizeof(DDraw));
-    if (!hchunks.empty()) std::memcpy(hs + lay.o_chunks, hchunks.data(), hchunks.size() * sizeof(DChunk));
+    if (!h_order.empty()) std::memcpy(hs + lay.o_order, h_order.data(), h_order.size() * sizeof(uint32_t));
     if (grid_tile != sched_tile) {
         frame_grids(num_sms, sched_tile, &raster_grid, &shade_grid);
         grid_tile = sched_tile;
     }
     uint8_t* tb = static_cast<uint8_t*>(tables.p);
     FrameArgs a{};
-    a.dyn = reinterpret_cast<const DFrameDyn*>(tb + lay.o_dyn);
+    a.dyn = reinterpret_cast<DFrameDyn*>(tb + lay.o_dyn);
     a.scenes = reinterpret_cast<const DScene*>(tb + lay.o_scenes);
-    a.views = reinterpret_cast<const DView*>(tb + lay.o_views);
-    a.draws = reinterpret_cast<const DDraw*>(tb + lay.o_draws);
-    a.chunks = reinterpret_cast<const DChunk*>(tb + lay.o_chunks);
+    a.views = reinterpret_cast<DView*>(tb + lay.o_views);
+    a.draws = reinterpret_cast<DDraw*>(tb + lay.o_draws);
+    a.chunks = reinterpret_cast<DChunk*>(tb + lay.o_chunks);
+    a.node_order = reinterpret_cast<const uint32_t*>(tb + lay.o_order);
+    a.slot_blocks = reinterpret_cast<uint4*>(tb + lay.o_slots);
+    a.slot_cap = order_cap;
+    a.draw_cap = draw_cap;
+    a.gpu_draws = 1u;
     a.chunk_cap = chunk_cap;
     a.tri_cap = tri_cap;
     a.extra_cap = (uint32_t)extra_cap;
@@ -356,11 +330,15 @@ swr_status FrameEngine::prepare(const std::vector<const SceneImpl*>& scenes, std
 
 swr_status FrameEngine::launch(cudaStream_t stream, cudaEvent_t* ev, std::string& err) {
     // The staging copy runs ahead of the kernels (graph or not) and is the
-    // only reader of h_stage: once it is done the host may stage the next
-    // frame while this one renders.
-    cudaError_t e = cudaMemcpyAsync(tables.p, h_stage.p, lay.total, cudaMemcpyHostToDevice, stream);
-    if (e == cudaSuccess) e = cudaEventRecord(stage_done, stream);
-    if (e == cudaSuccess) stage_pending = true;
+    // only reader of its staging buffer; with a ring of them the host stages
+    // up to kStageRing frames ahead of the device.
+    const int slot = stage_slot;
+    cudaError_t e = cudaMemcpyAsync(tables.p, h_stage[slot].p, lay.staged, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaEventRecord(stage_done[slot], stream);
+    if (e == cudaSuccess) {
+        stage_pending[slot] = true;
+        stage_slot = (slot + 1) % kStageRing;
+    }
     if (e == cudaSuccess && use_graph && !ev) {
         const bool same = graph_exec && std::memcmp(&graph_args, &args, sizeof(args)) == 0;
         if (!same) {

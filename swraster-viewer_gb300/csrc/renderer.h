@@ -60,9 +60,13 @@ struct HBuf {
 
 // Table region layout (host staging and device copy use the same offsets).
 struct TableLayout {
-    size_t o_dyn = 0, o_scenes = 0, o_views = 0, o_draws = 0, o_chunks = 0, total = 0;
+    // Staged from the host each frame: [0, staged). Device-written after it:
+    // per node slot counts and offsets, draws, chunks.
+    size_t o_dyn = 0, o_scenes = 0, o_views = 0, o_order = 0, staged = 0;
+    size_t o_slots = 0, o_draws = 0, o_chunks = 0, total = 0;
 };
-TableLayout table_layout(uint32_t scene_cap, uint32_t view_cap, uint32_t draw_cap, uint32_t chunk_cap);
+TableLayout table_layout(uint32_t scene_cap, uint32_t view_cap, uint32_t order_cap, uint32_t draw_cap,
+                         uint32_t chunk_cap);
 
 // Reusable frame engine: everything a batch of views needs on the device.
 // prepare() builds the per-frame tables on the host and grows capacities;
@@ -73,7 +77,8 @@ struct FrameEngine {
     int num_sms = 148;
     uint32_t sched_tile = 64;
     uint64_t bin_cap = 0, extra_cap = 0;
-    uint32_t scene_cap = 0, view_cap = 0, draw_cap = 0, chunk_cap = 0, tri_cap = 0, stile_cap = 0, quad_cap = 0;
+    uint32_t scene_cap = 0, view_cap = 0, order_cap = 0, draw_cap = 0, chunk_cap = 0, tri_cap = 0, stile_cap = 0,
+             quad_cap = 0;
     uint32_t pixel_cap = 0;
     uint64_t key_cap = 0;
     uint32_t raster_grid = 0, shade_grid = 0, grid_tile = 0;
@@ -81,12 +86,13 @@ struct FrameEngine {
     DBuf tile_count, tile_offset, tile_cursor, bins, keys, counters, rsqrt_tab;
     DBuf color;                // linear colour of views that need it (padded tile grids)
     bool defer_resolve = false;// the caller resolves (renderer frames with dt > 0)
-    HBuf h_stage;
-    std::vector<DDraw> h_draws;  // per-frame draw and chunk lists (capacity kept)
-    std::vector<DChunk> h_chunks;
+    static constexpr int kStageRing = 4;
+    HBuf h_stage[kStageRing];  // pinned staging of the per-frame tables, one per frame in flight
+    std::vector<uint32_t> h_order;  // per-frame node order of every view (capacity kept)
     TableLayout lay;
-    cudaEvent_t stage_done = nullptr;
-    bool stage_pending = false;
+    cudaEvent_t stage_done[kStageRing] = {};
+    bool stage_pending[kStageRing] = {};
+    int stage_slot = 0;
     uint32_t retries = 0;
     DCounters last{};
     DFrameDyn dyn{};
@@ -113,10 +119,9 @@ struct FrameEngine {
                    std::string& err, cudaEvent_t* ev = nullptr);
 };
 
-// Per-frame draw list for one view (render_scene's front half,
-// src/renderer.rs:201-210 and 357-468).
-void build_view_draws(const SceneImpl& s, const swr_camera& cam, uint32_t view_idx, uint32_t scene_idx,
-                      uint32_t& tri_cursor, std::vector<DDraw>& draws, std::vector<DChunk>& chunks);
+// compute_nodes_by_distance (src/renderer.rs:201-210): appends the scene's
+// node indices, nearest first, to `out`.
+void sort_nodes_by_distance(const SceneImpl& s, const swr_camera& cam, std::vector<uint32_t>& out);
 
 // Fill the view-geometry fields of a DView (tiles, pitches, camera).
 void init_view(DView& v, const swr_camera& cam, int32_t width, int32_t height, uint32_t sched_tile);

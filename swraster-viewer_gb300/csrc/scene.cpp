@@ -1026,11 +1026,49 @@ swr_status upload_scene(SceneImpl* s, std::string& err, bool to_device) {
         }
         idx.insert(idx.end(), p.idx.begin(), p.idx.end());
     }
+    // Per mesh: its primitives in render_mesh's order (opaque, then translucent).
+    std::vector<DMeshEntry> entries;
+    std::vector<uint32_t> mesh_begin;
+    for (const HMesh& m : s->meshes) {
+        mesh_begin.push_back((uint32_t)entries.size());
+        for (int pass = 0; pass < 2; ++pass)
+            for (uint32_t lp : pass == 0 ? m.opaque : m.translucent) {
+                const HPrimitive& p = s->prims[m.prims[lp]];
+                DMeshEntry me{};
+                for (int k = 0; k < 4; ++k) me.sphere[k] = p.sphere[k];
+                me.prim = m.prims[lp];
+                me.tri_count = (uint32_t)(p.idx.size() / 3);
+                me.tri_id_base = p.tri_id_base;
+                entries.push_back(me);
+            }
+    }
     std::vector<float> xf;
+    std::vector<DNodeInfo> node_info;
+    s->max_draws = 0;
+    s->max_chunks = 0;
+    s->any_translucent = false;
     for (const HNode& n : s->nodes) {
         float a[16];
         to_array(n.transform, a);
         xf.insert(xf.end(), a, a + 16);
+        DNodeInfo ni{};
+        std::memcpy(ni.xform, a, sizeof(a));
+        ni.tri_id_base = n.tri_id_base;
+        if (n.mesh >= 0) {
+            const HMesh& m = s->meshes[n.mesh];
+            ni.entry_begin = mesh_begin[n.mesh];
+            ni.n_opaque = (uint32_t)m.opaque.size();
+            ni.n_total = (uint32_t)(m.opaque.size() + m.translucent.size());
+            // Upper bounds of one view's draw list: every primitive drawn.
+            for (uint32_t gp : m.prims) {
+                const uint32_t tc = (uint32_t)(s->prims[gp].idx.size() / 3);
+                if (tc == 0) continue;
+                s->max_draws += 1;
+                s->max_chunks += (tc + kChunkTris - 1) / kChunkTris;
+            }
+            if (!m.translucent.empty()) s->any_translucent = true;
+        }
+        node_info.push_back(ni);
     }
     std::vector<DMaterial> mats;
     for (const swr_material_view& m : s->materials) {
@@ -1055,6 +1093,8 @@ swr_status upload_scene(SceneImpl* s, std::string& err, bool to_device) {
     const uint64_t o_prim = ar.add(prims.data(), prims.size() * sizeof(DPrimitive));
     const uint64_t o_xf = ar.add(xf.data(), xf.size() * sizeof(float));
     const uint64_t o_mat = ar.add(mats.data(), mats.size() * sizeof(DMaterial));
+    const uint64_t o_ninfo = ar.add(node_info.data(), node_info.size() * sizeof(DNodeInfo));
+    const uint64_t o_entries = ar.add(entries.data(), entries.size() * sizeof(DMeshEntry));
     std::vector<uint64_t> o_tex;
     std::vector<const HTexture*> all_tex;
     for (const HTexture& t : s->textures) all_tex.push_back(&t);
@@ -1090,6 +1130,8 @@ swr_status upload_scene(SceneImpl* s, std::string& err, bool to_device) {
     ds.materials = reinterpret_cast<const DMaterial*>(at(o_mat));
     ds.textures = reinterpret_cast<const DTexture*>(at(o_dtex));
     ds.voxel_light = reinterpret_cast<const float*>(at(o_vox));
+    ds.node_info = reinterpret_cast<const DNodeInfo*>(at(o_ninfo));
+    ds.mesh_entries = reinterpret_cast<const DMeshEntry*>(at(o_entries));
     ds.tex_cubemap = (uint32_t)s->textures.size();
     ds.tex_specular = ds.tex_cubemap + 1;
     ds.tex_brdf_lut = ds.tex_cubemap + 2;

@@ -62,6 +62,9 @@ struct SceneImpl {
     float gi_sh_scale = 0.25f, sky_visibility = 1.0f;
     float gi_const[4][4] = {};
     uint64_t tri_total = 0, vtx_total = 0;
+    // Draw-list bounds of one view (every primitive in the frustum).
+    uint32_t max_draws = 0, max_chunks = 0;
+    bool any_translucent = false;  // some node's mesh has translucent primitives
 
     // Export views.
     std::vector<swr_primitive_view> prim_views;

@@ -182,7 +182,7 @@ EXPORTS = [
     "swr_server_submit", "swr_server_poll", "swr_server_release", "swr_server_get_stats", "swr_copy_to_host",
     "swr_selftest_rsqrt", "swr_scene_load_gltf",
 ]
-STAGES = ["reset", "frontend", "clip", "scan", "scatter", "raster", "shade", "resolve"]
+STAGES = ["draws", "frontend", "clip", "scan", "scatter", "raster", "shade", "resolve"]
 
 _lib = None
 
