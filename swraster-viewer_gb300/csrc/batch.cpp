@@ -106,11 +106,6 @@ swr_status BatchImpl::sync(std::string& err) {
             return SWR_CUDA_ERROR;
         }
         eng.last = c;
-        if (c.status & ST_DRAW_OVERFLOW) {
-            pending = false;
-            err = "draw list above its capacity";
-            return SWR_OVERFLOW;
-        }
         if (!(c.status & kStRetry)) {
             pending = false;
             return SWR_OK;

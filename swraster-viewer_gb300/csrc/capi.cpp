@@ -365,7 +365,6 @@ swr_status check_frame(swr_renderer* r) {
         e = cudaMemcpy(&c, r->eng.counters.p, sizeof(c), cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) return cuda_fail(e, "counter readback");
         r->eng.last = c;
-        if (c.status & ST_DRAW_OVERFLOW) return fail(SWR_OVERFLOW, "draw list above its capacity");
         if (!(c.status & kStRetry)) {
             r->checked = true;
             return SWR_OK;

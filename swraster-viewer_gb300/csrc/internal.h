@@ -224,10 +224,11 @@ enum : uint32_t {
     ST_QUEUE_OVERFLOW = 4u,
     ST_TIMEOUT = 8u,
     ST_TRANS_OVERFLOW = 16u,   // a scheduling tile has more translucent packets than one sort holds
-    ST_DRAW_OVERFLOW = 32u,    // draw list above its capacity (the host sizes it from scene bounds)
+    ST_DRAW_OVERFLOW = 32u,    // the frame's draws have more triangles (or draws, chunks) than allocated
 };
 // Status bits after which a frame is incomplete and is rendered again.
-constexpr uint32_t kStRetry = ST_BIN_OVERFLOW | ST_CLIP_OVERFLOW | ST_QUEUE_OVERFLOW | ST_TRANS_OVERFLOW;
+constexpr uint32_t kStRetry =
+    ST_BIN_OVERFLOW | ST_CLIP_OVERFLOW | ST_QUEUE_OVERFLOW | ST_TRANS_OVERFLOW | ST_DRAW_OVERFLOW;
 
 // Frame-level counters (device).
 struct alignas(16) DCounters {
@@ -241,6 +242,8 @@ struct alignas(16) DCounters {
     uint32_t trans_packets;    // translucent (packet, tile) pairs
     uint32_t draw_tris;        // triangles of the frame's draws (the draw-list build's T)
     uint32_t draw_done;        // CTAs done counting draws (zero between frames)
+    uint32_t draw_chunks;      // chunks and draws of the frame's draw list
+    uint32_t draw_count;
 };
 
 // Per-frame counts, uploaded with the tables: kernels read them from device

@@ -615,9 +615,9 @@ __device__ __forceinline__ DrawCount slot_count(const FrameArgs& a, uint32_t i, 
     return node_draws<false>(a, vi, v, a.scenes[v.scene], a.node_order[i], DrawCount{0u, 0u, 0u}, unused);
 }
 
-// Frame totals from the draw-list sums; a frame past the capacities (sized
-// from the scenes' bounds, so only through a defect) draws nothing and
-// reports it.
+// Frame totals from the draw-list sums; a frame past the capacities draws
+// nothing and reports its totals, and the host renders it again with grown
+// buffers.
 __device__ __forceinline__ void set_draw_totals(const FrameArgs& a, const DrawCount& total) {
     if (total.tris > a.tri_cap || total.chunks > a.chunk_cap || total.draws > a.draw_cap) {
         atomicOr(&a.counters->status, ST_DRAW_OVERFLOW);
@@ -628,6 +628,8 @@ __device__ __forceinline__ void set_draw_totals(const FrameArgs& a, const DrawCo
         a.dyn->tri_total = total.tris;
     }
     a.counters->draw_tris = total.tris;
+    a.counters->draw_chunks = total.chunks;
+    a.counters->draw_count = total.draws;
 }
 
 // Counts per block of 256 node slots (run by k_reset's CTAs); the last CTA
@@ -758,9 +760,8 @@ __device__ __forceinline__ bool vtx_inside_all(const Vtx& v) {
 }
 
 // Thread per triangle of a 256-triangle chunk of one draw.
-__global__ void __launch_bounds__(kChunkTris) k_frontend(FrameArgs a) {
-    if (blockIdx.x >= a.dyn->n_chunks) return;
-    const DChunk ch = a.chunks[blockIdx.x];
+__device__ __forceinline__ void frontend_triangle(const FrameArgs& a, uint32_t chunk) {
+    const DChunk ch = a.chunks[chunk];
     const DDraw& d = a.draws[ch.draw];
     const uint32_t local = ch.tri_start + threadIdx.x;
     if (local >= d.tri_count) return;
@@ -796,6 +797,13 @@ __global__ void __launch_bounds__(kChunkTris) k_frontend(FrameArgs a) {
     if (ok) store_records(a, g, r, q);
     a.tri_state[g] = ok ? 1 : 0;
     warp_count(&a.counters->setup_tris, ok);
+}
+
+// Thread per triangle of a 256-triangle chunk; CTAs loop over the frame's
+// chunks (the grid is sized by the SM count, not by the capacity).
+__global__ void __launch_bounds__(kChunkTris) k_frontend(FrameArgs a) {
+    const uint32_t n = a.dyn->n_chunks;
+    for (uint32_t c = blockIdx.x; c < n; c += gridDim.x) frontend_triangle(a, c);
 }
 
 // intersect (src/renderer.rs:598-609).
@@ -971,19 +979,13 @@ __global__ void __launch_bounds__(1024) k_scan(FrameArgs a) {
     }
 }
 
-__global__ void k_scatter(FrameArgs a) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a.counters->status & (ST_BIN_OVERFLOW | ST_CLIP_OVERFLOW | ST_QUEUE_OVERFLOW)) return;
-    const uint32_t tri_total = a.dyn->tri_total;
-    uint32_t slot;
-    if (i < tri_total) {
-        if (a.tri_state[i] != 1) return;
-        slot = i;
-    } else {
-        const uint32_t x = i - tri_total;
-        if (x >= min(a.counters->extra_used, a.extra_cap)) return;
-        slot = i;
-        if (a.rec_r[slot].view == 0xFFFFFFFFu) return;
+// Record slots are the frame's main slots [0, T) and the clipper's extra
+// slots right after them.
+__device__ __forceinline__ void scatter_slot(const FrameArgs& a, uint32_t slot, uint32_t tri_total) {
+    if (slot < tri_total) {
+        if (a.tri_state[slot] != 1) return;
+    } else if (a.rec_r[slot].view == 0xFFFFFFFFu) {
+        return;
     }
     const RecRaster& r = a.rec_r[slot];
     const DView& view = a.views[r.view];
@@ -1000,6 +1002,14 @@ __global__ void k_scatter(FrameArgs a) {
         const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
         a.bins[base + rank] = slot;
     });
+}
+
+__global__ void k_scatter(FrameArgs a) {
+    if (a.counters->status & (ST_BIN_OVERFLOW | ST_CLIP_OVERFLOW | ST_QUEUE_OVERFLOW)) return;
+    const uint32_t tri_total = a.dyn->tri_total;
+    const uint32_t n = tri_total + min(a.counters->extra_used, a.extra_cap);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        scatter_slot(a, i, tri_total);
 }
 
 // --------------------------------------------------------------------------
@@ -2083,7 +2093,10 @@ void launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t* ev
         if (sg > 1u) k_draw_emit<<<sg, kSlotBlock, 0, s>>>(a);
     }
     mark(1);
-    if (a.chunk_cap > 0) k_frontend<<<a.chunk_cap, kChunkTris, 0, s>>>(a);
+    // Front end and scatter loop over the frame's counts with grids sized by
+    // the SM count: capacities follow the scenes' bounds and can be far
+    // larger than what a frame draws.
+    if (a.chunk_cap > 0) k_frontend<<<min(a.chunk_cap, (uint32_t)num_sms * 16u), kChunkTris, 0, s>>>(a);
     mark(2);
     k_clip<<<num_sms * 4, 128, 0, s>>>(a);
     mark(3);
@@ -2091,7 +2104,7 @@ void launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t* ev
     mark(4);
     {
         const uint64_t n = (uint64_t)a.tri_cap + a.extra_cap;
-        if (n > 0) k_scatter<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
+        if (n > 0) k_scatter<<<(unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)num_sms * 8u), 256, 0, s>>>(a);
     }
     mark(5);
     const uint32_t rg = SWR_RASTER_PERSISTENT ? (a.raster_grid > 0 ? a.raster_grid : (uint32_t)num_sms)

@@ -218,9 +218,14 @@ swr_status FrameEngine::prepare(const std::vector<const SceneImpl*>& scenes, std
     scene_cap = grow(scene_cap, scenes.size());
     view_cap = grow(view_cap, vws.size());
     order_cap = grow(order_cap, std::max<size_t>(1, h_order.size()));
+    // Draws and chunks are small: their bounds are allocated. Record slots
+    // (256 B per triangle) follow the bound up to kTriCapFromBound; past it
+    // they grow to what frames actually draw (a frame that finds more
+    // triangles than slots is rendered again with grown buffers), so
+    // batches of large scenes hold what is visible, not every triangle.
     draw_cap = grow(draw_cap, std::max<uint64_t>(1, draw_bound));
     chunk_cap = grow(chunk_cap, std::max<uint64_t>(1, chunk_bound));
-    tri_cap = grow(tri_cap, std::max<uint64_t>(1, tri_bound));
+    tri_cap = grow(tri_cap, std::max<uint64_t>(1, std::min<uint64_t>(tri_bound, kTriCapFromBound)));
     // Bins: opaque per scheduling tile, then (frames with translucent draws)
     // translucent per scheduling tile.
     stile_cap = grow(stile_cap, 2ull * stile_cursor + 1);
@@ -378,6 +383,11 @@ swr_status FrameEngine::launch(cudaStream_t stream, cudaEvent_t* ev, std::string
 }
 
 swr_status FrameEngine::grow_for(const DCounters& c, std::string& err) {
+    if (c.status & ST_DRAW_OVERFLOW) {
+        tri_cap = grow(tri_cap, c.draw_tris);
+        chunk_cap = grow(chunk_cap, c.draw_chunks);
+        draw_cap = grow(draw_cap, c.draw_count);
+    }
     if (c.status & ST_BIN_OVERFLOW) bin_cap = std::max<uint64_t>(bin_cap * 2, c.pairs + c.pairs / 4);
     if (c.status & ST_CLIP_OVERFLOW)
         extra_cap = std::max<uint64_t>(extra_cap * 2, (uint64_t)c.extra_used + c.extra_used / 4);

@@ -87,6 +87,7 @@ struct FrameEngine {
     DBuf color;                // linear colour of views that need it (padded tile grids)
     bool defer_resolve = false;// the caller resolves (renderer frames with dt > 0)
     static constexpr int kStageRing = 4;
+    static constexpr uint64_t kTriCapFromBound = 8u << 20;  // record slots sized from scene bounds, at most
     HBuf h_stage[kStageRing];  // pinned staging of the per-frame tables, one per frame in flight
     std::vector<uint32_t> h_order;  // per-frame node order of every view (capacity kept)
     TableLayout lay;

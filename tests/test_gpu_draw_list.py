@@ -81,3 +81,47 @@ def test_batch_views_over_many_slots():
     b.close()
     big.close()
     small.close()
+
+
+def instanced_grid(n_side=12, depth=16, subdiv=4, seed=24):
+    """One icosphere mesh instanced on a grid of n_side x n_side x depth nodes:
+    11.8M triangles drawn (more than the 10.5M record slots first sized from
+    the scene's bound) from a scene of one small mesh."""
+    rng = np.random.default_rng(seed)
+    P, F = scenes.icosphere(subdiv)
+    UV = scenes.spherical_uv(P)
+    nodes = []
+    for k in range(depth):
+        for j in range(n_side):
+            for i in range(n_side):
+                w = scenes.translate_scale(np.array([i * 3.0, j * 3.0, -k * 3.0], np.float32), 1.0)
+                nodes.append({"world": w, "local": w, "mesh": 0})
+    sd = {"meshes": [[{"positions": P, "normals": P.copy(), "texcoords": UV, "indices": F, "material": 0}]],
+          "nodes": nodes,
+          "materials": [{"base_color_factor": (0.8, 0.7, 0.6, 1.0), "metallic": 0.3, "roughness": 0.6,
+                         "base_color": (0, scenes.WRAP_REPEAT, scenes.WRAP_REPEAT)}],
+          "textures": [scenes.noise_texture(rng, 64)], "cubemap": scenes.cubemap_faces(rng, 16),
+          "cubemap_face_size": 16, "voxel_grid_size": 32, "specular_samples": 8, "brdf_lut_size": 32}
+    return swr.Scene(sd)
+
+
+def test_frame_past_initial_record_slots_is_rendered_again():
+    s = instanced_grid()
+    info = s.info()
+    assert info.triangle_count > (8 << 20) * 5 // 4 + 16
+    w, h = 96, 64
+    cam = swr.make_camera(*scenes.default_camera_params(info, w, h))
+    r = swr.Renderer(w, h)
+    r.render(s, cam)
+    rgba1, vis1 = r.blit(), r.visbuffer()
+    st = r.stats()
+    assert st.triangles_in == info.triangle_count
+    assert st.overflow_retries >= 1  # the first frame found more triangles than slots
+    r.render(s, cam)
+    rgba2, vis2 = r.blit(), r.visbuffer()
+    assert r.stats().overflow_retries == st.overflow_retries  # grown buffers hold the second frame
+    np.testing.assert_array_equal(vis1, vis2)
+    np.testing.assert_array_equal(rgba1, rgba2)
+    assert (vis1 != np.uint64(2**64 - 1)).sum() > w * h // 4
+    r.close()
+    s.close()
