@@ -47,6 +47,7 @@ struct Engine {
     cudaStream_t stream = nullptr;
     bool busy = false;
     uint64_t bytes = 0;  // device bytes of the engine's buffers, refreshed by the worker under the lock
+    uint64_t reserved = 0;  // bytes admitted for the batch in flight (its buffers may grow to it on a retry)
     std::atomic<bool> done{false};
     std::vector<Req> reqs;
     std::vector<FB*> fbs;
@@ -82,7 +83,7 @@ struct swr_server {
     // engine's buffers may have grown (never while another thread reads).
     uint64_t engine_bytes() {
         uint64_t t = 0;
-        for (auto& e : engines) t += e->bytes;
+        for (auto& e : engines) t += std::max(e->bytes, e->reserved);
         return t;
     }
 
@@ -118,8 +119,13 @@ struct swr_server {
         uint64_t t = 0;
         for (size_t i = 0; i < dims.size(); ++i) {
             const uint64_t tx = (uint64_t)(dims[i].first + 63) / 64, ty = (uint64_t)(dims[i].second + 63) / 64;
-            t += tx * ty * 64 * 64 * (trans[i] ? 8 + 12 : 8);
-            t += tris[i] * (80 + 176 + 4 + 8 + 1) * 5 / 4 + tris[i] * 2 * 4;
+            t += tx * ty * 64 * 64 * (trans[i] ? 8 + 12 : 8) * 5 / 4;  // with the keys' 25% headroom
+            // Record slots as the engine sizes them at most: every triangle of
+            // the view's scene plus the 25% growth headroom, clip fan slots
+            // (a quarter more), per-slot state, fan bases, clip queue and two
+            // bin entries per slot.
+            const uint64_t T = tris[i] * 5 / 4 + 16;
+            t += (T + T / 4) * (80 + 176) + T * (1 + 4 + 8) + T * 2 * 4;
         }
         return t + (1u << 20);
     }
@@ -187,6 +193,7 @@ struct swr_server {
                 e->reqs.clear();
                 e->fbs.clear();
                 e->busy = false;
+                e->reserved = 0;
                 e->done.store(false);
                 cv_done.notify_all();
             }
@@ -199,7 +206,8 @@ struct swr_server {
                 std::vector<std::pair<int32_t, int32_t>> dims;
                 std::vector<uint64_t> tris;
                 std::vector<bool> trans;
-                const uint64_t others = engine_bytes() - e.bytes;
+                const uint64_t others = engine_bytes() - std::max(e.bytes, e.reserved);
+                uint64_t admitted = 0;
                 while (!pending.empty() && reqs.size() < opts.max_batch_views) {
                     const Req& q = pending.front();
                     // Admission: this engine's buffers for the grown batch must
@@ -215,6 +223,7 @@ struct swr_server {
                     }
                     FB* f = get_fb(q.r.width, q.r.height);
                     if (!f) break;  // wait for framebuffers to be released
+                    admitted = need;
                     reqs.push_back(q);
                     fbs.push_back(f);
                     pending.pop_front();
@@ -234,6 +243,7 @@ struct swr_server {
                 e.reqs = std::move(reqs);
                 e.fbs = std::move(fbs);
                 e.busy = true;
+                e.reserved = admitted;
                 e.done.store(false);
                 e.t_launch = now_ms();
                 stats.batches++;
@@ -263,6 +273,7 @@ struct swr_server {
                     e.reqs.clear();
                     e.fbs.clear();
                     e.busy = false;
+                    e.reserved = 0;
                     cv_done.notify_all();
                 }
             }
