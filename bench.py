@@ -155,7 +155,7 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(sd, cam_params, cfg, frames, threads=None):
+def cpu_baseline(sd, cam_params, cfg, frames, threads=None, warmup=1):
     """The oracle (CPU restatement of the reference's rayon path) on all host
     cores over a bounded sample of the same workload."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -168,7 +168,8 @@ def cpu_baseline(sd, cam_params, cfg, frames, threads=None):
     cam = swr.make_camera(*cam_params) if cam_params else swr.make_camera(
         *scenes.default_camera_params(s.info(), cfg["width"], cfg["height"]))
     view = s.export()
-    oracle.render(view, cam, cfg["width"], cfg["height"], threads=threads)  # warm-up
+    for _ in range(warmup):
+        oracle.render(view, cam, cfg["width"], cfg["height"], threads=threads)
     t0 = time.perf_counter()
     for _ in range(frames):
         oracle.render(view, cam, cfg["width"], cfg["height"], threads=threads)
@@ -182,10 +183,13 @@ def run_reference(args):
     if rank != 0:
         return 0
     sd, cam_params, cfg = workload(args.workload)
+    # Bounded sample: at most 20 timed and 3 warm-up frames (a 4K frame takes
+    # about 0.3 s on 16 Grace cores).
     steps = max(1, min(args.steps, 20))
-    fps, cores, sample = cpu_baseline(sd, cam_params, cfg, steps)
+    warm = max(1, min(args.warmup, 3))
+    fps, cores, sample = cpu_baseline(sd, cam_params, cfg, steps, warmup=warm)
     line = {"metric": "4K frames/s" if args.workload == "4k" else "frames/s", "value": fps, "unit": "frames/s",
-            "impl": "reference", "n_gpus": args.gpus, "steps": steps, "warmup": 1,
+            "impl": "reference", "n_gpus": args.gpus, "steps": steps, "warmup": warm,
             "ms_per_step": 1000.0 / fps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic", "config": cfg,
             "gtri_per_s": fps * cfg["triangles"] / 1e9,
