@@ -58,6 +58,8 @@ def lib():
             getattr(L, n).restype = C.c_float
         L.oracle_frsqrts.argtypes = [C.c_float, C.c_float]
         L.oracle_frsqrts.restype = C.c_float
+        L.oracle_sun_visibility.argtypes = [C.POINTER(swr.SceneHostView), C.c_uint32, C.c_void_p]
+        L.oracle_sun_visibility.restype = C.c_int
         _lib = L
     return _lib
 
@@ -75,6 +77,16 @@ def render(view, cam, width, height, rsqrt_mode=swr.RSQRT_AARCH64, threads=1, dt
     if rc != 0:
         raise RuntimeError("oracle_render failed")
     return rgba, vis, tl, res
+
+
+def sun_visibility(view, threads=1):
+    """Blurred voxel sun visibility (voxel_size^3 floats, x fastest) of the
+    scene's load-time precompute, by brute force over every triangle."""
+    n = view.voxel_size
+    out = np.zeros(n * n * n, np.float32)
+    if lib().oracle_sun_visibility(C.byref(view), threads, out.ctypes.data_as(C.c_void_p)) != 0:
+        raise RuntimeError("oracle_sun_visibility failed")
+    return out
 
 
 if __name__ == "__main__":

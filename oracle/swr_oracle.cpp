@@ -1235,6 +1235,164 @@ int oracle_render(const swr_scene_host_view* s, const swr_camera* cam, int32_t w
     return 0;
 }
 
+// Voxel sun visibility of the load-time precompute: RayTracer::new's
+// triangles (src/raytracer.rs:71-133), build_active_voxel_mask's occupancy
+// and dilation (src/gi.rs:151-265), compute_sun_visibility's
+// trace_transmittance per active voxel centre (src/gi.rs:267-314,
+// src/raytracer.rs:172-207) and blur_grid (src/voxelgrid.rs:370-419). Every
+// ray tests every triangle (no acceleration structure: results depend only
+// on ray_triangle_intersect, src/raytracer.rs:225-260, and the hit order,
+// t ascending, equal t by triangle). Writes voxel_size^3 floats to `out`.
+int oracle_sun_visibility(const swr_scene_host_view* v, uint32_t threads, float* out) {
+    struct P3 {
+        float x, y, z;
+    };
+    auto sub = [](P3 a, P3 b) { return P3{a.x - b.x, a.y - b.y, a.z - b.z}; };
+    auto add = [](P3 a, P3 b) { return P3{a.x + b.x, a.y + b.y, a.z + b.z}; };
+    auto mul = [](P3 a, float s) { return P3{a.x * s, a.y * s, a.z * s}; };
+    auto dot = [](P3 a, P3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; };
+    auto cross = [](P3 a, P3 b) {
+        return P3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+    };
+    auto length = [&](P3 a) { return std::sqrt(dot(a, a)); };
+    auto normalize = [&](P3 a) { return mul(a, 1.0f / length(a)); };
+    struct Tri {
+        P3 p0, p1, p2;
+        uint32_t material;
+    };
+    // RayTracer::new: world positions (Mat4 * Vec4, x_axis*x + y_axis*y + z_axis*z + w_axis*w).
+    std::vector<Tri> tris;
+    for (uint32_t ni = 0; ni < v->node_count; ++ni) {
+        const swr_node_view& nd = v->nodes[ni];
+        if (nd.mesh < 0) continue;
+        const swr_mesh_view& m = v->meshes[nd.mesh];
+        const float* T = nd.transform;
+        for (uint32_t k = 0; k < m.primitive_count; ++k) {
+            const swr_primitive_view& p = v->primitives[m.primitives[k]];
+            for (uint32_t t = 0; t + 2 < p.index_count; t += 3) {
+                P3 w[3];
+                for (int c = 0; c < 3; ++c) {
+                    const float* q = p.positions + 4 * (size_t)p.indices[t + c];
+                    float r[4];
+                    for (int j = 0; j < 4; ++j) r[j] = ((T[j] * q[0] + T[4 + j] * q[1]) + T[8 + j] * q[2]) + T[12 + j] * q[3];
+                    w[c] = P3{r[0], r[1], r[2]};
+                }
+                const P3 fn = cross(sub(w[1], w[0]), sub(w[2], w[0]));
+                if (dot(fn, fn) <= 1.0e-12f) continue;
+                tris.push_back({w[0], w[1], w[2], p.material});
+            }
+        }
+    }
+    const uint32_t n = v->voxel_size;
+    const size_t nvox = (size_t)n * n * n;
+    const P3 bmn{v->voxel_world_min[0], v->voxel_world_min[1], v->voxel_world_min[2]};
+    const P3 bmx{v->voxel_world_max[0], v->voxel_world_max[1], v->voxel_world_max[2]};
+    const P3 wsz = sub(bmx, bmn);
+    const P3 vsz{wsz.x / (float)n, wsz.y / (float)n, wsz.z / (float)n};
+    // Occupancy from barycentric samples per triangle, then dilation by 2.
+    std::vector<uint8_t> occ(nvox, 0);
+    const float mine = std::fmax(std::fmin(vsz.x, std::fmin(vsz.y, vsz.z)), 1.0e-6f);
+    const float area_ref = mine * mine;
+    for (const Tri& t : tris) {
+        const float area = 0.5f * length(cross(sub(t.p1, t.p0), sub(t.p2, t.p0)));
+        const float ts = std::ceil((area / area_ref) * 2.0f);
+        size_t target = (ts != ts || ts <= 0.0f) ? 0 : (ts >= 1.8e19f ? SIZE_MAX : (size_t)ts);
+        target = std::min<size_t>(std::max<size_t>(target, 1), 4096);
+        const size_t ns = (size_t)std::ceil(std::sqrt((float)target));
+        for (size_t iu = 0; iu < ns; ++iu)
+            for (size_t iv = 0; iv < ns - iu; ++iv) {
+                const float u = ((float)iu + 0.5f) / (float)ns, w2 = ((float)iv + 0.5f) / (float)ns;
+                const float w = (1.0f - u) - w2;
+                if (w < 0.0f) continue;
+                const P3 p = add(add(mul(t.p0, w), mul(t.p1, u)), mul(t.p2, w2));
+                const float fx = (p.x - bmn.x) / vsz.x, fy = (p.y - bmn.y) / vsz.y, fz = (p.z - bmn.z) / vsz.z;
+                if (fx < 0.0f || fy < 0.0f || fz < 0.0f) continue;
+                const float x = std::floor(fx), y = std::floor(fy), z = std::floor(fz);
+                if (!(x < (float)n) || !(y < (float)n) || !(z < (float)n)) continue;
+                occ[(size_t)z * n * n + (size_t)y * n + (size_t)x] = 1;
+            }
+    }
+    std::vector<uint8_t> act(nvox, 0);
+    for (uint32_t z = 0; z < n; ++z)
+        for (uint32_t y = 0; y < n; ++y)
+            for (uint32_t x = 0; x < n; ++x) {
+                if (!occ[(size_t)z * n * n + (size_t)y * n + x]) continue;
+                for (uint32_t a = (z >= 2 ? z - 2 : 0); a <= std::min(z + 2, n - 1); ++a)
+                    for (uint32_t b = (y >= 2 ? y - 2 : 0); b <= std::min(y + 2, n - 1); ++b)
+                        for (uint32_t c = (x >= 2 ? x - 2 : 0); c <= std::min(x + 2, n - 1); ++c)
+                            act[(size_t)a * n * n + (size_t)b * n + c] = 1;
+            }
+    // Transmittance toward the sun.
+    const P3 ld = normalize(P3{v->light_direction[0], v->light_direction[1], v->light_direction[2]});
+    const P3 cmin = add(bmn, mul(vsz, 0.5f));
+    const float bias = length(vsz) * 3.0f;
+    std::vector<float> light(nvox, 1.0f);
+    auto trace = [&](P3 o) {
+        std::vector<std::pair<float, uint32_t>> hits;
+        for (uint32_t i = 0; i < (uint32_t)tris.size(); ++i) {
+            const Tri& t = tris[i];
+            const P3 e1 = sub(t.p1, t.p0), e2 = sub(t.p2, t.p0);
+            const P3 pv = cross(ld, e2);
+            const float det = dot(e1, pv);
+            if (std::fabs(det) <= 1.0e-8f) continue;
+            const float inv = 1.0f / det;
+            const P3 tv = sub(o, t.p0);
+            const float u = dot(tv, pv) * inv;
+            if (!(u >= 0.0f && u <= 1.0f)) continue;
+            const P3 qv = cross(tv, e1);
+            const float w = dot(ld, qv) * inv;
+            if (w < 0.0f || (u + w) > 1.0f) continue;
+            const float th = dot(e2, qv) * inv;
+            if (th < 1.0e-4f || th > INFINITY) continue;
+            if (!v->materials[t.material].is_translucent) return 0.0f;
+            hits.push_back({th, i});
+        }
+        std::sort(hits.begin(), hits.end(), [](const std::pair<float, uint32_t>& a, const std::pair<float, uint32_t>& b) {
+            const bool an = a.first != a.first, bn = b.first != b.first;
+            if (an != bn) return bn;
+            if (!an && a.first != b.first) return a.first < b.first;
+            return a.second < b.second;
+        });
+        float tr = 1.0f;
+        for (const auto& h : hits) {
+            tr *= v->materials[tris[h.second].material].transmission;
+            if (tr <= 0.0001f) return 0.0f;
+        }
+        return tr;
+    };
+    const uint32_t nt = std::max<uint32_t>(1, threads);
+    std::vector<std::thread> pool;
+    for (uint32_t w = 0; w < nt; ++w)
+        pool.emplace_back([&, w] {
+            for (size_t idx = w; idx < nvox; idx += nt) {
+                if (!act[idx]) continue;
+                const uint32_t z = (uint32_t)(idx / ((size_t)n * n)), rem = (uint32_t)(idx % ((size_t)n * n));
+                const uint32_t y = rem / n, x = rem % n;
+                const P3 vc = add(cmin, P3{(float)x * vsz.x, (float)y * vsz.y, (float)z * vsz.z});
+                light[idx] = trace(add(vc, mul(ld, bias)));
+            }
+        });
+    for (auto& t : pool) t.join();
+    // blur_grid: mean of the in-range 3x3x3 neighbours, squared.
+    for (uint32_t z = 0; z < n; ++z)
+        for (uint32_t y = 0; y < n; ++y)
+            for (uint32_t x = 0; x < n; ++x) {
+                float sum = 0.0f;
+                int count = 0;
+                for (int dz = -1; dz <= 1; ++dz)
+                    for (int dy = -1; dy <= 1; ++dy)
+                        for (int dx = -1; dx <= 1; ++dx) {
+                            const int a = (int)x + dx, b = (int)y + dy, c = (int)z + dz;
+                            if (a < 0 || b < 0 || c < 0 || a >= (int)n || b >= (int)n || c >= (int)n) continue;
+                            sum += light[(size_t)c * n * n + (size_t)b * n + a];
+                            count += 1;
+                        }
+                const float m = count > 0 ? sum / (float)count : 0.0f;
+                out[(size_t)z * n * n + (size_t)y * n + x] = count > 0 ? m * m : 0.0f;
+            }
+    return 0;
+}
+
 // Arm FRSQRTE/FRSQRTS emulation, exposed for the known-answer tests.
 float oracle_frsqrte(float x) { return orc::frsqrte(x); }
 float oracle_frsqrts(float a, float b) { return orc::frsqrts(a, b); }

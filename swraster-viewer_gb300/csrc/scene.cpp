@@ -6,6 +6,7 @@
 // with -ffp-contract=off. Transcendentals (powf, sinf, cosf, sqrtf) come from
 // the host libm, the same functions a Rust build links.
 #include "scene.h"
+#include "precompute.h"
 
 #include <cuda_runtime.h>
 
@@ -566,11 +567,14 @@ bool ray_tri(V3 o, V3 d, const RtTri& t, float tmin, float tmax, float& th) {
     th = tt;
     return true;
 }
-// trace_transmittance (src/raytracer.rs:172-207).
+// trace_transmittance (src/raytracer.rs:172-207). Translucent hits multiply
+// in (t, triangle index) order: the reference sorts by t and keeps its BVH's
+// visiting order for equal t, which no other traversal reproduces, so equal
+// t is ordered by triangle (the device version uses the same rule).
 float trace_transmittance(const Bvh& b, const std::vector<RtTri>& tris, const std::vector<swr_material_view>& mats,
                           V3 o, V3 d, float tmin, float tmax) {
     const float inv[3] = {1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
-    std::vector<std::pair<float, uint32_t>> hits;
+    std::vector<std::pair<float, uint32_t>> hits;  // (t, triangle)
     uint32_t stack[128];
     int sp = 0;
     stack[sp++] = 0;
@@ -602,13 +606,19 @@ float trace_transmittance(const Bvh& b, const std::vector<RtTri>& tris, const st
             float th;
             if (!ray_tri(o, d, t, tmin, tmax, th)) continue;
             if (!mats[t.material].is_translucent) return 0.0f;
-            hits.push_back({th, t.material});
+            hits.push_back({th, b.order[nd.left + i]});
         }
     }
-    std::stable_sort(hits.begin(), hits.end(), [](const auto& x, const auto& y) { return x.first < y.first; });
+    // t ascending (a NaN t, possible only with non-finite vertices, last), then triangle.
+    std::sort(hits.begin(), hits.end(), [](const std::pair<float, uint32_t>& x, const std::pair<float, uint32_t>& y) {
+        const bool xn = x.first != x.first, yn = y.first != y.first;
+        if (xn != yn) return yn;
+        if (!xn && x.first != y.first) return x.first < y.first;
+        return x.second < y.second;
+    });
     float tr = 1.0f;
     for (const auto& h : hits) {
-        tr *= mats[h.second].transmission;
+        tr *= mats[tris[h.second].material].transmission;
         if (tr <= 0.0001f) return 0.0f;
     }
     return tr;
@@ -849,48 +859,72 @@ swr_status build_scene(const swr_scene_desc* desc, SceneImpl* s, std::string& er
                     for (uint32_t b = y0; b <= y1; ++b)
                         for (uint32_t c = x0; c <= x1; ++c) active[(size_t)a * n * n + b * n + c] = 1;
             }
-    // compute_sun_visibility (src/gi.rs:267-314).
-    std::vector<float> light(nvox, 1.0f);
-    {
-        Bvh bvh;
-        if (!rt.empty()) bvh_build(rt, bvh);
+    // compute_sun_visibility (src/gi.rs:267-314) and blur_grid: on the device
+    // for scenes that go to the device, else (host-only scenes) here.
+    if (!(desc->flags & SWR_SCENE_HOST_ONLY)) {
+        std::vector<LightTri> lt(rt.size());
+        for (size_t i = 0; i < rt.size(); ++i) {
+            const RtTri& t = rt[i];
+            lt[i] = LightTri{{t.p0.x, t.p0.y, t.p0.z}, {t.p1.x, t.p1.y, t.p1.z}, {t.p2.x, t.p2.y, t.p2.z}, t.material};
+        }
+        std::vector<uint8_t> trans(s->materials.size());
+        std::vector<float> transm(s->materials.size());
+        for (size_t i = 0; i < s->materials.size(); ++i) {
+            trans[i] = s->materials[i].is_translucent ? 1 : 0;
+            transm[i] = s->materials[i].transmission;
+        }
         const V3 ld = normalize3(s->light_dir);
         const V3 cmin = add(bmn, mul(vsz, 0.5f));
-        const float bias = length3(vsz) * 3.0f;
-        size_t active_total = 0;
-        for (uint8_t a : active) active_total += a;
-        if (active_total > 0 && !rt.empty()) {
-            parallel_for(nvox, threads, [&](size_t idx) {
-                if (!active[idx]) return;
-                const size_t z = idx / ((size_t)n * n);
-                const size_t rem = idx % ((size_t)n * n);
-                const size_t y = rem / n, x = rem % n;
-                const V3 vc = add(cmin, mulv(V3{(float)x, (float)y, (float)z}, vsz));
-                const V3 o = add(vc, mul(ld, bias));
-                light[idx] = trace_transmittance(bvh, rt, s->materials, o, ld, 1.0e-4f, INFINITY);
-            });
-        }
-        // blur_grid (src/voxelgrid.rs:370-419): 3x3x3 mean, then squared.
-        std::vector<float> blurred(nvox, 0.0f);
-        parallel_for(n, threads, [&](size_t z) {
-            for (uint32_t y = 0; y < n; ++y)
-                for (uint32_t x = 0; x < n; ++x) {
-                    float sum = 0.0f;
-                    int count = 0;
-                    for (int dz = -1; dz <= 1; ++dz)
-                        for (int dy = -1; dy <= 1; ++dy)
-                            for (int dx = -1; dx <= 1; ++dx) {
-                                const int nx = (int)x + dx, ny = (int)y + dy, nz = (int)z + dz;
-                                if (nx >= 0 && nx < (int)n && ny >= 0 && ny < (int)n && nz >= 0 && nz < (int)n) {
-                                    sum += light[(size_t)nz * n * n + (size_t)ny * n + nx];
-                                    count += 1;
+        const float bmin3[3] = {bmn.x, bmn.y, bmn.z}, bmax3[3] = {bmx.x, bmx.y, bmx.z};
+        const float cmin3[3] = {cmin.x, cmin.y, cmin.z}, vsz3[3] = {vsz.x, vsz.y, vsz.z}, ld3[3] = {ld.x, ld.y, ld.z};
+        s->voxel_light.assign(nvox, 0.0f);
+        const swr_status vst = sun_visibility_device(lt.data(), lt.size(), trans.data(), transm.data(),
+                                                     (uint32_t)trans.size(), active.data(), n, bmin3, bmax3, cmin3,
+                                                     vsz3, ld3, length3(vsz) * 3.0f, s->voxel_light.data(), err);
+        if (vst != SWR_OK) return vst;
+    } else {
+        std::vector<float> light(nvox, 1.0f);
+        {
+            Bvh bvh;
+            if (!rt.empty()) bvh_build(rt, bvh);
+            const V3 ld = normalize3(s->light_dir);
+            const V3 cmin = add(bmn, mul(vsz, 0.5f));
+            const float bias = length3(vsz) * 3.0f;
+            size_t active_total = 0;
+            for (uint8_t a : active) active_total += a;
+            if (active_total > 0 && !rt.empty()) {
+                parallel_for(nvox, threads, [&](size_t idx) {
+                    if (!active[idx]) return;
+                    const size_t z = idx / ((size_t)n * n);
+                    const size_t rem = idx % ((size_t)n * n);
+                    const size_t y = rem / n, x = rem % n;
+                    const V3 vc = add(cmin, mulv(V3{(float)x, (float)y, (float)z}, vsz));
+                    const V3 o = add(vc, mul(ld, bias));
+                    light[idx] = trace_transmittance(bvh, rt, s->materials, o, ld, 1.0e-4f, INFINITY);
+                });
+            }
+            // blur_grid (src/voxelgrid.rs:370-419): 3x3x3 mean, then squared.
+            std::vector<float> blurred(nvox, 0.0f);
+            parallel_for(n, threads, [&](size_t z) {
+                for (uint32_t y = 0; y < n; ++y)
+                    for (uint32_t x = 0; x < n; ++x) {
+                        float sum = 0.0f;
+                        int count = 0;
+                        for (int dz = -1; dz <= 1; ++dz)
+                            for (int dy = -1; dy <= 1; ++dy)
+                                for (int dx = -1; dx <= 1; ++dx) {
+                                    const int nx = (int)x + dx, ny = (int)y + dy, nz = (int)z + dz;
+                                    if (nx >= 0 && nx < (int)n && ny >= 0 && ny < (int)n && nz >= 0 && nz < (int)n) {
+                                        sum += light[(size_t)nz * n * n + (size_t)ny * n + nx];
+                                        count += 1;
+                                    }
                                 }
-                            }
-                    float m = count > 0 ? sum / (float)count : 0.0f;
-                    blurred[z * n * n + (size_t)y * n + x] = count > 0 ? m * m : 0.0f;
-                }
-        });
-        s->voxel_light = std::move(blurred);
+                        float m = count > 0 ? sum / (float)count : 0.0f;
+                        blurred[z * n * n + (size_t)y * n + x] = count > 0 ? m * m : 0.0f;
+                    }
+            });
+            s->voxel_light = std::move(blurred);
+        }
     }
     // initialize_voxel_gi_from_scene (src/gi.rs:123-149).
     for (int i = 0; i < 4; ++i) {
