@@ -184,6 +184,9 @@ typedef struct swr_scene_desc {
 /* swr_scene_desc.flags */
 #define SWR_SCENE_HOST_ONLY 1u  /* build and precompute only; no device copy
                                    (swr_scene_export works, rendering does not) */
+#define SWR_SCENE_GI 2u         /* bake the voxel GI (the reference's --gi: bake_voxel_gi,
+                                   src/gi.rs:316-408) on the device and shade with
+                                   the full SH4 grid; not with SWR_SCENE_HOST_ONLY */
 
 typedef struct swr_scene swr_scene;
 
@@ -314,6 +317,7 @@ typedef struct swr_scene_host_view {
     float voxel_world_max[3];
     const float* voxel_light_intensity;   /* voxel_size^3 (sun visibility, blurred) */
     float voxel_gi_sh4_const[4][4];       /* per-voxel SH4 rgb (+w filled per voxel) */
+    const float* voxel_gi_sh4;            /* SWR_SCENE_GI: voxel_size^3 x 4 (r, g, b, w), else NULL */
 } swr_scene_host_view;
 
 swr_status swr_scene_export(const swr_scene* scene, swr_scene_host_view* out);

@@ -60,6 +60,8 @@ def lib():
         L.oracle_frsqrts.restype = C.c_float
         L.oracle_sun_visibility.argtypes = [C.POINTER(swr.SceneHostView), C.c_uint32, C.c_void_p]
         L.oracle_sun_visibility.restype = C.c_int
+        L.oracle_gi_bake.argtypes = [C.POINTER(swr.SceneHostView), C.c_uint32, C.c_void_p]
+        L.oracle_gi_bake.restype = C.c_int
         _lib = L
     return _lib
 
@@ -86,6 +88,16 @@ def sun_visibility(view, threads=1):
     out = np.zeros(n * n * n, np.float32)
     if lib().oracle_sun_visibility(C.byref(view), threads, out.ctypes.data_as(C.c_void_p)) != 0:
         raise RuntimeError("oracle_sun_visibility failed")
+    return out
+
+
+def gi_bake(view, threads=1):
+    """Blurred baked SH4 grid (voxel_size^3 x 4 x (r, g, b, w)) of the scene's
+    voxel GI bake, by brute force over every triangle."""
+    n = view.voxel_size
+    out = np.zeros((n * n * n, 4, 4), np.float32)
+    if lib().oracle_gi_bake(C.byref(view), threads, out.ctypes.data_as(C.c_void_p)) != 0:
+        raise RuntimeError("oracle_gi_bake failed")
     return out
 
 

@@ -383,9 +383,11 @@ struct Voxel {
     float min[3], vs[3];
     const float* light;
     float gi[4][4];
+    const float* sh4;  // baked grid (n^3 x 16), or null
 };
-// get_filtered_gi_sh4_packed_vec (src/voxelgrid.rs:264-368) over a grid whose
-// voxels all hold gi[c] except w of coefficient 0 (light intensity).
+// get_filtered_gi_sh4_packed_vec (src/voxelgrid.rs:264-368) over the baked
+// grid, or over a grid whose voxels all hold gi[c] except w of coefficient 0
+// (light intensity).
 static void voxel_gi(const Voxel& g, V3x4 p, V3x4 out_rgb[4], F4 out_w[4]) {
     const F4 vx = (p.x - g.min[0]) / splat(g.vs[0]);
     const F4 vy = (p.y - g.min[1]) / splat(g.vs[1]);
@@ -410,7 +412,9 @@ static void voxel_gi(const Voxel& g, V3x4 p, V3x4 out_rgb[4], F4 out_w[4]) {
     auto coeff = [&](int c, int comp, const uint64_t* X, const uint64_t* Y, const uint64_t* Z) {
         F4 r;
         for (int i = 0; i < 4; ++i) {
-            if (c == 0 && comp == 3)
+            if (g.sh4)
+                r.l[i] = g.sh4[(Z[i] * g.n * g.n + Y[i] * g.n + X[i]) * 16 + (uint64_t)c * 4 + comp];
+            else if (c == 0 && comp == 3)
                 r.l[i] = g.light[Z[i] * g.n * g.n + Y[i] * g.n + X[i]];
             else
                 r.l[i] = g.gi[c][comp];
@@ -1065,6 +1069,7 @@ int oracle_render(const swr_scene_host_view* s, const swr_camera* cam, int32_t w
     }
     f.vox.light = s->voxel_light_intensity;
     std::memcpy(f.vox.gi, s->voxel_gi_sh4_const, sizeof(f.vox.gi));
+    f.vox.sh4 = s->voxel_gi_sh4;
     for (int ty = 0; ty < f.tiles_y; ++ty)
         for (int tx = 0; tx < f.tiles_x; ++tx) {
             Tile* t = new Tile();
@@ -1389,6 +1394,380 @@ int oracle_sun_visibility(const swr_scene_host_view* v, uint32_t threads, float*
                         }
                 const float m = count > 0 ? sum / (float)count : 0.0f;
                 out[(size_t)z * n * n + (size_t)y * n + x] = count > 0 ? m * m : 0.0f;
+            }
+    return 0;
+}
+
+// bake_voxel_gi (src/gi.rs:316-408) + blur_gi_sh4 (src/voxelgrid.rs:422-472)
+// for a scene view whose voxel_light_intensity holds the blurred sun
+// visibility: per active voxel (occupancy + dilation as above) 64 rays from
+// its direction set; trace_nearest keeps the hit of smallest (t, triangle),
+// trace_transmittance multiplies translucent hits in that order; every ray
+// tests every triangle. Writes voxel_size^3 x 16 floats (four r, g, b, w).
+int oracle_gi_bake(const swr_scene_host_view* v, uint32_t threads, float* out) {
+    struct P3 {
+        float x, y, z;
+    };
+    auto sub = [](P3 a, P3 b) { return P3{a.x - b.x, a.y - b.y, a.z - b.z}; };
+    auto add = [](P3 a, P3 b) { return P3{a.x + b.x, a.y + b.y, a.z + b.z}; };
+    auto mul = [](P3 a, float s) { return P3{a.x * s, a.y * s, a.z * s}; };
+    auto mulv = [](P3 a, P3 b) { return P3{a.x * b.x, a.y * b.y, a.z * b.z}; };
+    auto dot = [](P3 a, P3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; };
+    auto cross = [](P3 a, P3 b) {
+        return P3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+    };
+    auto length = [&](P3 a) { return std::sqrt(dot(a, a)); };
+    auto normalize = [&](P3 a) { return mul(a, 1.0f / length(a)); };
+    auto vmax0 = [](P3 a) { return P3{std::fmax(a.x, 0.0f), std::fmax(a.y, 0.0f), std::fmax(a.z, 0.0f)}; };
+    auto srgb_lin = [](float s) { return s <= 0.04045f ? s / 12.92f : std::pow((s + 0.055f) / 1.055f, 2.4f); };
+    const float pi = 3.14159265358979323846f;
+    struct Tri {
+        P3 p0, p1, p2, n;
+        float uv[3][2];
+        uint32_t material;
+    };
+    std::vector<Tri> tris;
+    for (uint32_t ni = 0; ni < v->node_count; ++ni) {
+        const swr_node_view& nd = v->nodes[ni];
+        if (nd.mesh < 0) continue;
+        const swr_mesh_view& m = v->meshes[nd.mesh];
+        const float* T = nd.transform;
+        for (uint32_t k = 0; k < m.primitive_count; ++k) {
+            const swr_primitive_view& p = v->primitives[m.primitives[k]];
+            for (uint32_t t = 0; t + 2 < p.index_count; t += 3) {
+                P3 w[3];
+                Tri tr{};
+                for (int c = 0; c < 3; ++c) {
+                    const uint32_t vi = p.indices[t + c];
+                    const float* q = p.positions + 4 * (size_t)vi;
+                    float r[4];
+                    for (int j = 0; j < 4; ++j) r[j] = ((T[j] * q[0] + T[4 + j] * q[1]) + T[8 + j] * q[2]) + T[12 + j] * q[3];
+                    w[c] = P3{r[0], r[1], r[2]};
+                    tr.uv[c][0] = p.texcoords[2 * (size_t)vi];
+                    tr.uv[c][1] = p.texcoords[2 * (size_t)vi + 1];
+                }
+                const P3 fn = cross(sub(w[1], w[0]), sub(w[2], w[0]));
+                if (dot(fn, fn) <= 1.0e-12f) continue;
+                tr.p0 = w[0];
+                tr.p1 = w[1];
+                tr.p2 = w[2];
+                tr.n = normalize(fn);
+                tr.material = p.material;
+                tris.push_back(tr);
+            }
+        }
+    }
+    const uint32_t n = v->voxel_size;
+    const size_t nvox = (size_t)n * n * n;
+    const P3 bmn{v->voxel_world_min[0], v->voxel_world_min[1], v->voxel_world_min[2]};
+    const P3 bmx{v->voxel_world_max[0], v->voxel_world_max[1], v->voxel_world_max[2]};
+    const P3 wsz = sub(bmx, bmn);
+    const P3 vsz{wsz.x / (float)n, wsz.y / (float)n, wsz.z / (float)n};
+    // Active voxels: occupancy from barycentric samples, dilated by 2.
+    std::vector<uint8_t> occ(nvox, 0), act(nvox, 0);
+    {
+        const float mine = std::fmax(std::fmin(vsz.x, std::fmin(vsz.y, vsz.z)), 1.0e-6f);
+        const float area_ref = mine * mine;
+        for (const Tri& t : tris) {
+            const float area = 0.5f * length(cross(sub(t.p1, t.p0), sub(t.p2, t.p0)));
+            const float ts = std::ceil((area / area_ref) * 2.0f);
+            size_t target = (ts != ts || ts <= 0.0f) ? 0 : (ts >= 1.8e19f ? SIZE_MAX : (size_t)ts);
+            target = std::min<size_t>(std::max<size_t>(target, 1), 4096);
+            const size_t ns = (size_t)std::ceil(std::sqrt((float)target));
+            for (size_t iu = 0; iu < ns; ++iu)
+                for (size_t iv = 0; iv < ns - iu; ++iv) {
+                    const float u = ((float)iu + 0.5f) / (float)ns, w2 = ((float)iv + 0.5f) / (float)ns;
+                    const float w = (1.0f - u) - w2;
+                    if (w < 0.0f) continue;
+                    const P3 p = add(add(mul(t.p0, w), mul(t.p1, u)), mul(t.p2, w2));
+                    const float fx = (p.x - bmn.x) / vsz.x, fy = (p.y - bmn.y) / vsz.y, fz = (p.z - bmn.z) / vsz.z;
+                    if (fx < 0.0f || fy < 0.0f || fz < 0.0f) continue;
+                    const float x = std::floor(fx), y = std::floor(fy), z = std::floor(fz);
+                    if (!(x < (float)n) || !(y < (float)n) || !(z < (float)n)) continue;
+                    occ[(size_t)z * n * n + (size_t)y * n + (size_t)x] = 1;
+                }
+        }
+        for (uint32_t z = 0; z < n; ++z)
+            for (uint32_t y = 0; y < n; ++y)
+                for (uint32_t x = 0; x < n; ++x) {
+                    if (!occ[(size_t)z * n * n + (size_t)y * n + x]) continue;
+                    for (uint32_t a = (z >= 2 ? z - 2 : 0); a <= std::min(z + 2, n - 1); ++a)
+                        for (uint32_t b = (y >= 2 ? y - 2 : 0); b <= std::min(y + 2, n - 1); ++b)
+                            for (uint32_t c = (x >= 2 ? x - 2 : 0); c <= std::min(x + 2, n - 1); ++c)
+                                act[(size_t)a * n * n + (size_t)b * n + c] = 1;
+                }
+    }
+    auto ray_tri = [&](P3 o, P3 d, const Tri& t, float tmin, float& th, float& bu, float& bv) {
+        const P3 e1 = sub(t.p1, t.p0), e2 = sub(t.p2, t.p0);
+        const P3 pv = cross(d, e2);
+        const float det = dot(e1, pv);
+        if (std::fabs(det) <= 1.0e-8f) return false;
+        const float inv = 1.0f / det;
+        const P3 tv = sub(o, t.p0);
+        const float u = dot(tv, pv) * inv;
+        if (!(u >= 0.0f && u <= 1.0f)) return false;
+        const P3 qv = cross(tv, e1);
+        const float w = dot(d, qv) * inv;
+        if (w < 0.0f || (u + w) > 1.0f) return false;
+        const float tt = dot(e2, qv) * inv;
+        if (tt < tmin || tt > INFINITY) return false;
+        th = tt;
+        bu = u;
+        bv = w;
+        return true;
+    };
+    auto before = [](float ta, uint32_t ia, float tb, uint32_t ib) {
+        const bool an = ta != ta, bn = tb != tb;
+        if (an != bn) return bn;
+        if (!an && ta != tb) return ta < tb;
+        return ia < ib;
+    };
+    auto nearest = [&](P3 o, P3 d, float tmin, uint32_t& bi, float& bt, float& bu, float& bv) {
+        bool found = false;
+        for (uint32_t i = 0; i < (uint32_t)tris.size(); ++i) {
+            float t, u, w;
+            if (!ray_tri(o, d, tris[i], tmin, t, u, w)) continue;
+            if (!found || before(t, i, bt, bi)) {
+                found = true;
+                bi = i;
+                bt = t;
+                bu = u;
+                bv = w;
+            }
+        }
+        return found;
+    };
+    auto transmittance = [&](P3 o, P3 d, float tmin) {
+        std::vector<std::pair<float, uint32_t>> hits;
+        for (uint32_t i = 0; i < (uint32_t)tris.size(); ++i) {
+            float t, u, w;
+            if (!ray_tri(o, d, tris[i], tmin, t, u, w)) continue;
+            if (!v->materials[tris[i].material].is_translucent) return 0.0f;
+            hits.push_back({t, i});
+        }
+        std::sort(hits.begin(), hits.end(), [&](const std::pair<float, uint32_t>& a, const std::pair<float, uint32_t>& b) {
+            return before(a.first, a.second, b.first, b.second);
+        });
+        float tr = 1.0f;
+        for (const auto& h : hits) {
+            tr *= v->materials[tris[h.second].material].transmission;
+            if (tr <= 0.0001f) return 0.0f;
+        }
+        return tr;
+    };
+    // sample_bilinear_rgb at mip 0 with the slot's wrap modes, to linear.
+    auto wrapf = [](float t, float dim, uint32_t mode) {
+        if (mode == 0u) {
+            t = t - std::floor(t / dim) * dim;
+        } else if (mode == 1u) {
+            const float two = dim * 2.0f;
+            t = t - std::floor(t / two) * two;
+            t = std::fmin(t, two - t);
+        }
+        return std::fmin(t, dim - 1.0f);
+    };
+    auto to_u = [](float f) -> uint32_t {
+        if (!(f > 0.0f)) return 0;
+        if (f >= 4294967296.0f) return 0xFFFFFFFFu;
+        return (uint32_t)f;
+    };
+    auto bilinear = [&](int32_t tex, float u, float w, uint32_t ws, uint32_t wt) {
+        const swr_texture_view& T = v->textures[tex];
+        const float wf = (float)T.width, hf = (float)T.height;
+        const float xf = u * wf - 0.5f, yf = w * hf - 0.5f;
+        const float x0 = std::floor(xf), y0 = std::floor(yf);
+        const float fx = xf - x0, fy = yf - y0, ofx = 1.0f - fx, ofy = 1.0f - fy;
+        const uint32_t ix0 = to_u(wrapf(x0, wf, ws)), iy0 = to_u(wrapf(y0, hf, wt));
+        const uint32_t ix1 = to_u(wrapf(x0 + 1.0f, wf, ws)), iy1 = to_u(wrapf(y0 + 1.0f, hf, wt));
+        const uint32_t p00 = T.data[iy0 * T.width + ix0], p10 = T.data[iy0 * T.width + ix1];
+        const uint32_t p01 = T.data[iy1 * T.width + ix0], p11 = T.data[iy1 * T.width + ix1];
+        const float w00 = ofx * ofy, w10 = fx * ofy, w01 = ofx * fy, w11 = fx * fy;
+        float c[3];
+        for (int k = 0; k < 3; ++k) {
+            const int sh = 24 - 8 * k;
+            auto un = [&](uint32_t p) { return (float)((p >> sh) & 0xFFu) / 255.0f; };
+            c[k] = ((un(p00) * w00 + un(p10) * w10) + un(p01) * w01) + un(p11) * w11;
+        }
+        return P3{srgb_lin(c[0]), srgb_lin(c[1]), srgb_lin(c[2])};
+    };
+    // sample_sky_radiance: nearest texel of the cubemap's mip 0.
+    auto sky = [&](P3 d) {
+        const float ax = std::fabs(d.x), ay = std::fabs(d.y), az = std::fabs(d.z);
+        const bool mx = (ax >= ay) && (ax >= az), my = (ay > ax) && (ay >= az);
+        const float sx = d.x >= 0.0f ? 1.0f : -1.0f, sy = d.y >= 0.0f ? 1.0f : -1.0f, sz = d.z >= 0.0f ? 1.0f : -1.0f;
+        const float u = mx ? -d.z * sx : (my ? d.x : d.x * sz);
+        const float w = mx ? -d.y : (my ? d.z * sy : -d.y);
+        const float den = std::fmax(mx ? ax : (my ? ay : az), 1.0e-19f);
+        const float uf = 0.5f * (u / den + 1.0f), vf = 0.5f * (w / den + 1.0f);
+        const uint32_t slice = mx ? (d.x >= 0.0f ? 0u : 1u) : (my ? (d.y >= 0.0f ? 2u : 3u) : (d.z >= 0.0f ? 4u : 5u));
+        const uint32_t cs = v->cubemap.width;
+        const float wm1 = (float)cs - 1.0f;
+        auto rnd = [](float x) {
+            float t = std::trunc(x);
+            if (std::fabs(x - t) >= 0.5f) t += std::copysign(1.0f, x);
+            return t;
+        };
+        const uint32_t x = to_u(std::fmin(std::fmax(rnd(uf * wm1), 0.0f), wm1));
+        const uint32_t y = to_u(std::fmin(std::fmax(rnd(vf * wm1), 0.0f), wm1));
+        const uint32_t p = v->cubemap.data[slice * cs * cs + y * cs + x];
+        auto un = [&](int sh) { return srgb_lin((float)((p >> sh) & 0xFFu) / 255.0f); };
+        return P3{un(24), un(16), un(8)};
+    };
+    // Direction sets (build_uniform_sphere_samples, src/gi.rs:416-434).
+    auto rad_inv = [](uint32_t bits) {
+        bits = (bits << 16) | (bits >> 16);
+        bits = ((bits & 0x55555555u) << 1) | ((bits & 0xAAAAAAAAu) >> 1);
+        bits = ((bits & 0x33333333u) << 2) | ((bits & 0xCCCCCCCCu) >> 2);
+        bits = ((bits & 0x0F0F0F0Fu) << 4) | ((bits & 0xF0F0F0F0u) >> 4);
+        bits = ((bits & 0x00FF00FFu) << 8) | ((bits & 0xFF00FF00u) >> 8);
+        return (float)bits * 2.3283064e-10f;
+    };
+    std::vector<P3> dirs;
+    for (uint32_t set = 0; set < 9; ++set) {
+        const float ox = rad_inv(set + 1), oy = ((float)set + 0.5f) / 9.0f;
+        for (uint32_t i = 0; i < 64; ++i) {
+            float xx = (float)i / 64.0f + ox, xy = rad_inv(i) + oy;
+            xx = xx - std::trunc(xx);
+            xy = xy - std::trunc(xy);
+            const float z = 1.0f - 2.0f * xx;
+            const float r = std::sqrt(std::fmax(1.0f - z * z, 0.0f));
+            const float phi = 2.0f * pi * xy;
+            dirs.push_back(normalize(P3{r * std::cos(phi), r * std::sin(phi), z}));
+        }
+    }
+    const P3 ld = normalize(P3{v->light_direction[0], v->light_direction[1], v->light_direction[2]});
+    const P3 lc{v->light_color[0], v->light_color[1], v->light_color[2]};
+    P3 shc[4];
+    for (int i = 0; i < 4; ++i) shc[i] = P3{v->irradiance_sh[i][0], v->irradiance_sh[i][1], v->irradiance_sh[i][2]};
+    const float vlen = length(vsz);
+    const float min_edge = std::fmax(std::fmin(std::fmin(vsz.x, vsz.y), vsz.z), 1.0e-6f);
+    const float primary_weight = (4.0f * pi) / 64.0f;
+    const float primary_bias = std::fmax(vlen * 0.35f, 1.0e-4f * 4.0f);
+    const float hit_bias = std::fmax(vlen * 0.05f, 1.0e-4f * 8.0f);
+    const float gi_tmin = std::fmax(min_edge * 0.15f, 1.0e-4f);
+    const P3 cmin = add(bmn, mul(vsz, 0.5f));
+    // estimate_surface_bounce_radiance (src/gi.rs:466-547).
+    auto bounce = [&](uint32_t ti, float t, float bu, float bv, P3 o, P3 in_dir) {
+        const Tri& tri = tris[ti];
+        const swr_material_view& m = v->materials[tri.material];
+        P3 nrm = tri.n;
+        if (dot(nrm, mul(in_dir, -1.0f)) < 0.0f) nrm = mul(nrm, -1.0f);
+        const float bw = (1.0f - bu) - bv;
+        const float uvx = (tri.uv[0][0] * bw + tri.uv[1][0] * bu) + tri.uv[2][0] * bv;
+        const float uvy = (tri.uv[0][1] * bw + tri.uv[1][1] * bu) + tri.uv[2][1] * bv;
+        P3 em{m.emissive_factor[0], m.emissive_factor[1], m.emissive_factor[2]};
+        if (m.tex[3] >= 0) em = mulv(em, bilinear(m.tex[3], uvx, uvy, m.wrap_s[3], m.wrap_t[3]));
+        em = vmax0(em);
+        P3 alb{m.base_color_factor[0], m.base_color_factor[1], m.base_color_factor[2]};
+        if (m.tex[0] >= 0) alb = mulv(alb, bilinear(m.tex[0], uvx, uvy, m.wrap_s[0], m.wrap_t[0]));
+        alb = mul(P3{std::fmin(std::fmax(alb.x, 0.0f), 1.0f), std::fmin(std::fmax(alb.y, 0.0f), 1.0f),
+                     std::fmin(std::fmax(alb.z, 0.0f), 1.0f)}, 1.0f);
+        if (dot(alb, alb) <= 0.0f && dot(em, em) <= 0.0f) return P3{0.0f, 0.0f, 0.0f};
+        const float dir_bias = hit_bias * 0.5f;
+        const P3 so = add(add(o, mul(in_dir, t)), mul(nrm, hit_bias));
+        const float ndl = std::fmax(dot(nrm, ld), 0.0f);
+        P3 e_sun{0.0f, 0.0f, 0.0f};
+        if (ndl > 0.0f) e_sun = mul(lc, ndl * transmittance(add(so, mul(ld, dir_bias)), ld, gi_tmin));
+        // sky_visibility_hemisphere4 + tangent_basis (src/gi.rs:549-578).
+        const P3 up = std::fabs(nrm.z) < 0.999f ? P3{0.0f, 0.0f, 1.0f} : P3{1.0f, 0.0f, 0.0f};
+        const P3 tg = normalize(cross(nrm, up));
+        const P3 btg = cross(nrm, tg);
+        const float dl[4][3] = {{0.0f, 0.0f, 1.0f}, {0.8660254f, 0.0f, 0.5f}, {-0.4330127f, 0.75f, 0.5f},
+                                {-0.4330127f, -0.75f, 0.5f}};
+        float vis = 0.0f;
+        for (int i = 0; i < 4; ++i) {
+            const P3 dir = normalize(add(add(mul(tg, dl[i][0]), mul(btg, dl[i][1])), mul(nrm, dl[i][2])));
+            vis += transmittance(add(so, mul(dir, dir_bias)), dir, gi_tmin);
+        }
+        vis = vis * 0.25f;
+        const P3 e_sky = mul(vmax0(add(add(add(shc[0], mul(shc[1], nrm.y)), mul(shc[2], nrm.z)), mul(shc[3], nrm.x))), vis);
+        const P3 e_tot = vmax0(add(e_sun, e_sky));
+        const P3 bnc = dot(e_tot, e_tot) > 0.0f ? mulv(alb, P3{e_tot.x / pi, e_tot.y / pi, e_tot.z / pi}) : P3{0, 0, 0};
+        return add(bnc, em);
+    };
+    auto lum = [](P3 c) { return (0.2126f * c.x + 0.7152f * c.y) + 0.0722f * c.z; };
+    std::vector<float> raw(nvox * 16);
+    const uint32_t nt = std::max<uint32_t>(1, threads);
+    std::vector<std::thread> pool;
+    for (uint32_t wk = 0; wk < nt; ++wk)
+        pool.emplace_back([&, wk] {
+            for (size_t idx = wk; idx < nvox; idx += nt) {
+                float* o = raw.data() + idx * 16;
+                const float sun = v->voxel_light_intensity[idx];
+                if (!act[idx]) {  // initialize_voxel_gi_from_scene(scale 1, sky 1)
+                    for (int i = 0; i < 4; ++i) {
+                        o[4 * i] = shc[i].x * 1.0f;
+                        o[4 * i + 1] = shc[i].y * 1.0f;
+                        o[4 * i + 2] = shc[i].z * 1.0f;
+                        o[4 * i + 3] = 0.0f;
+                    }
+                    o[3] = sun;
+                    o[7] = 1.0f;
+                    continue;
+                }
+                const uint32_t z = (uint32_t)(idx / ((size_t)n * n)), rem = (uint32_t)(idx % ((size_t)n * n));
+                const uint32_t y = rem / n, x = rem % n;
+                const P3 vc = add(cmin, P3{(float)x * vsz.x, (float)y * vsz.y, (float)z * vsz.z});
+                const uint32_t set = ((x % 3u) + 3u * (y % 3u) + (z % 3u)) % 9u;
+                P3 rsh[4] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+                uint32_t sky_hits = 0;
+                for (uint32_t s = 0; s < 64; ++s) {
+                    const P3 dir = dirs[set * 64 + s];
+                    const P3 ro = add(vc, mul(dir, primary_bias));
+                    uint32_t ti = 0;
+                    float th = 0.0f, bu = 0.0f, bv = 0.0f;
+                    P3 rad;
+                    if (nearest(ro, dir, gi_tmin, ti, th, bu, bv)) {
+                        rad = bounce(ti, th, bu, bv, ro, dir);
+                    } else {
+                        ++sky_hits;
+                        rad = sky(dir);
+                    }
+                    if (dot(rad, rad) <= 0.0f) continue;
+                    const float basis[4] = {0.282095f, 0.488603f * dir.y, 0.488603f * dir.z, 0.488603f * dir.x};
+                    for (int i = 0; i < 4; ++i) rsh[i] = add(rsh[i], mul(rad, basis[i] * primary_weight));
+                }
+                rsh[0] = mul(rsh[0], pi * 0.282095f);
+                const float k1 = ((2.0f * pi) / 3.0f) * 0.488603f;
+                for (int i = 1; i < 4; ++i) rsh[i] = mul(rsh[i], k1);
+                P3 rgb[4];
+                for (int i = 0; i < 4; ++i) rgb[i] = vmax0(rsh[i]);
+                const float floor_lum = lum(mul(shc[0], 0.005f));
+                if (floor_lum > 0.0f) {
+                    const float cur = lum(rgb[0]);
+                    if (cur < floor_lum) {
+                        const float t = std::fmin(std::fmax((floor_lum - cur) / floor_lum, 0.0f), 1.0f);
+                        for (int i = 0; i < 4; ++i) rgb[i] = add(mul(rgb[i], 1.0f - t), mul(mul(shc[i], 0.005f), t));
+                    }
+                }
+                for (int i = 0; i < 4; ++i) {
+                    o[4 * i] = rgb[i].x;
+                    o[4 * i + 1] = rgb[i].y;
+                    o[4 * i + 2] = rgb[i].z;
+                    o[4 * i + 3] = 0.0f;
+                }
+                o[3] = sun;
+                o[7] = (float)sky_hits / 64.0f;
+            }
+        });
+    for (auto& t : pool) t.join();
+    // blur_gi_sh4.
+    for (uint32_t z = 0; z < n; ++z)
+        for (uint32_t y = 0; y < n; ++y)
+            for (uint32_t x = 0; x < n; ++x) {
+                float sum[16] = {};
+                float count = 0.0f;
+                for (int dz = -1; dz <= 1; ++dz)
+                    for (int dy = -1; dy <= 1; ++dy)
+                        for (int dx = -1; dx <= 1; ++dx) {
+                            const int a = (int)x + dx, b = (int)y + dy, c = (int)z + dz;
+                            if (a < 0 || b < 0 || c < 0 || a >= (int)n || b >= (int)n || c >= (int)n) continue;
+                            const float* s = raw.data() + ((size_t)c * n * n + (size_t)b * n + a) * 16;
+                            for (int k = 0; k < 16; ++k) sum[k] += s[k];
+                            count += 1.0f;
+                        }
+                float* o = out + ((size_t)z * n * n + (size_t)y * n + x) * 16;
+                for (int k = 0; k < 16; ++k) o[k] = sum[k] / count;
             }
     return 0;
 }

@@ -66,7 +66,7 @@ __device__ __forceinline__ float rsqrt_ieee(float x) { return __fdiv_rn(1.0f, __
 // FRSQRTE (single precision, FPCR.AH = 0): 8-bit estimate from the Arm
 // architecture's RecipSqrtEstimate, table-driven. `tab` holds estimate<7:0>
 // for the 9-bit scaled operand (128..511).
-__device__ __noinline__ float frsqrte_special(float x, const uint8_t* tab) {
+static __device__ __noinline__ float frsqrte_special(float x, const uint8_t* tab) {
     const uint32_t b = __float_as_uint(x);
     if (x != x) return __uint_as_float(b | 0x00400000u);
     if (x == 0.0f) return __uint_as_float((b & 0x80000000u) | 0x7F800000u);

@@ -115,6 +115,7 @@ struct alignas(16) DScene {
     const float* voxel_light;  // voxel_n^3
     const DNodeInfo* node_info;
     const DMeshEntry* mesh_entries;
+    const float4* voxel_sh4;   // baked GI: voxel_n^3 x 4 (r, g, b, w), or null (constant SH form)
     uint32_t tex_cubemap, tex_specular, tex_brdf_lut, voxel_n;
     float voxel_min[3];
     float voxel_size_f[3];     // (max - min) / n per axis

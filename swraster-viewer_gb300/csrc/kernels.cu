@@ -1525,8 +1525,37 @@ __device__ void voxel_gi(const DScene& sc, f3 pos, f3 sh[4], float& w0, float& w
     const uint32_t x1 = min(x0 + 1u, n - 1u), y1 = min(y0 + 1u, n - 1u), z1 = min(z0 + 1u, n - 1u);
     const float fx = vx - x0f, fy = vy - y0f, fz = vz - z0f;
     const float ofx = 1.0f - fx, ofy = 1.0f - fy, ofz = 1.0f - fz;
-    const float* L = sc.voxel_light;
     const uint32_t nn = n * n;
+    if (sc.voxel_sh4) {
+        // Baked grid: every coefficient's rgb and w trilinear.
+        const float4* G = sc.voxel_sh4;
+        const uint32_t c000 = z0 * nn + y0 * n + x0, c001 = z1 * nn + y0 * n + x0;
+        const uint32_t c010 = z0 * nn + y1 * n + x0, c011 = z1 * nn + y1 * n + x0;
+        const uint32_t c100 = z0 * nn + y0 * n + x1, c101 = z1 * nn + y0 * n + x1;
+        const uint32_t c110 = z0 * nn + y1 * n + x1, c111 = z1 * nn + y1 * n + x1;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const float4 a000 = __ldg(G + (size_t)c000 * 4 + c), a001 = __ldg(G + (size_t)c001 * 4 + c);
+            const float4 a010 = __ldg(G + (size_t)c010 * 4 + c), a011 = __ldg(G + (size_t)c011 * 4 + c);
+            const float4 a100 = __ldg(G + (size_t)c100 * 4 + c), a101 = __ldg(G + (size_t)c101 * 4 + c);
+            const float4 a110 = __ldg(G + (size_t)c110 * 4 + c), a111 = __ldg(G + (size_t)c111 * 4 + c);
+            auto tri = [&](float v000, float v001, float v010, float v011, float v100, float v101, float v110,
+                           float v111) {
+                const float v00 = v000 * ofx + v100 * fx, v01 = v001 * ofx + v101 * fx;
+                const float v10 = v010 * ofx + v110 * fx, v11 = v011 * ofx + v111 * fx;
+                const float v0 = v00 * ofy + v10 * fy, v1 = v01 * ofy + v11 * fy;
+                return v0 * ofz + v1 * fz;
+            };
+            sh[c] = mk3(tri(a000.x, a001.x, a010.x, a011.x, a100.x, a101.x, a110.x, a111.x),
+                        tri(a000.y, a001.y, a010.y, a011.y, a100.y, a101.y, a110.y, a111.y),
+                        tri(a000.z, a001.z, a010.z, a011.z, a100.z, a101.z, a110.z, a111.z));
+            const float w = tri(a000.w, a001.w, a010.w, a011.w, a100.w, a101.w, a110.w, a111.w);
+            if (c == 0) w0 = w;
+            if (c == 1) w1 = w;
+        }
+        return;
+    }
+    const float* L = sc.voxel_light;
     const float w000 = __ldg(L + z0 * nn + y0 * n + x0), w001 = __ldg(L + z1 * nn + y0 * n + x0);
     const float w010 = __ldg(L + z0 * nn + y1 * n + x0), w011 = __ldg(L + z1 * nn + y1 * n + x0);
     const float w100 = __ldg(L + z0 * nn + y0 * n + x1), w101 = __ldg(L + z1 * nn + y0 * n + x1);

@@ -29,4 +29,57 @@ swr_status sun_visibility_device(const LightTri* tris, size_t ntris, const uint8
                                  const float bounds_min[3], const float bounds_max[3], const float cmin[3],
                                  const float vsz[3], const float ld[3], float bias, float* out, std::string& err);
 
+// --- Voxel GI bake (bake_voxel_gi, src/gi.rs:316-408) --------------------
+// RayTracer triangle with what a bounce needs (src/raytracer.rs:35-45).
+struct BakeTri {
+    float p0[3], p1[3], p2[3], n[3];
+    float uv0[2], uv1[2], uv2[2];
+    uint32_t material;
+};
+// BVH node over BakeTri indices (leaves: triangles order[left .. left+count)).
+struct BakeNode {
+    float mn[3], mx[3];
+    uint32_t left, count;
+};
+struct BakeMaterial {
+    float base[3], emissive[3];
+    int32_t base_tex, emissive_tex;  // into BakeInput.textures, -1 none
+    uint32_t base_wrap_s, base_wrap_t, emissive_wrap_s, emissive_wrap_t;
+    uint32_t translucent;
+    float transmission;
+};
+struct BakeTexture {
+    uint32_t offset, width, height;  // mip 0 in the texel pool
+};
+struct BakeInput {
+    const BakeTri* tris = nullptr;
+    size_t ntris = 0;
+    const BakeNode* nodes = nullptr;
+    size_t nnodes = 0;
+    const uint32_t* order = nullptr;
+    const BakeMaterial* mats = nullptr;
+    uint32_t nmat = 0;
+    const uint32_t* texels = nullptr;  // RGBA8, R in the MSB
+    size_t ntexels = 0;
+    const BakeTexture* textures = nullptr;
+    uint32_t ntex = 0;
+    const uint32_t* cubemap = nullptr;  // mip 0, six faces
+    uint32_t cube_size = 0;
+    const float* sky_lut = nullptr;     // srgb_to_linear_scalar(b / 255) for every byte b
+    const float* dirs = nullptr;        // direction sets, 9 x 64 x 3
+    float irradiance_sh[4][3] = {};
+    float light_dir[3] = {}, light_color[3] = {};
+    uint32_t n = 0;
+    float bounds_min[3] = {}, vsz[3] = {}, cmin[3] = {};
+    const uint8_t* active = nullptr;    // n^3
+    const float* sun = nullptr;         // n^3, blurred sun visibility
+};
+constexpr uint32_t kGiSamples = 64, kGiSets = 9;
+
+// bake_voxel_gi + blur_gi_sh4 on the device: `out` gets n^3 voxels of four
+// (r, g, b, w) SH4 coefficients. Surface textures are sampled bilinearly and
+// converted to linear with the device's powf, so results equal the host
+// restatement up to its last-bit differences from the host's powf.
+swr_status gi_bake_device(const BakeInput& in, float* out, std::string& err);
+
 }  // namespace swr

@@ -624,6 +624,152 @@ float trace_transmittance(const Bvh& b, const std::vector<RtTri>& tris, const st
     return tr;
 }
 
+// build_uniform_sphere_samples (src/gi.rs:416-434) for every direction set
+// of bake_voxel_gi: Hammersley points with a Cranley-Patterson rotation per
+// set, mapped to the unit sphere.
+std::vector<float> gi_direction_sets() {
+    std::vector<float> d;
+    d.reserve((size_t)kGiSets * kGiSamples * 3);
+    const float pi = 3.14159265358979323846f;
+    for (uint32_t set = 0; set < kGiSets; ++set) {
+        const float ox = radical_inverse_vdc(set + 1), oy = ((float)set + 0.5f) / (float)kGiSets;
+        for (uint32_t i = 0; i < kGiSamples; ++i) {
+            float hx, hy;
+            hammersley(i, kGiSamples, hx, hy);
+            float xx = hx + ox, xy = hy + oy;
+            xx = xx - std::trunc(xx);  // f32::fract
+            xy = xy - std::trunc(xy);
+            const float z = 1.0f - 2.0f * xx;
+            const float r = std::sqrt(std::fmax(1.0f - z * z, 0.0f));
+            const float phi = 2.0f * pi * xy;
+            const V3 v = normalize3({r * std::cos(phi), r * std::sin(phi), z});
+            d.push_back(v.x);
+            d.push_back(v.y);
+            d.push_back(v.z);
+        }
+    }
+    return d;
+}
+
+// The voxel GI bake's inputs (the ray tracer's triangles with normals and
+// texture coordinates, its BVH, materials, mip-0 textures, the sky) and the
+// device bake; s->voxel_sh4 receives the blurred SH4 grid.
+swr_status bake_gi(SceneImpl* s, const std::vector<RtTri>& rt, const std::vector<uint8_t>& active, uint32_t n,
+                   V3 bmn, V3 vsz, std::string& err) {
+    std::vector<BakeTri> bt;
+    bt.reserve(rt.size());
+    for (const HNode& nd : s->nodes) {
+        if (nd.mesh < 0) continue;
+        for (uint32_t gp : s->meshes[nd.mesh].prims) {
+            const HPrimitive& p = s->prims[gp];
+            for (size_t t = 0; t + 2 < p.idx.size(); t += 3) {
+                V3 pp[3];
+                for (int k = 0; k < 3; ++k) {
+                    const float* q = &p.pos4[4 * (size_t)p.idx[t + k]];
+                    const V4 w = mulmv(nd.transform, {q[0], q[1], q[2], q[3]});
+                    pp[k] = {w.x, w.y, w.z};
+                }
+                const V3 fn = cross3(sub(pp[1], pp[0]), sub(pp[2], pp[0]));
+                if (dot3(fn, fn) <= 1.0e-12f) continue;
+                const V3 nn = normalize3(fn);
+                BakeTri b{};
+                const V3* P[3] = {&pp[0], &pp[1], &pp[2]};
+                float* dst[3] = {b.p0, b.p1, b.p2};
+                float* uv[3] = {b.uv0, b.uv1, b.uv2};
+                for (int k = 0; k < 3; ++k) {
+                    dst[k][0] = P[k]->x;
+                    dst[k][1] = P[k]->y;
+                    dst[k][2] = P[k]->z;
+                    uv[k][0] = p.uv2[2 * (size_t)p.idx[t + k]];
+                    uv[k][1] = p.uv2[2 * (size_t)p.idx[t + k] + 1];
+                }
+                b.n[0] = nn.x;
+                b.n[1] = nn.y;
+                b.n[2] = nn.z;
+                b.material = p.material;
+                bt.push_back(b);
+            }
+        }
+    }
+    Bvh bvh;
+    if (!rt.empty()) bvh_build(rt, bvh);
+    std::vector<BakeNode> nodes(bvh.nodes.size());
+    for (size_t i = 0; i < nodes.size(); ++i) {
+        for (int k = 0; k < 3; ++k) {
+            nodes[i].mn[k] = bvh.nodes[i].mn[k];
+            nodes[i].mx[k] = bvh.nodes[i].mx[k];
+        }
+        nodes[i].left = bvh.nodes[i].left;
+        nodes[i].count = bvh.nodes[i].count;
+    }
+    // Mip 0 of every scene texture in one pool.
+    std::vector<uint32_t> texels;
+    std::vector<BakeTexture> texs;
+    for (const HTexture& t : s->textures) {
+        texs.push_back({(uint32_t)texels.size(), t.width, t.height});
+        texels.insert(texels.end(), t.data.begin(), t.data.begin() + (size_t)t.width * t.height);
+    }
+    std::vector<BakeMaterial> mats;
+    for (const swr_material_view& m : s->materials) {
+        BakeMaterial b{};
+        for (int k = 0; k < 3; ++k) {
+            b.base[k] = m.base_color_factor[k];
+            b.emissive[k] = m.emissive_factor[k];
+        }
+        b.base_tex = m.tex[0];
+        b.emissive_tex = m.tex[3];
+        b.base_wrap_s = m.wrap_s[0];
+        b.base_wrap_t = m.wrap_t[0];
+        b.emissive_wrap_s = m.wrap_s[3];
+        b.emissive_wrap_t = m.wrap_t[3];
+        b.translucent = m.is_translucent;
+        b.transmission = m.transmission;
+        mats.push_back(b);
+    }
+    std::vector<float> lut(256);
+    for (int i = 0; i < 256; ++i) lut[i] = srgb_to_linear_scalar((float)i / 255.0f);
+    const std::vector<float> dirs = gi_direction_sets();
+    BakeInput in;
+    in.tris = bt.data();
+    in.ntris = bt.size();
+    in.nodes = nodes.data();
+    in.nnodes = nodes.size();
+    in.order = bvh.order.data();
+    in.mats = mats.data();
+    in.nmat = (uint32_t)mats.size();
+    in.texels = texels.data();
+    in.ntexels = texels.size();
+    in.textures = texs.data();
+    in.ntex = (uint32_t)texs.size();
+    in.cubemap = s->cubemap.data.data();
+    in.cube_size = s->cubemap.width;
+    in.sky_lut = lut.data();
+    in.dirs = dirs.data();
+    for (int i = 0; i < 4; ++i)
+        for (int c = 0; c < 3; ++c) in.irradiance_sh[i][c] = s->irradiance_sh[i][c];
+    const V3 ld = normalize3(s->light_dir);
+    const V3 cmin = add(bmn, mul(vsz, 0.5f));
+    const float l3[3] = {ld.x, ld.y, ld.z}, lc[3] = {s->light_color.x, s->light_color.y, s->light_color.z};
+    for (int k = 0; k < 3; ++k) {
+        in.light_dir[k] = l3[k];
+        in.light_color[k] = lc[k];
+    }
+    in.n = n;
+    in.bounds_min[0] = bmn.x;
+    in.bounds_min[1] = bmn.y;
+    in.bounds_min[2] = bmn.z;
+    in.vsz[0] = vsz.x;
+    in.vsz[1] = vsz.y;
+    in.vsz[2] = vsz.z;
+    in.cmin[0] = cmin.x;
+    in.cmin[1] = cmin.y;
+    in.cmin[2] = cmin.z;
+    in.active = active.data();
+    in.sun = s->voxel_light.data();
+    s->voxel_sh4.assign((size_t)n * n * n * 16, 0.0f);
+    return gi_bake_device(in, s->voxel_sh4.data(), err);
+}
+
 }  // namespace
 
 swr_status build_scene(const swr_scene_desc* desc, SceneImpl* s, std::string& err) {
@@ -926,6 +1072,15 @@ swr_status build_scene(const swr_scene_desc* desc, SceneImpl* s, std::string& er
             s->voxel_light = std::move(blurred);
         }
     }
+    // bake_voxel_gi (src/gi.rs:316-408) with the reference's --gi.
+    if (desc->flags & SWR_SCENE_GI) {
+        if (desc->flags & SWR_SCENE_HOST_ONLY) {
+            err = "the GI bake runs on the device: SWR_SCENE_GI cannot be combined with SWR_SCENE_HOST_ONLY";
+            return SWR_INVALID_ARG;
+        }
+        const swr_status gst = bake_gi(s, rt, active, n, bmn, vsz, err);
+        if (gst != SWR_OK) return gst;
+    }
     // initialize_voxel_gi_from_scene (src/gi.rs:123-149).
     for (int i = 0; i < 4; ++i) {
         for (int c = 0; c < 3; ++c) s->gi_const[i][c] = s->irradiance_sh[i][c] * s->gi_sh_scale;
@@ -1000,6 +1155,7 @@ void export_scene(const SceneImpl* s, swr_scene_host_view* o) {
     o->voxel_world_max[1] = s->voxel_max.y;
     o->voxel_world_max[2] = s->voxel_max.z;
     o->voxel_light_intensity = s->voxel_light.data();
+    o->voxel_gi_sh4 = s->voxel_sh4.empty() ? nullptr : s->voxel_sh4.data();
     for (int i = 0; i < 4; ++i)
         for (int c = 0; c < 4; ++c) o->voxel_gi_sh4_const[i][c] = s->gi_const[i][c];
 }
@@ -1137,6 +1293,7 @@ swr_status upload_scene(SceneImpl* s, std::string& err, bool to_device) {
     all_tex.push_back(&s->brdf_lut);
     for (const HTexture* t : all_tex) o_tex.push_back(ar.add(t->data.data(), t->data.size() * sizeof(uint32_t)));
     const uint64_t o_vox = ar.add(s->voxel_light.data(), s->voxel_light.size() * sizeof(float));
+    const uint64_t o_sh4 = ar.add(s->voxel_sh4.data(), s->voxel_sh4.size() * sizeof(float));
     const uint64_t o_dtex = ar.add(nullptr, all_tex.size() * sizeof(DTexture));
     const uint64_t o_dscene = ar.add(nullptr, sizeof(DScene));
     void* dblock = nullptr;
@@ -1164,6 +1321,7 @@ swr_status upload_scene(SceneImpl* s, std::string& err, bool to_device) {
     ds.materials = reinterpret_cast<const DMaterial*>(at(o_mat));
     ds.textures = reinterpret_cast<const DTexture*>(at(o_dtex));
     ds.voxel_light = reinterpret_cast<const float*>(at(o_vox));
+    ds.voxel_sh4 = s->voxel_sh4.empty() ? nullptr : reinterpret_cast<const float4*>(at(o_sh4));
     ds.node_info = reinterpret_cast<const DNodeInfo*>(at(o_ninfo));
     ds.mesh_entries = reinterpret_cast<const DMeshEntry*>(at(o_entries));
     ds.tex_cubemap = (uint32_t)s->textures.size();

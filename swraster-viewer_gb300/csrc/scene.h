@@ -59,6 +59,7 @@ struct SceneImpl {
     uint32_t voxel_n = 0;
     V3 voxel_min{}, voxel_max{};
     std::vector<float> voxel_light;
+    std::vector<float> voxel_sh4;  // SWR_SCENE_GI: n^3 x 4 (r, g, b, w), blurred; empty otherwise
     float gi_sh_scale = 0.25f, sky_visibility = 1.0f;
     float gi_const[4][4] = {};
     uint64_t tri_total = 0, vtx_total = 0;

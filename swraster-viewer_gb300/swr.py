@@ -18,6 +18,7 @@ TEX_SRGB, TEX_NORMAL, TEX_METALLIC_ROUGHNESS, TEX_CUBEMAP, TEX_LINEAR = 0, 1, 2,
 WRAP_REPEAT, WRAP_MIRRORED_REPEAT, WRAP_CLAMP_TO_EDGE = 0, 1, 2
 RSQRT_IEEE, RSQRT_AARCH64 = 0, 1
 SCENE_HOST_ONLY = 1
+SCENE_GI = 2
 
 u32p = C.POINTER(C.c_uint32)
 f32p = C.POINTER(C.c_float)
@@ -116,7 +117,7 @@ class SceneHostView(C.Structure):
                 ("brdf_lut", TextureView), ("irradiance_sh", (C.c_float * 3) * 4), ("light_direction", C.c_float * 3),
                 ("light_color", C.c_float * 3), ("voxel_world_min", C.c_float * 3),
                 ("voxel_world_max", C.c_float * 3), ("voxel_light_intensity", f32p),
-                ("voxel_gi_sh4_const", (C.c_float * 4) * 4)]
+                ("voxel_gi_sh4_const", (C.c_float * 4) * 4), ("voxel_gi_sh4", f32p)]
 
 
 class Camera(C.Structure):
@@ -273,7 +274,7 @@ def texref(index=-1, wrap_s=WRAP_REPEAT, wrap_t=WRAP_REPEAT):
 class Scene:
     """Owns a swr_scene built from a scene dict (see scenes.py)."""
 
-    def __init__(self, sd, host_only=False, host_threads=0):
+    def __init__(self, sd, host_only=False, host_threads=0, gi=False):
         self._keep = []
         keep = self._keep
         meshes = (MeshDesc * len(sd["meshes"]))()
@@ -301,7 +302,7 @@ class Scene:
             md.base_color_factor = (C.c_float * 4)(*m.get("base_color_factor", (1, 1, 1, 1)))
             md.metallic_factor = m.get("metallic", 1.0)
             md.roughness_factor = m.get("roughness", 1.0)
-            md.emissive_factor = (C.c_float * 3)(*m.get("emissive", (0, 0, 0)))
+            md.emissive_factor = (C.c_float * 3)(*m.get("emissive_factor", (0, 0, 0)))
             md.occlusion_strength = m.get("occlusion_strength", 1.0)
             md.alpha_cutoff = m.get("alpha_cutoff", 0.5)
             md.transmission = m.get("transmission", 0.0)
@@ -336,7 +337,7 @@ class Scene:
         desc.gi_sh_scale = sd.get("gi_sh_scale", 0.25)
         desc.sky_visibility = sd.get("sky_visibility", 1.0)
         desc.host_threads = host_threads
-        desc.flags = SCENE_HOST_ONLY if host_only else 0
+        desc.flags = (SCENE_HOST_ONLY if host_only else 0) | (SCENE_GI if gi else 0)
         h = C.c_void_p()
         check(lib().swr_scene_create(C.byref(desc), C.byref(h)))
         self.handle = h
@@ -344,7 +345,7 @@ class Scene:
 
     @classmethod
     def load_gltf(cls, path, cubemap_faces=None, cubemap_face_size=0, cubemap_path=None, voxel_grid_size=0,
-                  specular_samples=0, brdf_lut_size=0, host_only=False, host_threads=0):
+                  specular_samples=0, brdf_lut_size=0, host_only=False, host_threads=0, gi=False):
         """swr_scene_load_gltf: a .gltf/.glb file; the cubemap as raw faces or a cross image path."""
         o = GltfOpts()
         faces = None
@@ -358,7 +359,7 @@ class Scene:
         o.specular_samples = specular_samples
         o.brdf_lut_size = brdf_lut_size
         o.host_threads = host_threads
-        o.flags = SCENE_HOST_ONLY if host_only else 0
+        o.flags = (SCENE_HOST_ONLY if host_only else 0) | (SCENE_GI if gi else 0)
         h = C.c_void_p()
         check(lib().swr_scene_load_gltf(os.fsencode(path), C.byref(o), C.byref(h)))
         self = cls.__new__(cls)

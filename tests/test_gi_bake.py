@@ -1,0 +1,64 @@
+"""Voxel GI bake (the reference's --gi: bake_voxel_gi + blur_gi_sh4,
+src/gi.rs:316-408, src/voxelgrid.rs:422-472) on the device against the
+oracle's brute-force restatement, and frames shaded with the baked SH4 grid
+against the oracle. The bake samples surface textures bilinearly and converts
+them to linear with powf, which the device and the host's libm round
+differently in the last bit, so the grids are compared with a tolerance
+(2e-6 relative to the grid's largest value); frames shaded from the same
+grid are held to the usual bar (visibility bit-exact, colour within 1/255)."""
+import numpy as np
+import pytest
+
+import oracle
+import scenes
+import swr
+from test_gpu_parity import compare
+
+RTOL = 2e-6
+
+
+def gi_scene(kind, voxel=12):
+    if kind == "spheres":
+        sd = scenes.spheres_scene(seed=31, count=6, subdiv=2, box=4.0, radius=(0.6, 1.8), tex_size=32, cube_size=16,
+                                  voxel=voxel, specular_samples=8, brdf_lut_size=32)
+        # An emissive sphere: the bounce adds emissive radiance.
+        sd["materials"][2]["emissive_factor"] = (0.8, 0.5, 0.2)
+        return sd
+    sd = scenes.translucent_scene(count=6, tex_size=32, cube_size=16, voxel=voxel)
+    return sd
+
+
+def baked(scene):
+    v = scene.export()
+    n = v.voxel_size
+    assert bool(v.voxel_gi_sh4)
+    return np.ctypeslib.as_array(v.voxel_gi_sh4, shape=(n * n * n, 4, 4)).copy(), v
+
+
+def test_gi_requires_device():
+    with pytest.raises(swr.SwrError):
+        swr.Scene(gi_scene("spheres"), host_only=True, gi=True)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["spheres", "translucent"])
+def test_bake_matches_oracle(kind):
+    s = swr.Scene(gi_scene(kind), gi=True)
+    grid, v = baked(s)
+    ref = oracle.gi_bake(v, threads=16)
+    scale = float(np.abs(ref).max())
+    d = np.abs(grid - ref)
+    print("max abs %.3g (%.3g of max), exact %.4f" % (d.max(), d.max() / scale, (d == 0).mean()))
+    assert d.max() <= RTOL * scale
+    # Sky visibility (coefficient 1's w) counts escaped rays: exact.
+    np.testing.assert_array_equal(grid[:, 1, 3], ref[:, 1, 3])
+    s.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["spheres", "translucent"])
+def test_frames_with_baked_grid_match_oracle(kind):
+    s = swr.Scene(gi_scene(kind, voxel=16), gi=True)
+    cam = swr.make_camera(*scenes.default_camera_params(s.info(), 256, 160))
+    compare(s, cam, 256, 160)
+    s.close()
