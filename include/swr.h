@@ -480,8 +480,10 @@ swr_status swr_batch_render(swr_batch* b, const swr_view_desc* views, int32_t n,
  * overflowed. */
 swr_status swr_batch_sync(swr_batch* b);
 swr_status swr_batch_output(swr_batch* b, int32_t view, const uint32_t** rgba8, const uint64_t** vis);
-/* Times every scheduling tile size on these views and keeps the fastest for
- * the batch's class (pixel count, triangle count, view count). */
+/* Times every scheduling tile size (and, for 32-px tiles, shading fused
+ * into the raster kernel or run after it; 8- and 16-px tiles always fuse,
+ * 64-px tiles never) on these views and keeps the fastest for the batch's
+ * class (pixel count, triangle count, view count). */
 swr_status swr_batch_autotune(swr_batch* b, const swr_view_desc* views, int32_t n, void* stream,
                               uint32_t* best_tile, float* best_ms);
 /* Milliseconds of the last synced batch on the device (CUDA events). */

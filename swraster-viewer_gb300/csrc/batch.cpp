@@ -127,8 +127,10 @@ swr_status BatchImpl::sync(std::string& err) {
 swr_status BatchImpl::render(const swr_view_desc* vd, int32_t n, cudaStream_t stream, std::string& err) {
     swr_status st = sync(err);
     if (st != SWR_OK) return st;
-    const uint32_t want = opts.sched_tile ? opts.sched_tile : tuned_tile(vd, n);
-    eng.sched_tile = want;
+    // Tuned choices carry "32-px tiles shade inside the raster kernel" in bit 8.
+    const uint32_t want = opts.sched_tile ? opts.sched_tile | (opt_fuse32 ? 0x100u : 0u) : tuned_tile(vd, n);
+    eng.sched_tile = want & 0xFFu;
+    eng.fuse32 = (want & 0x100u) != 0u;
     saved.assign(vd, vd + n);
     saved_cams.resize((size_t)n);
     for (int32_t i = 0; i < n; ++i) saved_cams[i] = *vd[i].camera;
@@ -317,14 +319,17 @@ swr_status swr_batch_autotune(swr_batch* b, const swr_view_desc* views, int32_t 
     const swr_batch_opts keep = B.opts;
     uint32_t best = 64;
     float bms = 1e30f;
-    for (uint32_t S : {64u, 32u, 16u, 8u}) {
-        B.opts.sched_tile = S;
+    // Scheduling tiles, and 32-px tiles with the shading fused into the raster.
+    for (uint32_t code : {64u, 32u, 32u | 0x100u, 16u, 8u}) {
+        B.opts.sched_tile = code & 0xFFu;
+        B.opt_fuse32 = (code & 0x100u) != 0u;
         float total = 0.0f;
         for (int rep = 0; rep < 4; ++rep) {
             swr_status st = B.render(views, n, (cudaStream_t)stream, err);
             if (st == SWR_OK) st = B.sync(err);
             if (st != SWR_OK) {
                 B.opts = keep;
+                B.opt_fuse32 = false;
                 set_last_error(err.c_str());
                 return st;
             }
@@ -334,12 +339,13 @@ swr_status swr_batch_autotune(swr_batch* b, const swr_view_desc* views, int32_t 
         }
         if (total < bms) {
             bms = total;
-            best = S;
+            best = code;
         }
     }
     B.opts = keep;
+    B.opt_fuse32 = false;
     B.tuned[batch_class(views, n)] = best;
-    if (best_tile) *best_tile = best;
+    if (best_tile) *best_tile = best & 0xFFu;
     if (best_ms) *best_ms = bms / 3.0f;
     return SWR_OK;
 }

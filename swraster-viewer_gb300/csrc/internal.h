@@ -301,6 +301,7 @@ struct FrameArgs {
     uint4* slot_blocks;        // per 256 node slots: draws, triangles, chunks; then their exclusive offsets
     uint32_t draw_cap;
     uint32_t slot_cap;
+    uint32_t fused_shade;      // 32-px tiles: shade inside the raster kernel (8 and 16 px always do)
     uint32_t gpu_draws;        // build draws and chunks on the device (else the host staged them)
 };
 
@@ -314,6 +315,8 @@ cudaError_t launch_rsqrt_selftest(const float* in, float* out, uint64_t n, uint3
 // Per-device constant tables; call once per device outside stream capture.
 cudaError_t init_kernel_constants();
 // Persistent raster / grid-stride shading grid sizes for this device.
-void frame_grids(int num_sms, uint32_t sched_tile, uint32_t* raster_grid, uint32_t* shade_grid);
+void frame_grids(int num_sms, uint32_t sched_tile, bool fuse32, uint32_t* raster_grid, uint32_t* shade_grid);
+// Whether frames with this scheduling tile shade inside the raster kernel.
+bool shade_fused(uint32_t sched_tile, bool fuse32);
 
 }  // namespace swr

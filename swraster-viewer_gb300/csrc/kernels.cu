@@ -42,6 +42,15 @@
 #define SWR_RASTER_PERSISTENT 1
 #endif
 // Raster: prefetch into L2 the record each thread will likely load in the next round.
+// Shading fused into the raster kernel (k_raster<S, true>): each CTA shades
+// its tile from the depth keys in shared memory right after rasterizing it,
+// so raster and shading work of different tiles share the SMs and keys reach
+// HBM only for the translucent pass. Always for tiles of 8 and 16 px, on
+// request (FrameArgs.fused_shade, chosen by the batch autotuner) for 32;
+// 64-px tiles keep the separate shading kernel (fused, a 4K frame was 18%
+// slower: the two code bodies share the instruction cache and the shading
+// part spills).
+constexpr uint32_t kFusedShadeMaxTile = 16;
 #ifndef SWR_RASTER_PREFETCH
 #define SWR_RASTER_PREFETCH 1
 #endif
@@ -1171,6 +1180,7 @@ struct RasterShared {
     uint32_t p_seq8[kThreads], p_mat[kThreads], p_amip[kThreads], p_slot[kThreads];
     uint32_t scan[kThreads / 32][2];
     uint32_t n_regions, n_quads, n_slow, cur_tile;
+    uint8_t tab[512];           // FRSQRTE table for the fused shading
 };
 
 constexpr uint32_t kSlowRegion = 0x8000u;  // region replays the sequential additions
@@ -1333,12 +1343,17 @@ __device__ __forceinline__ void packet_regions(RasterShared<S>& s, const PacketC
         }
 }
 
+__device__ __forceinline__ bool shade_needed(const DView& v, int32_t qx, int32_t qy);
+__device__ __forceinline__ void shade_pixel(const FrameArgs& a, const uint8_t* tab, const DView& v,
+                                            const DScene& sc, int32_t qx, int32_t qy, int32_t k, bool needed,
+                                            unsigned long long key);
+
 // Persistent: each CTA pulls (view, scheduling tile) work items from a
 // device-side counter until every tile of every view is done. Per tile, the
 // bin's packets go through rounds of one packet per thread: pass 1 stages
 // regions (a block-wide scan places them), pass 2 rasterizes the exact
 // regions' quads flattened over all lanes, pass 3 the sequential regions.
-template <int S>
+template <int S, bool FUSE>
 __global__ void __launch_bounds__(RasterShared<S>::kThreads, RasterShared<S>::kMinBlocks) k_raster(FrameArgs a) {
     using Sh = RasterShared<S>;
     constexpr int NT = Sh::kThreads, R = Sh::kRegions, NW = NT / 32;
@@ -1346,6 +1361,9 @@ __global__ void __launch_bounds__(RasterShared<S>::kThreads, RasterShared<S>::kM
     Sh& s = *reinterpret_cast<Sh*>(raster_smem);
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t n_tiles = a.dyn->n_stiles;
+    constexpr bool kFuse = FUSE;
+    if (kFuse)
+        for (int i = threadIdx.x; i < 512; i += NT) s.tab[i] = a.rsqrt_table[i];
     for (uint32_t iter = 0;; ++iter) {
 #if SWR_RASTER_PERSISTENT
         if (threadIdx.x == 0) {
@@ -1473,9 +1491,27 @@ __global__ void __launch_bounds__(RasterShared<S>::kThreads, RasterShared<S>::kM
             __syncthreads();
         }
         unsigned long long* dst = a.keys + view.key_offset;
-        for (int i = threadIdx.x; i < S * S; i += NT) {
-            const int32_t ly = i / S, lx = i % S;
-            dst[(uint64_t)(sy0 + ly) * view.key_pitch + (uint64_t)(sx0 + lx)] = s.sk[i];
+        // Fused: keys go to HBM only for the translucent pass; the tile is
+        // shaded from shared memory, 4 lanes per quad, quads row by row.
+        if (!kFuse || (view.flags & kViewTranslucent))
+            for (int i = threadIdx.x; i < S * S; i += NT) {
+                const int32_t ly = i / S, lx = i % S;
+                dst[(uint64_t)(sy0 + ly) * view.key_pitch + (uint64_t)(sx0 + lx)] = s.sk[i];
+            }
+        constexpr int QS = S / 2;
+        // Lanes read keys other threads initialised or wrote: a tile without
+        // packets has had no barrier since the keys were reset.
+        if (kFuse) __syncthreads();
+        for (int base = 0; kFuse && base < S * S; base += NT) {
+            const int t = base + (int)threadIdx.x;
+            const bool live = t < S * S;
+            const int ql = live ? (t >> 2) : 0;
+            const int32_t k = t & 3;
+            const int32_t qx = (sx0 >> 1) + ql % QS, qy = (sy0 >> 1) + ql / QS;
+            const bool needed = live && shade_needed(view, qx, qy);
+            unsigned long long key = kEmptyKey;
+            if (needed) key = s.sk[(2 * (ql / QS) + (k >> 1)) * S + 2 * (ql % QS) + (k & 1)];
+            shade_pixel(a, s.tab, view, sc, qx, qy, k, needed, key);
         }
         __syncthreads();
     }
@@ -1730,23 +1766,22 @@ __device__ __forceinline__ uint32_t tonemap_pack(f3 c, float exposure) {
 
 // One lane of the shading pass; all 32 lanes of a warp call it together
 // (quad barycentrics and luminance are exchanged with warp shuffles).
-__device__ __forceinline__ void shade_thread(const FrameArgs& a, const uint8_t* tab, uint32_t gt, uint32_t total) {
-    const uint32_t gq = gt >> 2;
+// Whether pixel lane k of quad (qx, qy) of view v is shaded: inside the
+// view, or in the centre quad of a reference tile (the luminance meter).
+__device__ __forceinline__ bool shade_needed(const DView& v, int32_t qx, int32_t qy) {
+    const bool centre = ((qx & 31) == 0) && ((qy & 31) == 16);
+    return (2 * qx < v.width && 2 * qy < v.height) || centre;
+}
+
+// Shades lane k of quad (qx, qy) of view v given the pixel's depth key; all
+// 32 lanes of a warp call it together, 4 consecutive lanes per quad.
+__device__ __forceinline__ void shade_pixel(const FrameArgs& a, const uint8_t* tab, const DView& v,
+                                            const DScene& sc, int32_t qx, int32_t qy, int32_t k, bool needed,
+                                            unsigned long long key) {
     const uint32_t lane = threadIdx.x & 31u;
-    const bool live = gq < total;
-    const uint32_t vi = find_view_by_quad(a, live ? gq : 0u);
-    const DView& v = a.views[vi];
-    const DScene& sc = a.scenes[v.scene];
-    const uint32_t lq = gq - v.quad_base;
-    const int32_t qx = (int32_t)(lq % v.quad_pitch), qy = (int32_t)(lq / v.quad_pitch);
-    const int32_t k = (int32_t)(gt & 3u), kx = k & 1, ky = k >> 1;
+    const int32_t kx = k & 1, ky = k >> 1;
     const int32_t px = 2 * qx + kx, py = 2 * qy + ky;
     const bool centre = ((qx & 31) == 0) && ((qy & 31) == 16);
-    const bool needed = live && ((2 * qx < v.width && 2 * qy < v.height) || centre);
-
-    // Winner of this lane.
-    unsigned long long key = kEmptyKey;
-    if (needed) key = a.keys[v.key_offset + (uint64_t)py * v.key_pitch + (uint64_t)px];
     const bool writer = key != kEmptyKey;
     const float z = ordered_to_float((uint32_t)(key >> 32));
     const bool covered = writer && !(z == __int_as_float(0x7F800000));
@@ -1826,6 +1861,22 @@ __device__ __forceinline__ void shade_thread(const FrameArgs& a, const uint8_t* 
         v.rgba8[(uint64_t)py * v.out_pitch + (uint64_t)px] = c;
         if (v.rgba8_host) v.rgba8_host[(uint64_t)py * v.host_pitch + (uint64_t)px] = c;
     }
+}
+
+// One lane of the shading pass over the padded quad grid of every view.
+__device__ __forceinline__ void shade_thread(const FrameArgs& a, const uint8_t* tab, uint32_t gt, uint32_t total) {
+    const uint32_t gq = gt >> 2;
+    const bool live = gq < total;
+    const uint32_t vi = find_view_by_quad(a, live ? gq : 0u);
+    const DView& v = a.views[vi];
+    const uint32_t lq = gq - v.quad_base;
+    const int32_t qx = (int32_t)(lq % v.quad_pitch), qy = (int32_t)(lq / v.quad_pitch);
+    const int32_t k = (int32_t)(gt & 3u);
+    const bool needed = live && shade_needed(v, qx, qy);
+    unsigned long long key = kEmptyKey;
+    if (needed)
+        key = a.keys[v.key_offset + (uint64_t)(2 * qy + (k >> 1)) * v.key_pitch + (uint64_t)(2 * qx + (k & 1))];
+    shade_pixel(a, tab, v, a.scenes[v.scene], qx, qy, k, needed, key);
 }
 
 // Three CTAs per SM (<= 85 registers): 4K frame shade 0.652 ms, against
@@ -2055,9 +2106,9 @@ __global__ void k_resolve(FrameArgs a) {
 // --------------------------------------------------------------------------
 static uint64_t g_const_init_mask = 0;  // one bit per device
 
-template <int S>
+template <int S, bool FUSE>
 static cudaError_t raster_smem_attr() {
-    return cudaFuncSetAttribute(k_raster<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    return cudaFuncSetAttribute(k_raster<S, FUSE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)sizeof(RasterShared<S>));
 }
 
@@ -2069,29 +2120,32 @@ cudaError_t init_kernel_constants() {
     float t[256];
     for (int i = 0; i < 256; ++i) t[i] = (float)i / 255.0f;
     e = cudaMemcpyToSymbol(c_unorm8, t, sizeof(t));
-    if (e == cudaSuccess) e = raster_smem_attr<8>();
-    if (e == cudaSuccess) e = raster_smem_attr<16>();
-    if (e == cudaSuccess) e = raster_smem_attr<32>();
-    if (e == cudaSuccess) e = raster_smem_attr<64>();
+    if (e == cudaSuccess) e = raster_smem_attr<8, true>();
+    if (e == cudaSuccess) e = raster_smem_attr<16, true>();
+    if (e == cudaSuccess) e = raster_smem_attr<32, false>();
+    if (e == cudaSuccess) e = raster_smem_attr<32, true>();
+    if (e == cudaSuccess) e = raster_smem_attr<64, false>();
     if (e == cudaSuccess && dev < 64) g_const_init_mask |= 1ull << dev;
     return e;
 }
 
-template <int S>
+template <int S, bool FUSE>
 static int raster_blocks_per_sm() {
     int rb = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rb, k_raster<S>, RasterShared<S>::kThreads,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rb, k_raster<S, FUSE>, RasterShared<S>::kThreads,
                                                   sizeof(RasterShared<S>));
     return rb;
 }
 
-void frame_grids(int num_sms, uint32_t S, uint32_t* raster_grid, uint32_t* shade_grid) {
+bool shade_fused(uint32_t S, bool fuse32) { return S <= kFusedShadeMaxTile || (S == 32 && fuse32); }
+
+void frame_grids(int num_sms, uint32_t S, bool fuse32, uint32_t* raster_grid, uint32_t* shade_grid) {
     int rb = 1, sb = 1;
     switch (S) {
-        case 8: rb = raster_blocks_per_sm<8>(); break;
-        case 16: rb = raster_blocks_per_sm<16>(); break;
-        case 32: rb = raster_blocks_per_sm<32>(); break;
-        default: rb = raster_blocks_per_sm<64>(); break;
+        case 8: rb = raster_blocks_per_sm<8, true>(); break;
+        case 16: rb = raster_blocks_per_sm<16, true>(); break;
+        case 32: rb = fuse32 ? raster_blocks_per_sm<32, true>() : raster_blocks_per_sm<32, false>(); break;
+        default: rb = raster_blocks_per_sm<64, false>(); break;
     }
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sb, k_shade, 256, 0);
     cudaGetLastError();
@@ -2142,13 +2196,19 @@ void launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t* ev
     const uint32_t rg = SWR_RASTER_PERSISTENT ? (a.raster_grid > 0 ? a.raster_grid : (uint32_t)num_sms)
                                               : (a.stile_cap > 0 ? a.stile_cap : 1u);
     switch (a.sched_tile) {
-        case 8: k_raster<8><<<rg, RasterShared<8>::kThreads, sizeof(RasterShared<8>), s>>>(a); break;
-        case 16: k_raster<16><<<rg, RasterShared<16>::kThreads, sizeof(RasterShared<16>), s>>>(a); break;
-        case 32: k_raster<32><<<rg, RasterShared<32>::kThreads, sizeof(RasterShared<32>), s>>>(a); break;
-        default: k_raster<64><<<rg, RasterShared<64>::kThreads, sizeof(RasterShared<64>), s>>>(a); break;
+        case 8: k_raster<8, true><<<rg, RasterShared<8>::kThreads, sizeof(RasterShared<8>), s>>>(a); break;
+        case 16: k_raster<16, true><<<rg, RasterShared<16>::kThreads, sizeof(RasterShared<16>), s>>>(a); break;
+        case 32:
+            if (a.fused_shade)
+                k_raster<32, true><<<rg, RasterShared<32>::kThreads, sizeof(RasterShared<32>), s>>>(a);
+            else
+                k_raster<32, false><<<rg, RasterShared<32>::kThreads, sizeof(RasterShared<32>), s>>>(a);
+            break;
+        default: k_raster<64, false><<<rg, RasterShared<64>::kThreads, sizeof(RasterShared<64>), s>>>(a); break;
     }
     mark(6);
-    k_shade<<<a.shade_grid > 0 ? a.shade_grid : (uint32_t)num_sms, 256, 0, s>>>(a);
+    if (!shade_fused(a.sched_tile, a.fused_shade != 0))
+        k_shade<<<a.shade_grid > 0 ? a.shade_grid : (uint32_t)num_sms, 256, 0, s>>>(a);
     mark(7);
     if (a.has_translucent) {
         const uint32_t tg = (uint32_t)num_sms * 2u;

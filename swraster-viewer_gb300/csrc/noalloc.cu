@@ -158,7 +158,7 @@ extern "C" swr_status swr_render_frame_noalloc(const swr_scene* scene, const swr
         int sms = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         g_dev_sms[dev] = sms > 0 ? sms : 148;
-        frame_grids(g_dev_sms[dev], 64, &g_raster_grid[dev], &g_shade_grid[dev]);
+        frame_grids(g_dev_sms[dev], 64, false, &g_raster_grid[dev], &g_shade_grid[dev]);
         g_dev_ptr[dev] = static_cast<unsigned char*>(p);
     }
     unsigned char* base = g_dev_ptr[dev];

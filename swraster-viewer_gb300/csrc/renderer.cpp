@@ -286,9 +286,11 @@ swr_status FrameEngine::prepare(const std::vector<const SceneImpl*>& scenes, std
         std::memcpy(hs + lay.o_scenes + i * sizeof(DScene), &scenes[i]->dscene, sizeof(DScene));
     std::memcpy(hs + lay.o_views, vws.data(), vws.size() * sizeof(DView));
     if (!h_order.empty()) std::memcpy(hs + lay.o_order, h_order.data(), h_order.size() * sizeof(uint32_t));
-    if (grid_tile != sched_tile) {
-        frame_grids(num_sms, sched_tile, &raster_grid, &shade_grid);
+    const bool fused32 = fuse32 && sched_tile == 32;
+    if (grid_tile != sched_tile || grid_fused32 != fused32) {
+        frame_grids(num_sms, sched_tile, fused32, &raster_grid, &shade_grid);
         grid_tile = sched_tile;
+        grid_fused32 = fused32;
     }
     uint8_t* tb = static_cast<uint8_t*>(tables.p);
     FrameArgs a{};
@@ -302,6 +304,7 @@ swr_status FrameEngine::prepare(const std::vector<const SceneImpl*>& scenes, std
     a.slot_cap = order_cap;
     a.draw_cap = draw_cap;
     a.gpu_draws = 1u;
+    a.fused_shade = fused32 ? 1u : 0u;
     a.chunk_cap = chunk_cap;
     a.tri_cap = tri_cap;
     a.extra_cap = (uint32_t)extra_cap;

@@ -82,6 +82,8 @@ struct FrameEngine {
     uint32_t pixel_cap = 0;
     uint64_t key_cap = 0;
     uint32_t raster_grid = 0, shade_grid = 0, grid_tile = 0;
+    bool fuse32 = false;        // 32-px tiles shade inside the raster kernel (batch autotuner's choice)
+    bool grid_fused32 = false;
     DBuf tables, tri_state, rec_r, rec_s, fan_base, clip_queue;
     DBuf tile_count, tile_offset, tile_cursor, bins, keys, counters, rsqrt_tab;
     DBuf color;                // linear colour of views that need it (padded tile grids)
