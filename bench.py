@@ -304,6 +304,7 @@ def run_served(args):
             reqs.append((k, cam, w, h))
         # Served.
         lat = []
+        bviews = []
         done = [0]
         def submit():
             t0 = time.perf_counter()
@@ -321,12 +322,13 @@ def run_served(args):
         while done[0] < n:
             for c in srv.poll(256, wait_ms=5):
                 lat.append(c.latency_ms)
+                bviews.append(c.batch_views)
                 srv.release(c.ticket)
                 done[0] += 1
         t_end = time.perf_counter()
         th.join()
         served = {"completed": n, "frames_per_s": n / (t_end - t_start), "p50_ms": float(np.percentile(lat, 50)),
-                  "p99_ms": float(np.percentile(lat, 99))}
+                  "p99_ms": float(np.percentile(lat, 99)), "mean_batch_views": float(np.mean(bviews))}
         # Plain path: the same arrivals, served one at a time in order.
         plat = []
         t0 = time.perf_counter()

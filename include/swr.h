@@ -466,7 +466,13 @@ typedef struct swr_batch_opts {
     uint32_t sched_tile;        /* 8, 16, 32, 64; 0 = autotuned choice for the batch's class, else chosen from the view sizes */
     uint32_t use_graph;         /* replay the frame as a CUDA graph */
     uint64_t bin_capacity;      /* initial pair capacity, 0 = auto */
+    uint32_t flags;             /* SWR_BATCH_* */
+    uint32_t reserved;
 } swr_batch_opts;
+
+/* swr_batch_opts.flags */
+#define SWR_BATCH_FUSED_SHADE 1u  /* with sched_tile 32: shade inside the raster kernel
+                                     (8- and 16-px tiles always do, 64-px never) */
 
 typedef struct swr_batch swr_batch;
 

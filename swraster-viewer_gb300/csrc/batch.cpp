@@ -196,6 +196,7 @@ swr_status swr_batch_create(const swr_batch_opts* opts, swr_batch** out) {
         return SWR_NO_MEMORY;
     }
     b->impl.opts = o;
+    b->impl.opt_fuse32 = b->impl.base_fuse32 = (o.flags & SWR_BATCH_FUSED_SHADE) != 0u;
     b->impl.eng.bin_cap = o.bin_capacity;
     b->impl.eng.use_graph = o.use_graph != 0;
     std::string err;
@@ -329,7 +330,7 @@ swr_status swr_batch_autotune(swr_batch* b, const swr_view_desc* views, int32_t 
             if (st == SWR_OK) st = B.sync(err);
             if (st != SWR_OK) {
                 B.opts = keep;
-                B.opt_fuse32 = false;
+                B.opt_fuse32 = B.base_fuse32;
                 set_last_error(err.c_str());
                 return st;
             }
@@ -343,7 +344,7 @@ swr_status swr_batch_autotune(swr_batch* b, const swr_view_desc* views, int32_t 
         }
     }
     B.opts = keep;
-    B.opt_fuse32 = false;
+    B.opt_fuse32 = B.base_fuse32;
     B.tuned[batch_class(views, n)] = best;
     if (best_tile) *best_tile = best & 0xFFu;
     if (best_ms) *best_ms = bms / 3.0f;

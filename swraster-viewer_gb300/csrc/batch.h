@@ -26,6 +26,7 @@ struct BatchImpl {
     std::vector<swr_camera> saved_cams;
     std::map<uint32_t, uint32_t> tuned;  // class -> scheduling tile | 0x100 when 32-px tiles shade fused
     bool opt_fuse32 = false;             // with opts.sched_tile == 32: shade fused (autotuner trials)
+    bool base_fuse32 = false;            // SWR_BATCH_FUSED_SHADE
     cudaEvent_t ev_start = nullptr, ev_end = nullptr;
     cudaStream_t last_stream = nullptr;
     bool pending = false;

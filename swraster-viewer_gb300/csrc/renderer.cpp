@@ -232,7 +232,10 @@ swr_status FrameEngine::prepare(const std::vector<const SceneImpl*>& scenes, std
     quad_cap = grow(quad_cap, quad_cursor);
     pixel_cap = grow(pixel_cap, max_px);
     if (key_cursor > key_cap) key_cap = key_cursor + key_cursor / 4;
-    if (extra_cap < std::max<uint64_t>(4096, tri_cap / 4)) extra_cap = std::max<uint64_t>(4096, tri_cap / 4);
+    // Clip fan slots: a sixteenth of the triangles to start with (clipped
+    // triangles are a few percent of a frame); a frame that needs more is
+    // rendered again with them doubled.
+    if (extra_cap < std::max<uint64_t>(4096, tri_cap / 16)) extra_cap = std::max<uint64_t>(4096, tri_cap / 16);
     if (bin_cap < std::max<uint64_t>(65536, (uint64_t)tri_cap * 2 + stile_cap * 4ull))
         bin_cap = std::max<uint64_t>(65536, (uint64_t)tri_cap * 2 + stile_cap * 4ull);
     lay = table_layout(scene_cap, view_cap, order_cap, draw_cap, chunk_cap);

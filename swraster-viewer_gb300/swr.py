@@ -147,7 +147,8 @@ class ViewDesc(C.Structure):
 
 
 class BatchOpts(C.Structure):
-    _fields_ = [("sched_tile", C.c_uint32), ("use_graph", C.c_uint32), ("bin_capacity", C.c_uint64)]
+    _fields_ = [("sched_tile", C.c_uint32), ("use_graph", C.c_uint32), ("bin_capacity", C.c_uint64),
+                ("flags", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class ServerOpts(C.Structure):
@@ -495,9 +496,9 @@ def copy_device_to_host(dev_ptr, nbytes, out, stream=None):
 class Batch:
     """Many views per launch sequence (swr_batch_*)."""
 
-    def __init__(self, sched_tile=0, use_graph=False, bin_capacity=0):
+    def __init__(self, sched_tile=0, use_graph=False, bin_capacity=0, fused_shade=False):
         h = C.c_void_p()
-        o = BatchOpts(sched_tile, 1 if use_graph else 0, bin_capacity)
+        o = BatchOpts(sched_tile, 1 if use_graph else 0, bin_capacity, 1 if fused_shade else 0, 0)
         check(lib().swr_batch_create(C.byref(o), C.byref(h)))
         self.handle = h
 

@@ -45,14 +45,15 @@ def alone(scene, cam, w, h):
     return out
 
 
-@pytest.mark.parametrize("tile,graph", [(64, False), (32, True), (16, False)])
-def test_batch_views_equal_plain(two_scenes, tile, graph):
+@pytest.mark.parametrize("tile,graph,fused", [(64, False, False), (32, True, False), (32, False, True),
+                                              (16, False, False)])
+def test_batch_views_equal_plain(two_scenes, tile, graph, fused):
     sizes = [(320, 240), (160, 96), (257, 131), (64, 64)]
     items = []
     for k, sc in enumerate(two_scenes):
         for cam, w, h in sphere_cameras(sc, 5, sizes, seed=k):
             items.append((sc, cam, w, h))
-    b = swr.Batch(sched_tile=tile, use_graph=graph)
+    b = swr.Batch(sched_tile=tile, use_graph=graph, fused_shade=fused)
     arr = swr.Batch.views([(sc, cam, w, h, 2.0, swr.RSQRT_AARCH64) for sc, cam, w, h in items])
     for rep in range(2):  # the second run replays the captured graph
         b.render(arr)
