@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sched-tile", type=int, default=0,
                     help="raster scheduling tile (8, 16, 32, 64; 0 = the library's choice for the frame size)")
+    ap.add_argument("--gi", action="store_true",
+                    help="plain mode: bake the voxel GI at load (the reference's --gi) and shade with it")
     ap.add_argument("--mode", default="plain", choices=["plain", "batched", "hetero", "served"],
                     help="plain: 4K per-frame path (the headline); batched: 64 views of the 81,920-triangle scene "
                          "in one launch; hetero: 16 heterogeneous scenes in one launch; served: request loop")
@@ -385,7 +387,9 @@ def main():
     import swr
     sd, cam_params, cfg = workload(args.workload)
     W, H = cfg["width"], cfg["height"]
-    scene = swr.Scene(sd)
+    scene = swr.Scene(sd, gi=args.gi)
+    if args.gi:
+        cfg = dict(cfg, workload=cfg["workload"] + ", baked voxel GI", gi=True)
     cam = swr.make_camera(*cam_params) if cam_params else swr.make_camera(
         *scenes.default_camera_params(scene.info(), W, H))
     r = swr.Renderer(W, H, sched_tile=args.sched_tile)

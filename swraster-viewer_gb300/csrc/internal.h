@@ -302,6 +302,7 @@ struct FrameArgs {
     uint32_t draw_cap;
     uint32_t slot_cap;
     uint32_t fused_shade;      // 32-px tiles: shade inside the raster kernel (8 and 16 px always do)
+    uint32_t has_gi;           // some scene of the frame has a baked voxel grid
     uint32_t gpu_draws;        // build draws and chunks on the device (else the host staged them)
 };
 

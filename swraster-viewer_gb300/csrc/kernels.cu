@@ -808,11 +808,10 @@ __device__ __forceinline__ void frontend_triangle(const FrameArgs& a, uint32_t c
     warp_count(&a.counters->setup_tris, ok);
 }
 
-// Thread per triangle of a 256-triangle chunk; CTAs loop over the frame's
-// chunks (the grid is sized by the SM count, not by the capacity).
+// Thread per triangle of a 256-triangle chunk, CTA per chunk (a loop over
+// chunks per CTA made the kernel spill).
 __global__ void __launch_bounds__(kChunkTris) k_frontend(FrameArgs a) {
-    const uint32_t n = a.dyn->n_chunks;
-    for (uint32_t c = blockIdx.x; c < n; c += gridDim.x) frontend_triangle(a, c);
+    if (blockIdx.x < a.dyn->n_chunks) frontend_triangle(a, blockIdx.x);
 }
 
 // intersect (src/renderer.rs:598-609).
@@ -1344,6 +1343,7 @@ __device__ __forceinline__ void packet_regions(RasterShared<S>& s, const PacketC
 }
 
 __device__ __forceinline__ bool shade_needed(const DView& v, int32_t qx, int32_t qy);
+template <bool GI>
 __device__ __forceinline__ void shade_pixel(const FrameArgs& a, const uint8_t* tab, const DView& v,
                                             const DScene& sc, int32_t qx, int32_t qy, int32_t k, bool needed,
                                             unsigned long long key);
@@ -1511,7 +1511,7 @@ __global__ void __launch_bounds__(RasterShared<S>::kThreads, RasterShared<S>::kM
             const bool needed = live && shade_needed(view, qx, qy);
             unsigned long long key = kEmptyKey;
             if (needed) key = s.sk[(2 * (ql / QS) + (k >> 1)) * S + 2 * (ql % QS) + (k & 1)];
-            shade_pixel(a, s.tab, view, sc, qx, qy, k, needed, key);
+            shade_pixel<true>(a, s.tab, view, sc, qx, qy, k, needed, key);
         }
         __syncthreads();
     }
@@ -1548,8 +1548,43 @@ __device__ f3 skybox(const DView& v, const DScene& sc, int32_t qx_screen, int32_
     return srgb_fast3(sample_cube(sc.textures[sc.tex_cubemap], uf, vf, slice, 0u));
 }
 
+// get_filtered_gi_sh4_packed_vec over the baked grid: every coefficient's
+// rgb and w trilinear.
+__device__ __forceinline__ void voxel_gi_baked(const float4* G, uint32_t n, uint32_t x0, uint32_t y0, uint32_t z0,
+                                            uint32_t x1, uint32_t y1, uint32_t z1, float fx, float fy, float fz,
+                                            f3 sh[4], float& w0, float& w1) {
+    const float ofx = 1.0f - fx, ofy = 1.0f - fy, ofz = 1.0f - fz;
+    const uint32_t nn = n * n;
+    const uint32_t c000 = z0 * nn + y0 * n + x0, c001 = z1 * nn + y0 * n + x0;
+    const uint32_t c010 = z0 * nn + y1 * n + x0, c011 = z1 * nn + y1 * n + x0;
+    const uint32_t c100 = z0 * nn + y0 * n + x1, c101 = z1 * nn + y0 * n + x1;
+    const uint32_t c110 = z0 * nn + y1 * n + x1, c111 = z1 * nn + y1 * n + x1;
+    for (int c = 0; c < 4; ++c) {
+        const float4 a000 = __ldg(G + (size_t)c000 * 4 + c), a001 = __ldg(G + (size_t)c001 * 4 + c);
+        const float4 a010 = __ldg(G + (size_t)c010 * 4 + c), a011 = __ldg(G + (size_t)c011 * 4 + c);
+        const float4 a100 = __ldg(G + (size_t)c100 * 4 + c), a101 = __ldg(G + (size_t)c101 * 4 + c);
+        const float4 a110 = __ldg(G + (size_t)c110 * 4 + c), a111 = __ldg(G + (size_t)c111 * 4 + c);
+        auto tri = [&](float v000, float v001, float v010, float v011, float v100, float v101, float v110,
+                       float v111) {
+            const float v00 = v000 * ofx + v100 * fx, v01 = v001 * ofx + v101 * fx;
+            const float v10 = v010 * ofx + v110 * fx, v11 = v011 * ofx + v111 * fx;
+            const float v0 = v00 * ofy + v10 * fy, v1 = v01 * ofy + v11 * fy;
+            return v0 * ofz + v1 * fz;
+        };
+        sh[c] = mk3(tri(a000.x, a001.x, a010.x, a011.x, a100.x, a101.x, a110.x, a111.x),
+                    tri(a000.y, a001.y, a010.y, a011.y, a100.y, a101.y, a110.y, a111.y),
+                    tri(a000.z, a001.z, a010.z, a011.z, a100.z, a101.z, a110.z, a111.z));
+        const float w = tri(a000.w, a001.w, a010.w, a011.w, a100.w, a101.w, a110.w, a111.w);
+        if (c == 0) w0 = w;
+        if (c == 1) w1 = w;
+    }
+}
+
 // get_filtered_gi_sh4_packed_vec (src/voxelgrid.rs:264-368) for the
-// constant-SH voxel grid: w0 from the light grid, the rest constant.
+// constant-SH voxel grid: w0 from the light grid, the rest constant; with
+// GI, scenes with a baked grid read it instead (the variant without GI
+// keeps the baked path's registers out of the common kernels).
+template <bool GI>
 __device__ void voxel_gi(const DScene& sc, f3 pos, f3 sh[4], float& w0, float& w1) {
     const uint32_t n = sc.voxel_n;
     const float vx = (pos.x - sc.voxel_min[0]) / sc.voxel_size_f[0];
@@ -1562,33 +1597,8 @@ __device__ void voxel_gi(const DScene& sc, f3 pos, f3 sh[4], float& w0, float& w
     const float fx = vx - x0f, fy = vy - y0f, fz = vz - z0f;
     const float ofx = 1.0f - fx, ofy = 1.0f - fy, ofz = 1.0f - fz;
     const uint32_t nn = n * n;
-    if (sc.voxel_sh4) {
-        // Baked grid: every coefficient's rgb and w trilinear.
-        const float4* G = sc.voxel_sh4;
-        const uint32_t c000 = z0 * nn + y0 * n + x0, c001 = z1 * nn + y0 * n + x0;
-        const uint32_t c010 = z0 * nn + y1 * n + x0, c011 = z1 * nn + y1 * n + x0;
-        const uint32_t c100 = z0 * nn + y0 * n + x1, c101 = z1 * nn + y0 * n + x1;
-        const uint32_t c110 = z0 * nn + y1 * n + x1, c111 = z1 * nn + y1 * n + x1;
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            const float4 a000 = __ldg(G + (size_t)c000 * 4 + c), a001 = __ldg(G + (size_t)c001 * 4 + c);
-            const float4 a010 = __ldg(G + (size_t)c010 * 4 + c), a011 = __ldg(G + (size_t)c011 * 4 + c);
-            const float4 a100 = __ldg(G + (size_t)c100 * 4 + c), a101 = __ldg(G + (size_t)c101 * 4 + c);
-            const float4 a110 = __ldg(G + (size_t)c110 * 4 + c), a111 = __ldg(G + (size_t)c111 * 4 + c);
-            auto tri = [&](float v000, float v001, float v010, float v011, float v100, float v101, float v110,
-                           float v111) {
-                const float v00 = v000 * ofx + v100 * fx, v01 = v001 * ofx + v101 * fx;
-                const float v10 = v010 * ofx + v110 * fx, v11 = v011 * ofx + v111 * fx;
-                const float v0 = v00 * ofy + v10 * fy, v1 = v01 * ofy + v11 * fy;
-                return v0 * ofz + v1 * fz;
-            };
-            sh[c] = mk3(tri(a000.x, a001.x, a010.x, a011.x, a100.x, a101.x, a110.x, a111.x),
-                        tri(a000.y, a001.y, a010.y, a011.y, a100.y, a101.y, a110.y, a111.y),
-                        tri(a000.z, a001.z, a010.z, a011.z, a100.z, a101.z, a110.z, a111.z));
-            const float w = tri(a000.w, a001.w, a010.w, a011.w, a100.w, a101.w, a110.w, a111.w);
-            if (c == 0) w0 = w;
-            if (c == 1) w1 = w;
-        }
+    if (GI && sc.voxel_sh4) {
+        voxel_gi_baked(sc.voxel_sh4, n, x0, y0, z0, x1, y1, z1, fx, fy, fz, sh, w0, w1);
         return;
     }
     const float* L = sc.voxel_light;
@@ -1632,8 +1642,8 @@ __device__ __forceinline__ uint32_t sample_slot(const DScene& sc, const DMateria
 
 // pbr_shader<TRANS> for one lane (src/shader.rs:110-309). du_dv already holds
 // packet.du_dv * w with component i scaled by lane i's w (Q6 quirk). `cur` is
-// the colour under a translucent fragment.
-template <bool TRANS>
+// the colour under a translucent fragment. GI: read baked voxel grids.
+template <bool TRANS, bool GI>
 __device__ f3 pbr_lane(const DScene& sc, const DView& v, const DMaterial& m, const RecShade& q, float w, float b1,
                        float b2, const float du_dv[4], const uint8_t* tab, f3 cur) {
     const uint32_t md = v.rsqrt_mode;
@@ -1667,7 +1677,7 @@ __device__ f3 pbr_lane(const DScene& sc, const DView& v, const DMaterial& m, con
     const float vdh = fmaxf(dot(vn, hv), 0.0f);
     f3 sh[4];
     float gw0, gw1;
-    voxel_gi(sc, pw, sh, gw0, gw1);
+    voxel_gi<GI>(sc, pw, sh, gw0, gw1);
     const float vli = clampf(gw0, 0.0f, 1.0f);
     const float skyv = clampf(gw1, 0.0f, 1.0f);
     f3 bc = mk3(m.base_color[0], m.base_color[1], m.base_color[2]);
@@ -1775,6 +1785,7 @@ __device__ __forceinline__ bool shade_needed(const DView& v, int32_t qx, int32_t
 
 // Shades lane k of quad (qx, qy) of view v given the pixel's depth key; all
 // 32 lanes of a warp call it together, 4 consecutive lanes per quad.
+template <bool GI>
 __device__ __forceinline__ void shade_pixel(const FrameArgs& a, const uint8_t* tab, const DView& v,
                                             const DScene& sc, int32_t qx, int32_t qy, int32_t k, bool needed,
                                             unsigned long long key) {
@@ -1827,7 +1838,7 @@ __device__ __forceinline__ void shade_pixel(const FrameArgs& a, const uint8_t* t
             }
             const float w_own = k == 0 ? wq[0] : (k == 1 ? wq[1] : (k == 2 ? wq[2] : wq[3]));
             const DMaterial& m = sc.materials[r.material & kRecMaterialMask];
-            col = pbr_lane<false>(sc, v, m, q, w_own, b1, b2, dd, tab, col);
+            col = pbr_lane<false, GI>(sc, v, m, q, w_own, b1, b2, dd, tab, col);
             vis_hi = q.static_id;
             vis_fan = r.seq8 & 7u;
         } else {
@@ -1864,6 +1875,7 @@ __device__ __forceinline__ void shade_pixel(const FrameArgs& a, const uint8_t* t
 }
 
 // One lane of the shading pass over the padded quad grid of every view.
+template <bool GI>
 __device__ __forceinline__ void shade_thread(const FrameArgs& a, const uint8_t* tab, uint32_t gt, uint32_t total) {
     const uint32_t gq = gt >> 2;
     const bool live = gq < total;
@@ -1876,7 +1888,7 @@ __device__ __forceinline__ void shade_thread(const FrameArgs& a, const uint8_t* 
     unsigned long long key = kEmptyKey;
     if (needed)
         key = a.keys[v.key_offset + (uint64_t)(2 * qy + (k >> 1)) * v.key_pitch + (uint64_t)(2 * qx + (k & 1))];
-    shade_pixel(a, tab, v, a.scenes[v.scene], qx, qy, k, needed, key);
+    shade_pixel<GI>(a, tab, v, a.scenes[v.scene], qx, qy, k, needed, key);
 }
 
 // Three CTAs per SM (<= 85 registers): 4K frame shade 0.652 ms, against
@@ -1884,6 +1896,8 @@ __device__ __forceinline__ void shade_thread(const FrameArgs& a, const uint8_t* 
 #ifndef SWR_SHADE_MIN_BLOCKS
 #define SWR_SHADE_MIN_BLOCKS 3
 #endif
+// GI: the frame has scenes with a baked voxel grid.
+template <bool GI>
 __global__ void __launch_bounds__(256, SWR_SHADE_MIN_BLOCKS) k_shade(FrameArgs a) {
     __shared__ uint8_t tab[512];
     for (int i = threadIdx.x; i < 512; i += blockDim.x) tab[i] = a.rsqrt_table[i];
@@ -1892,7 +1906,7 @@ __global__ void __launch_bounds__(256, SWR_SHADE_MIN_BLOCKS) k_shade(FrameArgs a
     // either all live or all past the end (warp-uniform loop).
     const uint32_t total = a.dyn->total_quads;
     for (uint32_t base = blockIdx.x * blockDim.x; base < total * 4u; base += gridDim.x * blockDim.x)
-        shade_thread(a, tab, base + threadIdx.x, total);
+        shade_thread<GI>(a, tab, base + threadIdx.x, total);
 }
 
 __global__ void k_rsqrt_selftest(const float* in, float* out, uint64_t n, uint32_t mode, const uint8_t* table) {
@@ -2061,7 +2075,8 @@ __global__ void __launch_bounds__(kTransThreads) k_translucent(FrameArgs a) {
                 const DMaterial& m = sc.materials[c.r.material & kRecMaterialMask];
 #pragma unroll
                 for (int l = 0; l < 4; ++l)
-                    if (mask & (1u << l)) col[l] = pbr_lane<true>(sc, view, m, qs, wl[l], b1[l], b2[l], dd, tab, col[l]);
+                    if (mask & (1u << l))
+                        col[l] = pbr_lane<true, true>(sc, view, m, qs, wl[l], b1[l], b2[l], dd, tab, col[l]);
                 touched = true;
             }
             if (!touched) continue;
@@ -2147,7 +2162,7 @@ void frame_grids(int num_sms, uint32_t S, bool fuse32, uint32_t* raster_grid, ui
         case 32: rb = fuse32 ? raster_blocks_per_sm<32, true>() : raster_blocks_per_sm<32, false>(); break;
         default: rb = raster_blocks_per_sm<64, false>(); break;
     }
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sb, k_shade, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sb, k_shade<false>, 256, 0);
     cudaGetLastError();
     *raster_grid = (uint32_t)(num_sms * (rb > 0 ? rb : 1));
     *shade_grid = (uint32_t)(num_sms * (sb > 0 ? sb : 1));
@@ -2176,10 +2191,14 @@ void launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t* ev
         if (sg > 1u) k_draw_emit<<<sg, kSlotBlock, 0, s>>>(a);
     }
     mark(1);
-    // The front end loops over the frame's chunks with a grid sized by the SM
-    // count (the chunk capacity follows the scenes' bounds and can be far
-    // larger than what a frame draws).
-    if (a.chunk_cap > 0) k_frontend<<<min(a.chunk_cap, (uint32_t)num_sms * 16u), kChunkTris, 0, s>>>(a);
+    // A frame's chunks number at most T / 256 + draws: the grid follows the
+    // record slots, not the chunk capacity (sized from the scenes' bounds,
+    // it can be far larger than what a frame draws).
+    if (a.chunk_cap > 0) {
+        // Host-built draw lists (no-alloc frames) size chunk_cap exactly.
+        const uint64_t most = a.gpu_draws ? (uint64_t)a.tri_cap / kChunkTris + a.draw_cap + 1u : a.chunk_cap;
+        k_frontend<<<(uint32_t)std::min<uint64_t>(a.chunk_cap, most), kChunkTris, 0, s>>>(a);
+    }
     mark(2);
     k_clip<<<num_sms * 4, 128, 0, s>>>(a);
     mark(3);
@@ -2207,8 +2226,13 @@ void launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t* ev
         default: k_raster<64, false><<<rg, RasterShared<64>::kThreads, sizeof(RasterShared<64>), s>>>(a); break;
     }
     mark(6);
-    if (!shade_fused(a.sched_tile, a.fused_shade != 0))
-        k_shade<<<a.shade_grid > 0 ? a.shade_grid : (uint32_t)num_sms, 256, 0, s>>>(a);
+    if (!shade_fused(a.sched_tile, a.fused_shade != 0)) {
+        const uint32_t sg = a.shade_grid > 0 ? a.shade_grid : (uint32_t)num_sms;
+        if (a.has_gi)
+            k_shade<true><<<sg, 256, 0, s>>>(a);
+        else
+            k_shade<false><<<sg, 256, 0, s>>>(a);
+    }
     mark(7);
     if (a.has_translucent) {
         const uint32_t tg = (uint32_t)num_sms * 2u;

@@ -286,6 +286,7 @@ extern "C" swr_status swr_render_frame_noalloc(const swr_scene* scene, const swr
     a.counters = reinterpret_cast<DCounters*>(base + oCounters);
     a.rsqrt_table = base + oTab;
     a.exposure_dev = nullptr;
+    a.has_gi = s.voxel_sh4.empty() ? 0u : 1u;
     a.raster_grid = g_raster_grid[dev];
     a.shade_grid = g_shade_grid[dev];
     launch_frame(a, stream, g_dev_sms[dev]);

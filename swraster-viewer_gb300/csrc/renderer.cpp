@@ -334,6 +334,9 @@ swr_status FrameEngine::prepare(const std::vector<const SceneImpl*>& scenes, std
     a.raster_grid = raster_grid;
     a.shade_grid = shade_grid;
     a.has_translucent = any_translucent ? 1u : 0u;
+    a.has_gi = 0u;
+    for (const SceneImpl* sc : scenes)
+        if (!sc->voxel_sh4.empty()) a.has_gi = 1u;
     a.defer_resolve = defer_resolve ? 1u : 0u;
     args = a;
     return SWR_OK;
