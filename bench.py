@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sched-tile", type=int, default=0,
                     help="raster scheduling tile (8, 16, 32, 64; 0 = the library's choice for the frame size)")
+    ap.add_argument("--fused-shade", action="store_true",
+                    help="served: 32-px tiles shade inside the raster kernel (with --sched-tile 32)")
     ap.add_argument("--gi", action="store_true",
                     help="plain mode: bake the voxel GI at load (the reference's --gi) and shade with it")
     ap.add_argument("--mode", default="plain", choices=["plain", "batched", "hetero", "served"],
@@ -289,7 +291,7 @@ def run_served(args):
     scs = [swr.Scene(sd) for sd, _ in scenes.hetero_scenes(seed=31, count=8, max_triangles=args.max_tris or None)]
     res = [(640, 480), (1280, 720), (1920, 1080), (3840, 2160)]
     srv = swr.Server(memory_budget=40 << 30, max_batch_views=args.max_batch, inflight=args.inflight,
-                     use_graph=args.graph)
+                     use_graph=args.graph, sched_tile=args.sched_tile, fused_shade=args.fused_shade)
     ids = [srv.add_scene(s) for s in scs]
     rends = {r: swr.Renderer(r[0], r[1]) for r in res}
     results = {}
@@ -353,7 +355,8 @@ def run_served(args):
                                    "a sphere, resolution from {640x480, 1280x720, 1920x1080, 3840x2160}, 40 GB "
                                    "budget, continuous batching",
                        "triangles": int(sum(s.info().triangle_count for s in scs)), "inflight": args.inflight,
-                       "max_batch_views": args.max_batch, "graph": bool(args.graph)},
+                       "max_batch_views": args.max_batch, "graph": bool(args.graph),
+                       "sched_tile": args.sched_tile, "fused_shade": bool(args.fused_shade)},
             "rates": results, "batches": st.batches, "device_bytes": st.device_bytes, "data": "synthetic"}
     best_served = max((v["served"]["frames_per_s"] for v in results.values()), default=0.0)
     best_plain = max((v["plain"]["frames_per_s"] for v in results.values()), default=0.0)

@@ -508,6 +508,7 @@ typedef struct swr_server_opts {
     uint32_t sched_tile;        /* 0 = autotuned, else chosen from the view sizes */
     uint32_t rsqrt_mode;
     uint32_t use_graph;
+    uint32_t flags;             /* SWR_BATCH_* for every batch (SWR_BATCH_FUSED_SHADE) */
 } swr_server_opts;
 
 typedef struct swr_request {

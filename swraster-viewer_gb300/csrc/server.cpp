@@ -312,6 +312,7 @@ swr_status swr_server_create(const swr_server_opts* opts, swr_server** out) {
         auto e = std::make_unique<Engine>();
         e->b = std::make_unique<BatchImpl>();
         e->b->opts.sched_tile = o.sched_tile;
+        e->b->opt_fuse32 = e->b->base_fuse32 = (o.flags & SWR_BATCH_FUSED_SHADE) != 0u;
         e->b->eng.use_graph = o.use_graph != 0;
         std::string err;
         swr_status st = e->b->eng.init(err);

@@ -154,7 +154,7 @@ class BatchOpts(C.Structure):
 class ServerOpts(C.Structure):
     _fields_ = [("memory_budget", C.c_uint64), ("max_batch_views", C.c_uint32), ("max_queue", C.c_uint32),
                 ("inflight", C.c_uint32), ("sched_tile", C.c_uint32), ("rsqrt_mode", C.c_uint32),
-                ("use_graph", C.c_uint32)]
+                ("use_graph", C.c_uint32), ("flags", C.c_uint32)]
 
 
 class Request(C.Structure):
@@ -550,10 +550,10 @@ class Server:
     """Request loop with continuous batching (swr_server_*)."""
 
     def __init__(self, memory_budget=40 << 30, max_batch_views=64, max_queue=4096, inflight=2, sched_tile=0,
-                 rsqrt_mode=RSQRT_AARCH64, use_graph=False):
+                 rsqrt_mode=RSQRT_AARCH64, use_graph=False, fused_shade=False):
         h = C.c_void_p()
         o = ServerOpts(memory_budget, max_batch_views, max_queue, inflight, sched_tile, rsqrt_mode,
-                       1 if use_graph else 0)
+                       1 if use_graph else 0, 1 if fused_shade else 0)
         check(lib().swr_server_create(C.byref(o), C.byref(h)))
         self.handle = h
 
