@@ -463,7 +463,8 @@ typedef struct swr_view_desc {
 } swr_view_desc;
 
 typedef struct swr_batch_opts {
-    uint32_t sched_tile;        /* 8, 16, 32, 64; 0 = autotuned choice for the batch's class, else chosen from the view sizes */
+    uint32_t sched_tile;        /* 8, 16, 32, 64; 0 = autotuned choice for the batch's class, else chosen
+                                   from the view sizes (several views: 32 px with fused shading) */
     uint32_t use_graph;         /* replay the frame as a CUDA graph */
     uint64_t bin_capacity;      /* initial pair capacity, 0 = auto */
     uint32_t flags;             /* SWR_BATCH_* */
@@ -505,7 +506,7 @@ typedef struct swr_server_opts {
     uint32_t max_batch_views;   /* views per batch (default 64) */
     uint32_t max_queue;         /* pending requests before submit returns SWR_BUSY (default 4096) */
     uint32_t inflight;          /* batches in flight on separate streams (default 2) */
-    uint32_t sched_tile;        /* 0 = autotuned, else chosen from the view sizes */
+    uint32_t sched_tile;        /* 0 = chosen per batch (several views: 32 px with fused shading) */
     uint32_t rsqrt_mode;
     uint32_t use_graph;
     uint32_t flags;             /* SWR_BATCH_* for every batch (SWR_BATCH_FUSED_SHADE) */
