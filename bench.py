@@ -503,7 +503,8 @@ def main():
             "gtri_per_s": fps * cfg["triangles"] / 1e9, "gpix_per_s": fps * W * H / 1e9,
             "stage_ms": {k: round(v, 4) for k, v in prof.items()},
             "frame_stats": {"triangles_in": st.triangles_in, "clipped": st.triangles_clipped,
-                            "setup_triangles": st.setup_triangles, "bin_pairs": st.bin_pairs},
+                            "setup_triangles": st.setup_triangles, "bin_pairs": st.bin_pairs,
+                            "culled_pairs": st.culled_pairs},
             "issue_roofline": issue,
             "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,

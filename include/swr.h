@@ -427,6 +427,7 @@ typedef struct swr_frame_stats {
     float exposure;
     uint32_t sched_tile;        /* scheduling tile the renderer uses */
     uint64_t staged_bytes;      /* host-to-device bytes per frame (frame, scene and view headers, node order) */
+    uint64_t culled_pairs;      /* bin pairs the raster dropped as hidden behind depths already written */
 } swr_frame_stats;
 
 swr_status swr_renderer_get_stats(swr_renderer* r, swr_frame_stats* out);

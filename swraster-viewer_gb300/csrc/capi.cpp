@@ -513,6 +513,7 @@ swr_status swr_renderer_get_stats(swr_renderer* r, swr_frame_stats* o) {
     o->exposure = r->expo.exposure;
     o->sched_tile = r->opts.sched_tile;
     o->staged_bytes = r->eng.lay.staged;
+    o->culled_pairs = c.culled;
     return SWR_OK;
 }
 

@@ -245,6 +245,7 @@ struct alignas(16) DCounters {
     uint32_t draw_done;        // CTAs done counting draws (zero between frames)
     uint32_t draw_chunks;      // chunks and draws of the frame's draw list
     uint32_t draw_count;
+    uint32_t culled;           // (triangle, tile) pairs the raster dropped as hidden
 };
 
 // Per-frame counts, uploaded with the tables: kernels read them from device

@@ -731,6 +731,7 @@ __global__ void __launch_bounds__(256) k_reset(FrameArgs a) {
         a.counters->work_next = 0u;
         a.counters->trans_next = 0u;
         a.counters->trans_packets = 0u;
+        a.counters->culled = 0u;
         a.counters->draw_tris = a.gpu_draws ? 0u : a.dyn->tri_total;
     }
     if (a.gpu_draws) draw_count_blocks(a);
@@ -810,7 +811,12 @@ __device__ __forceinline__ void frontend_triangle(const FrameArgs& a, uint32_t c
 
 // Thread per triangle of a 256-triangle chunk, CTA per chunk (a loop over
 // chunks per CTA made the kernel spill).
-__global__ void __launch_bounds__(kChunkTris) k_frontend(FrameArgs a) {
+// Four CTAs per SM (64 registers, a few spilled): 4K front end 0.161 ms,
+// against 0.164 at three (80 registers) and 0.204 at two (108 registers).
+#ifndef SWR_FRONTEND_MIN_BLOCKS
+#define SWR_FRONTEND_MIN_BLOCKS 4
+#endif
+__global__ void __launch_bounds__(kChunkTris, SWR_FRONTEND_MIN_BLOCKS) k_frontend(FrameArgs a) {
     if (blockIdx.x < a.dyn->n_chunks) frontend_triangle(a, blockIdx.x);
 }
 
@@ -1178,6 +1184,7 @@ struct RasterShared {
     float p_ooa[kThreads], p_oow[3][kThreads], p_zow[3][kThreads];
     uint32_t p_seq8[kThreads], p_mat[kThreads], p_amip[kThreads], p_slot[kThreads];
     uint32_t scan[kThreads / 32][2];
+    uint32_t cell_far[(S / 8) * (S / 8)];  // farthest key depth of each 8x8-px cell (orderable bits)
     uint32_t n_regions, n_quads, n_slow, cur_tile;
     uint8_t tab[512];           // FRSQRTE table for the fused shading
 };
@@ -1291,6 +1298,138 @@ __device__ __forceinline__ void raster_slow_region(RasterShared<S>& s, const Fra
     }
 }
 
+// ---- Occlusion culling ----------------------------------------------------
+//
+// Between rounds the raster records, per 8x8-px cell of the scheduling tile,
+// the farthest depth its keys hold. A packet whose every depth lies beyond
+// that of each cell it can touch cannot lower a key (keys only decrease, and
+// winning a tie needs an equal depth), so it is dropped in pass 1: the keys
+// come out as if it had been rasterized. (Testing each 16-px block of a
+// coarse packet as well dropped 15% more pairs but made the 4K raster 6%
+// slower.) The floor
+// on the depths a packet can produce covers every rounding of the raster's
+// arithmetic (u = 2^-24):
+//  - edge values: the origin evaluation (a x + b y) + c and at most 16
+//    sequential additions err by at most 24u (|a| X + |b| Y + |c| +
+//    256 (|a| + |b|)) per edge, X and Y the largest sample coordinates. A
+//    covered lane has all three computed edge values >= 0 and the exact values
+//    sum to the doubled area A plus top-left biases (<= 0), so b1, b2 >= 0 and
+//    b1 + b2 <= B = (1 + (sum of the three errors) / A)(1 + u)^3;
+//  - zi and oi are three-term sums, within EZ = 5u (|Z0| + B |D1| + B |D2|)
+//    (EO likewise) of the exact affine values, and z = zi * (1 / oi) adds two
+//    roundings;
+//  - (exact zi - EZ) / (exact oi +- EO) is a ratio of affine functions of
+//    (b1, b2) with a positive denominator, so its minimum over the triangle
+//    {b1, b2 >= 0, b1 + b2 <= B} is at a corner; corners are evaluated with
+//    directed rounding.
+// Packets whose int32 setup arithmetic could have wrapped, whose 1/w
+// interpolant could reach 0, with non-finite inputs or with B > 1.5 are kept.
+constexpr float kUlp24 = 5.9604645e-8f;  // 2^-24
+
+// Error bound of one edge's computed values over the packet (false: the
+// edge's integer terms could have wrapped or lost exactness).
+__device__ __forceinline__ bool edge_error(long long xi, long long yi, long long xj, long long yj, float X, float Y,
+                                           float& err) {
+    const long long a = yj - yi, b = xi - xj, c = xj * yi - xi * yj;
+    const long long lim = 1ll << 24, climb = (1ll << 31) - 2;
+    if (a > lim || a < -lim || b > lim || b < -lim || c > climb || c < -climb) return false;
+    const float fa = fabsf((float)a), fb = fabsf((float)b), fc = fabsf((float)c) + 1.0f;
+    err = (32.0f * kUlp24) * (((fa * X + fb * Y) + fc) + 256.0f * (fa + fb));
+    return true;
+}
+
+// Lower bound of every depth the raster can compute for a covered lane of the
+// packet; false when no bound is taken.
+__device__ bool packet_depth_floor(const PacketCtx& c, float& zlo) {
+    const int32_t* p = c.r.p;
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+        if (p[i] > (1 << 28) || p[i] < -(1 << 28)) return false;
+    const long long x0 = p[0], y0 = p[1], x1 = p[2], y1 = p[3], x2 = p[4], y2 = p[5];
+    const long long area = (x1 - x0) * (y2 - y0) - (x2 - x0) * (y1 - y0);
+    if (area >= 0 || area <= -(1ll << 31)) return false;
+    const float X = (float)(c.xe + 32), Y = (float)(c.ye + 32);
+    float e12, e20, e01;
+    if (!edge_error(x1, y1, x2, y2, X, Y, e12) || !edge_error(x2, y2, x0, y0, X, Y, e20) ||
+        !edge_error(x0, y0, x1, y1, X, Y, e01))
+        return false;
+    const float A = (float)(-area) * (1.0f - 2.0f * kUlp24);
+    const float rel = ((e12 + e20) + e01) / A;
+    if (!(rel < 0.25f)) return false;
+    const float B = __fadd_ru(1.0f, __fmul_ru(rel + 8.0f * kUlp24, 1.125f));
+    const float Z0 = c.r.zow[0], D1 = c.r.zow[1], D2 = c.r.zow[2];
+    const float O0 = c.r.oow[0], P1 = c.r.oow[1], P2 = c.r.oow[2];
+    if (!(isfinite(Z0) && isfinite(D1) && isfinite(D2) && isfinite(O0) && isfinite(P1) && isfinite(P2))) return false;
+    const float EZ = (5.0f * kUlp24) * (fabsf(Z0) + B * (fabsf(D1) + fabsf(D2))) + 1e-30f;
+    const float EO = (5.0f * kUlp24) * (fabsf(O0) + B * (fabsf(P1) + fabsf(P2))) + 1e-30f;
+    if (!(isfinite(EZ) && isfinite(EO))) return false;
+    float lo = __int_as_float(0x7F800000);
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+        const float dz = v == 1 ? D1 : D2, dw = v == 1 ? P1 : P2;
+        const float zc = v == 0 ? Z0 : __fadd_rd(Z0, __fmul_rd(B, dz));
+        const float wlo = v == 0 ? O0 : __fadd_rd(O0, __fmul_rd(B, dw));
+        const float whi = v == 0 ? O0 : __fadd_ru(O0, __fmul_ru(B, dw));
+        const float n = __fsub_rd(zc, EZ);
+        const float dlo = __fsub_rd(wlo, EO), dhi = __fadd_ru(whi, EO);
+        if (!(dlo > 0.0f) || !isfinite(n)) return false;
+        lo = fminf(lo, fminf(__fdiv_rd(n, dhi), __fdiv_rd(n, dlo)));
+    }
+    lo = lo >= 0.0f ? __fmul_rd(lo, 1.0f - 4.0f * kUlp24) : __fmul_rd(lo, 1.0f + 4.0f * kUlp24);
+    zlo = __fsub_rd(lo, 1e-30f);
+    return zlo == zlo;
+}
+
+// Farthest key depth of each 8x8-px cell (four threads per cell, two rows
+// each), then a barrier.
+template <int S>
+__device__ __forceinline__ void cell_depths(RasterShared<S>& s) {
+    constexpr int CW = S / 8, NC = CW * CW;
+    const int t = (int)threadIdx.x;
+    if ((t & ~31) < NC * 4) {  // whole warps
+        uint32_t m = 0;
+        if (t < NC * 4) {
+            const int cell = t >> 2, part = t & 3;
+            const int cx = cell % CW, cy = cell / CW;
+#pragma unroll
+            for (int r = 0; r < 2; ++r) {
+                const ulonglong2* row = reinterpret_cast<const ulonglong2*>(s.sk + (cy * 8 + part * 2 + r) * S + cx * 8);
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const ulonglong2 v = row[i];
+                    m = max(m, max((uint32_t)(v.x >> 32), (uint32_t)(v.y >> 32)));
+                }
+            }
+        }
+        m = max(m, __shfl_xor_sync(0xFFFFFFFFu, m, 1));
+        m = max(m, __shfl_xor_sync(0xFFFFFFFFu, m, 2));
+        if (t < NC * 4 && (t & 3) == 0) s.cell_far[t >> 2] = m;
+    }
+    __syncthreads();
+}
+
+// Farthest key depth over the cells holding pixels [xl, xh] x [yl, yh]
+// clipped to the scheduling tile (all ones when none of them is in it).
+template <int S>
+__device__ __forceinline__ uint32_t cells_far(const RasterShared<S>& s, int32_t xl, int32_t xh, int32_t yl, int32_t yh,
+                                              int32_t sx0, int32_t sy0) {
+    xl = max(xl, sx0), xh = min(xh, sx0 + S - 1), yl = max(yl, sy0), yh = min(yh, sy0 + S - 1);
+    if (xh < xl || yh < yl) return 0xFFFFFFFFu;
+    const int32_t cx0 = (xl - sx0) >> 3, cx1 = (xh - sx0) >> 3, cy0 = (yl - sy0) >> 3, cy1 = (yh - sy0) >> 3;
+    uint32_t far = 0;
+    for (int32_t cy = cy0; cy <= cy1; ++cy)
+        for (int32_t cx = cx0; cx <= cx1; ++cx) far = max(far, s.cell_far[cy * (S / 8) + cx]);
+    return far;
+}
+
+// Orderable depth floor of the packet; 0 (below every key) when none is taken.
+// A packet is hidden when its floor is above the farthest depth of every cell
+// its covered lanes can fall in: pixels [x0 & ~1, x1] of its clipped rect.
+__device__ __forceinline__ uint32_t packet_floor(const PacketCtx& c) {
+    float z;
+    return packet_depth_floor(c, z) ? float_to_ordered(z) : 0u;
+}
+
 // Pass 1 of a round for one packet: classify and split into regions, and
 // either count them (regions, quads; the accepted 16-px blocks of a coarse
 // packet go to bmask) or stage them from the given positions (bmask as the
@@ -1348,6 +1487,17 @@ __device__ __forceinline__ void shade_pixel(const FrameArgs& a, const uint8_t* t
                                             const DScene& sc, int32_t qx, int32_t qy, int32_t k, bool needed,
                                             unsigned long long key);
 
+// Occlusion culling pays from 32-px scheduling tiles up (16-px tiles of the
+// 1280x720 small frame: 6,590 frames/s with it, 7,010 without). A first
+// round of 64 packets: 4K raster 0.444 ms, against 0.461 (32), 0.460 (128)
+// and 0.477 (a full round of 256).
+#ifndef SWR_CULL_MIN_TILE
+#define SWR_CULL_MIN_TILE 32
+#endif
+#ifndef SWR_CULL_FIRST
+#define SWR_CULL_FIRST 64
+#endif
+
 // Persistent: each CTA pulls (view, scheduling tile) work items from a
 // device-side counter until every tile of every view is done. Per tile, the
 // bin's packets go through rounds of one packet per thread: pass 1 stages
@@ -1362,8 +1512,14 @@ __global__ void __launch_bounds__(RasterShared<S>::kThreads, RasterShared<S>::kM
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t n_tiles = a.dyn->n_stiles;
     constexpr bool kFuse = FUSE;
+    // Occlusion culling for tiles of at least SWR_CULL_MIN_TILE px; the first
+    // round of a tile takes at most kFirst packets, so that later rounds
+    // meet the nearest depths sooner.
+    constexpr bool kCull = S >= SWR_CULL_MIN_TILE;
+    constexpr uint32_t kFirst = (kCull && SWR_CULL_FIRST > 0 && SWR_CULL_FIRST < NT) ? SWR_CULL_FIRST : NT;
     if (kFuse)
         for (int i = threadIdx.x; i < 512; i += NT) s.tab[i] = a.rsqrt_table[i];
+    uint32_t n_culled = 0;
     for (uint32_t iter = 0;; ++iter) {
 #if SWR_RASTER_PERSISTENT
         if (threadIdx.x == 0) {
@@ -1388,11 +1544,15 @@ __global__ void __launch_bounds__(RasterShared<S>::kThreads, RasterShared<S>::kM
         const uint32_t b0 = a.tile_offset[st], b1 = bad ? b0 : a.tile_offset[st + 1];
         const DScene& sc = a.scenes[view.scene];
         for (uint32_t cursor = b0; cursor < b1;) {
+            // The keys the previous rounds left, per cell, for occlusion culling.
+            if (kCull && cursor != b0) cell_depths<S>(s);
+            const uint32_t lim = cursor == b0 ? kFirst : (uint32_t)NT;
             // Pass 1: count this thread's regions and quads.
             const uint32_t pidx = cursor + threadIdx.x;
             PacketCtx c;
             uint32_t slot = 0, n_r = 0, n_q = 0, bmask = 0;
-            if (pidx < b1) {
+            bool hidden = false;
+            if (pidx < b1 && threadIdx.x < lim) {
                 slot = a.bins[pidx];
                 const uint32_t nidx = pidx + NT;  // this thread's likely packet next round
                 const uint32_t nslot = nidx < b1 ? __ldg(a.bins + nidx) : 0xFFFFFFFFu;
@@ -1404,7 +1564,12 @@ __global__ void __launch_bounds__(RasterShared<S>::kThreads, RasterShared<S>::kM
                     asm volatile("prefetch.global.L2 [%0];" ::"l"(np + sizeof(RecRaster) - 1));
                 }
 #endif
-                packet_regions<S>(s, c, sx0, sy0, false, threadIdx.x, n_r, n_q, bmask);
+                if (kCull && cursor != b0) {
+                    const uint32_t far = cells_far<S>(s, c.xs >> kSubpixelShift, c.xe >> kSubpixelShift,
+                                                      c.ys >> kSubpixelShift, c.ye >> kSubpixelShift, sx0, sy0);
+                    hidden = far < 0xFF800000u && packet_floor(c) > far;
+                }
+                if (!hidden) packet_regions<S>(s, c, sx0, sy0, false, threadIdx.x, n_r, n_q, bmask);
             }
             if (threadIdx.x == 0) s.n_slow = 0;
             // Block-wide exclusive scan of (regions, quads).
@@ -1429,8 +1594,9 @@ __global__ void __launch_bounds__(RasterShared<S>::kThreads, RasterShared<S>::kM
                 pq += s.scan[w][1];
             }
             // Packets are taken in order while their regions fit.
-            const bool taken = pr + n_r <= (uint32_t)R;
+            const bool taken = pr + n_r <= (uint32_t)R && threadIdx.x < lim;
             const uint32_t n_taken = (uint32_t)__syncthreads_count(taken);
+            n_culled += (hidden && taken) ? 1u : 0u;
             if (taken && threadIdx.x + 1u == n_taken) {
                 s.n_regions = pr + n_r;
                 s.n_quads = pq + n_q;
@@ -1515,6 +1681,8 @@ __global__ void __launch_bounds__(RasterShared<S>::kThreads, RasterShared<S>::kM
         }
         __syncthreads();
     }
+    n_culled = __reduce_add_sync(0xFFFFFFFFu, n_culled);
+    if (lane == 0u && n_culled) atomicAdd(&a.counters->culled, n_culled);
 }
 
 // --------------------------------------------------------------------------

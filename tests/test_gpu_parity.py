@@ -172,6 +172,54 @@ def test_overlapping_large_quads_and_depth_ties(tile):
     s.close()
 
 
+def tie_across_rounds_scene(n=80):
+    """n screen-covering quads front to back, then one wide quad in the plane of
+    the nearest one. Every vertex of the two lies in one plane facing the
+    camera, so they tie on depth at every pixel; the wide quad's bounding
+    sphere sits far to the side, so it sorts after every other quad and reaches
+    each tile rounds after the quad it ties. Being later in the canonical
+    order it must win wherever it covers, so occlusion culling has to keep
+    packets that only tie the depths already held."""
+    rng = np.random.default_rng(5)
+    P, UV, F = scenes.grid(1, 1)
+    tex = scenes.noise_texture(rng, 32)
+    meshes, nodes, mats = [], [], []
+
+    def world(sx, sy, t):
+        m = np.eye(4, dtype=np.float32)
+        m[0, 0], m[1, 1] = sx, sy
+        m[:3, 3] = t
+        return m.T.reshape(16).copy()
+
+    for i in range(n):
+        mats.append({"metallic": float(rng.random()), "roughness": float(rng.random()), "base_color": (0, 0, 0)})
+        meshes.append([{"positions": P, "normals": None, "texcoords": UV, "indices": F, "material": i}])
+        w = world(8.0 + 0.01 * i, 8.0 + 0.01 * i, (0.01 * i, -0.02 * i, -2.0 - 0.05 * i))
+        nodes.append({"world": w, "local": w, "mesh": i})
+    w = world(44.0, 8.0, (18.0, 0.0, -2.0))
+    nodes.append({"world": w, "local": w, "mesh": 0})
+    return {"meshes": meshes, "nodes": nodes, "materials": mats, "textures": [tex],
+            "cubemap": scenes.cubemap_faces(rng, 8), "cubemap_face_size": 8, "voxel_grid_size": 16,
+            "specular_samples": 8, "brdf_lut_size": 16}
+
+
+@pytest.mark.parametrize("tile", [64, 32])
+def test_depth_ties_across_rounds_with_culling(tile):
+    n = 80
+    s = swr.Scene(tie_across_rounds_scene(n))
+    cam = swr.make_camera((0.0, 0.0, 3.0), (0.0, 0.0, 0.0), 1.0, 192, 128, 40.0)
+    rgba, vis = compare(s, cam, 192, 128, sched_tile=tile)
+    covered = vis[vis != np.uint64(2 ** 64 - 1)] >> np.uint64(3)
+    assert np.isin(covered, [2 * n, 2 * n + 1]).mean() > 0.9
+    r = swr.Renderer(192, 128, sched_tile=tile)
+    r.render(s, cam)
+    st = r.stats()
+    print("culled %d of %d bin pairs" % (st.culled_pairs, st.bin_pairs))
+    assert st.culled_pairs > 0
+    r.close()
+    s.close()
+
+
 def test_stress_workload_reduced():
     sd, cp = scenes.stress_scene(seed=4, triangles=150_000, width=960, height=540, n_textures=2, tex_size=256,
                                  cube_size=32, voxel=32, specular_samples=16, brdf_lut_size=32)
