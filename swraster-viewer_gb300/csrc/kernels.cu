@@ -1487,12 +1487,17 @@ __device__ __forceinline__ void shade_pixel(const FrameArgs& a, const uint8_t* t
                                             const DScene& sc, int32_t qx, int32_t qy, int32_t k, bool needed,
                                             unsigned long long key);
 
-// Occlusion culling pays from 32-px scheduling tiles up (16-px tiles of the
-// 1280x720 small frame: 6,590 frames/s with it, 7,010 without). A first
-// round of 64 packets: 4K raster 0.444 ms, against 0.461 (32), 0.460 (128)
-// and 0.477 (a full round of 256).
+// Occlusion culling is on for 64-px scheduling tiles, the choice for large
+// single views. It pays where many packets of a tile lie behind near
+// geometry drawn first (the 2M-triangle 4K frame: 640 -> 728 frames/s) and
+// costs where triangles are small and seldom hidden: on the served mix of
+// orbiting cameras, culling in every tile size took the plain loop from
+// 1,210 to 1,030 frames/s and the served batches (32-px tiles) from 4,980
+// to 4,460; for the 16-px tiles of the 1280x720 small frame it cost 6%.
+// A first round of 64 packets: 4K raster 0.444 ms, against 0.461 (32),
+// 0.460 (128) and 0.477 (a full round of 256).
 #ifndef SWR_CULL_MIN_TILE
-#define SWR_CULL_MIN_TILE 32
+#define SWR_CULL_MIN_TILE 64
 #endif
 #ifndef SWR_CULL_FIRST
 #define SWR_CULL_FIRST 64
@@ -1514,7 +1519,8 @@ __global__ void __launch_bounds__(RasterShared<S>::kThreads, RasterShared<S>::kM
     constexpr bool kFuse = FUSE;
     // Occlusion culling for tiles of at least SWR_CULL_MIN_TILE px; the first
     // round of a tile takes at most kFirst packets, so that later rounds
-    // meet the nearest depths sooner.
+    // meet the nearest depths sooner (taking light tiles, at most one round
+    // of packets, whole instead: 4K 718 against 728 frames/s).
     constexpr bool kCull = S >= SWR_CULL_MIN_TILE;
     constexpr uint32_t kFirst = (kCull && SWR_CULL_FIRST > 0 && SWR_CULL_FIRST < NT) ? SWR_CULL_FIRST : NT;
     if (kFuse)
@@ -1543,9 +1549,13 @@ __global__ void __launch_bounds__(RasterShared<S>::kThreads, RasterShared<S>::kM
         const bool bad = (a.counters->status & (ST_BIN_OVERFLOW | ST_CLIP_OVERFLOW | ST_QUEUE_OVERFLOW)) != 0u;
         const uint32_t b0 = a.tile_offset[st], b1 = bad ? b0 : a.tile_offset[st + 1];
         const DScene& sc = a.scenes[view.scene];
+        bool keys_changed = false;  // a round since the last cell_depths had regions
         for (uint32_t cursor = b0; cursor < b1;) {
             // The keys the previous rounds left, per cell, for occlusion culling.
-            if (kCull && cursor != b0) cell_depths<S>(s);
+            if (kCull && keys_changed) {
+                cell_depths<S>(s);
+                keys_changed = false;
+            }
             const uint32_t lim = cursor == b0 ? kFirst : (uint32_t)NT;
             // Pass 1: count this thread's regions and quads.
             const uint32_t pidx = cursor + threadIdx.x;
@@ -1588,15 +1598,26 @@ __global__ void __launch_bounds__(RasterShared<S>::kThreads, RasterShared<S>::kM
                 s.scan[warp][1] = iq;
             }
             __syncthreads();
-            uint32_t pr = ir - n_r, pq = iq - n_q;
-            for (uint32_t w = 0; w < warp; ++w) {
-                pr += s.scan[w][0];
-                pq += s.scan[w][1];
+            uint32_t pr = ir - n_r, pq = iq - n_q, all_r = 0;
+            for (uint32_t w = 0; w < (uint32_t)NW; ++w) {
+                if (w < warp) {
+                    pr += s.scan[w][0];
+                    pq += s.scan[w][1];
+                }
+                all_r += s.scan[w][0];
             }
             // Packets are taken in order while their regions fit.
             const bool taken = pr + n_r <= (uint32_t)R && threadIdx.x < lim;
             const uint32_t n_taken = (uint32_t)__syncthreads_count(taken);
             n_culled += (hidden && taken) ? 1u : 0u;
+            // No packet of the round has a region (all culled or outside the
+            // tile): no key changes, and the next round starts at once (every
+            // thread has read the scan words before the barrier above).
+            if (all_r == 0u) {
+                cursor += n_taken;
+                continue;
+            }
+            keys_changed = true;
             if (taken && threadIdx.x + 1u == n_taken) {
                 s.n_regions = pr + n_r;
                 s.n_quads = pq + n_q;

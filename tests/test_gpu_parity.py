@@ -215,7 +215,8 @@ def test_depth_ties_across_rounds_with_culling(tile):
     r.render(s, cam)
     st = r.stats()
     print("culled %d of %d bin pairs" % (st.culled_pairs, st.bin_pairs))
-    assert st.culled_pairs > 0
+    # Occlusion culling runs for 64-px scheduling tiles.
+    assert (st.culled_pairs > 0) == (tile == 64)
     r.close()
     s.close()
 
