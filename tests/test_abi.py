@@ -102,3 +102,47 @@ def test_camera_matches_float64_model():
     assert abs(cam.yaw - yaw) < 1e-6 and abs(cam.pitch - pitch) < 1e-6
     view = np.array(cam.view[:], np.float64).reshape(4, 4).T
     assert np.allclose(view[:3, :3], _rx(pitch) @ _ry(yaw), atol=1e-6)
+
+
+# ctypes mirror in swr.py -> C struct of include/swr.h.
+MIRRORS = {"TextureDesc": "swr_texture_desc", "TexRef": "swr_texref", "MaterialDesc": "swr_material_desc",
+           "PrimitiveDesc": "swr_primitive_desc", "MeshDesc": "swr_mesh_desc", "NodeDesc": "swr_node_desc",
+           "SceneDesc": "swr_scene_desc", "GltfOpts": "swr_gltf_opts", "SceneInfo": "swr_scene_info",
+           "TextureView": "swr_texture_view", "PrimitiveView": "swr_primitive_view", "MeshView": "swr_mesh_view",
+           "NodeView": "swr_node_view", "MaterialView": "swr_material_view", "SceneHostView": "swr_scene_host_view",
+           "Camera": "swr_camera", "RendererOpts": "swr_renderer_opts", "FrameStats": "swr_frame_stats",
+           "ViewDesc": "swr_view_desc", "BatchOpts": "swr_batch_opts", "ServerOpts": "swr_server_opts",
+           "Request": "swr_request", "Completion": "swr_completion", "ServerStats": "swr_server_stats"}
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """Every ctypes structure of the binding has the size and field offsets
+    the C compiler gives the header's struct (a field added on one side only
+    shifts what the other reads)."""
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "swr.h"', "int main(void) {"]
+    for py, cn in MIRRORS.items():
+        lines.append('printf("%s %%zu\\n", sizeof(%s));' % (py, cn))
+        for f in getattr(swr, py)._fields_:
+            lines.append('printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (py, f[0], cn, f[0]))
+    lines.append("return 0; }")
+    src, exe = tmp_path / "layout.c", tmp_path / "layout"
+    src.write_text("\n".join(lines) + "\n")
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    declared = set(re.findall(r"\}\s*(swr_[a-z0-9_]+)\s*;", open(os.path.join(ROOT, "include", "swr.h")).read()))
+    assert set(MIRRORS.values()) <= declared
+    checked = 0
+    for line in filter(None, out):
+        key, value = line.split()
+        if "." in key:
+            cls, field = key.split(".")
+            got = getattr(getattr(swr, cls), field).offset
+        else:
+            got = C.sizeof(getattr(swr, key))
+        assert got == int(value), (key, got, int(value))
+        checked += 1
+    assert checked > len(MIRRORS)
