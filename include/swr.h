@@ -564,6 +564,16 @@ swr_status swr_copy_to_host(void* dst, const void* src_device, size_t bytes, voi
  * shading pass uses, src/math.rs:17-49), written to host `out`. */
 swr_status swr_selftest_rsqrt(const float* in, float* out, uint64_t n, uint32_t rsqrt_mode);
 
+/* Numerics self-test, host only: the lower bound the raster's occlusion
+ * culling takes on the depths of a packet (subpixel vertices p[6] = x0, y0,
+ * x1, y1, x2, y2; depth and 1/w interpolants zow[3], oow[3] as value at
+ * vertex 0 then differences; xe, ye the end of the packet's rect clipped to
+ * its 64-pixel tile, in subpixels), evaluated by the same source the device
+ * runs; -infinity when the raster takes no bound for the packet. No
+ * counterpart in the reference, whose raster tests every packet. */
+swr_status swr_selftest_depth_floor(const int32_t* p, const float* zow, const float* oow, int32_t xe, int32_t ye,
+                                    float* zlo);
+
 /* Allocation-free frame. No counterpart in the reference: an addition for
  * callers that cannot allocate device memory while they render (code running
  * under CUDA stream capture, processes whose device memory belongs to another

@@ -62,6 +62,9 @@ def lib():
         L.oracle_sun_visibility.restype = C.c_int
         L.oracle_gi_bake.argtypes = [C.POINTER(swr.SceneHostView), C.c_uint32, C.c_void_p]
         L.oracle_gi_bake.restype = C.c_int
+        L.oracle_packet_depths.argtypes = [C.c_void_p, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p,
+                                           C.POINTER(C.c_float), C.POINTER(C.c_uint64)]
+        L.oracle_packet_depths.restype = C.c_int
         _lib = L
     return _lib
 
@@ -79,6 +82,21 @@ def render(view, cam, width, height, rsqrt_mode=swr.RSQRT_AARCH64, threads=1, dt
     if rc != 0:
         raise RuntimeError("oracle_render failed")
     return rgba, vis, tl, res
+
+
+def packet_depths(p, ooa, zow, oow, rect):
+    """(smallest depth, covered lanes) of one packet as the reference's tile
+    raster computes them, without the depth test. p: 6 subpixel vertex
+    coordinates; zow, oow: interpolants (vertex 0, then differences); rect:
+    the packet's pixel rect clipped to its 64-px tile."""
+    p = np.ascontiguousarray(p, np.int32)
+    zow = np.ascontiguousarray(zow, np.float32)
+    oow = np.ascontiguousarray(oow, np.float32)
+    rect = np.ascontiguousarray(rect, np.int32)
+    zmin, n = C.c_float(), C.c_uint64()
+    lib().oracle_packet_depths(p.ctypes.data, float(ooa), zow.ctypes.data, oow.ctypes.data, rect.ctypes.data,
+                               C.byref(zmin), C.byref(n))
+    return zmin.value, n.value
 
 
 def sun_visibility(view, threads=1):

@@ -1772,6 +1772,77 @@ int oracle_gi_bake(const swr_scene_host_view* v, uint32_t threads, float* out) {
     return 0;
 }
 
+// Depths of one packet's covered lanes as rasterize_packet + coarse_raster +
+// fine_raster compute them (src/tilerasterizer.rs:114-383), without the depth
+// test: the smallest depth and the number of covered lanes. p holds the
+// subpixel vertices (x0, y0, x1, y1, x2, y2), zow and oow the interpolants
+// (value at vertex 0, differences to vertices 1 and 2), rect the packet's
+// pixel rect clipped to its 64-px tile (min x, min y, max x, max y). Checks
+// the raster's occlusion-culling depth floor.
+int oracle_packet_depths(const int32_t* p, float ooa, const float* zow, const float* oow, const int32_t* rect,
+                         float* zmin, uint64_t* covered) {
+    using namespace orc;
+    auto bias = [](int32_t a, int32_t b) { return (a < 0 || (a == 0 && b > 0)) ? 0 : -1; };
+    const int32_t a01 = wsub(p[3], p[1]), b01 = wsub(p[0], p[2]);
+    const int32_t c01 = wadd(wsub(wmul(p[2], p[1]), wmul(p[0], p[3])), bias(a01, b01));
+    const int32_t a12 = wsub(p[5], p[3]), b12 = wsub(p[2], p[4]);
+    const int32_t c12 = wadd(wsub(wmul(p[4], p[3]), wmul(p[2], p[5])), bias(a12, b12));
+    const int32_t a20 = wsub(p[1], p[5]), b20 = wsub(p[4], p[0]);
+    const int32_t c20 = wadd(wsub(wmul(p[0], p[5]), wmul(p[4], p[1])), bias(a20, b20));
+    const F4 A12 = splat((float)a12), B12 = splat((float)b12), C12 = splat((float)c12);
+    const F4 A20 = splat((float)a20), B20 = splat((float)b20), C20 = splat((float)c20);
+    const F4 A01 = splat((float)a01), B01 = splat((float)b01), C01 = splat((float)c01);
+    const F4 sx12 = splat((float)wmul(a12, 32)), sx20 = splat((float)wmul(a20, 32)), sx01 = splat((float)wmul(a01, 32));
+    const F4 sy12 = splat((float)wmul(b12, 32)), sy20 = splat((float)wmul(b20, 32)), sy01 = splat((float)wmul(b01, 32));
+    const SI Z = {zow[0], zow[1], zow[2]}, O = {oow[0], oow[1], oow[2]};
+    float zm = INFINITY;
+    uint64_t n = 0;
+    // fine_raster's walk over one region, depth of every covered lane.
+    auto walk = [&](int32_t xs, int32_t ys, int32_t xe, int32_t ye) {
+        const F4 x = mk((float)(xs + 8), (float)(xs + 24), (float)(xs + 8), (float)(xs + 24));
+        const F4 y = mk((float)(ys + 8), (float)(ys + 8), (float)(ys + 24), (float)(ys + 24));
+        F4 w0r = (A12 * x + B12 * y) + C12, w1r = (A20 * x + B20 * y) + C20, w2r = (A01 * x + B01 * y) + C01;
+        for (int32_t py = ys; py < ye; py += 32) {
+            F4 w0 = w0r, w1 = w1r, w2 = w2r;
+            for (int32_t px = xs; px < xe; px += 32) {
+                const F4 b1 = w1 * splat(ooa), b2 = w2 * splat(ooa);
+                const F4 w = 1.0f / O.interp(b1, b2);
+                const F4 z = Z.interp(b1, b2) * w;
+                for (int i = 0; i < 4; ++i) {
+                    if (!(w0.l[i] >= 0.0f && w1.l[i] >= 0.0f && w2.l[i] >= 0.0f)) continue;
+                    ++n;
+                    if (z.l[i] < zm) zm = z.l[i];  // a NaN depth never passes the depth test
+                }
+                w0 = w0 + sx12;
+                w1 = w1 + sx20;
+                w2 = w2 + sx01;
+            }
+            w0r = w0r + sy12;
+            w1r = w1r + sy20;
+            w2r = w2r + sy01;
+        }
+    };
+    const int32_t wp = rect[2] - rect[0], hp = rect[3] - rect[1];
+    const int32_t xs = (rect[0] & ~1) * 16, ys = (rect[1] & ~1) * 16, xe = rect[2] * 16, ye = rect[3] * 16;
+    if (wp > 16 || hp > 16) {
+        for (int32_t by = ys; by < ye; by += 256)
+            for (int32_t bx = xs; bx < xe; bx += 256) {
+                const F4 cx = mk((float)(bx + 8), (float)(bx + 256 - 8), (float)(bx + 8), (float)(bx + 256 - 8));
+                const F4 cy = mk((float)(by + 8), (float)(by + 8), (float)(by + 256 - 8), (float)(by + 256 - 8));
+                const F4 w0c = (A12 * cx + B12 * cy) + C12, w1c = (A20 * cx + B20 * cy) + C20;
+                const F4 w2c = (A01 * cx + B01 * cy) + C01;
+                auto maxel = [](F4 v) { return std::fmax(std::fmax(v.l[0], v.l[1]), std::fmax(v.l[2], v.l[3])); };
+                if (maxel(w0c) < 0.0f || maxel(w1c) < 0.0f || maxel(w2c) < 0.0f) continue;
+                walk(bx, by, std::min(bx + 256, xe), std::min(by + 256, ye));
+            }
+    } else {
+        walk(xs, ys, xe, ye);
+    }
+    *zmin = zm;
+    *covered = n;
+    return 0;
+}
+
 // Arm FRSQRTE/FRSQRTS emulation, exposed for the known-answer tests.
 float oracle_frsqrte(float x) { return orc::frsqrte(x); }
 float oracle_frsqrts(float a, float b) { return orc::frsqrts(a, b); }

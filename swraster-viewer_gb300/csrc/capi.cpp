@@ -4,6 +4,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <new>
 #include <string>
 
@@ -571,6 +572,14 @@ swr_status swr_selftest_rsqrt(const float* in, float* out, uint64_t n, uint32_t 
     if (e == cudaSuccess) e = cudaMemcpy(out, dout, bytes, cudaMemcpyDeviceToHost);
     cudaFree(d);
     if (e != cudaSuccess) return cuda_fail(e, "self-test");
+    return SWR_OK;
+}
+
+swr_status swr_selftest_depth_floor(const int32_t* p, const float* zow, const float* oow, int32_t xe, int32_t ye,
+                                    float* zlo) {
+    if (!p || !zow || !oow || !zlo) return fail(SWR_INVALID_ARG, "null argument");
+    float z = 0.0f;
+    *zlo = depth_floor_host(p, zow, oow, xe, ye, z) ? z : -std::numeric_limits<float>::infinity();
     return SWR_OK;
 }
 

@@ -314,6 +314,9 @@ void launch_reset(const FrameArgs& a, void* stream);
 void launch_resolve(const FrameArgs& a, void* stream);
 // rsqrt of n device values in the given mode (table: the 512-byte FRSQRTE table).
 cudaError_t launch_rsqrt_selftest(const float* in, float* out, uint64_t n, uint32_t mode, const uint8_t* table);
+// The raster's occlusion-culling depth floor evaluated on the host (the
+// device code's source compiled for the host).
+bool depth_floor_host(const int32_t p[6], const float zow[3], const float oow[3], int32_t xe, int32_t ye, float& zlo);
 // Per-device constant tables; call once per device outside stream capture.
 cudaError_t init_kernel_constants();
 // Persistent raster / grid-stride shading grid sizes for this device.

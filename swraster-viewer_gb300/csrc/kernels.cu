@@ -33,6 +33,7 @@
 #include <algorithm>
 #include <cstdint>
 
+#include "depthfloor.cuh"
 #include "devmath.cuh"
 #include "internal.h"
 
@@ -1306,79 +1307,8 @@ __device__ __forceinline__ void raster_slow_region(RasterShared<S>& s, const Fra
 // winning a tie needs an equal depth), so it is dropped in pass 1: the keys
 // come out as if it had been rasterized. (Testing each 16-px block of a
 // coarse packet as well dropped 15% more pairs but made the 4K raster 6%
-// slower.) The floor
-// on the depths a packet can produce covers every rounding of the raster's
-// arithmetic (u = 2^-24):
-//  - edge values: the origin evaluation (a x + b y) + c and at most 16
-//    sequential additions err by at most 24u (|a| X + |b| Y + |c| +
-//    256 (|a| + |b|)) per edge, X and Y the largest sample coordinates. A
-//    covered lane has all three computed edge values >= 0 and the exact values
-//    sum to the doubled area A plus top-left biases (<= 0), so b1, b2 >= 0 and
-//    b1 + b2 <= B = (1 + (sum of the three errors) / A)(1 + u)^3;
-//  - zi and oi are three-term sums, within EZ = 5u (|Z0| + B |D1| + B |D2|)
-//    (EO likewise) of the exact affine values, and z = zi * (1 / oi) adds two
-//    roundings;
-//  - (exact zi - EZ) / (exact oi +- EO) is a ratio of affine functions of
-//    (b1, b2) with a positive denominator, so its minimum over the triangle
-//    {b1, b2 >= 0, b1 + b2 <= B} is at a corner; corners are evaluated with
-//    directed rounding.
-// Packets whose int32 setup arithmetic could have wrapped, whose 1/w
-// interpolant could reach 0, with non-finite inputs or with B > 1.5 are kept.
-constexpr float kUlp24 = 5.9604645e-8f;  // 2^-24
-
-// Error bound of one edge's computed values over the packet (false: the
-// edge's integer terms could have wrapped or lost exactness).
-__device__ __forceinline__ bool edge_error(long long xi, long long yi, long long xj, long long yj, float X, float Y,
-                                           float& err) {
-    const long long a = yj - yi, b = xi - xj, c = xj * yi - xi * yj;
-    const long long lim = 1ll << 24, climb = (1ll << 31) - 2;
-    if (a > lim || a < -lim || b > lim || b < -lim || c > climb || c < -climb) return false;
-    const float fa = fabsf((float)a), fb = fabsf((float)b), fc = fabsf((float)c) + 1.0f;
-    err = (32.0f * kUlp24) * (((fa * X + fb * Y) + fc) + 256.0f * (fa + fb));
-    return true;
-}
-
-// Lower bound of every depth the raster can compute for a covered lane of the
-// packet; false when no bound is taken.
-__device__ bool packet_depth_floor(const PacketCtx& c, float& zlo) {
-    const int32_t* p = c.r.p;
-#pragma unroll
-    for (int i = 0; i < 6; ++i)
-        if (p[i] > (1 << 28) || p[i] < -(1 << 28)) return false;
-    const long long x0 = p[0], y0 = p[1], x1 = p[2], y1 = p[3], x2 = p[4], y2 = p[5];
-    const long long area = (x1 - x0) * (y2 - y0) - (x2 - x0) * (y1 - y0);
-    if (area >= 0 || area <= -(1ll << 31)) return false;
-    const float X = (float)(c.xe + 32), Y = (float)(c.ye + 32);
-    float e12, e20, e01;
-    if (!edge_error(x1, y1, x2, y2, X, Y, e12) || !edge_error(x2, y2, x0, y0, X, Y, e20) ||
-        !edge_error(x0, y0, x1, y1, X, Y, e01))
-        return false;
-    const float A = (float)(-area) * (1.0f - 2.0f * kUlp24);
-    const float rel = ((e12 + e20) + e01) / A;
-    if (!(rel < 0.25f)) return false;
-    const float B = __fadd_ru(1.0f, __fmul_ru(rel + 8.0f * kUlp24, 1.125f));
-    const float Z0 = c.r.zow[0], D1 = c.r.zow[1], D2 = c.r.zow[2];
-    const float O0 = c.r.oow[0], P1 = c.r.oow[1], P2 = c.r.oow[2];
-    if (!(isfinite(Z0) && isfinite(D1) && isfinite(D2) && isfinite(O0) && isfinite(P1) && isfinite(P2))) return false;
-    const float EZ = (5.0f * kUlp24) * (fabsf(Z0) + B * (fabsf(D1) + fabsf(D2))) + 1e-30f;
-    const float EO = (5.0f * kUlp24) * (fabsf(O0) + B * (fabsf(P1) + fabsf(P2))) + 1e-30f;
-    if (!(isfinite(EZ) && isfinite(EO))) return false;
-    float lo = __int_as_float(0x7F800000);
-#pragma unroll
-    for (int v = 0; v < 3; ++v) {
-        const float dz = v == 1 ? D1 : D2, dw = v == 1 ? P1 : P2;
-        const float zc = v == 0 ? Z0 : __fadd_rd(Z0, __fmul_rd(B, dz));
-        const float wlo = v == 0 ? O0 : __fadd_rd(O0, __fmul_rd(B, dw));
-        const float whi = v == 0 ? O0 : __fadd_ru(O0, __fmul_ru(B, dw));
-        const float n = __fsub_rd(zc, EZ);
-        const float dlo = __fsub_rd(wlo, EO), dhi = __fadd_ru(whi, EO);
-        if (!(dlo > 0.0f) || !isfinite(n)) return false;
-        lo = fminf(lo, fminf(__fdiv_rd(n, dhi), __fdiv_rd(n, dlo)));
-    }
-    lo = lo >= 0.0f ? __fmul_rd(lo, 1.0f - 4.0f * kUlp24) : __fmul_rd(lo, 1.0f + 4.0f * kUlp24);
-    zlo = __fsub_rd(lo, 1e-30f);
-    return zlo == zlo;
-}
+// slower.) The floor on a packet's depths, and the argument that it covers
+// every rounding of the raster's arithmetic, are in depthfloor.cuh.
 
 // Farthest key depth of each 8x8-px cell (four threads per cell, two rows
 // each), then a barrier.
@@ -1427,7 +1357,7 @@ __device__ __forceinline__ uint32_t cells_far(const RasterShared<S>& s, int32_t 
 // its covered lanes can fall in: pixels [x0 & ~1, x1] of its clipped rect.
 __device__ __forceinline__ uint32_t packet_floor(const PacketCtx& c) {
     float z;
-    return packet_depth_floor(c, z) ? float_to_ordered(z) : 0u;
+    return depth_floor(c.r.p, c.r.zow, c.r.oow, c.xe, c.ye, z) ? float_to_ordered(z) : 0u;
 }
 
 // Pass 1 of a round for one packet: classify and split into regions, and
@@ -2433,6 +2363,10 @@ void launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t* ev
         }
         if (!a.defer_resolve) launch_resolve(a, stream);
     }
+}
+
+bool depth_floor_host(const int32_t p[6], const float zow[3], const float oow[3], int32_t xe, int32_t ye, float& zlo) {
+    return depth_floor(p, zow, oow, xe, ye, zlo);
 }
 
 cudaError_t launch_rsqrt_selftest(const float* in, float* out, uint64_t n, uint32_t mode, const uint8_t* table) {

@@ -182,7 +182,7 @@ EXPORTS = [
     "swr_batch_create", "swr_batch_destroy", "swr_batch_render", "swr_batch_sync", "swr_batch_output",
     "swr_batch_autotune", "swr_batch_last_ms", "swr_server_create", "swr_server_destroy", "swr_server_add_scene",
     "swr_server_submit", "swr_server_poll", "swr_server_release", "swr_server_get_stats", "swr_copy_to_host",
-    "swr_selftest_rsqrt", "swr_scene_load_gltf",
+    "swr_selftest_rsqrt", "swr_scene_load_gltf", "swr_selftest_depth_floor",
 ]
 STAGES = ["draws", "frontend", "clip", "scan", "scatter", "raster", "shade", "resolve"]
 
@@ -220,6 +220,7 @@ def lib():
         "swr_renderer_set_profiling": ([vp, C.c_int32], C.c_int),
         "swr_renderer_get_profile": ([vp, f32p, C.c_int32, C.POINTER(C.c_uint32)], C.c_int),
         "swr_selftest_rsqrt": ([f32p, f32p, C.c_uint64, C.c_uint32], C.c_int),
+        "swr_selftest_depth_floor": ([C.c_void_p, f32p, f32p, C.c_int32, C.c_int32, f32p], C.c_int),
         "swr_scene_load_gltf": ([C.c_char_p, C.POINTER(GltfOpts), C.POINTER(vp)], C.c_int),
         "swr_render_frame_noalloc": ([vp, C.POINTER(Camera), C.c_int32, C.c_int32, C.c_float, C.c_uint32, vp, vp, vp],
                                      C.c_int),
@@ -485,6 +486,18 @@ def selftest_rsqrt(values, mode=RSQRT_AARCH64):
     out = np.empty_like(x)
     check(lib().swr_selftest_rsqrt(x.ctypes.data_as(f32p), out.ctypes.data_as(f32p), x.size, mode))
     return out
+
+
+def selftest_depth_floor(p, zow, oow, xe, ye):
+    """Occlusion-culling depth floor of one packet, evaluated on the host by
+    the raster's own source; -inf when no floor is taken."""
+    p = np.ascontiguousarray(p, np.int32)
+    zow = np.ascontiguousarray(zow, np.float32)
+    oow = np.ascontiguousarray(oow, np.float32)
+    z = np.zeros(1, np.float32)
+    check(lib().swr_selftest_depth_floor(p.ctypes.data, zow.ctypes.data_as(f32p), oow.ctypes.data_as(f32p), xe, ye,
+                                         z.ctypes.data_as(f32p)))
+    return float(z[0])
 
 
 def copy_device_to_host(dev_ptr, nbytes, out, stream=None):
