@@ -1479,12 +1479,16 @@ __global__ void __launch_bounds__(RasterShared<S>::kThreads, RasterShared<S>::kM
         const bool bad = (a.counters->status & (ST_BIN_OVERFLOW | ST_CLIP_OVERFLOW | ST_QUEUE_OVERFLOW)) != 0u;
         const uint32_t b0 = a.tile_offset[st], b1 = bad ? b0 : a.tile_offset[st + 1];
         const DScene& sc = a.scenes[view.scene];
-        bool keys_changed = false;  // a round since the last cell_depths had regions
+        // Cell depths are valid once taken for this tile (until then they
+        // hold another tile's, or nothing); they are taken again after a
+        // round that had regions.
+        bool keys_changed = false, cells_valid = false;
         for (uint32_t cursor = b0; cursor < b1;) {
             // The keys the previous rounds left, per cell, for occlusion culling.
             if (kCull && keys_changed) {
                 cell_depths<S>(s);
                 keys_changed = false;
+                cells_valid = true;
             }
             const uint32_t lim = cursor == b0 ? kFirst : (uint32_t)NT;
             // Pass 1: count this thread's regions and quads.
@@ -1504,7 +1508,7 @@ __global__ void __launch_bounds__(RasterShared<S>::kThreads, RasterShared<S>::kM
                     asm volatile("prefetch.global.L2 [%0];" ::"l"(np + sizeof(RecRaster) - 1));
                 }
 #endif
-                if (kCull && cursor != b0) {
+                if (kCull && cells_valid) {
                     const uint32_t far = cells_far<S>(s, c.xs >> kSubpixelShift, c.xe >> kSubpixelShift,
                                                       c.ys >> kSubpixelShift, c.ye >> kSubpixelShift, sx0, sy0);
                     hidden = far < 0xFF800000u && packet_floor(c) > far;
