@@ -15,6 +15,8 @@
 #include <string>
 #include <vector>
 
+#include <sys/stat.h>
+
 #include "../../include/swr.h"
 #include "hostmath.h"
 #include "imagedec.h"
@@ -28,6 +30,13 @@ namespace {
 using json::Value;
 
 bool read_file(const std::string& path, std::vector<uint8_t>& out, std::string& err) {
+    // Regular files only: a directory opens for reading on Linux and reports
+    // a size of LONG_MAX.
+    struct stat st;
+    if (::stat(path.c_str(), &st) != 0 || !S_ISREG(st.st_mode)) {
+        err = "cannot open '" + path + "'";
+        return false;
+    }
     FILE* f = std::fopen(path.c_str(), "rb");
     if (!f) {
         err = "cannot open '" + path + "'";
@@ -170,6 +179,15 @@ bool read_accessor(const Doc& d, int64_t idx, int want_comps, std::vector<double
         err = "unsupported accessor layout";
         return false;
     }
+    // Elements come from a bufferView and/or sparse substitutions, each read
+    // from the document's buffers; no accessor can hold more elements than
+    // the buffers have bytes, so larger counts are malformed.
+    size_t total_bytes = 0;
+    for (const std::vector<uint8_t>& b : d.buffers) total_bytes += b.size();
+    if ((uint64_t)count > (uint64_t)total_bytes) {
+        err = "accessor count beyond the document's buffers";
+        return false;
+    }
     out.assign((size_t)count * nc, 0.0);
     auto read_view = [&](int64_t view_idx, size_t byte_off, size_t n, int ncomp, int64_t ctype, bool norm,
                          const std::function<void(size_t, int, double)>& put) -> bool {
@@ -185,11 +203,21 @@ bool read_accessor(const Doc& d, int64_t idx, int want_comps, std::vector<double
             return false;
         }
         const std::vector<uint8_t>& buf = d.buffers[(size_t)bi];
-        const size_t voff = (size_t)json::integer(v->get("byteOffset"), 0);
-        const size_t vlen = (size_t)json::integer(v->get("byteLength"), 0);
+        const int64_t voff_i = json::integer(v->get("byteOffset"), 0);
+        const int64_t vlen_i = json::integer(v->get("byteLength"), 0);
+        const int64_t stride_i = json::integer(v->get("byteStride"), 0);
         const size_t elem = comp_size(ctype) * (size_t)ncomp;
-        const size_t stride = (size_t)json::integer(v->get("byteStride"), 0) ? (size_t)json::integer(v->get("byteStride"), 0) : elem;
-        if (voff + vlen > buf.size() || (n && byte_off + (n - 1) * stride + elem > vlen)) {
+        // Every term checked against the buffer before it is combined, so no
+        // sum or product below can wrap.
+        if (elem == 0 || voff_i < 0 || vlen_i < 0 || stride_i < 0 || (uint64_t)voff_i > buf.size() ||
+            (uint64_t)vlen_i > buf.size() - (size_t)voff_i || (uint64_t)stride_i > buf.size()) {
+            err = "accessor reads past its buffer";
+            return false;
+        }
+        const size_t voff = (size_t)voff_i, vlen = (size_t)vlen_i;
+        const size_t stride = stride_i ? (size_t)stride_i : elem;
+        if (n && (byte_off > vlen || elem > vlen - byte_off ||
+                  (n - 1 > 0 && (n - 1) > (vlen - byte_off - elem) / stride))) {
             err = "accessor reads past its buffer";
             return false;
         }
@@ -208,7 +236,7 @@ bool read_accessor(const Doc& d, int64_t idx, int want_comps, std::vector<double
         const int64_t sc = json::integer(sp->get("count"), 0);
         const Value* si = sp->get("indices");
         const Value* sv = sp->get("values");
-        if (!si || !sv) {
+        if (!si || !sv || sc < 0 || sc > count) {
             err = "bad sparse accessor";
             return false;
         }

@@ -638,11 +638,15 @@ bool decode_jpeg(const uint8_t* d, size_t n, uint32_t& w, uint32_t& h, std::vect
                 return false;
             }
             for (int k = 0; k < ns; ++k) {
-                const int cid = s[1 + 2 * k];
+                const int cid = s[1 + 2 * k], td = s[2 + 2 * k] >> 4, ta = s[2 + 2 * k] & 15;
+                if (td > 3 || ta > 3) {
+                    err = "jpeg: bad Huffman table id";
+                    return false;
+                }
                 for (JComp& c : comps)
                     if (c.id == cid) {
-                        c.td = s[2 + 2 * k] >> 4;
-                        c.ta = s[2 + 2 * k] & 3;
+                        c.td = td;
+                        c.ta = ta;
                     }
             }
             for (JComp& c : comps)

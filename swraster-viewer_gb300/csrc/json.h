@@ -36,8 +36,12 @@ struct Value {
 // Convenience lookups on a possibly-null value.
 inline const Value* get(const Value* v, const char* key) { return v ? v->get(key) : nullptr; }
 inline double num(const Value* v, double d) { return v ? v->num_or(d) : d; }
+// Out-of-range and non-finite numbers give INT64_MIN, which every index,
+// count and offset check rejects.
 inline int64_t integer(const Value* v, int64_t d) {
-    return (v && v->kind == Value::Number) ? (int64_t)v->num : d;
+    if (!v || v->kind != Value::Number) return d;
+    if (!(v->num >= -9.0e18 && v->num <= 9.0e18)) return INT64_MIN;
+    return (int64_t)v->num;
 }
 inline std::string string(const Value* v, const char* d = "") {
     return (v && v->kind == Value::String) ? v->str : std::string(d);

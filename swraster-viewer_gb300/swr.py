@@ -258,7 +258,7 @@ class SwrError(RuntimeError):
 
 def check(st):
     if st != SWR_OK:
-        raise SwrError(st, lib().swr_last_error().decode())
+        raise SwrError(st, lib().swr_last_error().decode(errors="replace"))
 
 
 def _fp(a):

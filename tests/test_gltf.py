@@ -307,6 +307,49 @@ def test_loader_errors(tmp_path):
     assert e.value.status == swr.SWR_INVALID_ARG
 
 
+def test_malformed_documents_are_rejected(tmp_path):
+    """Malformed inputs found by fuzzing the loader under AddressSanitizer:
+    each is an error, never an out-of-bounds read or a runaway allocation."""
+    rng = np.random.default_rng(6)
+    # A bufferView offset below zero (its sum with the length used to wrap).
+    b, _, _ = build_doc(str(tmp_path), rng)
+    b.doc["bufferViews"][0]["byteOffset"] = -8
+    expect_error(b.write(str(tmp_path / "negoff"), "glb"), swr.SWR_BAD_SCENE, "past its buffer")
+    # A stride so large the last element's offset would wrap.
+    b, _, _ = build_doc(str(tmp_path), rng)
+    b.doc["bufferViews"][0]["byteStride"] = 2 ** 62
+    expect_error(b.write(str(tmp_path / "stride"), "glb"), swr.SWR_BAD_SCENE, "past its buffer")
+    # Counts beyond the document's bytes, and numbers beyond int64.
+    for count in (10 ** 12, 1e300):
+        b, _, _ = build_doc(str(tmp_path), rng)
+        b.doc["accessors"][0]["count"] = count
+        with pytest.raises(swr.SwrError):
+            load(b.write(str(tmp_path / "count"), "data"))
+    # A buffer URI naming a directory.
+    (tmp_path / "dir.bin").mkdir()
+    b, _, _ = build_doc(str(tmp_path), rng)
+    doc = b.write(str(tmp_path / "dirbuf"), "bin")
+    text = open(doc).read().replace("geom%20data.bin", "dir.bin")
+    open(doc, "w").write(text)
+    expect_error(doc, swr.SWR_IO_ERROR, "cannot open")
+    # A JPEG scan naming Huffman table 15 (tables are 0-3).
+    rgb = rng.integers(0, 256, (16, 16, 3)).astype(np.uint8)
+    write_jpeg(str(tmp_path / "t.jpg"), rgb)
+    data = bytearray((tmp_path / "t.jpg").read_bytes())
+    sos = data.index(b"\xff\xda")
+    data[sos + 6] = 0xF0  # first component: DC table 15
+    (tmp_path / "t.jpg").write_bytes(bytes(data))
+    b = DocBuilder()
+    tri = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    b.doc["meshes"] = [{"primitives": [{"attributes": {"POSITION": b.accessor(tri, 5126, "VEC3")},
+                                        "indices": b.accessor(np.array([0, 1, 2], np.uint16), 5123, "SCALAR")}]}]
+    b.doc["nodes"] = [{"mesh": 0}]
+    b.doc["images"] = [{"uri": "t.jpg"}]
+    b.doc["textures"] = [{"source": 0}]
+    b.doc["materials"] = [{"pbrMetallicRoughness": {"baseColorTexture": {"index": 0}}}]
+    expect_error(b.write(str(tmp_path / "j"), "bin"), swr.SWR_IO_ERROR, "huffman table id")
+
+
 @pytest.mark.gpu
 def test_loaded_scene_renders_like_the_oracle(tmp_path):
     # A loaded document (alpha-masked textured quad, translucent sphere,
