@@ -171,10 +171,10 @@ typedef struct swr_scene_desc {
     /* Environment cubemap faces in +X,-X,+Y,-Y,+Z,-Z order, each
      * size*size RGBA8 (the unpacked cross of src/texture.rs:922-971). */
     uint32_t cubemap_face_size;
-    uint32_t voxel_grid_size;   /* 128 in the reference (src/main.rs:228) */
+    uint32_t voxel_grid_size;   /* 128 in the reference (src/main.rs:228); at most 1024 */
     const uint32_t* cubemap_faces;
-    uint32_t specular_samples;  /* GGX prefilter samples, 64 (src/scene.rs:179) */
-    uint32_t brdf_lut_size;     /* 128 (src/scene.rs:221) */
+    uint32_t specular_samples;  /* GGX prefilter samples, 64 (src/scene.rs:179); at most 65536 */
+    uint32_t brdf_lut_size;     /* 128 (src/scene.rs:221); at most 4096 */
     float gi_sh_scale;          /* 0.25 (src/main.rs:54) */
     float sky_visibility;       /* 1.0 (src/main.rs:280) */
     uint32_t host_threads;      /* precompute threads, 0 = all cores */

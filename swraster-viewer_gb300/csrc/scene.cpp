@@ -931,6 +931,13 @@ swr_status build_scene(const swr_scene_desc* desc, SceneImpl* s, std::string& er
         err = "cubemap faces missing";
         return SWR_INVALID_ARG;
     }
+    // Load-time tables grow with the square or cube of these sizes; past
+    // these limits a descriptor asks for more memory than any scene needs.
+    if (desc->cubemap_face_size > 16384u || desc->brdf_lut_size > 4096u || desc->voxel_grid_size > 1024u ||
+        desc->specular_samples > 65536u) {
+        err = "cubemap_face_size, brdf_lut_size, voxel_grid_size or specular_samples out of range";
+        return SWR_INVALID_ARG;
+    }
     s->cubemap = make_texture(desc->cubemap_face_size, desc->cubemap_face_size, SWR_TEX_CUBEMAP, desc->cubemap_faces, true);
     s->cubemap.generate_mipmaps();
     s->specular = generate_prefiltered_specular(s->cubemap, desc->specular_samples ? desc->specular_samples : 64u, threads);

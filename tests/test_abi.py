@@ -54,6 +54,13 @@ def test_bad_scene_is_rejected():
     sd["materials"][0]["base_color"] = (5, 0, 0)
     with pytest.raises(swr.SwrError):
         swr.Scene(sd, host_only=True)
+    # Load-time table sizes past their limits (a 2^20 BRDF LUT would be 4 TB).
+    for key, value in (("brdf_lut_size", 1 << 20), ("voxel_grid_size", 4097), ("specular_samples", 1 << 31)):
+        sd = scenes.small_scene()
+        sd[key] = value
+        with pytest.raises(swr.SwrError) as e:
+            swr.Scene(sd, host_only=True)
+        assert e.value.status == swr.SWR_INVALID_ARG
 
 
 def test_host_only_scene_export():
