@@ -1,7 +1,8 @@
 #!/usr/bin/env python3
-"""4K frames/s of the plain per-frame rasterization path on GB300.
+"""4K frames/s of the plain per-frame rasterization path on GB300, with the
+small, batched, heterogeneous and served workloads beside it.
 
-Workload (default): 2,000,000 triangles in seeded icospheres and displaced
+Headline workload: 2,000,000 triangles in seeded icospheres and displaced
 grids (per-object triangle screen area log-uniform over 0.5-5000 px, ~15% of
 objects straddling the near plane or a frustum side), 8 value-noise textures
 of 2048^2 with full mip chains, one 3840x2160 view. Seeded synthetic data:
@@ -9,11 +10,24 @@ no glTF sample assets exist on this machine.
 
 A step is one frame: render_scene + update_auto_exposure(dt = 0) + resolve to
 RGBA8 and the visibility buffer, all resident in HBM (`value`). `e2e` is the
-same metric through the C ABI with host buffers: every step also copies the
-RGBA8 frame and the visibility buffer into pinned host memory.
+same metric through the C ABI with host buffers: every step is
+swr_render_frame + swr_blit, with the per-frame tables uploaded and the
+RGBA8 frame (the reference's blit_to_buffer output) landing in pinned host
+memory; the visibility buffer stays on the device.
+
+Beside the headline (default run, one GPU), in the same JSON line:
+  small   - the 81,920-triangle sphere scene at 1280x720 through the plain path;
+  batched - 64 views of that scene at mixed resolutions in one graph-replayed
+            launch sequence, against the same views as sequential plain frames;
+  hetero  - 16 seeded scenes of 10k-4M triangles, one view each, in one launch
+            sequence, against 16 sequential plain frames;
+  served  - Poisson requests over 8 resident scenes: p50/p99 at fixed rates,
+            and the most frames/s each side sustains at equal p99 bounds
+            (bisection on the arrival rate), served form vs the plain loop.
 
 --impl reference times the CPU restatement of the reference's rayon path (the
-oracle) on the host cores over the same workload.
+oracle, which builds the scene and camera itself) on the host cores over the
+same workload.
 
 Multi-GPU: frames are independent, so N GPUs run N replicas (weak scaling, no
 collective on the data path); rank 0 prints the line.
@@ -30,8 +44,6 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "swraster-viewer_gb300"))
 
-KERNELS_PER_FRAME = 7  # reset, frontend, clip, scan, scatter, raster, shade
-
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -42,6 +54,7 @@ def parse():
     ap.add_argument("--workload", default="4k", choices=["4k", "small"])
     ap.add_argument("--cpu-frames", type=int, default=3, help="frames in the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-sub", action="store_true", help="plain mode: skip the small/batched/hetero/served blocks")
     ap.add_argument("--sched-tile", type=int, default=0,
                     help="raster scheduling tile (8, 16, 32, 64; 0 = the library's choice for the frame size)")
     ap.add_argument("--fused-shade", action="store_true",
@@ -51,12 +64,13 @@ def parse():
     ap.add_argument("--mode", default="plain", choices=["plain", "batched", "hetero", "served"],
                     help="plain: 4K per-frame path (the headline); batched: 64 views of the 81,920-triangle scene "
                          "in one launch; hetero: 16 heterogeneous scenes in one launch; served: request loop")
-    ap.add_argument("--rates", default="100,500,1000,2000,3000,5000", help="served arrival rates (requests/s)")
+    ap.add_argument("--rates", default="1000,3000,5000", help="served arrival rates (requests/s)")
+    ap.add_argument("--bounds", default="50,100", help="served: p99 bounds (ms) for the equal-p99 comparison")
     ap.add_argument("--inflight", type=int, default=3, help="served: batches in flight (one engine and stream each)")
     ap.add_argument("--max-batch", type=int, default=64, help="served: views per batch")
     ap.add_argument("--no-graph", dest="graph", action="store_false",
                     help="served: launch each batch's kernels directly instead of replaying a captured graph")
-    ap.add_argument("--seconds", type=float, default=2.0, help="served: arrival window per rate")
+    ap.add_argument("--seconds", type=float, default=1.5, help="served: arrival window per rate")
     ap.add_argument("--max-tris", type=int, default=0, help="hetero/served: cap on triangles per scene")
     return ap.parse_args()
 
@@ -107,7 +121,7 @@ def peaks():
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling during a timed region."""
 
     def __init__(self, index):
         self.index = index
@@ -161,25 +175,27 @@ class Clocks:
 
 def cpu_baseline(sd, cam_params, cfg, frames, threads=None, warmup=1):
     """The oracle (CPU restatement of the reference's rayon path) on all host
-    cores over a bounded sample of the same workload."""
+    cores over a bounded sample of the same workload. The oracle builds the
+    scene (load-time tables) and the camera itself; the product's library is
+    not loaded."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     import scenes
-    import swr
     oracle.build()
     threads = threads or os.cpu_count()
-    s = swr.Scene(sd, host_only=True)
-    cam = swr.make_camera(*cam_params) if cam_params else swr.make_camera(
-        *scenes.default_camera_params(s.info(), cfg["width"], cfg["height"]))
-    view = s.export()
+    s = oracle.Scene(sd, threads=threads)
+    if cam_params is None:
+        _, _, c, diag = s.bounds
+        cam_params = scenes.default_camera_params(scenes.Bounds(c, diag), cfg["width"], cfg["height"])
+    cam = oracle.camera(*cam_params)
     for _ in range(warmup):
-        oracle.render(view, cam, cfg["width"], cfg["height"], threads=threads)
+        oracle.render(s, cam, cfg["width"], cfg["height"], threads=threads)
     t0 = time.perf_counter()
     for _ in range(frames):
-        oracle.render(view, cam, cfg["width"], cfg["height"], threads=threads)
+        oracle.render(s, cam, cfg["width"], cfg["height"], threads=threads)
     dt = time.perf_counter() - t0
     s.close()
-    return frames / dt, threads, "%d frames of the full workload" % frames
+    return frames / dt, threads, "%d frames of the full workload (scene and camera built by the oracle)" % frames
 
 
 def run_reference(args):
@@ -215,7 +231,7 @@ def _timed(torch, fn, reps):
     return e0.elapsed_time(e1) / reps
 
 
-def run_batched(args, hetero):
+def measure_batched(args, hetero, steps, local=0):
     """One launch sequence for many views vs the same views rendered one per
     frame by the plain path, on the same GPU."""
     import numpy as np
@@ -224,16 +240,19 @@ def run_batched(args, hetero):
     import swr
     sh = torch.cuda.current_stream().cuda_stream
     rng = np.random.default_rng(3)
+    owned = []
     if hetero:
         items = []
         for sd, cp in scenes.hetero_scenes(max_triangles=args.max_tris or None):
             s = swr.Scene(sd)
+            owned.append(s)
             items.append((s, swr.make_camera(*cp), cp[3], cp[4]))
         cfg = {"workload": "16 heterogeneous scenes (10k-4M triangles log-uniform, 1-8 textures of 512-2048 px), "
                            "one view each at 640x480-3840x2160, all in one launch",
                "views": len(items), "triangles": int(sum(s.info().triangle_count for s, *_ in items))}
     else:
         s = swr.Scene(scenes.spheres_scene())
+        owned.append(s)
         res = [(320, 240), (640, 480), (1280, 720), (1920, 1080)]
         items = []
         for i in range(64):
@@ -249,37 +268,41 @@ def run_batched(args, hetero):
     for _ in range(max(3, args.warmup)):
         b.render(arr, sh)
     b.sync()
+
     def one():
         b.render(arr, sh)
-    ms_batch = _timed(torch, one, args.steps)
+
+    clocks = Clocks(local)
+    clocks.start()
+    ms_batch = _timed(torch, one, steps)
+    clk = clocks.stop()
     b.sync()
     # Plain path: one renderer per resolution, views one after another.
     rends = {}
     for sc, cam, w, h in items:
         if (w, h) not in rends:
             rends[(w, h)] = swr.Renderer(w, h)
+
     def seq():
         for sc, cam, w, h in items:
             rends[(w, h)].render(sc, cam, 0.0, sh)
+
     for _ in range(2):
         seq()
-    ms_seq = _timed(torch, seq, max(3, args.steps // 4))
+    ms_seq = _timed(torch, seq, max(3, steps // 4))
     for r in rends.values():
         r.close()
-    n = len(items)
-    line = {"metric": "batched views/s", "value": n / (ms_batch / 1000.0), "unit": "views/s", "n_gpus": 1,
-            "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms_batch,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": dict(cfg, sched_tile=tile, graph=True),
-            "plain_sequential": {"value": n / (ms_seq / 1000.0), "unit": "views/s", "ms_per_batch": ms_seq},
-            "speedup_vs_plain": ms_seq / ms_batch, "gpix_per_s": px / (ms_batch / 1000.0) / 1e9,
-            "gpu_launches": KERNELS_PER_FRAME * args.steps}
-    print(json.dumps(line), flush=True)
     b.close()
-    return 0
+    for s in owned:
+        s.close()
+    n = len(items)
+    return {"metric": "views/s", "value": n / (ms_batch / 1000.0), "unit": "views/s", "steps": steps,
+            "ms_per_step": ms_batch, "config": dict(cfg, sched_tile=tile, graph=True), "clocks": clk,
+            "plain_sequential": {"value": n / (ms_seq / 1000.0), "unit": "views/s", "ms_per_batch": ms_seq},
+            "speedup_vs_plain": ms_seq / ms_batch, "gpix_per_s": px / (ms_batch / 1000.0) / 1e9}
 
 
-def run_served(args):
+def measure_served(args, local=0):
     """Poisson request stream over 8 resident scenes: served form (continuous
     batching) vs the plain per-frame path (one request at a time, FIFO)."""
     import threading
@@ -289,30 +312,33 @@ def run_served(args):
     import swr
     sh = torch.cuda.current_stream().cuda_stream
     scs = [swr.Scene(sd) for sd, _ in scenes.hetero_scenes(seed=31, count=8, max_triangles=args.max_tris or None)]
+    infos = [s.info() for s in scs]
     res = [(640, 480), (1280, 720), (1920, 1080), (3840, 2160)]
     srv = swr.Server(memory_budget=40 << 30, max_batch_views=args.max_batch, inflight=args.inflight,
                      use_graph=args.graph, sched_tile=args.sched_tile, fused_shade=args.fused_shade)
     ids = [srv.add_scene(s) for s in scs]
     rends = {r: swr.Renderer(r[0], r[1]) for r in res}
-    results = {}
-    for rate in [float(x) for x in args.rates.split(",")]:
+
+    def requests(rate, seconds):
         rng = np.random.default_rng(int(rate))
-        n = max(20, min(int(rate * args.seconds), 4000))
+        n = max(20, min(int(rate * seconds), 6000))
         gaps = rng.exponential(1.0 / rate, n)
         reqs = []
         for i in range(n):
             k = int(rng.integers(len(scs)))
             w, h = res[int(rng.integers(len(res)))]
-            cam = swr.make_camera(*scenes.sphere_camera(rng, scs[k].info(), w, h, 0.7 * scs[k].info().bounds_diagonal,
-                                                        1.5 * scs[k].info().bounds_diagonal))
+            d = infos[k].bounds_diagonal
+            cam = swr.make_camera(*scenes.sphere_camera(rng, infos[k], w, h, 0.7 * d, 1.5 * d))
             reqs.append((k, cam, w, h))
-        # Served.
-        lat = []
-        bviews = []
-        done = [0]
+        return reqs, gaps
+
+    def served_at(rate, seconds):
+        reqs, gaps = requests(rate, seconds)
+        n = len(reqs)
+        lat, bviews = [], []
+
         def submit():
-            t0 = time.perf_counter()
-            t = t0
+            t = time.perf_counter()
             for i, (k, cam, w, h) in enumerate(reqs):
                 t += gaps[i]
                 d = t - time.perf_counter()
@@ -320,20 +346,26 @@ def run_served(args):
                     time.sleep(d)
                 while srv.submit(ids[k], cam, w, h, 2.0, tag=i) is None:
                     time.sleep(0.0005)
+
         th = threading.Thread(target=submit)
         t_start = time.perf_counter()
         th.start()
-        while done[0] < n:
+        done = 0
+        while done < n:
             for c in srv.poll(256, wait_ms=5):
                 lat.append(c.latency_ms)
                 bviews.append(c.batch_views)
                 srv.release(c.ticket)
-                done[0] += 1
+                done += 1
         t_end = time.perf_counter()
         th.join()
-        served = {"completed": n, "frames_per_s": n / (t_end - t_start), "p50_ms": float(np.percentile(lat, 50)),
-                  "p99_ms": float(np.percentile(lat, 99)), "mean_batch_views": float(np.mean(bviews))}
-        # Plain path: the same arrivals, served one at a time in order.
+        return {"rate": rate, "completed": n, "frames_per_s": n / (t_end - t_start),
+                "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "mean_batch_views": float(np.mean(bviews))}
+
+    def plain_at(rate, seconds):
+        reqs, gaps = requests(rate, seconds)
+        n = len(reqs)
         plat = []
         t0 = time.perf_counter()
         arr_t = t0 + np.cumsum(gaps)
@@ -346,67 +378,86 @@ def run_served(args):
             r.sync()
             plat.append((time.perf_counter() - arr_t[i]) * 1000.0)
         t1 = time.perf_counter()
-        plain = {"frames_per_s": n / (t1 - t0), "p50_ms": float(np.percentile(plat, 50)),
-                 "p99_ms": float(np.percentile(plat, 99))}
-        results[str(int(rate))] = {"served": served, "plain": plain}
-    st = srv.stats()
-    line = {"metric": "served frames/s + p99 latency vs plain GPU", "unit": "frames/s", "n_gpus": 1,
-            "config": {"workload": "8 resident scenes (10k-4M triangles), Poisson arrivals, random scene, camera on "
-                                   "a sphere, resolution from {640x480, 1280x720, 1920x1080, 3840x2160}, 40 GB "
-                                   "budget, continuous batching",
-                       "triangles": int(sum(s.info().triangle_count for s in scs)), "inflight": args.inflight,
-                       "max_batch_views": args.max_batch, "graph": bool(args.graph),
-                       "sched_tile": args.sched_tile, "fused_shade": bool(args.fused_shade)},
-            "rates": results, "batches": st.batches, "device_bytes": st.device_bytes, "data": "synthetic"}
-    best_served = max((v["served"]["frames_per_s"] for v in results.values()), default=0.0)
-    best_plain = max((v["plain"]["frames_per_s"] for v in results.values()), default=0.0)
-    line["value"] = best_served
-    line["plain_max_frames_per_s"] = best_plain
-    line["speedup_vs_plain"] = best_served / best_plain if best_plain else None
-    # Equal p99: the most frames/s each side delivered at a rate whose p99
-    # latency stayed within the bound.
+        return {"rate": rate, "frames_per_s": n / (t1 - t0), "p50_ms": float(np.percentile(plat, 50)),
+                "p99_ms": float(np.percentile(plat, 99))}
+
+    # Warm both sides (graph capture, pooled framebuffers, renderers).
+    served_at(500.0, 0.5)
+    plain_at(200.0, 0.3)
+    clocks = Clocks(local)
+    clocks.start()
+    fixed = {}
+    for rate in [float(x) for x in args.rates.split(",")]:
+        fixed[str(int(rate))] = {"served": served_at(rate, args.seconds), "plain": plain_at(rate, args.seconds)}
+
+    def best_rate(fn, bound, lo, hi, iters=4):
+        """Largest arrival rate in [lo, hi] (bisection on a log scale) whose
+        p99 stays within `bound`, with the measurement taken there."""
+        ok = fn(lo, args.seconds)
+        if ok["p99_ms"] > bound:
+            return ok, False
+        top = fn(hi, args.seconds)
+        if top["p99_ms"] <= bound:
+            return top, True
+        for _ in range(iters):
+            mid = (lo * hi) ** 0.5
+            m = fn(mid, args.seconds)
+            if m["p99_ms"] <= bound:
+                lo, ok = mid, m
+            else:
+                hi = mid
+        return ok, True
+
     eq = {}
-    for bound in (50.0, 100.0, 250.0):
-        s_ok = [v["served"]["frames_per_s"] for v in results.values() if v["served"]["p99_ms"] <= bound]
-        p_ok = [v["plain"]["frames_per_s"] for v in results.values() if v["plain"]["p99_ms"] <= bound]
-        sb, pb = max(s_ok, default=0.0), max(p_ok, default=0.0)
-        eq["p99<=%dms" % bound] = {"served": sb, "plain": pb, "ratio": sb / pb if pb else None}
-    line["at_equal_p99"] = eq
-    print(json.dumps(line), flush=True)
+    for bound in [float(x) for x in args.bounds.split(",")]:
+        s_m, s_ok = best_rate(served_at, bound, 500.0, 8000.0)
+        p_m, p_ok = best_rate(plain_at, bound, 100.0, 3000.0)
+        sb = s_m["frames_per_s"] if s_ok else 0.0
+        pb = p_m["frames_per_s"] if p_ok else 0.0
+        eq["p99<=%dms" % bound] = {"served": s_m, "plain": p_m, "served_frames_per_s": sb, "plain_frames_per_s": pb,
+                                   "ratio": sb / pb if pb else None}
+    clk = clocks.stop()
+    st = srv.stats()
+    out = {"metric": "served frames/s at equal p99 vs plain GPU", "unit": "frames/s",
+           "config": {"workload": "8 resident scenes (10k-4M triangles), Poisson arrivals, random scene, camera on "
+                                  "a sphere, resolution from {640x480, 1280x720, 1920x1080, 3840x2160}, 40 GB "
+                                  "budget, continuous batching",
+                      "triangles": int(sum(i.triangle_count for i in infos)), "inflight": args.inflight,
+                      "max_batch_views": args.max_batch, "graph": bool(args.graph),
+                      "sched_tile": args.sched_tile, "fused_shade": bool(args.fused_shade),
+                      "seconds_per_rate": args.seconds},
+           "fixed_rates": fixed, "at_equal_p99": eq, "batches": st.batches, "device_bytes": st.device_bytes,
+           "clocks": clk}
+    first = eq[sorted(eq)[-1]] if eq else None
+    out["value"] = first["served_frames_per_s"] if first else None
+    out["speedup_vs_plain_at_equal_p99"] = first["ratio"] if first else None
     srv.close()
     for r in rends.values():
         r.close()
-    return 0
+    for s in scs:
+        s.close()
+    return out
 
 
-def main():
-    args = parse()
-    if args.impl == "reference":
-        return run_reference(args)
-    if args.mode in ("batched", "hetero", "served"):
-        import torch
-        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        if args.mode == "served":
-            return run_served(args)
-        return run_batched(args, args.mode == "hetero")
-    world, rank, local = dist_init()
+def measure_plain(args, name, world=1, rank=0, local=0, with_e2e=True):
+    """The plain per-frame path on one workload: device-resident frames/s,
+    stage split, roofline of the dominant kernel, e2e through the C ABI."""
+    import ctypes as C
     import torch
-    torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
     import scenes
     import swr
-    sd, cam_params, cfg = workload(args.workload)
+    sd, cam_params, cfg = workload(name)
     W, H = cfg["width"], cfg["height"]
     scene = swr.Scene(sd, gi=args.gi)
     if args.gi:
         cfg = dict(cfg, workload=cfg["workload"] + ", baked voxel GI", gi=True)
-    cam = swr.make_camera(*cam_params) if cam_params else swr.make_camera(
-        *scenes.default_camera_params(scene.info(), W, H))
+    if cam_params is None:
+        cam_params = scenes.default_camera_params(scene.info(), W, H)
+    cam = swr.make_camera(*cam_params)
     r = swr.Renderer(W, H, sched_tile=args.sched_tile)
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
+    steps = args.steps if name == "4k" else max(args.steps // 2, 100)
 
     def barrier():
         if world > 1:
@@ -416,8 +467,8 @@ def main():
         r.render(scene, cam, 0.0, sh)
     r.sync()
     st = r.stats()
-    # Timed region: K frames, device-resident (inputs > L2: the scene is
-    # ~265 MB and each frame writes 100 MB of outputs).
+    # Timed region: K frames, device-resident (4K: inputs larger than L2, the
+    # scene is ~265 MB and each frame writes 100 MB of outputs).
     clocks = Clocks(local)
     clocks.start()
     r.set_profiling(True)
@@ -425,7 +476,7 @@ def main():
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         r.render(scene, cam, 0.0, sh)
     e1.record(stream)
     torch.cuda.synchronize()
@@ -435,92 +486,131 @@ def main():
     prof, nprof = r.profile()
     r.set_profiling(False)
     clk = clocks.stop()
+    st2 = r.stats()
+    # A frame that overflowed its bins is rendered again with grown buffers
+    # when its result is read; none may have happened in the timed region.
+    if st2.overflow_retries != st.overflow_retries:
+        raise RuntimeError("a timed frame overflowed and was rendered again (%d retries)"
+                           % (st2.overflow_retries - st.overflow_retries))
+    launches = st2.kernel_launches - st.kernel_launches
     ms = max_over_ranks(ms, world)
-    fps = aggregate_rate(world, args.steps, ms)
-    # End to end through the C ABI with host buffers (pinned): each step is
-    # the reference's frame, render_scene + update_auto_exposure +
-    # blit_to_buffer, with the RGBA8 framebuffer in host memory when the
-    # blit returns. Headline: the framebuffer is the renderer's blit target,
-    # so the shading pass writes it over the host link and the blit waits;
-    # also reported: the blit copying it after the frame.
-    rgba_h = torch.empty((H, W), dtype=torch.int32, pin_memory=True)
-    import ctypes as C
-    L = swr.lib()
-    e2e_steps = max(5, args.steps // 4)
+    fps = aggregate_rate(world, steps, ms)
+    out = {"metric": "4K frames/s" if name == "4k" else "frames/s", "value": fps, "unit": "frames/s",
+           "steps": steps, "ms_per_step": ms / steps, "config": dict(cfg, sched_tile=st.sched_tile),
+           "gtri_per_s": fps * cfg["triangles"] / 1e9, "gpix_per_s": fps * W * H / 1e9,
+           "stage_ms": {k: round(v, 4) for k, v in prof.items()},
+           "frame_stats": {"triangles_in": st.triangles_in, "clipped": st.triangles_clipped,
+                           "setup_triangles": st.setup_triangles, "bin_pairs": st.bin_pairs,
+                           "culled_pairs": st.culled_pairs},
+           "clocks": clk, "gpu_launches": launches, "kernels_per_frame": launches / steps}
+    if with_e2e:
+        # End to end through the C ABI with host buffers (pinned): each step
+        # is the reference's frame, render_scene + update_auto_exposure +
+        # blit_to_buffer, with the RGBA8 framebuffer in host memory when the
+        # blit returns. Headline: the framebuffer is the renderer's blit
+        # target, so the shading pass writes it over the host link and the
+        # blit waits; also reported: the blit copying it after the frame.
+        rgba_h = torch.empty((H, W), dtype=torch.int32, pin_memory=True)
+        L = swr.lib()
+        e2e_steps = max(5, steps // 4)
 
-    def e2e_run():
-        barrier()
-        torch.cuda.synchronize()
-        e2 = torch.cuda.Event(enable_timing=True)
-        e3 = torch.cuda.Event(enable_timing=True)
-        e2.record(stream)
-        for _ in range(e2e_steps):
-            r.render(scene, cam, 0.0, sh)
-            swr.check(L.swr_blit(r.handle, C.c_void_p(rgba_h.data_ptr()), W, sh))
-        e3.record(stream)
-        torch.cuda.synchronize()
-        barrier()
-        return aggregate_rate(world, e2e_steps, max_over_ranks(e2.elapsed_time(e3), world))
+        def e2e_run():
+            barrier()
+            torch.cuda.synchronize()
+            e2 = torch.cuda.Event(enable_timing=True)
+            e3 = torch.cuda.Event(enable_timing=True)
+            e2.record(stream)
+            for _ in range(e2e_steps):
+                r.render(scene, cam, 0.0, sh)
+                swr.check(L.swr_blit(r.handle, C.c_void_p(rgba_h.data_ptr()), W, sh))
+            e3.record(stream)
+            torch.cuda.synchronize()
+            barrier()
+            return aggregate_rate(world, e2e_steps, max_over_ranks(e2.elapsed_time(e3), world))
 
-    e2e_copy_fps = e2e_run()
-    r.set_blit_target(rgba_h.data_ptr(), W, keep=rgba_h)
-    e2e_fps = e2e_run()
-    r.set_blit_target(None)
-    h2d = st.staged_bytes  # per-frame tables: scene/view headers, draws, chunks
-    d2h = W * (H & ~1) * 4
+        e2e_copy_fps = e2e_run()
+        r.set_blit_target(rgba_h.data_ptr(), W, keep=rgba_h)
+        e2e_fps = e2e_run()
+        r.set_blit_target(None)
+        out["e2e"] = {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": st.staged_bytes,
+                      "d2h_bytes_per_step": W * (H & ~1) * 4,
+                      "blit": "shading pass writes the pinned host framebuffer (swr_renderer_set_blit_target)",
+                      "copy_blit_value": e2e_copy_fps}
     # Roofline for the dominant kernel (HBM: shading reads the 8-B depth key
     # and writes 4-B RGBA8 + 8-B visibility ID per pixel).
     dom = max(("raster", "shade", "frontend"), key=lambda k: prof[k])
     px = W * H
-    # raster: bins read (4 B/pair), raster records read (80 B/emitted triangle), depth keys
-    # written (8 B per pixel of the 64-px tile grid).
+    # raster: bins read (4 B/pair), raster records read (80 B/emitted triangle),
+    # depth keys written (8 B per pixel of the 64-px tile grid).
     alg = {"shade": 20.0 * px, "raster": 4.0 * st.bin_pairs + 80.0 * st.setup_triangles + 8.0 * st.tiles * 4096,
            "frontend": 12.0 * st.triangles_in + 48.0 * 3 * st.triangles_in + 256.0 * st.setup_triangles}[dom]
     peak, peak_kind = peaks()
     achieved = alg / (prof[dom] / 1000.0) / 1e9
-    traffic = None
-    issue = None
+    traffic, issue = None, None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
         tj = json.load(open(tp))
-        traffic = tj.get(args.workload, {}).get(dom)
+        traffic = tj.get(name, {}).get(dom)
         # The kernel is bound by instruction issue, not HBM: warp instructions
         # per launch (from the ncu capture) over the live duration, against
         # 4 issue slots per SM per cycle at the sampled clock.
-        winst = tj.get("warp_instructions", {}).get(args.workload, {}).get(dom)
+        winst = tj.get("warp_instructions", {}).get(name, {}).get(dom)
         if winst and clk.get("sm_mhz"):
-            import torch
             sms = torch.cuda.get_device_properties(local).multi_processor_count
             ach = winst / (prof[dom] / 1000.0)
             pk = 4.0 * sms * clk["sm_mhz"] * 1e6
             issue = {"kernel": dom, "warp_instructions_per_launch": winst, "achieved": ach, "peak": pk,
                      "unit": "warp instructions/s", "frac": ach / pk}
-    line = {"metric": "4K frames/s" if args.workload == "4k" else "frames/s", "value": fps, "unit": "frames/s",
-            "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded scene of the configured shape; inputs larger than L2)",
-            "config": dict(cfg, parallelism="replicas" if world > 1 else "single", sched_tile=st.sched_tile),
-            "gtri_per_s": fps * cfg["triangles"] / 1e9, "gpix_per_s": fps * W * H / 1e9,
-            "stage_ms": {k: round(v, 4) for k, v in prof.items()},
-            "frame_stats": {"triangles_in": st.triangles_in, "clipped": st.triangles_clipped,
-                            "setup_triangles": st.setup_triangles, "bin_pairs": st.bin_pairs,
-                            "culled_pairs": st.culled_pairs},
-            "issue_roofline": issue,
-            "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "algorithmic_bytes": alg},
-            "clocks": clk,
-            "gpu_launches": KERNELS_PER_FRAME * args.steps,
-            "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "blit": "shading pass writes the pinned host framebuffer (swr_renderer_set_blit_target)",
-                    "copy_blit_value": e2e_copy_fps}}
-    if rank == 0 and not args.no_cpu_baseline:
-        v, cores, sample = cpu_baseline(sd, cam_params, cfg, args.cpu_frames)
-        line["cpu_baseline"] = {"value": v, "unit": "frames/s", "cores": cores, "kind": "port", "sample": sample}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    out["issue_roofline"] = issue
+    out["roofline"] = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                       "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind, "algorithmic_bytes": alg}
     r.close()
     scene.close()
+    return out, sd, cam_params, cfg
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    world, rank, local = dist_init()
+    import torch
+    torch.cuda.set_device(local)
+    if args.mode in ("batched", "hetero"):
+        out = measure_batched(args, args.mode == "hetero", args.steps, local)
+        out.update({"n_gpus": 1, "warmup": max(3, args.warmup), "higher_is_better": True, "scaling": "weak",
+                    "vs_baseline": None, "dtype": "f32", "data": "synthetic"})
+        print(json.dumps(out), flush=True)
+        return 0
+    if args.mode == "served":
+        out = measure_served(args, local)
+        out.update({"n_gpus": 1, "data": "synthetic", "higher_is_better": True})
+        print(json.dumps(out), flush=True)
+        return 0
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    plain, sd, cam_params, cfg = measure_plain(args, args.workload, world, rank, local)
+    line = {"metric": plain["metric"], "value": plain["value"], "unit": "frames/s", "n_gpus": world,
+            "steps": plain["steps"], "warmup": max(3, args.warmup), "ms_per_step": plain["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded scene of the configured shape; inputs larger than L2)",
+            "config": dict(plain["config"], parallelism="replicas" if world > 1 else "single")}
+    for k in ("gtri_per_s", "gpix_per_s", "stage_ms", "frame_stats", "issue_roofline", "roofline", "clocks",
+              "gpu_launches", "kernels_per_frame", "e2e"):
+        line[k] = plain[k]
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, cores, sample = cpu_baseline(sd, cam_params, cfg, args.cpu_frames)
+        line["cpu_baseline"] = {"value": v, "unit": "frames/s", "cores": cores, "kind": "port", "sample": sample}
+    if world == 1 and not args.no_sub and args.workload == "4k" and not args.gi:
+        small, _, _, _ = measure_plain(args, "small", with_e2e=True, local=local)
+        line["small"] = {k: small[k] for k in ("value", "unit", "ms_per_step", "steps", "config", "gtri_per_s",
+                                               "gpix_per_s", "stage_ms", "clocks", "gpu_launches", "e2e")}
+        line["batched"] = measure_batched(args, False, 100, local)
+        line["hetero"] = measure_batched(args, True, 20, local)
+        line["served"] = measure_served(args, local)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0

@@ -428,6 +428,8 @@ typedef struct swr_frame_stats {
     uint32_t sched_tile;        /* scheduling tile the renderer uses */
     uint64_t staged_bytes;      /* host-to-device bytes per frame (frame, scene and view headers, node order) */
     uint64_t culled_pairs;      /* bin pairs the raster dropped as hidden behind depths already written */
+    uint64_t kernel_launches;   /* kernels the renderer has enqueued since it was created (re-renders after
+                                   an overflow included) */
 } swr_frame_stats;
 
 swr_status swr_renderer_get_stats(swr_renderer* r, swr_frame_stats* out);
@@ -575,21 +577,22 @@ swr_status swr_selftest_depth_floor(const int32_t* p, const float* zow, const fl
                                     float* zlo);
 
 /* Allocation-free frame. No counterpart in the reference: an addition for
- * callers that cannot allocate device memory while they render (code running
- * under CUDA stream capture, processes whose device memory belongs to another
- * allocator, real-time loops that cannot afford a synchronizing cudaMalloc).
- * Renders `scene` (already resident) from `camera` into the caller's device
- * buffers rgba8 (width*height, row pitch width; an odd last row is left
- * untouched) and vis (width*height), with a fixed `exposure` (2.0 is a fresh
- * renderer's) and without allocating anything: all per-frame work buffers
- * live in one fixed __device__ array of about 9 MB. Limits: width, height
- * <= 512, at most 16384 triangles passing the frustum test, 4096 nodes, 4096
- * draws, 65536 (triangle, tile) pairs, no translucent primitives; larger
- * inputs return SWR_INVALID_ARG,
- * capacity overflow on the device returns SWR_OVERFLOW. Returns after the
- * frame has finished. The first call on each device looks up the array's
- * address and must come before any stream capture; all calls share the array,
- * so calls whose GPU work overlaps race. */
+ * callers that cannot allocate device memory while they render (processes
+ * whose device memory belongs to another allocator or a fixed budget,
+ * real-time loops that cannot afford a cudaMalloc that may synchronize the
+ * device). Renders `scene` (already resident) from `camera` into the
+ * caller's device buffers rgba8 (width*height, row pitch width; an odd last
+ * row is left untouched) and vis (width*height), with a fixed `exposure`
+ * (2.0 is a fresh renderer's) and without allocating anything: all per-frame
+ * work buffers live in one fixed __device__ array of about 9 MB that every
+ * GPU loading the library holds until exit. Limits: width, height <= 512, at
+ * most 16384 triangles passing the frustum test, 4096 nodes, 4096 draws,
+ * 65536 (triangle, tile) pairs, no translucent primitives; larger inputs
+ * return SWR_INVALID_ARG, capacity overflow on the device returns
+ * SWR_OVERFLOW. The first call on a device looks up the array's address.
+ * Returns after the frame has finished; a per-device lock held until then
+ * serializes calls on one device (they share its array, and would race on
+ * it if their GPU work overlapped). */
 swr_status swr_render_frame_noalloc(const swr_scene* scene, const swr_camera* camera, int32_t width,
                                     int32_t height, float exposure, uint32_t rsqrt_mode, uint32_t* rgba8,
                                     uint64_t* vis, void* stream);

@@ -25,6 +25,7 @@
 // multi-threaded (the timed CPU baseline). Translucent packets are sorted back
 // to front per tile by average clip z, equal keys in queue order.
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstdint>
@@ -1247,8 +1248,13 @@ int oracle_render(const swr_scene_host_view* s, const swr_camera* cam, int32_t w
 // src/raytracer.rs:172-207) and blur_grid (src/voxelgrid.rs:370-419). Every
 // ray tests every triangle (no acceleration structure: results depend only
 // on ray_triangle_intersect, src/raytracer.rs:225-260, and the hit order,
-// t ascending, equal t by triangle). Writes voxel_size^3 floats to `out`.
-int oracle_sun_visibility(const swr_scene_host_view* v, uint32_t threads, float* out) {
+// t ascending, equal t by triangle). With `brute` = 0 a bounding-volume
+// hierarchy of its own prunes the candidates conservatively: boxes are
+// padded by 1e-4 of the scene's extent (plus 1e-5), far more than the
+// rounding of the slab test or the tolerance of the triangle test, so every
+// triangle the exact test could accept is still tested and the hit set is
+// that of the brute-force loop. Writes voxel_size^3 floats to `out`.
+int oracle_sun_visibility_ex(const swr_scene_host_view* v, uint32_t threads, float* out, int brute) {
     struct P3 {
         float x, y, z;
     };
@@ -1332,9 +1338,101 @@ int oracle_sun_visibility(const swr_scene_host_view* v, uint32_t threads, float*
     const P3 cmin = add(bmn, mul(vsz, 0.5f));
     const float bias = length(vsz) * 3.0f;
     std::vector<float> light(nvox, 1.0f);
+    // Conservative BVH over the triangles: median split of the centroids on
+    // the longest axis, at most 4 triangles per leaf, padded boxes.
+    struct BNode {
+        float mn[3], mx[3];
+        uint32_t left, first, count;  // count > 0: leaf over order[first, first + count)
+    };
+    std::vector<BNode> bvh;
+    std::vector<uint32_t> order(tris.size());
+    std::iota(order.begin(), order.end(), 0u);
+    if (!brute && !tris.empty()) {
+        const float pad = 1.0e-4f * length(wsz) + 1.0e-5f;
+        auto tmin3 = [](const Tri& t, int k) { const float* a = &t.p0.x; const float* b = &t.p1.x; const float* c = &t.p2.x; return std::fmin(a[k], std::fmin(b[k], c[k])); };
+        auto tmax3 = [](const Tri& t, int k) { const float* a = &t.p0.x; const float* b = &t.p1.x; const float* c = &t.p2.x; return std::fmax(a[k], std::fmax(b[k], c[k])); };
+        std::vector<std::array<uint32_t, 3>> work{{0u, (uint32_t)tris.size(), 0u}};
+        bvh.push_back(BNode{});
+        while (!work.empty()) {
+            const auto w = work.back();
+            work.pop_back();
+            const uint32_t a = w[0], b = w[1], ni = w[2];
+            BNode nd{};
+            float cmn[3] = {INFINITY, INFINITY, INFINITY}, cmx[3] = {-INFINITY, -INFINITY, -INFINITY};
+            for (int k = 0; k < 3; ++k) nd.mn[k] = INFINITY, nd.mx[k] = -INFINITY;
+            for (uint32_t i = a; i < b; ++i) {
+                const Tri& t = tris[order[i]];
+                for (int k = 0; k < 3; ++k) {
+                    nd.mn[k] = std::fmin(nd.mn[k], tmin3(t, k));
+                    nd.mx[k] = std::fmax(nd.mx[k], tmax3(t, k));
+                    const float c = (tmin3(t, k) + tmax3(t, k)) * 0.5f;
+                    cmn[k] = std::fmin(cmn[k], c);
+                    cmx[k] = std::fmax(cmx[k], c);
+                }
+            }
+            for (int k = 0; k < 3; ++k) nd.mn[k] -= pad, nd.mx[k] += pad;
+            if (b - a <= 4) {
+                nd.first = a;
+                nd.count = b - a;
+                bvh[ni] = nd;
+                continue;
+            }
+            int ax = 0;
+            for (int k = 1; k < 3; ++k)
+                if (cmx[k] - cmn[k] > cmx[ax] - cmn[ax]) ax = k;
+            const uint32_t mid = a + (b - a) / 2;
+            std::nth_element(order.begin() + a, order.begin() + mid, order.begin() + b, [&](uint32_t x, uint32_t y) {
+                return (tmin3(tris[x], ax) + tmax3(tris[x], ax)) < (tmin3(tris[y], ax) + tmax3(tris[y], ax));
+            });
+            nd.left = (uint32_t)bvh.size();
+            nd.count = 0;
+            bvh[ni] = nd;
+            bvh.push_back(BNode{});
+            bvh.push_back(BNode{});
+            work.push_back({a, mid, nd.left});
+            work.push_back({mid, b, nd.left + 1});
+        }
+    }
+    auto slab = [&](const BNode& b, P3 o) {
+        const float oo[3] = {o.x, o.y, o.z}, dd[3] = {ld.x, ld.y, ld.z};
+        float tn = -INFINITY, tf = INFINITY;
+        for (int k = 0; k < 3; ++k) {
+            if (std::fabs(dd[k]) < 1.0e-30f) {
+                if (oo[k] < b.mn[k] || oo[k] > b.mx[k]) return false;
+                continue;
+            }
+            float t0 = (b.mn[k] - oo[k]) / dd[k], t1 = (b.mx[k] - oo[k]) / dd[k];
+            if (t0 > t1) std::swap(t0, t1);
+            tn = std::fmax(tn, t0);
+            tf = std::fmin(tf, t1);
+        }
+        return tf >= std::fmax(tn, 0.0f);
+    };
+    std::atomic<bool> too_deep{false};
     auto trace = [&](P3 o) {
         std::vector<std::pair<float, uint32_t>> hits;
-        for (uint32_t i = 0; i < (uint32_t)tris.size(); ++i) {
+        std::vector<uint32_t> cand;
+        if (brute || bvh.empty()) {
+            cand = order;
+        } else {
+            uint32_t stack[128];
+            int sp = 0;
+            stack[sp++] = 0;
+            while (sp > 0) {
+                const BNode& b = bvh[stack[--sp]];
+                if (!slab(b, o)) continue;
+                if (b.count > 0) {
+                    for (uint32_t i = 0; i < b.count; ++i) cand.push_back(order[b.first + i]);
+                } else if (sp + 2 <= 128) {
+                    stack[sp++] = b.left;
+                    stack[sp++] = b.left + 1;
+                } else {
+                    too_deep = true;  // a median split of 2^32 triangles is 32 levels deep: never
+                    return 0.0f;
+                }
+            }
+        }
+        for (uint32_t i : cand) {
             const Tri& t = tris[i];
             const P3 e1 = sub(t.p1, t.p0), e2 = sub(t.p2, t.p0);
             const P3 pv = cross(ld, e2);
@@ -1378,6 +1476,7 @@ int oracle_sun_visibility(const swr_scene_host_view* v, uint32_t threads, float*
             }
         });
     for (auto& t : pool) t.join();
+    if (too_deep) return 1;
     // blur_grid: mean of the in-range 3x3x3 neighbours, squared.
     for (uint32_t z = 0; z < n; ++z)
         for (uint32_t y = 0; y < n; ++y)
@@ -1396,6 +1495,10 @@ int oracle_sun_visibility(const swr_scene_host_view* v, uint32_t threads, float*
                 out[(size_t)z * n * n + (size_t)y * n + x] = count > 0 ? m * m : 0.0f;
             }
     return 0;
+}
+
+int oracle_sun_visibility(const swr_scene_host_view* v, uint32_t threads, float* out) {
+    return oracle_sun_visibility_ex(v, threads, out, 0);
 }
 
 // bake_voxel_gi (src/gi.rs:316-408) + blur_gi_sh4 (src/voxelgrid.rs:422-472)

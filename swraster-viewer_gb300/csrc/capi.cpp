@@ -319,6 +319,7 @@ swr_status enqueue_frame(swr_renderer* r, const swr_scene* scene, const swr_came
         a.exposure_dev = r->d_expo;
         if (ev) cudaEventRecord(ev[8], stream);
         launch_resolve(a, stream);
+        r->eng.kernel_launches++;
         if (ev) cudaEventRecord(ev[9], stream);
         cudaEventRecord(r->expo_done, stream);
         r->expo_pending = true;
@@ -515,6 +516,7 @@ swr_status swr_renderer_get_stats(swr_renderer* r, swr_frame_stats* o) {
     o->sched_tile = r->opts.sched_tile;
     o->staged_bytes = r->eng.lay.staged;
     o->culled_pairs = c.culled;
+    o->kernel_launches = r->eng.kernel_launches;
     return SWR_OK;
 }
 

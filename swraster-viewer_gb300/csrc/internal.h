@@ -309,7 +309,8 @@ struct FrameArgs {
 
 // Launch wrappers (kernels.cu). `ev`, when given, holds 8 events recorded
 // before reset, frontend, clip, scan, scatter, raster, shade and after shade.
-void launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t* ev = nullptr);
+// Enqueues one frame's kernels; returns how many it launched.
+uint32_t launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t* ev = nullptr);
 void launch_reset(const FrameArgs& a, void* stream);
 void launch_resolve(const FrameArgs& a, void* stream);
 // rsqrt of n device values in the given mode (table: the 512-byte FRSQRTE table).

@@ -2299,19 +2299,24 @@ void launch_reset(const FrameArgs& a, void* stream) {
     k_reset<<<min(max((n + 255) / 256, slot_blocks), 1024u), 256, 0, s>>>(a);
 }
 
-void launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t* ev) {
+uint32_t launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t* ev) {
     cudaStream_t s = (cudaStream_t)stream;
     auto mark = [&](int i) {
         if (ev) cudaEventRecord(ev[i], s);
     };
+    uint32_t launches = 0;
     mark(0);
     launch_reset(a, stream);
+    launches++;
     // Frames of at most 256 node slots are emitted inside k_reset
     // (k_draw_emit returns at once); with a slot capacity of at most 256 it
     // is not launched.
     if (a.gpu_draws) {
         const uint32_t sg = (a.slot_cap + kSlotBlock - 1u) / kSlotBlock;
-        if (sg > 1u) k_draw_emit<<<sg, kSlotBlock, 0, s>>>(a);
+        if (sg > 1u) {
+            k_draw_emit<<<sg, kSlotBlock, 0, s>>>(a);
+            launches++;
+        }
     }
     mark(1);
     // A frame's chunks number at most T / 256 + draws: the grid follows the
@@ -2321,18 +2326,23 @@ void launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t* ev
         // Host-built draw lists (no-alloc frames) size chunk_cap exactly.
         const uint64_t most = a.gpu_draws ? (uint64_t)a.tri_cap / kChunkTris + a.draw_cap + 1u : a.chunk_cap;
         k_frontend<<<(uint32_t)std::min<uint64_t>(a.chunk_cap, most), kChunkTris, 0, s>>>(a);
+        launches++;
     }
     mark(2);
     k_clip<<<num_sms * 4, 128, 0, s>>>(a);
     mark(3);
     k_scan<<<1, 1024, 0, s>>>(a);
+    launches += 2;
     mark(4);
     {
         // Thread per record slot over the capacity: blocks start in slot order,
         // so bins list records mostly in slot order and the raster's record
         // loads stay coalesced (a grid-stride loop here made k_raster 2% slower).
         const uint64_t n = (uint64_t)a.tri_cap + a.extra_cap;
-        if (n > 0) k_scatter<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
+        if (n > 0) {
+            k_scatter<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
+            launches++;
+        }
     }
     mark(5);
     const uint32_t rg = SWR_RASTER_PERSISTENT ? (a.raster_grid > 0 ? a.raster_grid : (uint32_t)num_sms)
@@ -2348,6 +2358,7 @@ void launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t* ev
             break;
         default: k_raster<64, false><<<rg, RasterShared<64>::kThreads, sizeof(RasterShared<64>), s>>>(a); break;
     }
+    launches++;
     mark(6);
     if (!shade_fused(a.sched_tile, a.fused_shade != 0)) {
         const uint32_t sg = a.shade_grid > 0 ? a.shade_grid : (uint32_t)num_sms;
@@ -2355,6 +2366,7 @@ void launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t* ev
             k_shade<true><<<sg, 256, 0, s>>>(a);
         else
             k_shade<false><<<sg, 256, 0, s>>>(a);
+        launches++;
     }
     mark(7);
     if (a.has_translucent) {
@@ -2365,8 +2377,13 @@ void launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t* ev
             case 32: k_translucent<32><<<tg, kTransThreads, 0, s>>>(a); break;
             default: k_translucent<64><<<tg, kTransThreads, 0, s>>>(a); break;
         }
-        if (!a.defer_resolve) launch_resolve(a, stream);
+        launches++;
+        if (!a.defer_resolve) {
+            launch_resolve(a, stream);
+            launches++;
+        }
     }
+    return launches;
 }
 
 bool depth_floor_host(const int32_t p[6], const float zow[3], const float oow[3], int32_t xe, int32_t ye, float& zlo) {

@@ -1,27 +1,31 @@
 // swr_render_frame_noalloc: one frame with no memory allocation at all.
 //
 // Who needs it: callers that cannot call cudaMalloc/cudaFree while they
-// render — code that runs while a CUDA stream is being captured into a graph
-// (allocation calls are not capturable), processes whose device memory is
-// owned by another allocator (a framework's caching allocator, a fixed
-// budget), and real-time loops that cannot afford cudaMalloc/cudaFree, which
-// may synchronize the whole device. The caller passes the scene (already
+// render: processes whose device memory is owned by another allocator (a
+// framework's caching allocator, a fixed budget carved out at start-up), and
+// real-time loops that cannot afford cudaMalloc/cudaFree, which may
+// synchronize the whole device. The caller passes the scene (already
 // resident), the camera and its own device output buffers; every per-frame
 // work buffer lives in one file-scope __device__ array of fixed size.
 //
 // Limits: width, height <= 512; at most 16384 triangles pass the
 // sphere/frustum test; at most 4096 nodes and 4096 draws; at most 65536
 // (triangle, tile) pairs and 8192 extra clipped fan triangles. Larger frames
-// are rejected before any GPU work.
+// are rejected before any GPU work; a frame whose (triangle, tile) pairs or
+// clipped triangles exceed the fixed capacity on the device returns
+// SWR_OVERFLOW.
 //
 // The array (about 9 MB) stays allocated on every GPU that loads the library
 // until the process exits. Its device address is looked up with
-// cudaGetSymbolAddress on the first call per device; that first call should
-// therefore happen before any stream capture begins. All calls share the
-// array and it keeps the last call's contents: the frame's counters and tile
-// counts are cleared by the first kernel of every call. Calls whose work
-// overlaps on the GPU (different streams or threads without ordering) race
-// on the array; a host mutex serializes the host side only.
+// cudaGetSymbolAddress on the first call on each device. All calls on a
+// device share that device's array and it keeps the last call's contents:
+// the frame's counters and tile counts are cleared by the first kernel of
+// every call. A call holds its device's lock until its frame has finished
+// (it waits for its stream before returning), so calls in one process never
+// overlap on a GPU; were that lock or that wait removed, calls whose work
+// overlapped on the GPU would race on the array. Calls on different devices
+// run concurrently; they share only the host staging buffers, under a
+// separate lock held while the tables are staged.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -73,7 +77,8 @@ __device__ __align__(256) unsigned char g_noalloc_scratch[kNaScratchBytes];
 constexpr int kMaxDevices = 64;
 unsigned char* g_dev_ptr[kMaxDevices] = {};
 int g_dev_sms[kMaxDevices] = {};
-std::mutex g_mu;
+std::mutex g_dev_mu[kMaxDevices];  // per device: its scratch array and set-up
+std::mutex g_stage_mu;              // the host staging buffers below
 
 // Host staging (static, no heap): scene, view, draws, chunks.
 unsigned char g_stage[al(sizeof(DFrameDyn)) + al(sizeof(DScene)) + al(sizeof(DView)) + al(sizeof(DDraw) * kNaMaxDraws) +
@@ -131,13 +136,14 @@ extern "C" swr_status swr_render_frame_noalloc(const swr_scene* scene, const swr
     if (!s.d_scene) return na_fail(SWR_INVALID_ARG, "scene was created host-only");
     if (s.nodes.size() > kNaMaxNodes)
         return na_fail(SWR_INVALID_ARG, "swr_render_frame_noalloc: the scene has more than 4096 nodes");
-    std::lock_guard<std::mutex> lock(g_mu);
     cudaStream_t stream = (cudaStream_t)stream_v;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
         return na_fail(SWR_CUDA_ERROR, "cudaGetDevice failed");
+    // Lock order: the device's lock, then (while staging) the staging lock.
+    std::lock_guard<std::mutex> dev_lock(g_dev_mu[dev]);
     if (!g_dev_ptr[dev]) {
-        // One-time set-up for this device (must precede any stream capture).
+        // One-time set-up for this device.
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p) {
@@ -162,6 +168,7 @@ extern "C" swr_status swr_render_frame_noalloc(const swr_scene* scene, const swr
         g_dev_ptr[dev] = static_cast<unsigned char*>(p);
     }
     unsigned char* base = g_dev_ptr[dev];
+    std::unique_lock<std::mutex> stage_lock(g_stage_mu);
     // Draws in canonical order (compute_nodes_by_distance + render_node +
     // render_mesh + test_sphere_frustum), into static host arrays.
     const uint32_t nn = (uint32_t)s.nodes.size();
@@ -257,6 +264,7 @@ extern "C" swr_status swr_render_frame_noalloc(const swr_scene* scene, const swr
         cudaGetLastError();
         return na_fail(SWR_CUDA_ERROR, "table upload failed");
     }
+    stage_lock.unlock();  // the copies above have taken the staged tables
     FrameArgs a{};
     a.dyn = reinterpret_cast<DFrameDyn*>(base + oDyn);
     a.scenes = reinterpret_cast<const DScene*>(base + oScene);

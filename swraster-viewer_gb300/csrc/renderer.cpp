@@ -364,7 +364,7 @@ swr_status FrameEngine::launch(cudaStream_t stream, cudaEvent_t* ev, std::string
             // into the caller's stream (which may be the legacy default one).
             if (e == cudaSuccess) e = cudaStreamBeginCapture(capture_stream, cudaStreamCaptureModeThreadLocal);
             if (e == cudaSuccess) {
-                launch_frame(args, capture_stream, num_sms, nullptr);
+                graph_kernels = launch_frame(args, capture_stream, num_sms, nullptr);
                 e = cudaStreamEndCapture(capture_stream, &g);
             }
             if (e == cudaSuccess) e = cudaGraphInstantiate(&graph_exec, g, 0);
@@ -379,8 +379,9 @@ swr_status FrameEngine::launch(cudaStream_t stream, cudaEvent_t* ev, std::string
             graph_stream = stream;
         }
         e = cudaGraphLaunch(graph_exec, stream);
+        if (e == cudaSuccess) kernel_launches += graph_kernels;
     } else if (e == cudaSuccess) {
-        launch_frame(args, stream, num_sms, ev);
+        kernel_launches += launch_frame(args, stream, num_sms, ev);
         e = cudaGetLastError();
     }
     if (e != cudaSuccess) {

@@ -97,6 +97,8 @@ struct FrameEngine {
     bool stage_pending[kStageRing] = {};
     int stage_slot = 0;
     uint32_t retries = 0;
+    uint64_t kernel_launches = 0;  // kernels enqueued (graph replays count the graph's kernels)
+    uint32_t graph_kernels = 0;    // kernels in the captured graph
     DCounters last{};
     DFrameDyn dyn{};
     FrameArgs args{};

@@ -786,11 +786,13 @@ swr_status build_scene(const swr_scene_desc* desc, SceneImpl* s, std::string& er
         v.metallic_factor = m.metallic_factor;
         v.roughness_factor = m.roughness_factor;
         for (int k = 0; k < 3; ++k) v.emissive_factor[k] = m.emissive_factor[k];
-        v.occlusion_strength = m.occlusion_strength;
         v.alpha_cutoff = m.alpha_cutoff;
         v.transmission = m.has_transmission ? m.transmission : 0.0f;
+        // The transmission texture belongs to KHR_materials_transmission: a
+        // material without the extension has none (src/scene.rs:770-779).
+        const swr_texref none = {-1, 0, 0, 0};
         const swr_texref refs[6] = {m.base_color, m.metallic_roughness, m.normal, m.emissive, m.occlusion,
-                                    m.transmission_texture};
+                                    m.has_transmission ? m.transmission_texture : none};
         for (int k = 0; k < 6; ++k) {
             if (refs[k].texture >= (int32_t)desc->texture_count) {
                 err = "material references a missing texture";
@@ -804,6 +806,9 @@ swr_status build_scene(const swr_scene_desc* desc, SceneImpl* s, std::string& er
                 return SWR_INVALID_ARG;
             }
         }
+        // The occlusion strength is read from the occlusion texture info: 1
+        // without one (src/scene.rs:756-759).
+        v.occlusion_strength = v.tex[4] >= 0 ? m.occlusion_strength : 1.0f;
         v.is_alpha_tested = (m.alpha_mask && v.tex[0] >= 0) ? 1u : 0u;
         v.is_translucent = m.has_transmission ? 1u : 0u;
         s->materials.push_back(v);

@@ -196,6 +196,16 @@ def translucent_scene(seed=11, count=8, subdiv=2, box=4.0, tex_size=64, cube_siz
             "specular_samples": 16, "brdf_lut_size": 32}
 
 
+class Bounds:
+    """Scene bounds in the shape default_camera_params and sphere_camera read
+    (bounds_center, bounds_diagonal), for bounds that do not come from
+    swr_scene_get_info."""
+
+    def __init__(self, center, diagonal):
+        self.bounds_center = tuple(center)
+        self.bounds_diagonal = diagonal
+
+
 def default_camera_params(info, width, height, fov=math.pi / 3.0):
     """load_scene's default camera (src/main.rs:210-225): distance = scene
     diagonal along +z from the bounds centre, far = 2 * diagonal."""

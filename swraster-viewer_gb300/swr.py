@@ -138,7 +138,8 @@ class FrameStats(C.Structure):
     _fields_ = [("triangles_in", C.c_uint64), ("triangles_clipped", C.c_uint64), ("setup_triangles", C.c_uint64),
                 ("bin_pairs", C.c_uint64), ("bin_capacity", C.c_uint64), ("tiles", C.c_uint32),
                 ("overflow_retries", C.c_uint32), ("tile_luminance_mean", C.c_float), ("exposure", C.c_float),
-                ("sched_tile", C.c_uint32), ("staged_bytes", C.c_uint64), ("culled_pairs", C.c_uint64)]
+                ("sched_tile", C.c_uint32), ("staged_bytes", C.c_uint64), ("culled_pairs", C.c_uint64),
+                ("kernel_launches", C.c_uint64)]
 
 
 class ViewDesc(C.Structure):
@@ -273,77 +274,87 @@ def texref(index=-1, wrap_s=WRAP_REPEAT, wrap_t=WRAP_REPEAT):
     return TexRef(index, wrap_s, wrap_t, 0)
 
 
+def scene_desc(sd, flags=0, host_threads=0):
+    """swr_scene_desc of a scene dict (see scenes.py), and the arrays it points
+    into (keep them alive while the descriptor is used). Builds structures
+    only: the library is not loaded."""
+    keep = []
+    meshes = (MeshDesc * len(sd["meshes"]))()
+    for mi, prims in enumerate(sd["meshes"]):
+        arr = (PrimitiveDesc * len(prims))()
+        for pi, p in enumerate(prims):
+            pos = np.ascontiguousarray(p["positions"], np.float32)
+            idx = np.ascontiguousarray(p["indices"], np.uint32)
+            nrm = None if p.get("normals") is None else np.ascontiguousarray(p["normals"], np.float32)
+            tan = None if p.get("tangents") is None else np.ascontiguousarray(p["tangents"], np.float32)
+            uv = None if p.get("texcoords") is None else np.ascontiguousarray(p["texcoords"], np.float32)
+            keep += [pos, idx, nrm, tan, uv]
+            arr[pi] = PrimitiveDesc(pos.shape[0], idx.size, _fp(pos), _fp(nrm), _fp(tan), _fp(uv), _up(idx),
+                                    p.get("material", -1), 0)
+        keep.append(arr)
+        meshes[mi] = MeshDesc(len(prims), 0, C.cast(arr, C.POINTER(PrimitiveDesc)))
+    nodes = (NodeDesc * len(sd["nodes"]))()
+    for ni, n in enumerate(sd["nodes"]):
+        w = np.asarray(n["world"], np.float32).reshape(16)
+        loc = np.asarray(n.get("local", n["world"]), np.float32).reshape(16)
+        nodes[ni] = NodeDesc((C.c_float * 16)(*w), (C.c_float * 16)(*loc), n["mesh"], 0)
+    mats = (MaterialDesc * len(sd["materials"]))()
+    for i, m in enumerate(sd["materials"]):
+        md = MaterialDesc()
+        md.base_color_factor = (C.c_float * 4)(*m.get("base_color_factor", (1, 1, 1, 1)))
+        md.metallic_factor = m.get("metallic", 1.0)
+        md.roughness_factor = m.get("roughness", 1.0)
+        md.emissive_factor = (C.c_float * 3)(*m.get("emissive_factor", (0, 0, 0)))
+        md.occlusion_strength = m.get("occlusion_strength", 1.0)
+        md.alpha_cutoff = m.get("alpha_cutoff", 0.5)
+        md.transmission = m.get("transmission", 0.0)
+        md.alpha_mask = 1 if m.get("alpha_mask") else 0
+        md.has_transmission = 1 if m.get("has_transmission") else 0
+        for slot in ("base_color", "metallic_roughness", "normal", "emissive", "occlusion",
+                     "transmission_texture"):
+            t = m.get(slot)
+            setattr(md, slot, texref(*t) if t is not None else texref())
+        mats[i] = md
+    texs = (TextureDesc * max(1, len(sd["textures"])))()
+    for i, t in enumerate(sd["textures"]):
+        data = np.ascontiguousarray(t["rgba8"], np.uint32)
+        keep.append(data)
+        texs[i] = TextureDesc(t["width"], t["height"], t["type"], 0, _up(data))
+    cube = np.ascontiguousarray(sd["cubemap"], np.uint32)
+    keep += [meshes, nodes, mats, texs, cube]
+    desc = SceneDesc()
+    desc.mesh_count = len(sd["meshes"])
+    desc.node_count = len(sd["nodes"])
+    desc.material_count = len(sd["materials"])
+    desc.texture_count = len(sd["textures"])
+    desc.meshes = C.cast(meshes, C.POINTER(MeshDesc))
+    desc.nodes = C.cast(nodes, C.POINTER(NodeDesc))
+    desc.materials = C.cast(mats, C.POINTER(MaterialDesc))
+    desc.textures = C.cast(texs, C.POINTER(TextureDesc))
+    desc.cubemap_face_size = sd["cubemap_face_size"]
+    desc.voxel_grid_size = sd.get("voxel_grid_size", 128)
+    desc.cubemap_faces = _up(cube)
+    desc.specular_samples = sd.get("specular_samples", 64)
+    desc.brdf_lut_size = sd.get("brdf_lut_size", 128)
+    desc.gi_sh_scale = sd.get("gi_sh_scale", 0.25)
+    desc.sky_visibility = sd.get("sky_visibility", 1.0)
+    desc.host_threads = host_threads
+    desc.flags = flags
+    return desc, keep
+
+
 class Scene:
     """Owns a swr_scene built from a scene dict (see scenes.py)."""
 
     def __init__(self, sd, host_only=False, host_threads=0, gi=False):
-        self._keep = []
-        keep = self._keep
-        meshes = (MeshDesc * len(sd["meshes"]))()
-        for mi, prims in enumerate(sd["meshes"]):
-            arr = (PrimitiveDesc * len(prims))()
-            for pi, p in enumerate(prims):
-                pos = np.ascontiguousarray(p["positions"], np.float32)
-                idx = np.ascontiguousarray(p["indices"], np.uint32)
-                nrm = None if p.get("normals") is None else np.ascontiguousarray(p["normals"], np.float32)
-                tan = None if p.get("tangents") is None else np.ascontiguousarray(p["tangents"], np.float32)
-                uv = None if p.get("texcoords") is None else np.ascontiguousarray(p["texcoords"], np.float32)
-                keep += [pos, idx, nrm, tan, uv]
-                arr[pi] = PrimitiveDesc(pos.shape[0], idx.size, _fp(pos), _fp(nrm), _fp(tan), _fp(uv), _up(idx),
-                                        p.get("material", -1), 0)
-            keep.append(arr)
-            meshes[mi] = MeshDesc(len(prims), 0, C.cast(arr, C.POINTER(PrimitiveDesc)))
-        nodes = (NodeDesc * len(sd["nodes"]))()
-        for ni, n in enumerate(sd["nodes"]):
-            w = np.asarray(n["world"], np.float32).reshape(16)
-            loc = np.asarray(n.get("local", n["world"]), np.float32).reshape(16)
-            nodes[ni] = NodeDesc((C.c_float * 16)(*w), (C.c_float * 16)(*loc), n["mesh"], 0)
-        mats = (MaterialDesc * len(sd["materials"]))()
-        for i, m in enumerate(sd["materials"]):
-            md = MaterialDesc()
-            md.base_color_factor = (C.c_float * 4)(*m.get("base_color_factor", (1, 1, 1, 1)))
-            md.metallic_factor = m.get("metallic", 1.0)
-            md.roughness_factor = m.get("roughness", 1.0)
-            md.emissive_factor = (C.c_float * 3)(*m.get("emissive_factor", (0, 0, 0)))
-            md.occlusion_strength = m.get("occlusion_strength", 1.0)
-            md.alpha_cutoff = m.get("alpha_cutoff", 0.5)
-            md.transmission = m.get("transmission", 0.0)
-            md.alpha_mask = 1 if m.get("alpha_mask") else 0
-            md.has_transmission = 1 if m.get("has_transmission") else 0
-            for slot in ("base_color", "metallic_roughness", "normal", "emissive", "occlusion",
-                         "transmission_texture"):
-                t = m.get(slot)
-                setattr(md, slot, texref(*t) if t is not None else texref())
-            mats[i] = md
-        texs = (TextureDesc * max(1, len(sd["textures"])))()
-        for i, t in enumerate(sd["textures"]):
-            data = np.ascontiguousarray(t["rgba8"], np.uint32)
-            keep.append(data)
-            texs[i] = TextureDesc(t["width"], t["height"], t["type"], 0, _up(data))
-        cube = np.ascontiguousarray(sd["cubemap"], np.uint32)
-        keep += [meshes, nodes, mats, texs, cube]
-        desc = SceneDesc()
-        desc.mesh_count = len(sd["meshes"])
-        desc.node_count = len(sd["nodes"])
-        desc.material_count = len(sd["materials"])
-        desc.texture_count = len(sd["textures"])
-        desc.meshes = C.cast(meshes, C.POINTER(MeshDesc))
-        desc.nodes = C.cast(nodes, C.POINTER(NodeDesc))
-        desc.materials = C.cast(mats, C.POINTER(MaterialDesc))
-        desc.textures = C.cast(texs, C.POINTER(TextureDesc))
-        desc.cubemap_face_size = sd["cubemap_face_size"]
-        desc.voxel_grid_size = sd.get("voxel_grid_size", 128)
-        desc.cubemap_faces = _up(cube)
-        desc.specular_samples = sd.get("specular_samples", 64)
-        desc.brdf_lut_size = sd.get("brdf_lut_size", 128)
-        desc.gi_sh_scale = sd.get("gi_sh_scale", 0.25)
-        desc.sky_visibility = sd.get("sky_visibility", 1.0)
-        desc.host_threads = host_threads
-        desc.flags = (SCENE_HOST_ONLY if host_only else 0) | (SCENE_GI if gi else 0)
+        flags = (SCENE_HOST_ONLY if host_only else 0) | (SCENE_GI if gi else 0)
+        desc, keep = scene_desc(sd, flags, host_threads)
         h = C.c_void_p()
         check(lib().swr_scene_create(C.byref(desc), C.byref(h)))
         self.handle = h
-        self._keep = None  # the library copied everything it needs
+        # The scene dict and flags the scene was made from; the library
+        # copied everything it needs.
+        self.source, self.flags = sd, flags
 
     @classmethod
     def load_gltf(cls, path, cubemap_faces=None, cubemap_face_size=0, cubemap_path=None, voxel_grid_size=0,
@@ -365,8 +376,8 @@ class Scene:
         h = C.c_void_p()
         check(lib().swr_scene_load_gltf(os.fsencode(path), C.byref(o), C.byref(h)))
         self = cls.__new__(cls)
-        self._keep = None
         self.handle = h
+        self.source, self.flags = None, o.flags
         return self
 
     def info(self):
@@ -397,6 +408,7 @@ def make_camera(position, look_at, fov, width, height, far_plane):
     t = (C.c_float * 3)(*look_at)
     check(lib().swr_camera_init(C.byref(cam), p, t, fov, float(width), float(height), far_plane))
     check(lib().swr_camera_update(C.byref(cam)))
+    cam.args = (tuple(position), tuple(look_at), fov, width, height, far_plane)
     return cam
 
 

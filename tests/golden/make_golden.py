@@ -1,7 +1,8 @@
 """Generates tests/golden/oracle_frames.json: hashes and sample values of the
-oracle's frames on seeded scenes. They pin the oracle (and the host-side
-scene precompute it consumes) against regressions; the reference itself
-cannot be run here, so these are not reference outputs.
+oracle's frames on seeded scenes, each scene and camera built by the oracle
+itself. They pin the oracle (its load-time scene build and its frame)
+against regressions; the reference itself cannot be run here, so these are
+not reference outputs.
 
 Run: python tests/golden/make_golden.py
 """
@@ -20,7 +21,6 @@ import numpy as np  # noqa: E402
 
 import oracle  # noqa: E402
 import scenes  # noqa: E402
-import swr  # noqa: E402
 
 CASES = [
     {"name": "small_default", "scene": ("small", 3), "size": (320, 200), "rsqrt": 1, "dt": 0.0},
@@ -33,20 +33,21 @@ CASES = [
 def build(spec, w, h):
     kind, seed = spec
     if kind == "small":
-        s = swr.Scene(scenes.small_scene(seed=seed), host_only=True)
-        cam = swr.make_camera(*scenes.default_camera_params(s.info(), w, h))
+        s = oracle.Scene(scenes.small_scene(seed=seed))
+        _, _, c, diag = s.bounds
+        cam = oracle.camera(*scenes.default_camera_params(scenes.Bounds(c, diag), w, h))
     else:
         sd, cp = scenes.stress_scene(seed=seed, triangles=20_000, width=w, height=h, n_textures=2, tex_size=64,
                                      cube_size=16, voxel=16, specular_samples=8, brdf_lut_size=16)
-        s = swr.Scene(sd, host_only=True)
-        cam = swr.make_camera(*cp)
+        s = oracle.Scene(sd)
+        cam = oracle.camera(*cp)
     return s, cam
 
 
 def render_case(c):
     w, h = c["size"]
     s, cam = build(tuple(c["scene"]), w, h)
-    rgba, vis, tl, res = oracle.render(s.export(), cam, w, h, rsqrt_mode=c["rsqrt"], threads=1, dt=c["dt"])
+    rgba, vis, tl, res = oracle.render(s, cam, w, h, rsqrt_mode=c["rsqrt"], threads=1, dt=c["dt"])
     s.close()
     return {"rgba_sha256": hashlib.sha256(rgba.tobytes()).hexdigest(),
             "vis_sha256": hashlib.sha256(vis.tobytes()).hexdigest(),

@@ -1,11 +1,12 @@
 """Voxel GI bake (the reference's --gi: bake_voxel_gi + blur_gi_sh4,
 src/gi.rs:316-408, src/voxelgrid.rs:422-472) on the device against the
-oracle's brute-force restatement, and frames shaded with the baked SH4 grid
-against the oracle. The bake samples surface textures bilinearly and converts
-them to linear with powf, which the device and the host's libm round
-differently in the last bit, so the grids are compared with a tolerance
-(2e-6 relative to the grid's largest value); frames shaded from the same
-grid are held to the usual bar (visibility bit-exact, colour within 1/255)."""
+oracle's own build of the scene with its brute-force bake, and frames shaded
+with the baked SH4 grid against the oracle's frames from its own grid. The
+bake samples surface textures bilinearly and converts them to linear with
+powf, which the device and the host's libm round differently in the last
+bit, so the grids are compared with a tolerance (2e-6 relative to the grid's
+largest value); frames are held to the usual bar (visibility bit-exact,
+colour within 1/255)."""
 import numpy as np
 import pytest
 
@@ -43,9 +44,12 @@ def test_gi_requires_device():
 @pytest.mark.gpu
 @pytest.mark.parametrize("kind", ["spheres", "translucent"])
 def test_bake_matches_oracle(kind):
-    s = swr.Scene(gi_scene(kind), gi=True)
+    sd = gi_scene(kind)
+    s = swr.Scene(sd, gi=True)
     grid, v = baked(s)
-    ref = oracle.gi_bake(v, threads=16)
+    o = oracle.Scene(sd, gi=True, threads=16)
+    n = o.view.voxel_size
+    ref = np.ctypeslib.as_array(o.view.voxel_gi_sh4, shape=(n * n * n, 4, 4)).copy()
     scale = float(np.abs(ref).max())
     d = np.abs(grid - ref)
     print("max abs %.3g (%.3g of max), exact %.4f" % (d.max(), d.max() / scale, (d == 0).mean()))

@@ -354,11 +354,15 @@ def test_malformed_documents_are_rejected(tmp_path):
 def test_loaded_scene_renders_like_the_oracle(tmp_path):
     # A loaded document (alpha-masked textured quad, translucent sphere,
     # sparse-accessor triangle) through the kernels and the oracle.
+    # The oracle builds the scene from the document itself (gltf_reference).
+    import gltf_reference
     from test_gpu_parity import compare
     rng = np.random.default_rng(9)
-    b, _, _ = build_doc(str(tmp_path), rng)
+    b, img, mr = build_doc(str(tmp_path), rng)
     s = swr.Scene.load_gltf(b.write(str(tmp_path / "r"), "glb"), cubemap_faces=cube_faces(), cubemap_face_size=FACE,
                             voxel_grid_size=16, specular_samples=8, brdf_lut_size=16)
+    s.source = gltf_reference.scene_dict(b, {"base.png": img, "orm.png": mr}, cube_faces(), FACE, voxel_grid_size=16,
+                                         specular_samples=8, brdf_lut_size=16)
     cam = swr.make_camera(*scenes.default_camera_params(s.info(), 200, 150))
     compare(s, cam, 200, 150)
     s.close()

@@ -60,7 +60,7 @@ def test_target_equals_copy(small, w, h):
 def test_target_matches_oracle(small):
     w, h = 256, 160
     arr, _, cam = frame_via_target(small, w, h)
-    orgba, _, _, _ = oracle.render(small.export(), cam, w, h, threads=1)
+    orgba, _, _, _ = oracle.render(small, cam, w, h, threads=1)
     d = np.abs(arr[:h].view(np.uint8).astype(np.int32) - orgba[:h].view(np.uint8).astype(np.int32))
     assert d.max() <= 1
 

@@ -20,7 +20,7 @@ def compare(scene, cam, w, h, **kw):
     rgba = r.blit()
     vis = r.visbuffer()
     tl = r.tile_luminance()
-    orgba, ovis, otl, res = oracle.render(scene.export(), cam, w, h, rsqrt_mode=mode, threads=1, dt=kw.get("dt", 0.0))
+    orgba, ovis, otl, res = oracle.render(scene, cam, w, h, rsqrt_mode=mode, threads=1, dt=kw.get("dt", 0.0))
     bad = int((vis != ovis).sum())
     assert bad == 0, "visibility differs in %d of %d pixels" % (bad, vis.size)
     rows = h & ~1

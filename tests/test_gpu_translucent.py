@@ -64,7 +64,7 @@ def test_translucent_sort_overflow_retries_smaller_tile():
     vis = r.visbuffer()
     st = r.stats()
     assert st.overflow_retries >= 1 and st.sched_tile < 64
-    orgba, ovis, otl, res = oracle.render(s.export(), cam, 160, 128, threads=1)
+    orgba, ovis, otl, res = oracle.render(s, cam, 160, 128, threads=1)
     assert int((vis != ovis).sum()) == 0
     d = np.abs(rgba.view(np.uint8).astype(np.int32) - orgba.view(np.uint8).astype(np.int32))
     assert d.max() <= 1

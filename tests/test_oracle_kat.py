@@ -3,7 +3,6 @@
 import numpy as np
 
 import oracle
-import swr
 from helpers import BACKGROUND, tri_scene
 
 W, H = 64, 48
@@ -11,9 +10,8 @@ CAM = ((0.0, 0.0, 5.0), (0.0, 0.0, 0.0), np.pi / 3, W, H, 20.0)
 
 
 def render(tris, **kw):
-    s = swr.Scene(tri_scene(tris), host_only=True)
-    cam = swr.make_camera(*CAM)
-    out = oracle.render(s.export(), cam, W, H, **kw)
+    s = oracle.Scene(tri_scene(tris))
+    out = oracle.render(s, oracle.camera(*CAM), W, H, **kw)
     s.close()
     return out
 
