@@ -430,6 +430,8 @@ typedef struct swr_frame_stats {
     uint64_t culled_pairs;      /* bin pairs the raster dropped as hidden behind depths already written */
     uint64_t kernel_launches;   /* kernels the renderer has enqueued since it was created (re-renders after
                                    an overflow included) */
+    uint64_t triangles_clip_path; /* triangles of primitives whose bounding sphere intersects the frustum:
+                                     the ones the reference sends through clip_against_frustum */
 } swr_frame_stats;
 
 swr_status swr_renderer_get_stats(swr_renderer* r, swr_frame_stats* out);

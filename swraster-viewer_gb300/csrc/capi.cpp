@@ -517,6 +517,7 @@ swr_status swr_renderer_get_stats(swr_renderer* r, swr_frame_stats* o) {
     o->staged_bytes = r->eng.lay.staged;
     o->culled_pairs = c.culled;
     o->kernel_launches = r->eng.kernel_launches;
+    o->triangles_clip_path = c.clip_path;
     return SWR_OK;
 }
 

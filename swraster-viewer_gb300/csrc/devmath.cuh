@@ -115,7 +115,18 @@ __device__ __forceinline__ float frsqrts(float a, float b) {
     return __fmul_rn(__fmaf_rn(-a, b, 3.0f), 0.5f);
 }
 // src/math.rs:17-25: y0 = vrsqrteq(x); y1 = y0 * vrsqrtsq(x * y0, y0).
+// For a positive normal x the estimate y0 is a positive normal and x * y0
+// (about sqrt(x)) is finite, so FRSQRTS takes its finite branch: that path
+// is evaluated inline, the rest goes through the general functions.
 __device__ __forceinline__ float rsqrt_aarch64(float x, const uint8_t* tab) {
+    const uint32_t b = __float_as_uint(x);
+    const uint32_t e = b >> 23;
+    if (e - 1u < 254u) {
+        const uint32_t m = b & 0x7FFFFFu;
+        const uint32_t scaled = (e & 1u) ? (128u | (m >> 16)) : (256u | (m >> 15));
+        const float y0 = __uint_as_float((((380u - e) >> 1) << 23) | ((uint32_t)tab[scaled] << 15));
+        return __fmul_rn(y0, __fmul_rn(__fmaf_rn(-__fmul_rn(x, y0), y0, 3.0f), 0.5f));
+    }
     const float y0 = frsqrte(x, tab);
     return __fmul_rn(y0, frsqrts(__fmul_rn(x, y0), y0));
 }

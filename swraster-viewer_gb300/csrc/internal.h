@@ -12,7 +12,7 @@
 //   draws      DDraw[D]     (node, primitive) pairs in canonical order, + MVP
 //   chunks     DChunk[]     256-triangle slices of draws, one CTA each
 //   tri_state  u8[T]        0 none, 1 record in slot g, 2 clipped
-//   rec_r      RecRaster[T + extra]   80 B: screen vertices, bbox, z/w, 1/w
+//   rec_r      RecRaster[T + extra]   80 B: screen vertices, bbox, z/w, 1/w, depth floor
 //   rec_s      RecShade [T + extra]  176 B: shading interpolators
 //   fan_base   u32[T]       first extra slot of a clipped triangle's fans 1..6
 //   bins       u32[cap]     record indices grouped by scheduling tile
@@ -157,7 +157,8 @@ struct alignas(16) DView {
     float cam_planes[24];      // view_clip_planes, view space
     uint32_t order_base;       // this view's sorted nodes in FrameArgs.node_order
     uint32_t n_order;
-    uint32_t pad3[2];
+    uint32_t tiles_x_magic;    // ceil(2^32 / tiles_x), 0 when tiles_x == 1 (quad row = (q >> 5) * magic >> 32)
+    uint32_t pad3;
 };
 
 // DView.flags
@@ -194,13 +195,15 @@ constexpr uint32_t kRecMaterialMask = 0x3FFFFFFFu;
 // Raster-side triangle record (one per emitted, non-culled triangle).
 struct alignas(16) RecRaster {
     int32_t p[6];              // screen subpixel positions p0, p1, p2
-    int32_t bb[4];             // screen_min_pixels.xy, screen_max_pixels.xy
+    uint16_t bb[4];            // screen_min_pixels.xy, screen_max_pixels.xy (0..32769)
     float ooa;                 // one_over_area
     float zow[3];              // z_over_w interpolator (a, da, db)
     float oow[3];              // one_over_w interpolator
     uint32_t seq8;             // (global triangle index << 3) | fan
     uint32_t material;
     uint32_t view;
+    uint32_t zfloor;           // orderable depth floor of the whole triangle (occlusion culling), 0 = none
+    uint32_t pad;
 };
 static_assert(sizeof(RecRaster) == 80, "RecRaster layout");
 
@@ -246,6 +249,7 @@ struct alignas(16) DCounters {
     uint32_t draw_chunks;      // chunks and draws of the frame's draw list
     uint32_t draw_count;
     uint32_t culled;           // (triangle, tile) pairs the raster dropped as hidden
+    uint32_t clip_path;        // triangles of draws whose sphere intersects the frustum (the clip path)
 };
 
 // Per-frame counts, uploaded with the tables: kernels read them from device
@@ -305,6 +309,7 @@ struct FrameArgs {
     uint32_t fused_shade;      // 32-px tiles: shade inside the raster kernel (8 and 16 px always do)
     uint32_t has_gi;           // some scene of the frame has a baked voxel grid
     uint32_t gpu_draws;        // build draws and chunks on the device (else the host staged them)
+    uint32_t rsqrt_uniform;    // 1 + the rsqrt mode all views share, 0 = per view
 };
 
 // Launch wrappers (kernels.cu). `ev`, when given, holds 8 events recorded

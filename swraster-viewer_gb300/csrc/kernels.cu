@@ -61,15 +61,54 @@ namespace swr {
 // --------------------------------------------------------------------------
 // Small vector helpers (one lane of Vec3x4 / Vec4).
 // --------------------------------------------------------------------------
+// Paired FP32 (sm_100 FADD2 / FMUL2): one instruction performs two IEEE
+// round-to-nearest additions or multiplications, each component exactly the
+// scalar operation, so vector arithmetic keeps the reference's results while
+// issuing fewer instructions.
+#ifndef SWR_PAIRED_FP32
+#define SWR_PAIRED_FP32 1
+#endif
+__device__ __forceinline__ float2 p2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 p_add(float2 a, float2 b) {
+#if SWR_PAIRED_FP32
+    return __fadd2_rn(a, b);
+#else
+    return make_float2(a.x + b.x, a.y + b.y);
+#endif
+}
+__device__ __forceinline__ float2 p_sub(float2 a, float2 b) { return p_add(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 p_mul(float2 a, float2 b) {
+#if SWR_PAIRED_FP32
+    return __fmul2_rn(a, b);
+#else
+    return make_float2(a.x * b.x, a.y * b.y);
+#endif
+}
+
 struct f3 {
     float x, y, z;
 };
 __device__ __forceinline__ f3 mk3(float x, float y, float z) { return {x, y, z}; }
-__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
-__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
-__device__ __forceinline__ f3 operator*(f3 a, f3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
-__device__ __forceinline__ f3 operator*(f3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
-__device__ __forceinline__ float dot(f3 a, f3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) {
+    const float2 r = p_add(p2(a.x, a.y), p2(b.x, b.y));
+    return {r.x, r.y, a.z + b.z};
+}
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) {
+    const float2 r = p_sub(p2(a.x, a.y), p2(b.x, b.y));
+    return {r.x, r.y, a.z - b.z};
+}
+__device__ __forceinline__ f3 operator*(f3 a, f3 b) {
+    const float2 r = p_mul(p2(a.x, a.y), p2(b.x, b.y));
+    return {r.x, r.y, a.z * b.z};
+}
+__device__ __forceinline__ f3 operator*(f3 a, float s) {
+    const float2 r = p_mul(p2(a.x, a.y), p2(s, s));
+    return {r.x, r.y, a.z * s};
+}
+__device__ __forceinline__ float dot(f3 a, f3 b) {
+    const float2 m = p_mul(p2(a.x, a.y), p2(b.x, b.y));
+    return (m.x + m.y) + a.z * b.z;
+}
 __device__ __forceinline__ f3 cross(f3 a, f3 b) {
     return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
 }
@@ -84,7 +123,8 @@ __device__ __forceinline__ float clampf(float v, float lo, float hi) { return fm
 // ScalarInterpolator::interpolate: (a + b1*da) + b2*db (src/util.rs:169-171).
 __device__ __forceinline__ float interp(const float* s, float b1, float b2) { return (s[0] + b1 * s[1]) + b2 * s[2]; }
 __device__ __forceinline__ f3 interp3(const float* s, float b1, float b2) {
-    return {(s[0] + b1 * s[3]) + b2 * s[6], (s[1] + b1 * s[4]) + b2 * s[7], (s[2] + b1 * s[5]) + b2 * s[8]};
+    const float2 xy = p_add(p_add(p2(s[0], s[1]), p_mul(p2(b1, b1), p2(s[3], s[4]))), p_mul(p2(b2, b2), p2(s[6], s[7])));
+    return {xy.x, xy.y, (s[2] + b1 * s[5]) + b2 * s[8]};
 }
 
 __constant__ float c_unorm8[256];  // i / 255.0 (src/util.rs:83-89)
@@ -95,7 +135,13 @@ __device__ __forceinline__ f3 unpack_rgb(uint32_t t) {
 
 // srgb_to_linear_fast (src/util.rs:111-113).
 __device__ __forceinline__ float srgb_fast(float x) { return x * (x * (x * 0.305306011f + 0.682171111f) + 0.012522878f); }
-__device__ __forceinline__ f3 srgb_fast3(f3 c) { return {srgb_fast(c.x), srgb_fast(c.y), srgb_fast(c.z)}; }
+__device__ __forceinline__ f3 srgb_fast3(f3 c) {
+    const float2 x = p2(c.x, c.y);
+    const float2 inner = p_add(p_mul(x, p2(0.305306011f, 0.305306011f)), p2(0.682171111f, 0.682171111f));
+    const float2 mid = p_add(p_mul(x, inner), p2(0.012522878f, 0.012522878f));
+    const float2 r = p_mul(x, mid);
+    return {r.x, r.y, srgb_fast(c.z)};
+}
 
 // --------------------------------------------------------------------------
 // Texture sampling (src/texture.rs:578-863)
@@ -363,6 +409,12 @@ __device__ __forceinline__ void for_each_stile(const DView& v, int32_t S, int32_
     }
 }
 
+// Occlusion culling runs for scheduling tiles of at least this many pixels
+// (the raster drops packets hidden behind the depths of earlier rounds).
+#ifndef SWR_CULL_MIN_TILE
+#define SWR_CULL_MIN_TILE 64
+#endif
+
 // bin_triangle (src/renderer.rs:668-831): setup + count. Returns true when
 // the triangle covers at least one tile; its records are then in r and q.
 __device__ bool setup_triangle(const FrameArgs& a, const DView& view, const Vtx& v0, const Vtx& v1, const Vtx& v2,
@@ -404,13 +456,15 @@ __device__ bool setup_triangle(const FrameArgs& a, const DView& view, const Vtx&
     const float s = ooa * 16.0f;
 
     r.p[0] = p0x; r.p[1] = p0y; r.p[2] = p1x; r.p[3] = p1y; r.p[4] = p2x; r.p[5] = p2y;
-    r.bb[0] = mnx; r.bb[1] = mny; r.bb[2] = mxx; r.bb[3] = mxy;
+    r.bb[0] = (uint16_t)mnx; r.bb[1] = (uint16_t)mny; r.bb[2] = (uint16_t)mxx; r.bb[3] = (uint16_t)mxy;
     r.ooa = ooa;
     r.zow[0] = zow0; r.zow[1] = zow1 - zow0; r.zow[2] = zow2 - zow0;
     r.oow[0] = oow0; r.oow[1] = oow1 - oow0; r.oow[2] = oow2 - oow0;
     r.seq8 = seq8;
     r.material = material;
     r.view = view_idx;
+    r.zfloor = 0u;  // taken by k_scatter when the frame culls
+    r.pad = 0u;
     q.nrm[0] = v0.nx; q.nrm[1] = v0.ny; q.nrm[2] = v0.nz;
     q.nrm[3] = v1.nx - v0.nx; q.nrm[4] = v1.ny - v0.ny; q.nrm[5] = v1.nz - v0.nz;
     q.nrm[6] = v2.nx - v0.nx; q.nrm[7] = v2.ny - v0.ny; q.nrm[8] = v2.nz - v0.nz;
@@ -733,6 +787,7 @@ __global__ void __launch_bounds__(256) k_reset(FrameArgs a) {
         a.counters->trans_next = 0u;
         a.counters->trans_packets = 0u;
         a.counters->culled = 0u;
+        a.counters->clip_path = 0u;
         a.counters->draw_tris = a.gpu_draws ? 0u : a.dyn->tri_total;
     }
     if (a.gpu_draws) draw_count_blocks(a);
@@ -774,6 +829,9 @@ __device__ __forceinline__ bool vtx_inside_all(const Vtx& v) {
 __device__ __forceinline__ void frontend_triangle(const FrameArgs& a, uint32_t chunk) {
     const DChunk ch = a.chunks[chunk];
     const DDraw& d = a.draws[ch.draw];
+    // The CTA's triangles are one draw's: count the chunk once for the
+    // reference's clip path (every triangle of an intersecting primitive).
+    if (threadIdx.x == 0 && d.clip) atomicAdd(&a.counters->clip_path, min((uint32_t)kChunkTris, d.tri_count - ch.tri_start));
     const uint32_t local = ch.tri_start + threadIdx.x;
     if (local >= d.tri_count) return;
     const uint32_t g = d.tri_begin + local;
@@ -1005,6 +1063,15 @@ __device__ __forceinline__ void scatter_slot(const FrameArgs& a, uint32_t slot, 
     const RecRaster& r = a.rec_r[slot];
     const DView& view = a.views[r.view];
     const uint32_t bin_off = (r.material & kRecTransBit) ? a.dyn->n_stiles : 0u;
+    if ((int32_t)a.sched_tile >= SWR_CULL_MIN_TILE && !(r.material & kRecTransBit)) {
+        // The depth floor of the whole triangle for the raster's occlusion
+        // culling: every packet's sample coordinates lie below the bbox end,
+        // so one floor bounds the depths of all its packets; taken once here
+        // instead of per packet and round in the raster.
+        float zl;
+        if (depth_floor(r.p, r.zow, r.oow, (int32_t)r.bb[2] * kSubpixelScale, (int32_t)r.bb[3] * kSubpixelScale, zl))
+            a.rec_r[slot].zfloor = float_to_ordered(zl);
+    }
     for_each_stile(view, (int32_t)a.sched_tile, r.bb[0], r.bb[1], r.bb[2], r.bb[3], [&](uint32_t b) {
         const uint32_t st = bin_off + b;
         const uint32_t active = __activemask();
@@ -1352,13 +1419,11 @@ __device__ __forceinline__ uint32_t cells_far(const RasterShared<S>& s, int32_t 
     return far;
 }
 
-// Orderable depth floor of the packet; 0 (below every key) when none is taken.
-// A packet is hidden when its floor is above the farthest depth of every cell
-// its covered lanes can fall in: pixels [x0 & ~1, x1] of its clipped rect.
-__device__ __forceinline__ uint32_t packet_floor(const PacketCtx& c) {
-    float z;
-    return depth_floor(c.r.p, c.r.zow, c.r.oow, c.xe, c.ye, z) ? float_to_ordered(z) : 0u;
-}
+// Orderable depth floor of the packet (its triangle's, taken by the front
+// end); 0 (below every key) when none is taken. A packet is hidden when its
+// floor is above the farthest depth of every cell its covered lanes can fall
+// in: pixels [x0 & ~1, x1] of its clipped rect.
+__device__ __forceinline__ uint32_t packet_floor(const PacketCtx& c) { return c.r.zfloor; }
 
 // Pass 1 of a round for one packet: classify and split into regions, and
 // either count them (regions, quads; the accepted 16-px blocks of a coarse
@@ -1412,7 +1477,10 @@ __device__ __forceinline__ void packet_regions(RasterShared<S>& s, const PacketC
 }
 
 __device__ __forceinline__ bool shade_needed(const DView& v, int32_t qx, int32_t qy);
-template <bool GI>
+// Shading variants by reciprocal square root: the values of SWR_RSQRT_IEEE and
+// SWR_RSQRT_AARCH64, or any (read per view).
+constexpr int kModeIeee = 0, kModeArm = 1, kModeAny = 2;
+template <bool GI, int MODE>
 __device__ __forceinline__ void shade_pixel(const FrameArgs& a, const uint8_t* tab, const DView& v,
                                             const DScene& sc, int32_t qx, int32_t qy, int32_t k, bool needed,
                                             unsigned long long key);
@@ -1426,9 +1494,6 @@ __device__ __forceinline__ void shade_pixel(const FrameArgs& a, const uint8_t* t
 // to 4,460; for the 16-px tiles of the 1280x720 small frame it cost 6%.
 // A first round of 64 packets: 4K raster 0.444 ms, against 0.461 (32),
 // 0.460 (128) and 0.477 (a full round of 256).
-#ifndef SWR_CULL_MIN_TILE
-#define SWR_CULL_MIN_TILE 64
-#endif
 #ifndef SWR_CULL_FIRST
 #define SWR_CULL_FIRST 64
 #endif
@@ -1632,7 +1697,7 @@ __global__ void __launch_bounds__(RasterShared<S>::kThreads, RasterShared<S>::kM
             const bool needed = live && shade_needed(view, qx, qy);
             unsigned long long key = kEmptyKey;
             if (needed) key = s.sk[(2 * (ql / QS) + (k >> 1)) * S + 2 * (ql % QS) + (k & 1)];
-            shade_pixel<true>(a, s.tab, view, sc, qx, qy, k, needed, key);
+            shade_pixel<true, kModeAny>(a, s.tab, view, sc, qx, qy, k, needed, key);
         }
         __syncthreads();
     }
@@ -1653,8 +1718,8 @@ __device__ __forceinline__ uint32_t find_view_by_quad(const FrameArgs& a, uint32
 }
 
 // compute_skybox for one lane (src/tilerasterizer.rs:478-508).
-__device__ f3 skybox(const DView& v, const DScene& sc, int32_t qx_screen, int32_t qy_screen, int32_t kx, int32_t ky,
-                     const uint8_t* tab) {
+__device__ __forceinline__ f3 skybox(const DView& v, const DScene& sc, int32_t qx_screen, int32_t qy_screen,
+                                     int32_t kx, int32_t ky, uint32_t md, const uint8_t* tab) {
     const float pxf = i2f(qx_screen) + (kx ? 1.5f : 0.5f);
     const float pyf = i2f(qy_screen) + (ky ? 1.5f : 0.5f);
     const float ndc_x = ((pxf * v.one_over_width) * 2.0f) - 1.0f;
@@ -1664,7 +1729,7 @@ __device__ f3 skybox(const DView& v, const DScene& sc, int32_t qx_screen, int32_
     d.x = ((ndc_x * m[0] + ndc_y * m[1]) + 1.0f * m[2]) + m[3];
     d.y = ((ndc_x * m[4] + ndc_y * m[5]) + 1.0f * m[6]) + m[7];
     d.z = ((ndc_x * m[8] + ndc_y * m[9]) + 1.0f * m[10]) + m[11];
-    const f3 n = normalize(d, v.rsqrt_mode, tab);
+    const f3 n = normalize(d, md, tab);
     float uf, vf;
     uint32_t slice;
     cube_uv(n, uf, vf, slice);
@@ -1735,24 +1800,30 @@ __device__ void voxel_gi(const DScene& sc, f3 pos, f3 sh[4], float& w0, float& w
         const float v0 = v00 * ofy + v10 * fy, v1 = v01 * ofy + v11 * fy;
         w0 = v0 * ofz + v1 * fz;
     }
+    // The constant channels (sky visibility and the 12 SH values): per
+    // channel ((c ofx + c fx) ofy + (..) fy) ofz + (..) fz, two channels per
+    // paired instruction.
+    const float2 OFX = p2(ofx, ofx), FX = p2(fx, fx), OFY = p2(ofy, ofy), FY = p2(fy, fy);
+    const float2 OFZ = p2(ofz, ofz), FZ = p2(fz, fz);
+    auto tri2 = [&](float2 c) {
+        const float2 v00 = p_add(p_mul(c, OFX), p_mul(c, FX));
+        const float2 v0 = p_add(p_mul(v00, OFY), p_mul(v00, FY));
+        return p_add(p_mul(v0, OFZ), p_mul(v0, FZ));
+    };
+    float o[14];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+        const int a0 = 2 * j, a1 = 2 * j + 1;
+        const float2 r = tri2(p2(sc.gi_rgb[a0 / 3][a0 % 3], sc.gi_rgb[a1 / 3][a1 % 3]));
+        o[a0] = r.x;
+        o[a1] = r.y;
+    }
     {
-        const float c = sc.sky_visibility;
-        const float v00 = c * ofx + c * fx;
-        const float v0 = v00 * ofy + v00 * fy;
-        w1 = v0 * ofz + v0 * fz;
+        const float2 r = tri2(p2(sc.sky_visibility, sc.sky_visibility));
+        w1 = r.x;
     }
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        float o[3];
-#pragma unroll
-        for (int ch = 0; ch < 3; ++ch) {
-            const float c = sc.gi_rgb[i][ch];
-            const float v00 = c * ofx + c * fx;
-            const float v0 = v00 * ofy + v00 * fy;
-            o[ch] = v0 * ofz + v0 * fz;
-        }
-        sh[i] = mk3(o[0], o[1], o[2]);
-    }
+    for (int i = 0; i < 4; ++i) sh[i] = mk3(o[3 * i], o[3 * i + 1], o[3 * i + 2]);
 }
 
 // One material texture of a lane: quad mip (compute_mip_level) and point
@@ -1767,9 +1838,9 @@ __device__ __forceinline__ uint32_t sample_slot(const DScene& sc, const DMateria
 // packet.du_dv * w with component i scaled by lane i's w (Q6 quirk). `cur` is
 // the colour under a translucent fragment. GI: read baked voxel grids.
 template <bool TRANS, bool GI>
-__device__ f3 pbr_lane(const DScene& sc, const DView& v, const DMaterial& m, const RecShade& q, float w, float b1,
-                       float b2, const float du_dv[4], const uint8_t* tab, f3 cur) {
-    const uint32_t md = v.rsqrt_mode;
+__device__ __forceinline__ f3 pbr_lane(const DScene& sc, const DView& v, const DMaterial& m, const RecShade& q,
+                                       float w, float b1, float b2, const float du_dv[4], uint32_t md,
+                                       const uint8_t* tab, f3 cur) {
     const float PI = 3.14159265358979f;
     const float EPS = 1e-6f;
     const float INV_PI = 1.0f / 3.14159265358979f;
@@ -1818,7 +1889,8 @@ __device__ f3 pbr_lane(const DScene& sc, const DView& v, const DMaterial& m, con
         ao = unpack_rgb(sample_slot(sc, m, TS_OCCLUSION, uvx, uvy, du_dv)).x;
         ao = 1.0f + (ao - 1.0f) * m.occlusion_strength;
     }
-    const f3 f0 = mk3(0.04f + (bc.x - 0.04f) * metal, 0.04f + (bc.y - 0.04f) * metal, 0.04f + (bc.z - 0.04f) * metal);
+    const f3 c004 = mk3(0.04f, 0.04f, 0.04f);
+    const f3 f0 = c004 + (bc - c004) * metal;
     const float omvh = 1.0f - vdh;
     const float omvh2 = omvh * omvh;
     const float omvh4 = omvh2 * omvh2;
@@ -1841,10 +1913,8 @@ __device__ f3 pbr_lane(const DScene& sc, const DView& v, const DMaterial& m, con
     const f3 cdd = (((lc * kd) * lambert) * ndl) * vli;
     const f3 cds = (((lc * fd) * spec_dg) * ndl) * vli;
     const f3 kdi = (one - f0) * (1.0f - metal);
-    f3 irr;
-    irr.x = fmaxf(((sh[0].x + sh[1].x * nw.y) + sh[2].x * nw.z) + sh[3].x * nw.x, 0.0f);
-    irr.y = fmaxf(((sh[0].y + sh[1].y * nw.y) + sh[2].y * nw.z) + sh[3].y * nw.x, 0.0f);
-    irr.z = fmaxf(((sh[0].z + sh[1].z * nw.y) + sh[2].z * nw.z) + sh[3].z * nw.x, 0.0f);
+    f3 irr = ((sh[0] + sh[1] * nw.y) + sh[2] * nw.z) + sh[3] * nw.x;
+    irr = mk3(fmaxf(irr.x, 0.0f), fmaxf(irr.y, 0.0f), fmaxf(irr.z, 0.0f));
     const f3 cid = ((irr * bc) * kdi) * INV_PI;
     // reflect: self - normal * self.dot(normal) * 2 (src/math.rs:118-120).
     const f3 iv = vn * -1.0f;
@@ -1863,11 +1933,10 @@ __device__ f3 pbr_lane(const DScene& sc, const DView& v, const DMaterial& m, con
         cube_uv(rd, uf, vf, slice);
         const f3 c0 = sample_cube(spec, uf, vf, slice, f2u_sat(m0));
         const f3 c1 = sample_cube(spec, uf, vf, slice, f2u_sat(m1));
-        env = mk3(c0.x + (c1.x - c0.x) * t, c0.y + (c1.y - c0.y) * t, c0.z + (c1.z - c0.z) * t);
+        env = c0 + (c1 - c0) * t;
     }
     const f3 lut = sample_bilinear(sc.textures[sc.tex_brdf_lut], clampf(ndv, 0.0f, 1.0f), clampf(rough, 0.0f, 1.0f));
-    f3 bsf = f0 * lut.x;
-    bsf = mk3(bsf.x + lut.y, bsf.y + lut.y, bsf.z + lut.y);
+    const f3 bsf = f0 * lut.x + mk3(lut.y, lut.y, lut.y);
     f3 cis = env * bsf;
     const float ao_spec = 1.0f + (ao - 1.0f) * 0.5f;
     cis = cis * (ao_spec * skyv);
@@ -1892,8 +1961,10 @@ __device__ __forceinline__ uint32_t tonemap_pack(f3 c, float exposure) {
     const float k = 0.2f;
     const float kk = 1.0f + k;
     c = c * exposure;
-    c = mk3((c.x / (c.x + k)) * kk, (c.y / (c.y + k)) * kk, (c.z / (c.z + k)) * kk);
-    const uint32_t r = f2u8_sat(c.x * 255.0f), g = f2u8_sat(c.y * 255.0f), b = f2u8_sat(c.z * 255.0f);
+    const f3 d = c + mk3(k, k, k);
+    c = mk3(c.x / d.x, c.y / d.y, c.z / d.z) * kk;
+    c = c * 255.0f;
+    const uint32_t r = f2u8_sat(c.x), g = f2u8_sat(c.y), b = f2u8_sat(c.z);
     return (r << 24) | (g << 16) | (b << 8) | 0xFFu;
 }
 
@@ -1907,11 +1978,14 @@ __device__ __forceinline__ bool shade_needed(const DView& v, int32_t qx, int32_t
 }
 
 // Shades lane k of quad (qx, qy) of view v given the pixel's depth key; all
-// 32 lanes of a warp call it together, 4 consecutive lanes per quad.
-template <bool GI>
+// 32 lanes of a warp call it together, 4 consecutive lanes per quad. MODE:
+// the reciprocal square root of every view of the launch, so only that one
+// is compiled in, or kModeAny to read it from the view.
+template <bool GI, int MODE>
 __device__ __forceinline__ void shade_pixel(const FrameArgs& a, const uint8_t* tab, const DView& v,
                                             const DScene& sc, int32_t qx, int32_t qy, int32_t k, bool needed,
                                             unsigned long long key) {
+    const uint32_t md = MODE == kModeAny ? v.rsqrt_mode : (uint32_t)MODE;
     const uint32_t lane = threadIdx.x & 31u;
     const int32_t kx = k & 1, ky = k >> 1;
     const int32_t px = 2 * qx + kx, py = 2 * qy + ky;
@@ -1961,11 +2035,11 @@ __device__ __forceinline__ void shade_pixel(const FrameArgs& a, const uint8_t* t
             }
             const float w_own = k == 0 ? wq[0] : (k == 1 ? wq[1] : (k == 2 ? wq[2] : wq[3]));
             const DMaterial& m = sc.materials[r.material & kRecMaterialMask];
-            col = pbr_lane<false, GI>(sc, v, m, q, w_own, b1, b2, dd, tab, col);
+            col = pbr_lane<false, GI>(sc, v, m, q, w_own, b1, b2, dd, md, tab, col);
             vis_hi = q.static_id;
             vis_fan = r.seq8 & 7u;
         } else {
-            col = skybox(v, sc, 2 * qx, 2 * qy, kx, ky, tab);
+            col = skybox(v, sc, 2 * qx, 2 * qy, kx, ky, md, tab);
         }
     }
     // Tile-centre luminance (src/tilerasterizer.rs:103-106): quad (0, 16).
@@ -1997,21 +2071,72 @@ __device__ __forceinline__ void shade_pixel(const FrameArgs& a, const uint8_t* t
     }
 }
 
+// Quad (qx, qy) of view-local quad index lq: rows of quad_pitch = tiles_x * 32
+// quads; the row is (lq >> 5) / tiles_x by a multiply with the view's
+// reciprocal (exact: lq >> 5 < 2^23, tiles_x <= 512).
+__device__ __forceinline__ void quad_xy(const DView& v, uint32_t lq, int32_t& qx, int32_t& qy) {
+    const uint32_t n = lq >> 5;
+    const uint32_t row = v.tiles_x_magic ? __umulhi(n, v.tiles_x_magic) : n;
+    qy = (int32_t)row;
+    qx = (int32_t)(lq - row * v.quad_pitch);
+}
+
 // One lane of the shading pass over the padded quad grid of every view.
-template <bool GI>
+template <bool GI, int MODE>
 __device__ __forceinline__ void shade_thread(const FrameArgs& a, const uint8_t* tab, uint32_t gt, uint32_t total) {
     const uint32_t gq = gt >> 2;
     const bool live = gq < total;
     const uint32_t vi = find_view_by_quad(a, live ? gq : 0u);
     const DView& v = a.views[vi];
-    const uint32_t lq = gq - v.quad_base;
-    const int32_t qx = (int32_t)(lq % v.quad_pitch), qy = (int32_t)(lq / v.quad_pitch);
+    int32_t qx, qy;
+    quad_xy(v, gq - v.quad_base, qx, qy);
     const int32_t k = (int32_t)(gt & 3u);
     const bool needed = live && shade_needed(v, qx, qy);
     unsigned long long key = kEmptyKey;
     if (needed)
         key = a.keys[v.key_offset + (uint64_t)(2 * qy + (k >> 1)) * v.key_pitch + (uint64_t)(2 * qx + (k & 1))];
-    shade_pixel<GI>(a, tab, v, a.scenes[v.scene], qx, qy, k, needed, key);
+    shade_pixel<GI, MODE>(a, tab, v, a.scenes[v.scene], qx, qy, k, needed, key);
+}
+
+// Before shading a pixel, the lane brings into L1 the depth key of the
+// pixel it shades next and the two records of that pixel's key as far as
+// the key is already cached, so the next iteration does not wait on memory
+// for them.
+#ifndef SWR_SHADE_PREFETCH
+#define SWR_SHADE_PREFETCH 1
+#endif
+__device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+__device__ __forceinline__ void shade_prefetch(const FrameArgs& a, uint32_t gt, uint32_t total) {
+    const uint32_t gq = gt >> 2;
+    if (gq >= total) return;
+    const DView& v = a.views[find_view_by_quad(a, gq)];
+    int32_t qx, qy;
+    quad_xy(v, gq - v.quad_base, qx, qy);
+    const int32_t k = (int32_t)(gt & 3u);
+    if (!shade_needed(v, qx, qy)) return;
+    const unsigned long long* kp =
+        a.keys + v.key_offset + (uint64_t)(2 * qy + (k >> 1)) * v.key_pitch + (uint64_t)(2 * qx + (k & 1));
+    prefetch_l1(kp);
+}
+__device__ __forceinline__ void record_prefetch(const FrameArgs& a, uint32_t gt, uint32_t total) {
+    const uint32_t gq = gt >> 2;
+    if (gq >= total) return;
+    const DView& v = a.views[find_view_by_quad(a, gq)];
+    int32_t qx, qy;
+    quad_xy(v, gq - v.quad_base, qx, qy);
+    const int32_t k = (int32_t)(gt & 3u);
+    if (!shade_needed(v, qx, qy)) return;
+    const unsigned long long key =
+        __ldg(a.keys + v.key_offset + (uint64_t)(2 * qy + (k >> 1)) * v.key_pitch + (uint64_t)(2 * qx + (k & 1)));
+    if (key == kEmptyKey) return;
+    const uint32_t s8 = key_seq8(key);
+    if ((s8 & 7u) != 0u) return;  // clipped fans: leave them to the regular load
+    const char* r = reinterpret_cast<const char*>(a.rec_r + (s8 >> 3));
+    const char* q = reinterpret_cast<const char*>(a.rec_s + (s8 >> 3));
+    prefetch_l1(r);
+    prefetch_l1(r + sizeof(RecRaster) - 1);
+    prefetch_l1(q);
+    prefetch_l1(q + 128);
 }
 
 // Three CTAs per SM (<= 85 registers): 4K frame shade 0.652 ms, against
@@ -2019,17 +2144,28 @@ __device__ __forceinline__ void shade_thread(const FrameArgs& a, const uint8_t* 
 #ifndef SWR_SHADE_MIN_BLOCKS
 #define SWR_SHADE_MIN_BLOCKS 3
 #endif
-// GI: the frame has scenes with a baked voxel grid.
-template <bool GI>
-__global__ void __launch_bounds__(256, SWR_SHADE_MIN_BLOCKS) k_shade(FrameArgs a) {
+#ifndef SWR_SHADE_THREADS
+#define SWR_SHADE_THREADS 256
+#endif
+// GI: the frame has scenes with a baked voxel grid. MODE: see shade_pixel.
+template <bool GI, int MODE>
+__global__ void __launch_bounds__(SWR_SHADE_THREADS, SWR_SHADE_MIN_BLOCKS) k_shade(FrameArgs a) {
     __shared__ uint8_t tab[512];
     for (int i = threadIdx.x; i < 512; i += blockDim.x) tab[i] = a.rsqrt_table[i];
     __syncthreads();
     // Every view's quad count is a multiple of 32, so each warp's lanes are
     // either all live or all past the end (warp-uniform loop).
     const uint32_t total = a.dyn->total_quads;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < total * 4u; base += gridDim.x * blockDim.x)
-        shade_thread<GI>(a, tab, base + threadIdx.x, total);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < total * 4u; base += stride) {
+#if SWR_SHADE_PREFETCH
+        // The key of the iteration after next, and the records of the next
+        // one (its key was brought in one iteration ago).
+        shade_prefetch(a, base + 2u * stride + threadIdx.x, total);
+        record_prefetch(a, base + stride + threadIdx.x, total);
+#endif
+        shade_thread<GI, MODE>(a, tab, base + threadIdx.x, total);
+    }
 }
 
 __global__ void k_rsqrt_selftest(const float* in, float* out, uint64_t n, uint32_t mode, const uint8_t* table) {
@@ -2199,7 +2335,8 @@ __global__ void __launch_bounds__(kTransThreads) k_translucent(FrameArgs a) {
 #pragma unroll
                 for (int l = 0; l < 4; ++l)
                     if (mask & (1u << l))
-                        col[l] = pbr_lane<true, true>(sc, view, m, qs, wl[l], b1[l], b2[l], dd, tab, col[l]);
+                        col[l] = pbr_lane<true, true>(sc, view, m, qs, wl[l], b1[l], b2[l], dd, view.rsqrt_mode,
+                                                      tab, col[l]);
                 touched = true;
             }
             if (!touched) continue;
@@ -2285,7 +2422,7 @@ void frame_grids(int num_sms, uint32_t S, bool fuse32, uint32_t* raster_grid, ui
         case 32: rb = fuse32 ? raster_blocks_per_sm<32, true>() : raster_blocks_per_sm<32, false>(); break;
         default: rb = raster_blocks_per_sm<64, false>(); break;
     }
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sb, k_shade<false>, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sb, k_shade<false, kModeArm>, SWR_SHADE_THREADS, 0);
     cudaGetLastError();
     *raster_grid = (uint32_t)(num_sms * (rb > 0 ? rb : 1));
     *shade_grid = (uint32_t)(num_sms * (sb > 0 ? sb : 1));
@@ -2362,10 +2499,16 @@ uint32_t launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t
     mark(6);
     if (!shade_fused(a.sched_tile, a.fused_shade != 0)) {
         const uint32_t sg = a.shade_grid > 0 ? a.shade_grid : (uint32_t)num_sms;
-        if (a.has_gi)
-            k_shade<true><<<sg, 256, 0, s>>>(a);
-        else
-            k_shade<false><<<sg, 256, 0, s>>>(a);
+        const uint32_t T = SWR_SHADE_THREADS;
+        if (a.has_gi) {
+            if (a.rsqrt_uniform == 1u + kModeArm) k_shade<true, kModeArm><<<sg, T, 0, s>>>(a);
+            else if (a.rsqrt_uniform == 1u + kModeIeee) k_shade<true, kModeIeee><<<sg, T, 0, s>>>(a);
+            else k_shade<true, kModeAny><<<sg, T, 0, s>>>(a);
+        } else {
+            if (a.rsqrt_uniform == 1u + kModeArm) k_shade<false, kModeArm><<<sg, T, 0, s>>>(a);
+            else if (a.rsqrt_uniform == 1u + kModeIeee) k_shade<false, kModeIeee><<<sg, T, 0, s>>>(a);
+            else k_shade<false, kModeAny><<<sg, T, 0, s>>>(a);
+        }
         launches++;
     }
     mark(7);

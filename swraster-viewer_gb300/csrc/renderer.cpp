@@ -55,6 +55,7 @@ void init_view(DView& v, const swr_camera& cam, int32_t width, int32_t height, u
     v.stiles_x = v.tiles_x * (kRefTile / (int32_t)S);
     v.stiles_y = v.tiles_y * (kRefTile / (int32_t)S);
     v.quad_pitch = (uint32_t)v.tiles_x * 32u;
+    v.tiles_x_magic = v.tiles_x > 1 ? (uint32_t)((0x100000000ull + (uint64_t)v.tiles_x - 1u) / (uint64_t)v.tiles_x) : 0u;
     v.key_pitch = (uint64_t)v.tiles_x * kRefTile;
 }
 
@@ -334,6 +335,12 @@ swr_status FrameEngine::prepare(const std::vector<const SceneImpl*>& scenes, std
     a.raster_grid = raster_grid;
     a.shade_grid = shade_grid;
     a.has_translucent = any_translucent ? 1u : 0u;
+    a.rsqrt_uniform = 0u;
+    if (!vws.empty()) {
+        bool same = true;
+        for (const DView& v : vws) same = same && v.rsqrt_mode == vws[0].rsqrt_mode;
+        if (same && vws[0].rsqrt_mode <= 1u) a.rsqrt_uniform = 1u + vws[0].rsqrt_mode;
+    }
     a.has_gi = 0u;
     for (const SceneImpl* sc : scenes)
         if (!sc->voxel_sh4.empty()) a.has_gi = 1u;

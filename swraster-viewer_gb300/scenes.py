@@ -95,6 +95,34 @@ def noise_texture(rng, size, cells=16, tint=None):
     return {"width": size, "height": size, "type": TEX_SRGB, "rgba8": pack_rgba8(n)}
 
 
+def normal_map_texture(rng, size, cells=8, strength=0.6):
+    """Tangent-space normal map of seeded value noise, (n + 1) / 2 in RGB."""
+    n = value_noise(rng, size, cells, channels=2)
+    x = (n[..., 0] - 0.5) * (2.0 * strength)
+    y = (n[..., 1] - 0.5) * (2.0 * strength)
+    z = np.sqrt(np.clip(1.0 - x * x - y * y, 0.05, 1.0))
+    inv = 1.0 / np.sqrt(x * x + y * y + z * z)
+    nm = np.stack([x * inv, y * inv, z * inv], -1)
+    return {"width": size, "height": size, "type": TEX_NORMAL, "rgba8": pack_rgba8(nm * 0.5 + 0.5)}
+
+
+def metallic_roughness_texture(rng, size, cells=8):
+    """glTF metallic-roughness layout: G roughness, B metallic (R unused)."""
+    n = value_noise(rng, size, cells)
+    return {"width": size, "height": size, "type": TEX_METALLIC_ROUGHNESS, "rgba8": pack_rgba8(n)}
+
+
+def occlusion_texture(rng, size, cells=8):
+    """Ambient occlusion in R, in [0.3, 1]."""
+    n = 0.3 + 0.7 * value_noise(rng, size, cells)
+    return {"width": size, "height": size, "type": TEX_LINEAR, "rgba8": pack_rgba8(n)}
+
+
+def emissive_texture(rng, size, cells=8):
+    n = value_noise(rng, size, cells) * rng.uniform(0.2, 1.0, 3).astype(np.float32)
+    return {"width": size, "height": size, "type": TEX_SRGB, "rgba8": pack_rgba8(n)}
+
+
 def cubemap_faces(rng, size):
     """Six seeded faces (+X,-X,+Y,-Y,+Z,-Z): a vertical sky gradient plus noise."""
     faces = []
@@ -138,6 +166,60 @@ def spheres_scene(seed=1, count=64, subdiv=3, box=10.0, radius=(0.5, 2.0), tex_s
     return {"meshes": meshes, "nodes": nodes, "materials": mats, "textures": [tex],
             "cubemap": cubemap_faces(rng, cube_size), "cubemap_face_size": cube_size, "voxel_grid_size": voxel,
             "specular_samples": specular_samples, "brdf_lut_size": brdf_lut_size}
+
+
+def textured_scene(seed=13, count=12, subdiv=2, box=4.0, tex_size=64, cube_size=16, voxel=24):
+    """Opaque materials with every texture slot of pbrMetallicRoughness in
+    play: base colour, metallic-roughness, normal map (generated tangents),
+    emissive texture and occlusion texture, each present or absent per
+    material, with mixed wrap modes; icospheres (normals given) and displaced
+    grids (normals generated)."""
+    rng = np.random.default_rng(seed)
+    P, F = icosphere(subdiv)
+    UV = spherical_uv(P)
+    GP, GUV, GF = grid(6, 6)
+    GP = GP.copy()
+    GP[:, 2] = 0.1 * np.sin(GP[:, 0] * 9.0) * np.cos(GP[:, 1] * 7.0)
+    textures = [noise_texture(rng, tex_size), metallic_roughness_texture(rng, tex_size),
+                normal_map_texture(rng, tex_size), emissive_texture(rng, tex_size // 2),
+                occlusion_texture(rng, tex_size), normal_map_texture(rng, tex_size * 2, strength=0.9)]
+    wraps = (WRAP_REPEAT, WRAP_MIRRORED, 2)
+
+    def ref(t):
+        return (t, int(rng.choice(wraps)), int(rng.choice(wraps)))
+
+    meshes, nodes, mats = [], [], []
+    centers = rng.uniform(-box, box, (count, 3)).astype(np.float32)
+    radii = rng.uniform(0.8, 2.0, count).astype(np.float32)
+    for i in range(count):
+        m = {"base_color_factor": tuple(float(x) for x in rng.uniform(0.4, 1.0, 3)) + (1.0,),
+             "metallic": float(rng.uniform(0.2, 1.0)), "roughness": float(rng.uniform(0.2, 1.0)),
+             "base_color": ref(0)}
+        if i % 3 != 2:
+            m["metallic_roughness"] = ref(1)
+        if i % 4 != 3:
+            m["normal"] = ref(2 if i % 2 == 0 else 5)
+        if i % 2 == 1:
+            m["emissive"] = ref(3)
+            m["emissive_factor"] = tuple(float(x) for x in rng.uniform(0.2, 1.5, 3))
+        elif i % 4 == 0:
+            m["emissive_factor"] = (0.3, 0.2, 0.1)
+        if i % 3 != 1:
+            m["occlusion"] = ref(4)
+            m["occlusion_strength"] = float(rng.uniform(0.3, 1.0))
+        mats.append(m)
+        if i % 3 == 0:
+            prim = {"positions": GP, "normals": None, "texcoords": GUV * np.float32(3.0), "indices": GF,
+                    "material": i}
+            w = translate_scale(centers[i], 2.5 * radii[i])
+        else:
+            prim = {"positions": P, "normals": P.copy(), "texcoords": UV, "indices": F, "material": i}
+            w = translate_scale(centers[i], radii[i])
+        meshes.append([prim])
+        nodes.append({"world": w, "local": w, "mesh": i})
+    return {"meshes": meshes, "nodes": nodes, "materials": mats, "textures": textures,
+            "cubemap": cubemap_faces(rng, cube_size), "cubemap_face_size": cube_size, "voxel_grid_size": voxel,
+            "specular_samples": 16, "brdf_lut_size": 32}
 
 
 def translucent_scene(seed=11, count=8, subdiv=2, box=4.0, tex_size=64, cube_size=16, voxel=32):
@@ -243,24 +325,36 @@ def _look_rotation(forward, up=(0.0, 1.0, 0.0)):
 
 def stress_scene(seed=2, triangles=2_000_000, width=3840, height=2160, fov=math.pi / 3.0, far=400.0,
                  n_textures=8, tex_size=2048, cube_size=128, voxel=128, area=(0.5, 5000.0), side_fraction=0.15,
-                 specular_samples=64, brdf_lut_size=128):
+                 specular_samples=64, brdf_lut_size=128, all_slots=False):
     """Plain method, large: `triangles` triangles in icospheres and displaced
     grids seen by a camera at the origin looking down -z.
 
     Each object draws its mean front-facing triangle screen area A
     log-uniformly from `area` px and gets about c / sqrt(A) triangles, so the
     per-object triangle area is log-uniform over 0.5-5000 px while the total
-    coverage stays near 8x the screen. About `side_fraction` of the objects
-    straddle a frustum side or the near plane. `n_textures` value-noise
-    textures of `tex_size`^2 (full mip chains) are shared by the materials.
+    coverage stays near 8x the screen. Objects centred on a frustum side
+    hold about `side_fraction` of the triangles (all of them take the clip
+    path); about 3% of the others cross the near plane. `n_textures` value-noise
+    textures of `tex_size`^2 (full mip chains) are shared by the materials. With
+    `all_slots` every material also carries a metallic-roughness, normal,
+    emissive and occlusion texture (four more shared textures of each kind).
     Returns (scene dict, camera params)."""
     rng = np.random.default_rng(seed)
     near = far * 0.01
     fpx = (height / 2.0) / math.tan(fov / 2.0)
     aspect = width / height
     textures = [noise_texture(rng, tex_size, cells=32, tint=rng.uniform(0.4, 1.0, 3)) for _ in range(n_textures)]
+    slot_base = len(textures)
+    if all_slots:
+        ssz = max(16, tex_size // 2)
+        for make in (metallic_roughness_texture, normal_map_texture, emissive_texture, occlusion_texture):
+            textures += [make(np.random.default_rng(seed * 7 + k), ssz) for k in range(4)]
     meshes, nodes, mats = [], [], []
-    total = 0
+    total = edge_tris = 0
+    tan_y = math.tan(fov / 2.0)
+    tan_x = tan_y * aspect
+    side_planes = [np.array(p) / np.linalg.norm(p) for p in
+                   ((1.0, 0.0, tan_x), (-1.0, 0.0, tan_x), (0.0, 1.0, tan_y), (0.0, -1.0, tan_y))]
     # c such that E[c / sqrt(A)] * objects ~= triangles with ~1000 tris per object.
     lo, hi = math.log(area[0]), math.log(area[1])
     e_inv_sqrt = (area[0] ** -0.5 - area[1] ** -0.5) / (0.5 * (hi - lo))
@@ -270,19 +364,26 @@ def stress_scene(seed=2, triangles=2_000_000, width=3840, height=2160, fov=math.
         T = int(max(8, min(8192, round(c / math.sqrt(A)))))
         if total + T > triangles:
             T = max(8, triangles - total)
-        edge = rng.random() < side_fraction
+        # Objects centred on a frustum side plane are chosen so that they hold
+        # about `side_fraction` of all triangles: their bounding spheres
+        # intersect the frustum, so all their triangles take the reference's
+        # clip path (src/renderer.rs:423-468). A few more objects cross the
+        # near plane; the reference's view-space near plane (0, 0, -1, near)
+        # is positive for every point in front of the camera
+        # (src/rendercamera.rs:141), so those stay off the clip path.
+        edge = edge_tris < side_fraction * (total + T)
+        near_obj = not edge and rng.random() < 0.03
         z = math.exp(rng.uniform(math.log(near * 3.0), math.log(far * 0.8)))
         if edge:
-            if rng.random() < 0.3:
-                z = near * rng.uniform(0.6, 2.0)  # crosses the near plane
-                nx, ny = rng.uniform(-0.8, 0.8), rng.uniform(-0.8, 0.8)
-            else:
-                side = rng.integers(4)
-                nx, ny = rng.uniform(-1.0, 1.0), rng.uniform(-1.0, 1.0)
-                if side == 0: nx = rng.uniform(0.95, 1.1)
-                elif side == 1: nx = -rng.uniform(0.95, 1.1)
-                elif side == 2: ny = rng.uniform(0.95, 1.1)
-                else: ny = -rng.uniform(0.95, 1.1)
+            side = rng.integers(4)
+            nx, ny = rng.uniform(-1.0, 1.0), rng.uniform(-1.0, 1.0)
+            if side == 0: nx = 1.0
+            elif side == 1: nx = -1.0
+            elif side == 2: ny = 1.0
+            else: ny = -1.0
+        elif near_obj:
+            z = near * rng.uniform(0.6, 2.0)  # crosses the near plane
+            nx, ny = rng.uniform(-0.8, 0.8), rng.uniform(-0.8, 0.8)
         else:
             nx, ny = rng.uniform(-0.95, 0.95), rng.uniform(-0.95, 0.95)
         center = np.array([nx * z * aspect * math.tan(fov / 2), ny * z * math.tan(fov / 2), -z], np.float32)
@@ -290,12 +391,21 @@ def stress_scene(seed=2, triangles=2_000_000, width=3840, height=2160, fov=math.
         ti = int(rng.integers(n_textures))
         mats.append({"base_color_factor": (1.0, 1.0, 1.0, 1.0), "metallic": float(rng.random()),
                      "roughness": float(rng.random()), "base_color": (ti, WRAP_REPEAT, WRAP_REPEAT)})
+        if all_slots:
+            k = len(mats) % 4
+            mats[-1].update({"metallic_roughness": (slot_base + k, WRAP_REPEAT, WRAP_REPEAT),
+                             "normal": (slot_base + 4 + k, WRAP_REPEAT, WRAP_REPEAT),
+                             "emissive": (slot_base + 8 + k, WRAP_MIRRORED, WRAP_REPEAT),
+                             "emissive_factor": (0.4, 0.3, 0.2),
+                             "occlusion": (slot_base + 12 + k, WRAP_REPEAT, WRAP_MIRRORED),
+                             "occlusion_strength": 0.8})
         if sphere:
             sub = int(np.clip(round(math.log(max(T, 20) / 20.0, 4)), 0, 5))
             P, UV, F = _ico(sub)
             T = F.size // 3
             r_px = math.sqrt(A * T / (2.0 * math.pi))
             r = r_px * z / fpx
+            bound = r * math.sqrt(3.0)  # bounding sphere of the unit icosphere's box, scaled
             M = np.eye(4, dtype=np.float32)
             M[:3, :3] *= r
             M[:3, 3] = center
@@ -306,6 +416,7 @@ def stress_scene(seed=2, triangles=2_000_000, width=3840, height=2160, fov=math.
             T = F.size // 3
             L_px = math.sqrt(A * T)
             L = L_px * z / fpx
+            bound = L * math.sqrt(0.5 + 0.08 * 0.08)
             P = P.copy()
             P[:, 2] = 0.08 * np.sin(P[:, 0] * rng.uniform(4, 12)) * np.cos(P[:, 1] * rng.uniform(4, 12))
             UV = UV * np.float32(rng.integers(1, 6))
@@ -320,6 +431,10 @@ def stress_scene(seed=2, triangles=2_000_000, width=3840, height=2160, fov=math.
         w = M.T.reshape(16).astype(np.float32).copy()
         nodes.append({"world": w, "local": w, "mesh": len(meshes) - 1})
         total += T
+        # Triangles on the clip path: the object's bounding sphere crosses a
+        # side plane (view space = world space for this camera).
+        if any(abs(float(np.dot(pn, center))) < bound for pn in side_planes):
+            edge_tris += T
     sd = {"meshes": meshes, "nodes": nodes, "materials": mats, "textures": textures,
           "cubemap": cubemap_faces(rng, cube_size), "cubemap_face_size": cube_size, "voxel_grid_size": voxel,
           "specular_samples": specular_samples, "brdf_lut_size": brdf_lut_size}

@@ -139,7 +139,7 @@ class FrameStats(C.Structure):
                 ("bin_pairs", C.c_uint64), ("bin_capacity", C.c_uint64), ("tiles", C.c_uint32),
                 ("overflow_retries", C.c_uint32), ("tile_luminance_mean", C.c_float), ("exposure", C.c_float),
                 ("sched_tile", C.c_uint32), ("staged_bytes", C.c_uint64), ("culled_pairs", C.c_uint64),
-                ("kernel_launches", C.c_uint64)]
+                ("kernel_launches", C.c_uint64), ("triangles_clip_path", C.c_uint64)]
 
 
 class ViewDesc(C.Structure):

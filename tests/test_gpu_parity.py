@@ -236,3 +236,40 @@ def test_stress_workload_full_4k():
     cam = swr.make_camera(*cp)
     compare(s, cam, 3840, 2160)
     s.close()
+
+
+@pytest.fixture(scope="module")
+def textured():
+    s = swr.Scene(scenes.textured_scene())
+    yield s
+    s.close()
+
+
+@pytest.mark.parametrize("tile", [16, 64])
+@pytest.mark.parametrize("mode", [swr.RSQRT_AARCH64, swr.RSQRT_IEEE])
+def test_opaque_texture_slots(textured, mode, tile):
+    # Opaque materials with normal maps over generated tangents
+    # (shader.rs:132-146), metallic-roughness and occlusion textures
+    # (shader.rs:182-200) and emissive textures (shader.rs:285-291), present
+    # or absent per material, with every wrap mode.
+    cam = swr.make_camera(*scenes.default_camera_params(textured.info(), 320, 200))
+    compare(textured, cam, 320, 200, rsqrt_mode=mode, sched_tile=tile)
+
+
+@pytest.mark.parametrize("tile", [8, 32])
+def test_opaque_texture_slots_close_up(textured, tile):
+    # Close to a displaced grid: magnified textures (mip 0), clipping.
+    c = np.array(textured.info().bounds_center[:])
+    cam = swr.make_camera((float(c[0]) + 0.3, float(c[1]) + 0.2, float(c[2]) + 2.0),
+                          (float(c[0]), float(c[1]), float(c[2]) - 1.0), 1.1, 256, 192, 40.0)
+    compare(textured, cam, 256, 192, sched_tile=tile)
+
+
+def test_stress_all_texture_slots_4k():
+    # The 4K workload with every material carrying metallic-roughness,
+    # normal, emissive and occlusion textures beside its base colour.
+    sd, cp = scenes.stress_scene(all_slots=True)
+    s = swr.Scene(sd)
+    cam = swr.make_camera(*cp)
+    compare(s, cam, 3840, 2160)
+    s.close()

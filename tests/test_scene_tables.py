@@ -148,6 +148,7 @@ SCENES = {
     "small": lambda: scenes.small_scene(seed=3),
     "translucent": lambda: scenes.translucent_scene(),
     "mixed": mixed_scene,
+    "textured": lambda: scenes.textured_scene(),
     "c1_spheres": lambda: scenes.spheres_scene(),
     "c2_reduced": lambda: scenes.stress_scene(seed=2, triangles=200_000, n_textures=2, tex_size=512)[0],
 }
