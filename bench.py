@@ -268,6 +268,7 @@ def measure_batched(args, hetero, steps, local=0):
     b = swr.Batch(use_graph=True)
     arr = swr.Batch.views([(sc, cam, w, h, 2.0, swr.RSQRT_AARCH64) for sc, cam, w, h in items])
     tile, _ = b.autotune(arr, sh)
+    tuning = b.tuning(arr)
     for _ in range(max(3, args.warmup)):
         b.render(arr, sh)
     b.sync()
@@ -309,7 +310,8 @@ def measure_batched(args, hetero, steps, local=0):
         s.close()
     n = len(items)
     out = {"metric": "views/s", "value": n / (ms_batch / 1000.0), "unit": "views/s", "steps": steps,
-           "ms_per_step": ms_batch, "config": dict(cfg, sched_tile=tile, graph=True), "clocks": clk,
+           "ms_per_step": ms_batch, "config": dict(cfg, sched_tile=tile, graph=True), "tuning": tuning,
+           "clocks": clk,
            "plain_sequential": {"value": n / (ms_seq / 1000.0), "unit": "views/s", "ms_per_batch": ms_seq},
            "speedup_vs_plain": ms_seq / ms_batch, "gpix_per_s": px / (ms_batch / 1000.0) / 1e9}
     if per_view:

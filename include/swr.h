@@ -473,7 +473,7 @@ typedef struct swr_batch_opts {
     uint32_t use_graph;         /* replay the frame as a CUDA graph */
     uint64_t bin_capacity;      /* initial pair capacity, 0 = auto */
     uint32_t flags;             /* SWR_BATCH_* */
-    uint32_t reserved;
+    uint32_t raster_ctas_per_sm;/* with sched_tile set: persistent raster CTAs per SM, 0 = as many as fit */
 } swr_batch_opts;
 
 /* swr_batch_opts.flags */
@@ -494,12 +494,33 @@ swr_status swr_batch_sync(swr_batch* b);
 swr_status swr_batch_output(swr_batch* b, int32_t view, const uint32_t** rgba8, const uint64_t** vis);
 /* Times every scheduling tile size (and, for 32-px tiles, shading fused
  * into the raster kernel or run after it; 8- and 16-px tiles always fuse,
- * 64-px tiles never) on these views and keeps the fastest for the batch's
- * class (pixel count, triangle count, view count). */
+ * 64-px tiles never), each with the persistent raster at 1, 2 or as many
+ * CTAs per SM as fit, on these views and keeps the fastest for the batch's
+ * class (pixel count, triangle count, view count), with the bin capacity it
+ * needed (swr_batch_get_tuning reports the choice). */
 swr_status swr_batch_autotune(swr_batch* b, const swr_view_desc* views, int32_t n, void* stream,
                               uint32_t* best_tile, float* best_ms);
 /* Milliseconds of the last synced batch on the device (CUDA events). */
 swr_status swr_batch_last_ms(swr_batch* b, float* ms);
+
+/* What the batch would use for these views: the autotuner's choice for
+ * their class (log2 pixels, log2 triangles, log2 views) when it has one,
+ * else the default choice. The autotuner sweeps the scheduling tile (8, 16,
+ * 32, 32 with shading fused into the raster kernel, 64) by the persistent
+ * raster's CTAs per SM (all that fit, 1, 2) and keeps, besides the fastest,
+ * the (triangle, tile) pair capacity that configuration needed, with which
+ * later batches of the class start. No counterpart in the reference. */
+typedef struct swr_batch_tuning {
+    uint32_t batch_class;
+    uint32_t tuned;               /* 1 when the autotuner measured this class */
+    uint32_t sched_tile;
+    uint32_t fused_shade;
+    uint32_t raster_ctas_per_sm;  /* 0 = as many as the registers allow */
+    uint32_t reserved;
+    uint64_t bin_capacity;        /* 0 = grown from overflow counters */
+} swr_batch_tuning;
+
+swr_status swr_batch_get_tuning(const swr_batch* b, const swr_view_desc* views, int32_t n, swr_batch_tuning* out);
 
 /* ------------------------------------------------------------------ */
 /* Served form: a request loop over resident scenes with memory-budget */

@@ -127,10 +127,20 @@ swr_status BatchImpl::sync(std::string& err) {
 swr_status BatchImpl::render(const swr_view_desc* vd, int32_t n, cudaStream_t stream, std::string& err) {
     swr_status st = sync(err);
     if (st != SWR_OK) return st;
-    // Tuned choices carry "32-px tiles shade inside the raster kernel" in bit 8.
-    const uint32_t want = opts.sched_tile ? opts.sched_tile | (opt_fuse32 ? 0x100u : 0u) : tuned_tile(vd, n);
+    // Tuned choices carry "32-px tiles shade inside the raster kernel" in bit 8
+    // and the raster CTAs per SM in bits 12-15.
+    const uint32_t cap = std::min<uint32_t>(opt_raster_cap ? opt_raster_cap : opts.raster_ctas_per_sm, 15u);
+    const uint32_t want = opts.sched_tile ? opts.sched_tile | (opt_fuse32 ? 0x100u : 0u) | (cap << 12)
+                                          : tuned_tile(vd, n);
     eng.sched_tile = want & 0xFFu;
     eng.fuse32 = (want & 0x100u) != 0u;
+    eng.raster_cta_cap = (want >> 12) & 0xFu;
+    if (!opts.sched_tile) {
+        // A tuned class starts with the bin capacity it needed, so its first
+        // batch is not rendered twice after a bin overflow.
+        auto it = tuned_bins.find(batch_class(vd, n));
+        if (it != tuned_bins.end() && eng.bin_cap < it->second) eng.bin_cap = it->second;
+    }
     saved.assign(vd, vd + n);
     saved_cams.resize((size_t)n);
     for (int32_t i = 0; i < n; ++i) saved_cams[i] = *vd[i].camera;
@@ -325,35 +335,72 @@ swr_status swr_batch_autotune(swr_batch* b, const swr_view_desc* views, int32_t 
     BatchImpl& B = b->impl;
     const swr_batch_opts keep = B.opts;
     uint32_t best = 64;
+    uint64_t best_pairs = 0;
     float bms = 1e30f;
-    // Scheduling tiles, and 32-px tiles with the shading fused into the raster.
+    // Scheduling tiles (32-px tiles also with the shading fused into the
+    // raster kernel) by raster CTAs per SM (0: as many as the registers
+    // allow); the bin capacity the best one needed is kept for the class.
     for (uint32_t code : {64u, 32u, 32u | 0x100u, 16u, 8u}) {
-        B.opts.sched_tile = code & 0xFFu;
-        B.opt_fuse32 = (code & 0x100u) != 0u;
-        float total = 0.0f;
-        for (int rep = 0; rep < 4; ++rep) {
-            swr_status st = B.render(views, n, (cudaStream_t)stream, err);
-            if (st == SWR_OK) st = B.sync(err);
-            if (st != SWR_OK) {
-                B.opts = keep;
-                B.opt_fuse32 = B.base_fuse32;
-                set_last_error(err.c_str());
-                return st;
+        for (uint32_t cap : {0u, 1u, 2u}) {
+            B.opts.sched_tile = code & 0xFFu;
+            B.opt_fuse32 = (code & 0x100u) != 0u;
+            B.opt_raster_cap = cap;
+            float total = 0.0f;
+            uint64_t pairs = 0;
+            for (int rep = 0; rep < 4; ++rep) {
+                swr_status st = B.render(views, n, (cudaStream_t)stream, err);
+                if (st == SWR_OK) st = B.sync(err);
+                if (st != SWR_OK) {
+                    B.opts = keep;
+                    B.opt_fuse32 = B.base_fuse32;
+                    B.opt_raster_cap = 0;
+                    set_last_error(err.c_str());
+                    return st;
+                }
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, B.ev_start, B.ev_end);
+                if (rep > 0) total += ms;  // first run warms capacities and graphs
+                pairs = B.eng.last.pairs;
             }
-            float ms = 0.0f;
-            cudaEventElapsedTime(&ms, B.ev_start, B.ev_end);
-            if (rep > 0) total += ms;  // first run warms capacities and graphs
-        }
-        if (total < bms) {
-            bms = total;
-            best = code;
+            if (total < bms) {
+                bms = total;
+                best = code | (cap << 12);
+                best_pairs = pairs;
+            }
         }
     }
     B.opts = keep;
     B.opt_fuse32 = B.base_fuse32;
-    B.tuned[batch_class(views, n)] = best;
+    B.opt_raster_cap = 0;
+    const uint32_t cls = batch_class(views, n);
+    B.tuned[cls] = best;
+    B.tuned_bins[cls] = best_pairs + best_pairs / 8 + 1024;
     if (best_tile) *best_tile = best & 0xFFu;
     if (best_ms) *best_ms = bms / 3.0f;
+    return SWR_OK;
+}
+
+swr_status swr_batch_get_tuning(const swr_batch* b, const swr_view_desc* views, int32_t n, swr_batch_tuning* out) {
+    std::string err;
+    if (!b || !out) {
+        set_last_error("null argument");
+        return SWR_INVALID_ARG;
+    }
+    if (!valid_views(views, n, err)) {
+        set_last_error(err.c_str());
+        return SWR_INVALID_ARG;
+    }
+    const BatchImpl& B = b->impl;
+    std::memset(out, 0, sizeof(*out));
+    out->batch_class = batch_class(views, n);
+    auto it = B.tuned.find(out->batch_class);
+    out->tuned = it != B.tuned.end() ? 1u : 0u;
+    const uint32_t code = B.tuned_tile(views, n);
+    out->sched_tile = code & 0xFFu;
+    out->fused_shade = (code & 0x100u) ? 1u : 0u;
+    out->raster_ctas_per_sm = (code >> 12) & 0xFu;
+    auto bt = B.tuned_bins.find(out->batch_class);
+    out->bin_capacity = bt != B.tuned_bins.end() ? bt->second : 0u;
     return SWR_OK;
 }
 

@@ -24,8 +24,11 @@ struct BatchImpl {
     DBuf tile_lum;
     std::vector<swr_view_desc> saved;
     std::vector<swr_camera> saved_cams;
-    std::map<uint32_t, uint32_t> tuned;  // class -> scheduling tile | 0x100 when 32-px tiles shade fused
+    // class -> scheduling tile | 0x100 when 32-px tiles shade fused | raster CTAs per SM << 12 (0: all that fit)
+    std::map<uint32_t, uint32_t> tuned;
+    std::map<uint32_t, uint64_t> tuned_bins;  // class -> (triangle, tile) pair capacity to start a batch with
     bool opt_fuse32 = false;             // with opts.sched_tile == 32: shade fused (autotuner trials)
+    uint32_t opt_raster_cap = 0;         // with opts.sched_tile set: raster CTAs per SM (autotuner trials)
     bool base_fuse32 = false;            // SWR_BATCH_FUSED_SHADE
     cudaEvent_t ev_start = nullptr, ev_end = nullptr;
     cudaStream_t last_stream = nullptr;

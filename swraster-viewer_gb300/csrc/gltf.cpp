@@ -179,13 +179,16 @@ bool read_accessor(const Doc& d, int64_t idx, int want_comps, std::vector<double
         err = "unsupported accessor layout";
         return false;
     }
-    // Elements come from a bufferView and/or sparse substitutions, each read
-    // from the document's buffers; no accessor can hold more elements than
-    // the buffers have bytes, so larger counts are malformed.
+    // An accessor with a bufferView reads every element from the document's
+    // buffers, so it cannot hold more elements than they have bytes. One
+    // without a bufferView starts as zeros (glTF 2.0, 3.6.2) and may take
+    // sparse substitutions: its count is capped by a fixed element limit.
+    constexpr int64_t kMaxZeroElements = int64_t(1) << 24;
     size_t total_bytes = 0;
     for (const std::vector<uint8_t>& b : d.buffers) total_bytes += b.size();
-    if ((uint64_t)count > (uint64_t)total_bytes) {
-        err = "accessor count beyond the document's buffers";
+    if (a->get("bufferView") ? (uint64_t)count > (uint64_t)total_bytes : count > kMaxZeroElements) {
+        err = a->get("bufferView") ? "accessor count beyond the document's buffers"
+                                   : "accessor without a bufferView has more than 2^24 elements";
         return false;
     }
     out.assign((size_t)count * nc, 0.0);

@@ -66,12 +66,28 @@ namespace swr {
 // scalar operation, so vector arithmetic keeps the reference's results while
 // issuing fewer instructions.
 #ifndef SWR_PAIRED_FP32
-#define SWR_PAIRED_FP32 1
+#define SWR_PAIRED_FP32 0
 #endif
 __device__ __forceinline__ float2 p2(float a, float b) { return make_float2(a, b); }
+#if SWR_PAIRED_FP32
+// Explicitly rounded PTX f32x2 operations: an add or multiply with a rounding
+// modifier is never contracted into a fused multiply-add.
+__device__ __forceinline__ unsigned long long p_pack(float2 a) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+    return r;
+}
+__device__ __forceinline__ float2 p_unpack(unsigned long long r) {
+    float2 a;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+    return a;
+}
+#endif
 __device__ __forceinline__ float2 p_add(float2 a, float2 b) {
 #if SWR_PAIRED_FP32
-    return __fadd2_rn(a, b);
+    unsigned long long r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(p_pack(a)), "l"(p_pack(b)));
+    return p_unpack(r);
 #else
     return make_float2(a.x + b.x, a.y + b.y);
 #endif
@@ -79,7 +95,9 @@ __device__ __forceinline__ float2 p_add(float2 a, float2 b) {
 __device__ __forceinline__ float2 p_sub(float2 a, float2 b) { return p_add(a, make_float2(-b.x, -b.y)); }
 __device__ __forceinline__ float2 p_mul(float2 a, float2 b) {
 #if SWR_PAIRED_FP32
-    return __fmul2_rn(a, b);
+    unsigned long long r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(p_pack(a)), "l"(p_pack(b)));
+    return p_unpack(r);
 #else
     return make_float2(a.x * b.x, a.y * b.y);
 #endif
@@ -2098,47 +2116,6 @@ __device__ __forceinline__ void shade_thread(const FrameArgs& a, const uint8_t* 
     shade_pixel<GI, MODE>(a, tab, v, a.scenes[v.scene], qx, qy, k, needed, key);
 }
 
-// Before shading a pixel, the lane brings into L1 the depth key of the
-// pixel it shades next and the two records of that pixel's key as far as
-// the key is already cached, so the next iteration does not wait on memory
-// for them.
-#ifndef SWR_SHADE_PREFETCH
-#define SWR_SHADE_PREFETCH 1
-#endif
-__device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
-__device__ __forceinline__ void shade_prefetch(const FrameArgs& a, uint32_t gt, uint32_t total) {
-    const uint32_t gq = gt >> 2;
-    if (gq >= total) return;
-    const DView& v = a.views[find_view_by_quad(a, gq)];
-    int32_t qx, qy;
-    quad_xy(v, gq - v.quad_base, qx, qy);
-    const int32_t k = (int32_t)(gt & 3u);
-    if (!shade_needed(v, qx, qy)) return;
-    const unsigned long long* kp =
-        a.keys + v.key_offset + (uint64_t)(2 * qy + (k >> 1)) * v.key_pitch + (uint64_t)(2 * qx + (k & 1));
-    prefetch_l1(kp);
-}
-__device__ __forceinline__ void record_prefetch(const FrameArgs& a, uint32_t gt, uint32_t total) {
-    const uint32_t gq = gt >> 2;
-    if (gq >= total) return;
-    const DView& v = a.views[find_view_by_quad(a, gq)];
-    int32_t qx, qy;
-    quad_xy(v, gq - v.quad_base, qx, qy);
-    const int32_t k = (int32_t)(gt & 3u);
-    if (!shade_needed(v, qx, qy)) return;
-    const unsigned long long key =
-        __ldg(a.keys + v.key_offset + (uint64_t)(2 * qy + (k >> 1)) * v.key_pitch + (uint64_t)(2 * qx + (k & 1)));
-    if (key == kEmptyKey) return;
-    const uint32_t s8 = key_seq8(key);
-    if ((s8 & 7u) != 0u) return;  // clipped fans: leave them to the regular load
-    const char* r = reinterpret_cast<const char*>(a.rec_r + (s8 >> 3));
-    const char* q = reinterpret_cast<const char*>(a.rec_s + (s8 >> 3));
-    prefetch_l1(r);
-    prefetch_l1(r + sizeof(RecRaster) - 1);
-    prefetch_l1(q);
-    prefetch_l1(q + 128);
-}
-
 // Three CTAs per SM (<= 85 registers): 4K frame shade 0.652 ms, against
 // 0.741 ms at two (95 registers) and 0.663 ms at four (64 registers).
 #ifndef SWR_SHADE_MIN_BLOCKS
@@ -2157,15 +2134,8 @@ __global__ void __launch_bounds__(SWR_SHADE_THREADS, SWR_SHADE_MIN_BLOCKS) k_sha
     // either all live or all past the end (warp-uniform loop).
     const uint32_t total = a.dyn->total_quads;
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < total * 4u; base += stride) {
-#if SWR_SHADE_PREFETCH
-        // The key of the iteration after next, and the records of the next
-        // one (its key was brought in one iteration ago).
-        shade_prefetch(a, base + 2u * stride + threadIdx.x, total);
-        record_prefetch(a, base + stride + threadIdx.x, total);
-#endif
+    for (uint32_t base = blockIdx.x * blockDim.x; base < total * 4u; base += stride)
         shade_thread<GI, MODE>(a, tab, base + threadIdx.x, total);
-    }
 }
 
 __global__ void k_rsqrt_selftest(const float* in, float* out, uint64_t n, uint32_t mode, const uint8_t* table) {

@@ -291,10 +291,12 @@ swr_status FrameEngine::prepare(const std::vector<const SceneImpl*>& scenes, std
     std::memcpy(hs + lay.o_views, vws.data(), vws.size() * sizeof(DView));
     if (!h_order.empty()) std::memcpy(hs + lay.o_order, h_order.data(), h_order.size() * sizeof(uint32_t));
     const bool fused32 = fuse32 && sched_tile == 32;
-    if (grid_tile != sched_tile || grid_fused32 != fused32) {
+    if (grid_tile != sched_tile || grid_fused32 != fused32 || grid_cap != raster_cta_cap) {
         frame_grids(num_sms, sched_tile, fused32, &raster_grid, &shade_grid);
+        if (raster_cta_cap) raster_grid = std::min<uint32_t>(raster_grid, (uint32_t)num_sms * raster_cta_cap);
         grid_tile = sched_tile;
         grid_fused32 = fused32;
+        grid_cap = raster_cta_cap;
     }
     uint8_t* tb = static_cast<uint8_t*>(tables.p);
     FrameArgs a{};

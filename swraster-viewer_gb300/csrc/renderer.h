@@ -82,6 +82,7 @@ struct FrameEngine {
     uint32_t pixel_cap = 0;
     uint64_t key_cap = 0;
     uint32_t raster_grid = 0, shade_grid = 0, grid_tile = 0;
+    uint32_t raster_cta_cap = 0, grid_cap = 0;  // raster CTAs per SM (0: as many as fit; batch autotuner's choice)
     bool fuse32 = false;        // 32-px tiles shade inside the raster kernel (batch autotuner's choice)
     bool grid_fused32 = false;
     DBuf tables, tri_state, rec_r, rec_s, fan_base, clip_queue;

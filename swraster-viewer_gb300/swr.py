@@ -142,6 +142,12 @@ class FrameStats(C.Structure):
                 ("kernel_launches", C.c_uint64), ("triangles_clip_path", C.c_uint64)]
 
 
+class BatchTuning(C.Structure):
+    _fields_ = [("batch_class", C.c_uint32), ("tuned", C.c_uint32), ("sched_tile", C.c_uint32),
+                ("fused_shade", C.c_uint32), ("raster_ctas_per_sm", C.c_uint32), ("reserved", C.c_uint32),
+                ("bin_capacity", C.c_uint64)]
+
+
 class ViewDesc(C.Structure):
     _fields_ = [("scene", C.c_void_p), ("camera", C.POINTER(Camera)), ("width", C.c_int32), ("height", C.c_int32),
                 ("exposure", C.c_float), ("rsqrt_mode", C.c_uint32), ("rgba8", C.c_void_p), ("vis", C.c_void_p)]
@@ -149,7 +155,7 @@ class ViewDesc(C.Structure):
 
 class BatchOpts(C.Structure):
     _fields_ = [("sched_tile", C.c_uint32), ("use_graph", C.c_uint32), ("bin_capacity", C.c_uint64),
-                ("flags", C.c_uint32), ("reserved", C.c_uint32)]
+                ("flags", C.c_uint32), ("raster_ctas_per_sm", C.c_uint32)]
 
 
 class ServerOpts(C.Structure):
@@ -181,7 +187,7 @@ EXPORTS = [
     "swr_renderer_set_exposure", "swr_renderer_get_stats", "swr_renderer_get_tile_luminance", "swr_last_error",
     "swr_abi_version", "swr_renderer_set_profiling", "swr_renderer_get_profile", "swr_render_frame_noalloc",
     "swr_batch_create", "swr_batch_destroy", "swr_batch_render", "swr_batch_sync", "swr_batch_output",
-    "swr_batch_autotune", "swr_batch_last_ms", "swr_server_create", "swr_server_destroy", "swr_server_add_scene",
+    "swr_batch_autotune", "swr_batch_last_ms", "swr_batch_get_tuning", "swr_server_create", "swr_server_destroy", "swr_server_add_scene",
     "swr_server_submit", "swr_server_poll", "swr_server_release", "swr_server_get_stats", "swr_copy_to_host",
     "swr_selftest_rsqrt", "swr_scene_load_gltf", "swr_selftest_depth_floor",
 ]
@@ -232,6 +238,7 @@ def lib():
         "swr_batch_output": ([vp, C.c_int32, C.POINTER(vp), C.POINTER(vp)], C.c_int),
         "swr_batch_autotune": ([vp, C.POINTER(ViewDesc), C.c_int32, vp, C.POINTER(C.c_uint32), f32p], C.c_int),
         "swr_batch_last_ms": ([vp, f32p], C.c_int),
+        "swr_batch_get_tuning": ([vp, C.POINTER(ViewDesc), C.c_int32, C.POINTER(BatchTuning)], C.c_int),
         "swr_server_create": ([C.POINTER(ServerOpts), C.POINTER(vp)], C.c_int),
         "swr_server_destroy": ([vp], None),
         "swr_server_add_scene": ([vp, vp, C.POINTER(C.c_int32)], C.c_int),
@@ -521,9 +528,9 @@ def copy_device_to_host(dev_ptr, nbytes, out, stream=None):
 class Batch:
     """Many views per launch sequence (swr_batch_*)."""
 
-    def __init__(self, sched_tile=0, use_graph=False, bin_capacity=0, fused_shade=False):
+    def __init__(self, sched_tile=0, use_graph=False, bin_capacity=0, fused_shade=False, raster_ctas_per_sm=0):
         h = C.c_void_p()
-        o = BatchOpts(sched_tile, 1 if use_graph else 0, bin_capacity, 1 if fused_shade else 0, 0)
+        o = BatchOpts(sched_tile, 1 if use_graph else 0, bin_capacity, 1 if fused_shade else 0, raster_ctas_per_sm)
         check(lib().swr_batch_create(C.byref(o), C.byref(h)))
         self.handle = h
 
@@ -553,6 +560,12 @@ class Batch:
         ms = C.c_float()
         check(lib().swr_batch_autotune(self.handle, arr, len(arr), stream, C.byref(t), C.byref(ms)))
         return t.value, ms.value
+
+    def tuning(self, arr):
+        """swr_batch_get_tuning: the configuration the batch uses for these views."""
+        t = BatchTuning()
+        check(lib().swr_batch_get_tuning(self.handle, arr, len(arr), C.byref(t)))
+        return {f: getattr(t, f) for f, _ in BatchTuning._fields_ if f != "reserved"}
 
     def last_ms(self):
         ms = C.c_float()

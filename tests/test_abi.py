@@ -119,7 +119,8 @@ MIRRORS = {"TextureDesc": "swr_texture_desc", "TexRef": "swr_texref", "MaterialD
            "NodeView": "swr_node_view", "MaterialView": "swr_material_view", "SceneHostView": "swr_scene_host_view",
            "Camera": "swr_camera", "RendererOpts": "swr_renderer_opts", "FrameStats": "swr_frame_stats",
            "ViewDesc": "swr_view_desc", "BatchOpts": "swr_batch_opts", "ServerOpts": "swr_server_opts",
-           "Request": "swr_request", "Completion": "swr_completion", "ServerStats": "swr_server_stats"}
+           "Request": "swr_request", "Completion": "swr_completion", "ServerStats": "swr_server_stats",
+           "BatchTuning": "swr_batch_tuning"}
 
 
 def test_struct_layouts_match_header(tmp_path):

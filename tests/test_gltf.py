@@ -366,3 +366,29 @@ def test_loaded_scene_renders_like_the_oracle(tmp_path):
     cam = swr.make_camera(*scenes.default_camera_params(s.info(), 200, 150))
     compare(s, cam, 200, 150)
     s.close()
+
+
+def test_zero_accessor_larger_than_the_buffers_loads(tmp_path):
+    # A POSITION accessor without a bufferView starts as zeros (glTF 2.0
+    # 3.6.2); sparse substitutions set three of its 100 vertices. Its count
+    # exceeds the buffer's bytes, which is valid for such an accessor.
+    b = DocBuilder()
+    si = b.accessor(np.array([0, 1, 2], np.uint8), 5121, "SCALAR")
+    sv = b.accessor(np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32), 5126, "VEC3")
+    idx = b.accessor(np.array([0, 1, 2], np.uint16), 5123, "SCALAR")
+    b.doc["accessors"].append({"componentType": 5126, "count": 100, "type": "VEC3",
+                               "sparse": {"count": 3,
+                                          "indices": {"bufferView": b.doc["accessors"][si]["bufferView"],
+                                                      "componentType": 5121},
+                                          "values": {"bufferView": b.doc["accessors"][sv]["bufferView"]}}})
+    pos = len(b.doc["accessors"]) - 1
+    b.doc["meshes"] = [{"primitives": [{"attributes": {"POSITION": pos}, "indices": idx}]}]
+    b.doc["nodes"] = [{"mesh": 0}]
+    assert len(b.bin) < 100
+    s = load(b.write(str(tmp_path / "z"), "glb"))
+    p = s.export().primitives[0]
+    assert p.vertex_count == 100
+    P = np.ctypeslib.as_array(p.positions, (400,)).reshape(100, 4)
+    np.testing.assert_array_equal(P[:3, :3], [[0, 0, 0], [1, 0, 0], [0, 1, 0]])
+    assert not P[3:, :3].any()
+    s.close()

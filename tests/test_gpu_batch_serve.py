@@ -74,9 +74,36 @@ def test_autotune_picks_a_tile(two_scenes):
     arr = swr.Batch.views(items)
     tile, ms = b.autotune(arr)
     assert tile in (8, 16, 32, 64) and ms > 0
+    t = b.tuning(arr)
+    assert t["tuned"] == 1 and t["sched_tile"] == tile
+    assert t["raster_ctas_per_sm"] in (0, 1, 2) and t["bin_capacity"] > 0
+    # The tuned configuration (its raster grid, its starting bin capacity)
+    # renders every view as the plain path does.
     b.render(arr)
     b.sync()
+    for i, (sc, cam, w, h, _, _) in enumerate(items):
+        rgba, vis = b.output(i, w, h)
+        ref_rgba, ref_vis = alone(sc, cam, w, h)
+        assert np.array_equal(vis, ref_vis), "view %d" % i
+        assert np.array_equal(rgba[:h & ~1], ref_rgba[:h & ~1]), "view %d" % i
     b.close()
+
+
+@pytest.mark.parametrize("cap", [1, 2])
+def test_raster_ctas_per_sm_equal_plain(two_scenes, cap):
+    # The persistent raster with fewer CTAs per SM than fit (autotuner trials).
+    sc = two_scenes[1]
+    items = [(sc, cam, w, h) for cam, w, h in sphere_cameras(sc, 3, [(320, 240), (200, 130)], seed=6)]
+    for tile in (64, 16):
+        b = swr.Batch(sched_tile=tile, raster_ctas_per_sm=cap)
+        arr = swr.Batch.views([(s, cam, w, h, 2.0, swr.RSQRT_AARCH64) for s, cam, w, h in items])
+        b.render(arr)
+        b.sync()
+        for i, (s, cam, w, h) in enumerate(items):
+            rgba, vis = b.output(i, w, h)
+            ref_rgba, ref_vis = alone(s, cam, w, h)
+            assert np.array_equal(vis, ref_vis), "tile %d view %d" % (tile, i)
+        b.close()
 
 
 def test_served_results_equal_alone(two_scenes):
