@@ -198,7 +198,7 @@ swr_status swr_scene_create(const swr_scene_desc* desc, swr_scene** out);
  * base64 data: buffers) and .glb files; every document node is kept
  * (compute_final_transform_recursive), primitives need positions and
  * indices, texture images are loaded from their URI relative to the file's
- * directory (PNG, or baseline JPEG) and images embedded in buffer views are
+ * directory (PNG, or sequential or progressive JPEG) and images embedded in buffer views are
  * skipped, as the reference does. The environment cubemap is given as raw
  * faces or as the path of a cross-layout image (the reference's
  * assets/cubemap.jpg). Errors: SWR_IO_ERROR (file, buffer or image),

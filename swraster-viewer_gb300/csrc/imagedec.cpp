@@ -526,6 +526,188 @@ void idct8x8(const float in[64], uint8_t* out, int stride) {
 
 }  // namespace
 
+namespace {
+
+// One scan (ITU T.81 B.2.3) into the components' coefficient blocks:
+// sequential (every coefficient of each block), or one progressive pass
+// (Annex G.1.2: DC first / refinement, AC first / refinement of the band
+// Ss..Se at bit Al, with end-of-band runs). One component: its blocks in
+// raster order over the component's own size; several: MCU order.
+struct JScan {
+    std::vector<JComp*> comps;
+    int ss = 0, se = 63, ah = 0, al = 0;
+    bool progressive = false;
+};
+
+bool decode_scan(JBits& b, const JScan& sc, const JHuff* hdc, const JHuff* hac, std::vector<std::vector<int16_t>>& coef,
+                 const std::vector<JComp>& all, uint32_t w, uint32_t h, int hmax, int vmax, int mcux, int mcuy,
+                 int restart, std::string& err) {
+    int eobrun = 0;
+    const bool single = sc.comps.size() == 1;
+    int units_x = mcux, units_y = mcuy;
+    if (single) {
+        const JComp& c = *sc.comps[0];
+        const uint32_t cw = (w * (uint32_t)c.h + (uint32_t)hmax - 1) / (uint32_t)hmax;
+        const uint32_t ch = (h * (uint32_t)c.v + (uint32_t)vmax - 1) / (uint32_t)vmax;
+        units_x = (int)((cw + 7) / 8);
+        units_y = (int)((ch + 7) / 8);
+    }
+    auto block = [&](JComp& c, int bx, int by) -> bool {
+        const size_t ci = (size_t)(&c - all.data());
+        int16_t* k0 = &coef[ci][((size_t)by * c.bw + bx) * 64];
+        const int p1 = 1 << sc.al, m1 = -(1 << sc.al);
+        if (!sc.progressive || sc.ss == 0) {
+            // DC (and, in a sequential scan, the AC coefficients after it).
+            if (sc.ah == 0) {
+                const int t = jhuff_decode(b, hdc[c.td]);
+                if (t < 0 || t > 11) {
+                    err = "jpeg: bad DC code";
+                    return false;
+                }
+                c.dc_pred += extend(b.bits(t), t);
+                k0[0] = (int16_t)(c.dc_pred * (1 << sc.al));
+            } else if (b.bit()) {
+                k0[0] = (int16_t)(k0[0] | p1);
+            }
+            if (sc.progressive) return true;
+            for (int k = 1; k < 64;) {
+                const int rs = jhuff_decode(b, hac[c.ta]);
+                if (rs < 0) {
+                    err = "jpeg: bad AC code";
+                    return false;
+                }
+                const int r = rs >> 4, sz = rs & 15;
+                if (sz == 0) {
+                    if (r != 15) break;  // end of block
+                    k += 16;
+                    continue;
+                }
+                k += r;
+                if (k > 63) {
+                    err = "jpeg: AC run past the block";
+                    return false;
+                }
+                k0[kZigzag[k]] = (int16_t)extend(b.bits(sz), sz);
+                ++k;
+            }
+            return true;
+        }
+        if (sc.ah == 0) {  // AC first pass
+            if (eobrun > 0) {
+                --eobrun;
+                return true;
+            }
+            for (int k = sc.ss; k <= sc.se;) {
+                const int rs = jhuff_decode(b, hac[c.ta]);
+                if (rs < 0) {
+                    err = "jpeg: bad AC code";
+                    return false;
+                }
+                const int r = rs >> 4, sz = rs & 15;
+                if (sz == 0) {
+                    if (r < 15) {  // end-of-band run of 2^r + r bits blocks, this one included
+                        eobrun = (1 << r) - 1;
+                        if (r) eobrun += b.bits(r);
+                        break;
+                    }
+                    k += 16;
+                    continue;
+                }
+                k += r;
+                if (k > sc.se) {
+                    err = "jpeg: AC run past the band";
+                    return false;
+                }
+                k0[kZigzag[k]] = (int16_t)(extend(b.bits(sz), sz) * (1 << sc.al));
+                ++k;
+            }
+            return true;
+        }
+        // AC refinement (G.1.2.3): a correction bit for each coefficient
+        // already nonzero, and new coefficients of magnitude 2^Al.
+        auto refine = [&](int16_t& v) {
+            if (b.bit() && (v & p1) == 0) v = (int16_t)(v + (v >= 0 ? p1 : m1));
+        };
+        int k = sc.ss;
+        if (eobrun == 0) {
+            for (; k <= sc.se; ++k) {
+                const int rs = jhuff_decode(b, hac[c.ta]);
+                if (rs < 0) {
+                    err = "jpeg: bad AC code";
+                    return false;
+                }
+                int r = rs >> 4;
+                const int sz = rs & 15;
+                int val = 0;
+                if (sz) {
+                    if (sz != 1) {
+                        err = "jpeg: bad AC refinement size";
+                        return false;
+                    }
+                    val = b.bit() ? p1 : m1;
+                } else if (r != 15) {
+                    eobrun = 1 << r;
+                    if (r) eobrun += b.bits(r);
+                    break;
+                }
+                // Skip r zero coefficients (refining the nonzero ones passed on
+                // the way); a new coefficient lands on the next zero one.
+                for (; k <= sc.se; ++k) {
+                    int16_t& cv = k0[kZigzag[k]];
+                    if (cv != 0) {
+                        refine(cv);
+                    } else {
+                        if (r == 0) break;
+                        --r;
+                    }
+                }
+                if (val) {
+                    if (k > sc.se) {
+                        err = "jpeg: AC refinement past the band";
+                        return false;
+                    }
+                    k0[kZigzag[k]] = (int16_t)val;
+                }
+            }
+        }
+        if (eobrun > 0) {
+            for (; k <= sc.se; ++k) {
+                int16_t& cv = k0[kZigzag[k]];
+                if (cv != 0) refine(cv);
+            }
+            --eobrun;
+        }
+        return true;
+    };
+    int todo = restart;
+    for (int uy = 0; uy < units_y; ++uy)
+        for (int ux = 0; ux < units_x; ++ux) {
+            if (restart && todo == 0) {
+                // Expect RSTn: realign to the byte after it.
+                b.cnt = 0;
+                b.marker = false;
+                while (b.pos + 1 < b.n && !(b.p[b.pos] == 0xFF && b.p[b.pos + 1] >= 0xD0 && b.p[b.pos + 1] <= 0xD7))
+                    ++b.pos;
+                b.pos += 2;
+                for (JComp* c : sc.comps) c->dc_pred = 0;
+                eobrun = 0;
+                todo = restart;
+            }
+            if (single) {
+                if (!block(*sc.comps[0], ux, uy)) return false;
+            } else {
+                for (JComp* c : sc.comps)
+                    for (int by = 0; by < c->v; ++by)
+                        for (int bx = 0; bx < c->h; ++bx)
+                            if (!block(*c, ux * c->h + bx, uy * c->v + by)) return false;
+            }
+            if (restart) --todo;
+        }
+    return true;
+}
+
+}  // namespace
+
 bool decode_jpeg(const uint8_t* d, size_t n, uint32_t& w, uint32_t& h, std::vector<uint8_t>& rgba,
                  std::string& err) {
     if (n < 4 || d[0] != 0xFF || d[1] != 0xD8) {
@@ -535,8 +717,9 @@ bool decode_jpeg(const uint8_t* d, size_t n, uint32_t& w, uint32_t& h, std::vect
     uint16_t qt[4][64] = {};
     JHuff hdc[4], hac[4];
     std::vector<JComp> comps;
+    std::vector<std::vector<int16_t>> coef;
     int hmax = 1, vmax = 1, restart = 0, mcux = 0, mcuy = 0;
-    bool have_frame = false;
+    bool have_frame = false, progressive = false, any_scan = false;
     size_t pos = 2;
     while (pos + 4 <= n) {
         if (d[pos] != 0xFF) {
@@ -589,11 +772,16 @@ bool decode_jpeg(const uint8_t* d, size_t n, uint32_t& w, uint32_t& h, std::vect
                 jhuff_build(t, counts);
                 i += total;
             }
-        } else if (m == 0xC0 || m == 0xC1) {  // SOF0 / SOF1
-            if (sl < 6 || s[0] != 8) {
-                err = "jpeg: only 8-bit sequential JPEG is supported";
+        } else if (m == 0xC0 || m == 0xC1 || m == 0xC2) {  // SOF0 / SOF1 / SOF2 (progressive)
+            if (have_frame) {
+                err = "jpeg: more than one frame";
                 return false;
             }
+            if (sl < 6 || s[0] != 8) {
+                err = "jpeg: only 8-bit JPEG is supported";
+                return false;
+            }
+            progressive = m == 0xC2;
             h = (uint32_t)(s[1] << 8 | s[2]);
             w = (uint32_t)(s[3] << 8 | s[4]);
             const int nc = s[5];
@@ -616,122 +804,120 @@ bool decode_jpeg(const uint8_t* d, size_t n, uint32_t& w, uint32_t& h, std::vect
             }
             mcux = (int)((w + 8 * hmax - 1) / (8 * hmax));
             mcuy = (int)((h + 8 * vmax - 1) / (8 * vmax));
-            for (JComp& c : comps) {
-                c.bw = mcux * c.h;
-                c.bh = mcuy * c.v;
-                c.pix.assign((size_t)c.bw * 8 * c.bh * 8, 0);
+            coef.resize(nc);
+            for (int c = 0; c < nc; ++c) {
+                comps[c].bw = mcux * comps[c].h;
+                comps[c].bh = mcuy * comps[c].v;
+                comps[c].pix.assign((size_t)comps[c].bw * 8 * comps[c].bh * 8, 0);
+                coef[c].assign((size_t)comps[c].bw * comps[c].bh * 64, 0);
             }
             have_frame = true;
-        } else if (m >= 0xC2 && m <= 0xCF && m != 0xC4 && m != 0xC8 && m != 0xCC) {
-            err = "jpeg: progressive, lossless and arithmetic-coded JPEG are not supported";
+        } else if (m >= 0xC3 && m <= 0xCF && m != 0xC4 && m != 0xC8 && m != 0xCC) {
+            err = "jpeg: lossless, hierarchical and arithmetic-coded JPEG are not supported";
             return false;
         } else if (m == 0xDD) {  // DRI
             if (sl >= 2) restart = s[0] << 8 | s[1];
-        } else if (m == 0xDA) {  // SOS: one interleaved scan covers the image
+        } else if (m == 0xDA) {  // SOS
             if (!have_frame || sl < 1) {
                 err = "jpeg: scan before frame";
                 return false;
             }
             const int ns = s[0];
-            if (ns != (int)comps.size() || sl < 1 + 2 * (size_t)ns + 3) {
-                err = "jpeg: only single-scan interleaved JPEG is supported";
+            if (ns < 1 || ns > (int)comps.size() || sl < 1 + 2 * (size_t)ns + 3) {
+                err = "jpeg: bad scan header";
                 return false;
             }
+            JScan sc;
+            sc.progressive = progressive;
             for (int k = 0; k < ns; ++k) {
                 const int cid = s[1 + 2 * k], td = s[2 + 2 * k] >> 4, ta = s[2 + 2 * k] & 15;
                 if (td > 3 || ta > 3) {
                     err = "jpeg: bad Huffman table id";
                     return false;
                 }
+                JComp* found = nullptr;
                 for (JComp& c : comps)
-                    if (c.id == cid) {
-                        c.td = td;
-                        c.ta = ta;
-                    }
+                    if (c.id == cid) found = &c;
+                if (!found) {
+                    err = "jpeg: scan names an unknown component";
+                    return false;
+                }
+                found->td = td;
+                found->ta = ta;
+                sc.comps.push_back(found);
             }
-            for (JComp& c : comps)
-                if (!hdc[c.td].present || !hac[c.ta].present) {
+            sc.ss = s[1 + 2 * ns];
+            sc.se = s[2 + 2 * ns];
+            sc.ah = s[3 + 2 * ns] >> 4;
+            sc.al = s[3 + 2 * ns] & 15;
+            if (progressive) {
+                // G.1.1.1.1: a DC scan has Ss = Se = 0; an AC scan one component
+                // and 1 <= Ss <= Se <= 63; refinement lowers Al by one.
+                const bool dc = sc.ss == 0;
+                if ((dc && sc.se != 0) || (!dc && (sc.se < sc.ss || sc.se > 63 || ns != 1)) || sc.al > 13 ||
+                    (sc.ah && sc.ah != sc.al + 1)) {
+                    err = "jpeg: bad progressive scan parameters";
+                    return false;
+                }
+            } else if (sc.ss != 0 || sc.se != 63 || sc.ah || sc.al) {
+                err = "jpeg: bad sequential scan parameters";
+                return false;
+            }
+            const bool needs_dc = !progressive || (sc.ss == 0 && sc.ah == 0);
+            const bool needs_ac = !progressive || sc.ss > 0;
+            for (JComp* c : sc.comps)
+                if ((needs_dc && !hdc[c->td].present) || (needs_ac && !hac[c->ta].present)) {
                     err = "jpeg: missing Huffman table";
                     return false;
                 }
+            for (JComp* c : sc.comps) c->dc_pred = 0;
             JBits b{d, n, pos + len};
-            int todo = restart;
-            for (int my = 0; my < mcuy; ++my)
-                for (int mx = 0; mx < mcux; ++mx) {
-                    if (restart && todo == 0) {
-                        // Expect RSTn: realign to the byte after it.
-                        b.cnt = 0;
-                        b.marker = false;
-                        while (b.pos + 1 < n && !(b.p[b.pos] == 0xFF && b.p[b.pos + 1] >= 0xD0 && b.p[b.pos + 1] <= 0xD7))
-                            ++b.pos;
-                        b.pos += 2;
-                        for (JComp& c : comps) c.dc_pred = 0;
-                        todo = restart;
-                    }
-                    for (JComp& c : comps)
-                        for (int by = 0; by < c.v; ++by)
-                            for (int bx = 0; bx < c.h; ++bx) {
-                                int coef[64] = {};
-                                const int t = jhuff_decode(b, hdc[c.td]);
-                                if (t < 0 || t > 11) {
-                                    err = "jpeg: bad DC code";
-                                    return false;
-                                }
-                                c.dc_pred += extend(b.bits(t), t);
-                                coef[0] = c.dc_pred;
-                                for (int k = 1; k < 64;) {
-                                    const int rs = jhuff_decode(b, hac[c.ta]);
-                                    if (rs < 0) {
-                                        err = "jpeg: bad AC code";
-                                        return false;
-                                    }
-                                    const int r = rs >> 4, sz = rs & 15;
-                                    if (sz == 0) {
-                                        if (r != 15) break;  // end of block
-                                        k += 16;
-                                        continue;
-                                    }
-                                    k += r;
-                                    if (k > 63) {
-                                        err = "jpeg: AC run past the block";
-                                        return false;
-                                    }
-                                    coef[kZigzag[k]] = extend(b.bits(sz), sz);
-                                    ++k;
-                                }
-                                float f[64];
-                                for (int k = 0; k < 64; ++k) f[k] = (float)coef[k] * (float)qt[c.tq][k];
-                                const int ox = (mx * c.h + bx) * 8, oy = (my * c.v + by) * 8;
-                                idct8x8(f, c.pix.data() + (size_t)oy * c.bw * 8 + ox, c.bw * 8);
-                            }
-                    if (restart) --todo;
-                }
-            // Colour: replicate subsampled components, JFIF YCbCr -> RGB.
-            rgba.assign((size_t)w * h * 4, 255);
-            for (uint32_t y = 0; y < h; ++y)
-                for (uint32_t x = 0; x < w; ++x) {
-                    float v[3];
-                    for (size_t k = 0; k < comps.size(); ++k) {
-                        const JComp& c = comps[k];
-                        const uint32_t sx = x * (uint32_t)c.h / (uint32_t)hmax, sy = y * (uint32_t)c.v / (uint32_t)vmax;
-                        v[k] = c.pix[(size_t)sy * c.bw * 8 + sx];
-                    }
-                    uint8_t* o = &rgba[((size_t)y * w + x) * 4];
-                    if (comps.size() == 1) {
-                        o[0] = o[1] = o[2] = (uint8_t)v[0];
-                    } else {
-                        const float Y = v[0], cb = v[1] - 128.0f, cr = v[2] - 128.0f;
-                        const float rgb[3] = {Y + 1.402f * cr, Y - 0.344136f * cb - 0.714136f * cr, Y + 1.772f * cb};
-                        for (int k = 0; k < 3; ++k)
-                            o[k] = (uint8_t)std::min(255.0f, std::max(0.0f, std::round(rgb[k])));
-                    }
-                }
-            return true;
+            if (!decode_scan(b, sc, hdc, hac, coef, comps, w, h, hmax, vmax, mcux, mcuy, restart, err)) return false;
+            any_scan = true;
+            // Continue after the entropy-coded data: the next marker that is
+            // not a stuffed byte or a restart marker.
+            size_t q = b.pos;
+            while (q + 1 < n && !(d[q] == 0xFF && d[q + 1] != 0x00 && !(d[q + 1] >= 0xD0 && d[q + 1] <= 0xD7))) ++q;
+            pos = q;
+            continue;
         }
         pos += len;
     }
-    err = "jpeg: no image data";
-    return false;
+    if (!any_scan) {
+        err = "jpeg: no image data";
+        return false;
+    }
+    // Dequantize and inverse-transform every block, then colour.
+    for (size_t ci = 0; ci < comps.size(); ++ci) {
+        JComp& c = comps[ci];
+        for (int by = 0; by < c.bh; ++by)
+            for (int bx = 0; bx < c.bw; ++bx) {
+                const int16_t* k0 = &coef[ci][((size_t)by * c.bw + bx) * 64];
+                float f[64];
+                for (int k = 0; k < 64; ++k) f[k] = (float)k0[k] * (float)qt[c.tq][k];
+                idct8x8(f, c.pix.data() + (size_t)by * 8 * c.bw * 8 + (size_t)bx * 8, c.bw * 8);
+            }
+    }
+    // Colour: replicate subsampled components, JFIF YCbCr -> RGB.
+    rgba.assign((size_t)w * h * 4, 255);
+    for (uint32_t y = 0; y < h; ++y)
+        for (uint32_t x = 0; x < w; ++x) {
+            float v[3];
+            for (size_t k = 0; k < comps.size(); ++k) {
+                const JComp& c = comps[k];
+                const uint32_t sx = x * (uint32_t)c.h / (uint32_t)hmax, sy = y * (uint32_t)c.v / (uint32_t)vmax;
+                v[k] = c.pix[(size_t)sy * c.bw * 8 + sx];
+            }
+            uint8_t* o = &rgba[((size_t)y * w + x) * 4];
+            if (comps.size() == 1) {
+                o[0] = o[1] = o[2] = (uint8_t)v[0];
+            } else {
+                const float Y = v[0], cb = v[1] - 128.0f, cr = v[2] - 128.0f;
+                const float rgb[3] = {Y + 1.402f * cr, Y - 0.344136f * cb - 0.714136f * cr, Y + 1.772f * cb};
+                for (int k = 0; k < 3; ++k) o[k] = (uint8_t)std::min(255.0f, std::max(0.0f, std::round(rgb[k])));
+            }
+        }
+    return true;
 }
 
 bool decode_image(const uint8_t* data, size_t n, uint32_t& w, uint32_t& h, std::vector<uint8_t>& rgba,

@@ -61,72 +61,15 @@ namespace swr {
 // --------------------------------------------------------------------------
 // Small vector helpers (one lane of Vec3x4 / Vec4).
 // --------------------------------------------------------------------------
-// Paired FP32 (sm_100 FADD2 / FMUL2): one instruction performs two IEEE
-// round-to-nearest additions or multiplications, each component exactly the
-// scalar operation, so vector arithmetic keeps the reference's results while
-// issuing fewer instructions.
-#ifndef SWR_PAIRED_FP32
-#define SWR_PAIRED_FP32 0
-#endif
-__device__ __forceinline__ float2 p2(float a, float b) { return make_float2(a, b); }
-#if SWR_PAIRED_FP32
-// Explicitly rounded PTX f32x2 operations: an add or multiply with a rounding
-// modifier is never contracted into a fused multiply-add.
-__device__ __forceinline__ unsigned long long p_pack(float2 a) {
-    unsigned long long r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
-    return r;
-}
-__device__ __forceinline__ float2 p_unpack(unsigned long long r) {
-    float2 a;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
-    return a;
-}
-#endif
-__device__ __forceinline__ float2 p_add(float2 a, float2 b) {
-#if SWR_PAIRED_FP32
-    unsigned long long r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(p_pack(a)), "l"(p_pack(b)));
-    return p_unpack(r);
-#else
-    return make_float2(a.x + b.x, a.y + b.y);
-#endif
-}
-__device__ __forceinline__ float2 p_sub(float2 a, float2 b) { return p_add(a, make_float2(-b.x, -b.y)); }
-__device__ __forceinline__ float2 p_mul(float2 a, float2 b) {
-#if SWR_PAIRED_FP32
-    unsigned long long r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(p_pack(a)), "l"(p_pack(b)));
-    return p_unpack(r);
-#else
-    return make_float2(a.x * b.x, a.y * b.y);
-#endif
-}
-
 struct f3 {
     float x, y, z;
 };
 __device__ __forceinline__ f3 mk3(float x, float y, float z) { return {x, y, z}; }
-__device__ __forceinline__ f3 operator+(f3 a, f3 b) {
-    const float2 r = p_add(p2(a.x, a.y), p2(b.x, b.y));
-    return {r.x, r.y, a.z + b.z};
-}
-__device__ __forceinline__ f3 operator-(f3 a, f3 b) {
-    const float2 r = p_sub(p2(a.x, a.y), p2(b.x, b.y));
-    return {r.x, r.y, a.z - b.z};
-}
-__device__ __forceinline__ f3 operator*(f3 a, f3 b) {
-    const float2 r = p_mul(p2(a.x, a.y), p2(b.x, b.y));
-    return {r.x, r.y, a.z * b.z};
-}
-__device__ __forceinline__ f3 operator*(f3 a, float s) {
-    const float2 r = p_mul(p2(a.x, a.y), p2(s, s));
-    return {r.x, r.y, a.z * s};
-}
-__device__ __forceinline__ float dot(f3 a, f3 b) {
-    const float2 m = p_mul(p2(a.x, a.y), p2(b.x, b.y));
-    return (m.x + m.y) + a.z * b.z;
-}
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ f3 operator*(f3 a, f3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+__device__ __forceinline__ f3 operator*(f3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ float dot(f3 a, f3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
 __device__ __forceinline__ f3 cross(f3 a, f3 b) {
     return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
 }
@@ -141,8 +84,7 @@ __device__ __forceinline__ float clampf(float v, float lo, float hi) { return fm
 // ScalarInterpolator::interpolate: (a + b1*da) + b2*db (src/util.rs:169-171).
 __device__ __forceinline__ float interp(const float* s, float b1, float b2) { return (s[0] + b1 * s[1]) + b2 * s[2]; }
 __device__ __forceinline__ f3 interp3(const float* s, float b1, float b2) {
-    const float2 xy = p_add(p_add(p2(s[0], s[1]), p_mul(p2(b1, b1), p2(s[3], s[4]))), p_mul(p2(b2, b2), p2(s[6], s[7])));
-    return {xy.x, xy.y, (s[2] + b1 * s[5]) + b2 * s[8]};
+    return {(s[0] + b1 * s[3]) + b2 * s[6], (s[1] + b1 * s[4]) + b2 * s[7], (s[2] + b1 * s[5]) + b2 * s[8]};
 }
 
 __constant__ float c_unorm8[256];  // i / 255.0 (src/util.rs:83-89)
@@ -153,13 +95,7 @@ __device__ __forceinline__ f3 unpack_rgb(uint32_t t) {
 
 // srgb_to_linear_fast (src/util.rs:111-113).
 __device__ __forceinline__ float srgb_fast(float x) { return x * (x * (x * 0.305306011f + 0.682171111f) + 0.012522878f); }
-__device__ __forceinline__ f3 srgb_fast3(f3 c) {
-    const float2 x = p2(c.x, c.y);
-    const float2 inner = p_add(p_mul(x, p2(0.305306011f, 0.305306011f)), p2(0.682171111f, 0.682171111f));
-    const float2 mid = p_add(p_mul(x, inner), p2(0.012522878f, 0.012522878f));
-    const float2 r = p_mul(x, mid);
-    return {r.x, r.y, srgb_fast(c.z)};
-}
+__device__ __forceinline__ f3 srgb_fast3(f3 c) { return {srgb_fast(c.x), srgb_fast(c.y), srgb_fast(c.z)}; }
 
 // --------------------------------------------------------------------------
 // Texture sampling (src/texture.rs:578-863)
@@ -1818,30 +1754,24 @@ __device__ void voxel_gi(const DScene& sc, f3 pos, f3 sh[4], float& w0, float& w
         const float v0 = v00 * ofy + v10 * fy, v1 = v01 * ofy + v11 * fy;
         w0 = v0 * ofz + v1 * fz;
     }
-    // The constant channels (sky visibility and the 12 SH values): per
-    // channel ((c ofx + c fx) ofy + (..) fy) ofz + (..) fz, two channels per
-    // paired instruction.
-    const float2 OFX = p2(ofx, ofx), FX = p2(fx, fx), OFY = p2(ofy, ofy), FY = p2(fy, fy);
-    const float2 OFZ = p2(ofz, ofz), FZ = p2(fz, fz);
-    auto tri2 = [&](float2 c) {
-        const float2 v00 = p_add(p_mul(c, OFX), p_mul(c, FX));
-        const float2 v0 = p_add(p_mul(v00, OFY), p_mul(v00, FY));
-        return p_add(p_mul(v0, OFZ), p_mul(v0, FZ));
-    };
-    float o[14];
-#pragma unroll
-    for (int j = 0; j < 6; ++j) {
-        const int a0 = 2 * j, a1 = 2 * j + 1;
-        const float2 r = tri2(p2(sc.gi_rgb[a0 / 3][a0 % 3], sc.gi_rgb[a1 / 3][a1 % 3]));
-        o[a0] = r.x;
-        o[a1] = r.y;
-    }
     {
-        const float2 r = tri2(p2(sc.sky_visibility, sc.sky_visibility));
-        w1 = r.x;
+        const float c = sc.sky_visibility;
+        const float v00 = c * ofx + c * fx;
+        const float v0 = v00 * ofy + v00 * fy;
+        w1 = v0 * ofz + v0 * fz;
     }
 #pragma unroll
-    for (int i = 0; i < 4; ++i) sh[i] = mk3(o[3 * i], o[3 * i + 1], o[3 * i + 2]);
+    for (int i = 0; i < 4; ++i) {
+        float o[3];
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+            const float c = sc.gi_rgb[i][ch];
+            const float v00 = c * ofx + c * fx;
+            const float v0 = v00 * ofy + v00 * fy;
+            o[ch] = v0 * ofz + v0 * fz;
+        }
+        sh[i] = mk3(o[0], o[1], o[2]);
+    }
 }
 
 // One material texture of a lane: quad mip (compute_mip_level) and point

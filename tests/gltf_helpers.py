@@ -142,8 +142,9 @@ def _cat(v):
     return 0 if v == 0 else int(v).bit_length()
 
 
-def write_jpeg(path, rgb, subsample=False, restart=0):
-    """Baseline JPEG of (h, w, 3) uint8 (or (h, w) grey): unit quantisers."""
+def _jpeg_blocks(rgb, subsample):
+    """Component planes -> (sampling factors, per-component zigzag blocks
+    [by][bx], MCU grid, padded block grid) with unit quantisers."""
     grey = rgb.ndim == 2
     h, w = rgb.shape[:2]
     x = rgb.astype(np.float64)
@@ -156,7 +157,9 @@ def write_jpeg(path, rgb, subsample=False, restart=0):
     hs = [2 if (subsample and i == 0) else 1 for i in range(len(planes))]
     hmax = max(hs)
     mw, mh = -(-w // (8 * hmax)), -(-h // (8 * hmax))
-    comps = []
+    C = np.array([[(np.sqrt(0.5) if u == 0 else 1.0) * np.cos((2 * xx + 1) * u * np.pi / 16) for xx in range(8)]
+                  for u in range(8)]) / 2.0
+    blocks = []
     for i, p in enumerate(planes):
         f = hs[i]
         pw, ph = mw * 8 * f, mh * 8 * f
@@ -165,27 +168,62 @@ def write_jpeg(path, rgb, subsample=False, restart=0):
             q = pad.reshape(mh * 8, 2, mw * 8, 2).mean(axis=(1, 3))
         else:
             q = np.pad(p, ((0, ph - h), (0, pw - w)), mode="edge")
-        comps.append(q)
-    C = np.array([[(np.sqrt(0.5) if u == 0 else 1.0) * np.cos((2 * xx + 1) * u * np.pi / 16) for xx in range(8)]
-                  for u in range(8)]) / 2.0
+        grid = []
+        for by in range(mh * f):
+            row = []
+            for bx in range(mw * f):
+                coef = np.rint(C @ (q[by * 8:by * 8 + 8, bx * 8:bx * 8 + 8] - 128.0) @ C.T).astype(int).reshape(-1)
+                row.append([int(coef[_ZZ[k]]) for k in range(64)])
+            grid.append(row)
+        blocks.append(grid)
+    return hs, hmax, blocks, mw, mh
+
+
+def _seg(m, body):
+    return bytes([0xFF, m]) + struct.pack(">H", len(body) + 2) + body
+
+
+def write_jpeg(path, rgb, subsample=False, restart=0, progressive=False):
+    """Baseline (or progressive) JPEG of (h, w, 3) uint8 (or (h, w) grey)
+    with unit quantisers. Both forms carry the same coefficients, so a
+    decoder must give them identical pixels."""
+    h, w = rgb.shape[:2]
+    hs, hmax, blocks, mw, mh = _jpeg_blocks(rgb, subsample)
+    nc = len(blocks)
+    out = b"\xff\xd8" + _seg(0xDB, bytes([0]) + bytes([1] * 64))
+    sof = struct.pack(">BHHB", 8, h, w, nc)
+    for i in range(nc):
+        sof += bytes([i + 1, (hs[i] << 4) | hs[i], 0])
+    out += _seg(0xC2 if progressive else 0xC0, sof)
+    if progressive:
+        out += _progressive_scans(h, w, hs, hmax, blocks, mw, mh, restart)
+    else:
+        out += _seg(0xC4, bytes([0x00]) + bytes(_DC_BITS) + bytes(_DC_VALS))
+        out += _seg(0xC4, bytes([0x10]) + bytes(_AC_BITS) + bytes(_AC_VALS))
+        if restart:
+            out += _seg(0xDD, struct.pack(">H", restart))
+        out += _baseline_scan(hs, blocks, mw, mh, restart)
+    with open(path, "wb") as f:
+        f.write(out + b"\xff\xd9")
+
+
+def _baseline_scan(hs, blocks, mw, mh, restart):
     dc_codes, ac_codes = _codes(_DC_BITS, _DC_VALS), _codes(_AC_BITS, _AC_VALS)
+    nc = len(blocks)
     bw = _BitWriter()
-    pred = [0] * len(comps)
-    nmcu, mcu = mw * mh, 0
+    pred = [0] * nc
+    mcu = 0
     for my in range(mh):
         for mx in range(mw):
             if restart and mcu and mcu % restart == 0:
                 bw.flush()
                 bw.out += bytes([0xFF, 0xD0 + ((mcu // restart - 1) % 8)])
-                pred = [0] * len(comps)
-            for ci, q in enumerate(comps):
+                pred = [0] * nc
+            for ci in range(nc):
                 f = hs[ci]
                 for by in range(f):
                     for bx in range(f):
-                        y0, x0 = (my * f + by) * 8, (mx * f + bx) * 8
-                        blk = q[y0:y0 + 8, x0:x0 + 8] - 128.0
-                        coef = np.rint(C @ blk @ C.T).astype(int).reshape(-1)
-                        zz = [coef[_ZZ[k]] for k in range(64)]
+                        zz = blocks[ci][my * f + by][mx * f + bx]
                         d = zz[0] - pred[ci]
                         pred[ci] = zz[0]
                         s = _cat(d)
@@ -209,23 +247,146 @@ def write_jpeg(path, rgb, subsample=False, restart=0):
                             bw.put(*ac_codes[0x00])
             mcu += 1
     bw.flush()
-    assert mcu == nmcu
-    seg = lambda m, body: bytes([0xFF, m]) + struct.pack(">H", len(body) + 2) + body
-    out = b"\xff\xd8"
-    out += seg(0xDB, bytes([0]) + bytes([1] * 64))
-    nc = len(comps)
-    sof = struct.pack(">BHHB", 8, h, w, nc)
-    for i in range(nc):
-        sof += bytes([i + 1, (hs[i] << 4) | hs[i], 0])
-    out += seg(0xC0, sof)
-    out += seg(0xC4, bytes([0x00]) + bytes(_DC_BITS) + bytes(_DC_VALS))
-    out += seg(0xC4, bytes([0x10]) + bytes(_AC_BITS) + bytes(_AC_VALS))
-    if restart:
-        out += seg(0xDD, struct.pack(">H", restart))
     sos = bytes([nc]) + b"".join(bytes([i + 1, 0x00]) for i in range(nc)) + bytes([0, 63, 0])
-    out += seg(0xDA, sos) + bytes(bw.out) + b"\xff\xd9"
-    with open(path, "wb") as f:
-        f.write(out)
+    return _seg(0xDA, sos) + bytes(bw.out)
+
+
+# Progressive tables: every DC size 0-11 in 4 bits, every AC run/size symbol
+# (runs 0-15, sizes 0-10: end-of-band runs, ZRL, coefficients) in 8 bits.
+_PDC_BITS = [0, 0, 0, 12] + [0] * 12
+_PDC_VALS = list(range(12))
+_PAC_VALS = [(r << 4) | s for r in range(16) for s in range(11)]
+_PAC_BITS = [0] * 7 + [len(_PAC_VALS)] + [0] * 8
+
+
+def _progressive_scans(h, w, hs, hmax, blocks, mw, mh, restart):
+    """Scans of T.81 Annex G: DC first (all components, Al 1), luma AC
+    bands 1-5 and 6-63 at Al 2, chroma AC 1-63 at Al 1, luma AC refinement
+    to Al 1, DC refinement, then every component's AC refinement to Al 0."""
+    dc_codes, ac_codes = _codes(_PDC_BITS, _PDC_VALS), _codes(_PAC_BITS, _PAC_VALS)
+    nc = len(blocks)
+    out = _seg(0xC4, bytes([0x00]) + bytes(_PDC_BITS) + bytes(_PDC_VALS))
+    out += _seg(0xC4, bytes([0x10]) + bytes(_PAC_BITS) + bytes(_PAC_VALS))
+    if restart:
+        out += _seg(0xDD, struct.pack(">H", restart))
+    script = [(list(range(nc)), 0, 0, 0, 1)]
+    if nc == 3:
+        script += [([0], 1, 5, 0, 2), ([0], 6, 63, 0, 2), ([1], 1, 63, 0, 1), ([2], 1, 63, 0, 1),
+                   ([0], 1, 63, 2, 1), (list(range(nc)), 0, 0, 1, 0), ([0], 1, 63, 1, 0), ([1], 1, 63, 1, 0),
+                   ([2], 1, 63, 1, 0)]
+    else:
+        script += [([0], 1, 9, 0, 1), ([0], 10, 63, 0, 1), (list(range(nc)), 0, 0, 1, 0), ([0], 1, 63, 1, 0)]
+    for comps, ss, se, ah, al in script:
+        out += _progressive_scan(h, w, hs, hmax, blocks, mw, mh, restart, comps, ss, se, ah, al, dc_codes, ac_codes)
+    return out
+
+
+def _progressive_scan(h, w, hs, hmax, blocks, mw, mh, restart, comps, ss, se, ah, al, dc_codes, ac_codes):
+    bw = _BitWriter()
+    st = {"eobrun": 0, "be": []}
+    pred = {c: 0 for c in comps}
+
+    def emit_eobrun():
+        n = st["eobrun"]
+        if n > 0:
+            nb = n.bit_length() - 1
+            bw.put(*ac_codes[nb << 4])
+            if nb:
+                bw.put(n & ((1 << nb) - 1), nb)
+            for bit in st["be"]:
+                bw.put(bit, 1)
+            st["eobrun"], st["be"] = 0, []
+
+    def block(ci, zz):
+        if ss == 0:
+            if ah == 0:
+                v = zz[0] >> al
+                d = v - pred[ci]
+                pred[ci] = v
+                s = _cat(d)
+                bw.put(*dc_codes[s])
+                if s:
+                    bw.put(d if d > 0 else d + (1 << s) - 1, s)
+            else:
+                bw.put((zz[0] >> al) & 1, 1)
+            return
+        if ah == 0:
+            r = 0
+            for k in range(ss, se + 1):
+                a = abs(zz[k]) >> al
+                if a == 0:
+                    r += 1
+                    continue
+                emit_eobrun()
+                while r > 15:
+                    bw.put(*ac_codes[0xF0])
+                    r -= 16
+                s = a.bit_length()
+                bw.put(*ac_codes[(r << 4) | s])
+                bw.put(a if zz[k] > 0 else (~a) & ((1 << s) - 1), s)
+                r = 0
+            if r > 0:
+                st["eobrun"] += 1
+                if st["eobrun"] == 0x7FFF:
+                    emit_eobrun()
+            return
+        absv = [abs(zz[k]) >> al for k in range(64)]
+        eob = 0
+        for k in range(ss, se + 1):
+            if absv[k] == 1:
+                eob = k
+        r, br = 0, []
+        for k in range(ss, se + 1):
+            a = absv[k]
+            if a == 0:
+                r += 1
+                continue
+            while r > 15 and k <= eob:
+                emit_eobrun()
+                bw.put(*ac_codes[0xF0])
+                r -= 16
+                for bit in br:
+                    bw.put(bit, 1)
+                br = []
+            if a > 1:
+                br.append(a & 1)
+                continue
+            emit_eobrun()
+            bw.put(*ac_codes[(r << 4) | 1])
+            bw.put(1 if zz[k] > 0 else 0, 1)
+            for bit in br:
+                bw.put(bit, 1)
+            br, r = [], 0
+        if r > 0 or br:
+            st["eobrun"] += 1
+            st["be"] += br
+            if st["eobrun"] == 0x7FFF or len(st["be"]) > 900:
+                emit_eobrun()
+
+    units = []
+    if len(comps) == 1:
+        c = comps[0]
+        cw, chh = -(-w * hs[c] // hmax), -(-h * hs[c] // hmax)
+        for by in range(-(-chh // 8)):
+            for bx in range(-(-cw // 8)):
+                units.append([(c, by, bx)])
+    else:
+        for my in range(mh):
+            for mx in range(mw):
+                units.append([(c, my * hs[c] + by, mx * hs[c] + bx) for c in comps
+                              for by in range(hs[c]) for bx in range(hs[c])])
+    for u, unit in enumerate(units):
+        if restart and u and u % restart == 0:
+            emit_eobrun()
+            bw.flush()
+            bw.out += bytes([0xFF, 0xD0 + ((u // restart - 1) % 8)])
+            pred = {c: 0 for c in comps}
+        for c, by, bx in unit:
+            block(c, blocks[c][by][bx])
+    emit_eobrun()
+    bw.flush()
+    sos = bytes([len(comps)]) + b"".join(bytes([c + 1, 0x00]) for c in comps) + bytes([ss, se, (ah << 4) | al])
+    return _seg(0xDA, sos) + bytes(bw.out)
 
 
 # ---------------------------------------------------------------------------- glTF

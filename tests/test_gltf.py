@@ -392,3 +392,40 @@ def test_zero_accessor_larger_than_the_buffers_loads(tmp_path):
     np.testing.assert_array_equal(P[:3, :3], [[0, 0, 0], [1, 0, 0], [0, 1, 0]])
     assert not P[3:, :3].any()
     s.close()
+
+
+def _jpeg_texels(tmp_path, name):
+    b = DocBuilder()
+    tri = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    b.doc["meshes"] = [{"primitives": [{"attributes": {"POSITION": b.accessor(tri, 5126, "VEC3")},
+                                        "indices": b.accessor(np.array([0, 1, 2], np.uint16), 5123, "SCALAR")}]}]
+    b.doc["nodes"] = [{"mesh": 0}]
+    b.doc["images"] = [{"uri": name}]
+    b.doc["textures"] = [{"source": 0}]
+    b.doc["materials"] = [{"pbrMetallicRoughness": {"baseColorTexture": {"index": 0}}}]
+    sc = load(b.write(str(tmp_path / (name + "_doc")), "bin"))
+    d, w, h, _ = tex_mip0(sc.export(), 0)
+    sc.close()
+    return d, w, h
+
+
+@pytest.mark.parametrize("shape,subsample,restart", [((21, 19, 3), False, 0), ((40, 37, 3), True, 0),
+                                                     ((33, 50, 3), True, 4), ((21, 19), False, 3),
+                                                     ((64, 48, 3), False, 7)])
+def test_progressive_jpeg_equals_baseline(tmp_path, shape, subsample, restart):
+    # A progressive file (DC first and refinement scans, luma AC split into
+    # two spectral bands, successive approximation from bit 2 to bit 0, end-
+    # of-band runs, restart intervals) carries the coefficients of the
+    # baseline file written from the same image: the decoder must give
+    # identical texels for both.
+    rng = np.random.default_rng(sum(shape) + restart)
+    img = rng.integers(0, 256, shape).astype(np.uint8)
+    if len(shape) == 3:
+        img[::3] = (scenes.value_noise(rng, max(shape[:2]), 4)[:shape[0], :shape[1]] * 255).astype(np.uint8)[::3]
+    write_jpeg(str(tmp_path / "b.jpg"), img, subsample=subsample, restart=restart)
+    write_jpeg(str(tmp_path / "p.jpg"), img, subsample=subsample, restart=restart, progressive=True)
+    assert (tmp_path / "p.jpg").read_bytes()[2:].find(b"\xff\xc2") >= 0
+    db, w, h = _jpeg_texels(tmp_path, "b.jpg")
+    dp, w2, h2 = _jpeg_texels(tmp_path, "p.jpg")
+    assert (w, h) == (w2, h2) == (shape[1], shape[0])
+    np.testing.assert_array_equal(dp, db)
