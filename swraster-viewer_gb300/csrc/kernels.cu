@@ -2046,17 +2046,18 @@ __device__ __forceinline__ void shade_thread(const FrameArgs& a, const uint8_t* 
     shade_pixel<GI, MODE>(a, tab, v, a.scenes[v.scene], qx, qy, k, needed, key);
 }
 
-// Three CTAs per SM (<= 85 registers): 4K frame shade 0.652 ms, against
-// 0.741 ms at two (95 registers) and 0.663 ms at four (64 registers).
-#ifndef SWR_SHADE_MIN_BLOCKS
-#define SWR_SHADE_MIN_BLOCKS 3
-#endif
-#ifndef SWR_SHADE_THREADS
-#define SWR_SHADE_THREADS 256
-#endif
+// CTA shape of the grid-stride shading kernel. Without voxel GI, seven
+// 128-thread CTAs per SM (<= 72 registers): 4K frame shade 0.604 ms, against
+// 0.612 ms at three 256-thread CTAs (80 registers), 0.741 ms at two (95) and
+// 0.663 ms at four (64). The GI variant keeps three 256-thread CTAs: at 72
+// registers its cone-tracing loop spills 216 B per thread.
+template <bool GI> struct ShadeShape {
+    static constexpr int kThreads = GI ? 256 : 128;
+    static constexpr int kMinBlocks = GI ? 3 : 7;
+};
 // GI: the frame has scenes with a baked voxel grid. MODE: see shade_pixel.
 template <bool GI, int MODE>
-__global__ void __launch_bounds__(SWR_SHADE_THREADS, SWR_SHADE_MIN_BLOCKS) k_shade(FrameArgs a) {
+__global__ void __launch_bounds__(ShadeShape<GI>::kThreads, ShadeShape<GI>::kMinBlocks) k_shade(FrameArgs a) {
     __shared__ uint8_t tab[512];
     for (int i = threadIdx.x; i < 512; i += blockDim.x) tab[i] = a.rsqrt_table[i];
     __syncthreads();
@@ -2322,7 +2323,7 @@ void frame_grids(int num_sms, uint32_t S, bool fuse32, uint32_t* raster_grid, ui
         case 32: rb = fuse32 ? raster_blocks_per_sm<32, true>() : raster_blocks_per_sm<32, false>(); break;
         default: rb = raster_blocks_per_sm<64, false>(); break;
     }
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sb, k_shade<false, kModeArm>, SWR_SHADE_THREADS, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sb, k_shade<false, kModeArm>, ShadeShape<false>::kThreads, 0);
     cudaGetLastError();
     *raster_grid = (uint32_t)(num_sms * (rb > 0 ? rb : 1));
     *shade_grid = (uint32_t)(num_sms * (sb > 0 ? sb : 1));
@@ -2398,13 +2399,23 @@ uint32_t launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t
     launches++;
     mark(6);
     if (!shade_fused(a.sched_tile, a.fused_shade != 0)) {
-        const uint32_t sg = a.shade_grid > 0 ? a.shade_grid : (uint32_t)num_sms;
-        const uint32_t T = SWR_SHADE_THREADS;
         if (a.has_gi) {
+            // a.shade_grid is sized for the variant without GI; this one's
+            // CTAs per SM are taken once (the same on every GB300).
+            static const uint32_t gi_blocks = [] {
+                int b = 0;
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shade<true, kModeArm>, ShadeShape<true>::kThreads, 0);
+                cudaGetLastError();
+                return (uint32_t)(b > 0 ? b : 1);
+            }();
+            const uint32_t sg = (uint32_t)num_sms * gi_blocks;
+            const uint32_t T = ShadeShape<true>::kThreads;
             if (a.rsqrt_uniform == 1u + kModeArm) k_shade<true, kModeArm><<<sg, T, 0, s>>>(a);
             else if (a.rsqrt_uniform == 1u + kModeIeee) k_shade<true, kModeIeee><<<sg, T, 0, s>>>(a);
             else k_shade<true, kModeAny><<<sg, T, 0, s>>>(a);
         } else {
+            const uint32_t sg = a.shade_grid > 0 ? a.shade_grid : (uint32_t)num_sms;
+            const uint32_t T = ShadeShape<false>::kThreads;
             if (a.rsqrt_uniform == 1u + kModeArm) k_shade<false, kModeArm><<<sg, T, 0, s>>>(a);
             else if (a.rsqrt_uniform == 1u + kModeIeee) k_shade<false, kModeIeee><<<sg, T, 0, s>>>(a);
             else k_shade<false, kModeAny><<<sg, T, 0, s>>>(a);
