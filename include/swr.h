@@ -46,7 +46,7 @@
 extern "C" {
 #endif
 
-#define SWR_ABI_VERSION 1
+#define SWR_ABI_VERSION 2
 
 typedef enum swr_status {
     SWR_OK = 0,
@@ -179,7 +179,27 @@ typedef struct swr_scene_desc {
     float sky_visibility;       /* 1.0 (src/main.rs:280) */
     uint32_t host_threads;      /* precompute threads, 0 = all cores */
     uint32_t flags;             /* SWR_SCENE_* */
+    /* Cache files (NULL = none), read when valid and written after the
+     * table is computed, as load_scene does. ggx_cache_path: the
+     * GGX-prefiltered environment (the reference's assets/cubemap.ggx,
+     * "GGX0" v1, src/texture.rs:425-554, src/scene.rs:164-205; keyed on the
+     * face size only, as there). gi_cache_path: with SWR_SCENE_GI, the baked
+     * grid (the reference's <scene>.gi, "VGI0" v8, src/gi.rs:30-117,
+     * src/main.rs:248-279); a valid file replaces the bake, which also lets
+     * SWR_SCENE_HOST_ONLY scenes carry a baked grid. Both are brotli
+     * streams, through the system's libbrotlienc/libbrotlidec; without
+     * them the tables are computed (swr_scene_info reports
+     * SWR_CACHE_NO_CODEC). */
+    const char* gi_cache_path;
+    const char* ggx_cache_path;
 } swr_scene_desc;
+
+/* swr_scene_info.gi_cache / ggx_cache */
+#define SWR_CACHE_NONE 0u          /* no path given */
+#define SWR_CACHE_LOADED 1u        /* the table was read from the file */
+#define SWR_CACHE_WRITTEN 2u       /* absent, stale or unreadable: computed, then written */
+#define SWR_CACHE_WRITE_FAILED 3u  /* computed; writing the file failed */
+#define SWR_CACHE_NO_CODEC 4u      /* computed; no brotli library to read or write it */
 
 /* swr_scene_desc.flags */
 #define SWR_SCENE_HOST_ONLY 1u  /* build and precompute only; no device copy
@@ -213,6 +233,9 @@ typedef struct swr_gltf_opts {
     uint32_t brdf_lut_size;         /* 0 = 128 */
     uint32_t host_threads;          /* precompute threads, 0 = all cores */
     uint32_t flags;                 /* SWR_SCENE_* */
+    const char* gi_cache_path;      /* as swr_scene_desc; the reference's is the
+                                       file's path with extension .gi */
+    const char* ggx_cache_path;     /* as swr_scene_desc (assets/cubemap.ggx there) */
 } swr_gltf_opts;
 
 swr_status swr_scene_load_gltf(const char* path, const swr_gltf_opts* opts, swr_scene** out);
@@ -228,9 +251,19 @@ typedef struct swr_scene_info {
     float bounds_max[3];
     float bounds_center[3];
     float bounds_diagonal;
+    uint32_t gi_cache;          /* SWR_CACHE_* */
+    uint32_t ggx_cache;         /* SWR_CACHE_* */
 } swr_scene_info;
 
 swr_status swr_scene_get_info(const swr_scene* scene, swr_scene_info* out);
+
+/* save_gi_cache (src/gi.rs:82-113) and save_prefiltered_specular_cubemap_cache
+ * (src/texture.rs:520-554): write the scene's baked GI grid / prefiltered
+ * environment to a cache file. SWR_INVALID_ARG when the scene has no baked
+ * grid; SWR_IO_ERROR when the file cannot be written or no brotli library
+ * is present. */
+swr_status swr_scene_save_gi_cache(const swr_scene* scene, const char* path);
+swr_status swr_scene_save_ggx_cache(const swr_scene* scene, const char* path);
 
 /* Read-only host view of the processed scene (generated normals and
  * tangents, mip chains, prefiltered cubemap, BRDF LUT, voxel grid). Test

@@ -9,6 +9,7 @@
 #include <string>
 
 #include "../../include/swr.h"
+#include "caches.h"
 #include "renderer.h"
 #include "scene.h"
 
@@ -91,6 +92,31 @@ swr_status swr_scene_get_info(const swr_scene* s, swr_scene_info* o) {
     o->bounds_center[0] = m.bounds_center.x; o->bounds_center[1] = m.bounds_center.y;
     o->bounds_center[2] = m.bounds_center.z;
     o->bounds_diagonal = m.bounds_diagonal;
+    o->gi_cache = m.gi_cache;
+    o->ggx_cache = m.ggx_cache;
+    return SWR_OK;
+}
+
+swr_status swr_scene_save_gi_cache(const swr_scene* s, const char* path) {
+    if (!s || !path) return fail(SWR_INVALID_ARG, "null argument");
+    if (s->impl.voxel_sh4.empty()) return fail(SWR_INVALID_ARG, "the scene has no baked GI grid (SWR_SCENE_GI)");
+    std::string err;
+    try {
+        if (!write_gi_cache(path, s->impl.voxel_n, s->impl.voxel_sh4, err)) return fail(SWR_IO_ERROR, err);
+    } catch (const std::bad_alloc&) {
+        return fail(SWR_NO_MEMORY, "out of host memory");
+    }
+    return SWR_OK;
+}
+
+swr_status swr_scene_save_ggx_cache(const swr_scene* s, const char* path) {
+    if (!s || !path) return fail(SWR_INVALID_ARG, "null argument");
+    std::string err;
+    try {
+        if (!write_ggx_cache(path, s->impl.specular, err)) return fail(SWR_IO_ERROR, err);
+    } catch (const std::bad_alloc&) {
+        return fail(SWR_NO_MEMORY, "out of host memory");
+    }
     return SWR_OK;
 }
 

@@ -647,6 +647,8 @@ extern "C" swr_status swr_scene_load_gltf(const char* path, const swr_gltf_opts*
         sd.sky_visibility = 1.0f;
         sd.host_threads = o.host_threads;
         sd.flags = o.flags;
+        sd.gi_cache_path = o.gi_cache_path;
+        sd.ggx_cache_path = o.ggx_cache_path;
         return swr_scene_create(&sd, out);
     } catch (const std::bad_alloc&) {
         return fail(SWR_NO_MEMORY, "out of host memory");

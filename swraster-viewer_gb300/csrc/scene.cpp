@@ -6,6 +6,8 @@
 // with -ffp-contract=off. Transcendentals (powf, sinf, cosf, sqrtf) come from
 // the host libm, the same functions a Rust build links.
 #include "scene.h"
+
+#include "caches.h"
 #include "precompute.h"
 
 #include <cuda_runtime.h>
@@ -945,7 +947,24 @@ swr_status build_scene(const swr_scene_desc* desc, SceneImpl* s, std::string& er
     }
     s->cubemap = make_texture(desc->cubemap_face_size, desc->cubemap_face_size, SWR_TEX_CUBEMAP, desc->cubemap_faces, true);
     s->cubemap.generate_mipmaps();
-    s->specular = generate_prefiltered_specular(s->cubemap, desc->specular_samples ? desc->specular_samples : 64u, threads);
+    // The GGX-prefiltered environment, read from its cache file when one is
+    // given and valid, else computed and written there (src/scene.rs:164-205).
+    bool specular_loaded = false;
+    if (desc->ggx_cache_path) {
+        std::string msg;
+        const CacheRead r = read_ggx_cache(desc->ggx_cache_path, s->cubemap.width, s->cubemap.height, s->specular, msg);
+        specular_loaded = r == CacheRead::Loaded;
+        s->ggx_cache = specular_loaded ? SWR_CACHE_LOADED : (r == CacheRead::NoCodec ? SWR_CACHE_NO_CODEC : 0u);
+    }
+    if (!specular_loaded) {
+        s->specular = generate_prefiltered_specular(s->cubemap, desc->specular_samples ? desc->specular_samples : 64u,
+                                                    threads);
+        if (desc->ggx_cache_path && s->ggx_cache != SWR_CACHE_NO_CODEC) {
+            std::string werr;
+            s->ggx_cache = write_ggx_cache(desc->ggx_cache_path, s->specular, werr) ? SWR_CACHE_WRITTEN
+                                                                                    : SWR_CACHE_WRITE_FAILED;
+        }
+    }
     compute_irradiance_sh4(s->cubemap, s->irradiance_sh);
     s->brdf_lut = generate_brdf_lut(desc->brdf_lut_size ? desc->brdf_lut_size : 128u, threads);
     // Voxel grid (src/main.rs:227-281).
@@ -1085,13 +1104,29 @@ swr_status build_scene(const swr_scene_desc* desc, SceneImpl* s, std::string& er
         }
     }
     // bake_voxel_gi (src/gi.rs:316-408) with the reference's --gi.
+    // The grid comes from the scene's .gi cache when one is given and valid
+    // (try_load_gi_cache, src/main.rs:248-279), else it is baked and written.
     if (desc->flags & SWR_SCENE_GI) {
-        if (desc->flags & SWR_SCENE_HOST_ONLY) {
-            err = "the GI bake runs on the device: SWR_SCENE_GI cannot be combined with SWR_SCENE_HOST_ONLY";
-            return SWR_INVALID_ARG;
+        bool gi_loaded = false;
+        if (desc->gi_cache_path) {
+            std::string msg;
+            const CacheRead r = read_gi_cache(desc->gi_cache_path, n, s->voxel_sh4, msg);
+            gi_loaded = r == CacheRead::Loaded;
+            s->gi_cache = gi_loaded ? SWR_CACHE_LOADED : (r == CacheRead::NoCodec ? SWR_CACHE_NO_CODEC : 0u);
         }
-        const swr_status gst = bake_gi(s, rt, active, n, bmn, vsz, err);
-        if (gst != SWR_OK) return gst;
+        if (!gi_loaded) {
+            if (desc->flags & SWR_SCENE_HOST_ONLY) {
+                err = "the GI bake runs on the device: SWR_SCENE_GI with SWR_SCENE_HOST_ONLY needs a valid GI cache file";
+                return SWR_INVALID_ARG;
+            }
+            const swr_status gst = bake_gi(s, rt, active, n, bmn, vsz, err);
+            if (gst != SWR_OK) return gst;
+            if (desc->gi_cache_path && s->gi_cache != SWR_CACHE_NO_CODEC) {
+                std::string werr;
+                s->gi_cache = write_gi_cache(desc->gi_cache_path, n, s->voxel_sh4, werr) ? SWR_CACHE_WRITTEN
+                                                                                          : SWR_CACHE_WRITE_FAILED;
+            }
+        }
     }
     // initialize_voxel_gi_from_scene (src/gi.rs:123-149).
     for (int i = 0; i < 4; ++i) {

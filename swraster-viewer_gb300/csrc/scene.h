@@ -66,6 +66,7 @@ struct SceneImpl {
     // Draw-list bounds of one view (every primitive in the frustum).
     uint32_t max_draws = 0, max_chunks = 0;
     bool any_translucent = false;  // some node's mesh has translucent primitives
+    uint32_t gi_cache = 0, ggx_cache = 0;  // SWR_CACHE_*
 
     // Export views.
     std::vector<swr_primitive_view> prim_views;

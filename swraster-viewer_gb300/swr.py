@@ -19,6 +19,8 @@ WRAP_REPEAT, WRAP_MIRRORED_REPEAT, WRAP_CLAMP_TO_EDGE = 0, 1, 2
 RSQRT_IEEE, RSQRT_AARCH64 = 0, 1
 SCENE_HOST_ONLY = 1
 SCENE_GI = 2
+# swr_scene_info.gi_cache / ggx_cache
+CACHE_NONE, CACHE_LOADED, CACHE_WRITTEN, CACHE_WRITE_FAILED, CACHE_NO_CODEC = 0, 1, 2, 3, 4
 
 u32p = C.POINTER(C.c_uint32)
 f32p = C.POINTER(C.c_float)
@@ -63,19 +65,22 @@ class SceneDesc(C.Structure):
                 ("materials", C.POINTER(MaterialDesc)), ("textures", C.POINTER(TextureDesc)),
                 ("cubemap_face_size", C.c_uint32), ("voxel_grid_size", C.c_uint32), ("cubemap_faces", u32p),
                 ("specular_samples", C.c_uint32), ("brdf_lut_size", C.c_uint32), ("gi_sh_scale", C.c_float),
-                ("sky_visibility", C.c_float), ("host_threads", C.c_uint32), ("flags", C.c_uint32)]
+                ("sky_visibility", C.c_float), ("host_threads", C.c_uint32), ("flags", C.c_uint32),
+                ("gi_cache_path", C.c_char_p), ("ggx_cache_path", C.c_char_p)]
 
 
 class GltfOpts(C.Structure):
     _fields_ = [("cubemap_faces", u32p), ("cubemap_face_size", C.c_uint32), ("voxel_grid_size", C.c_uint32),
                 ("cubemap_path", C.c_char_p), ("specular_samples", C.c_uint32), ("brdf_lut_size", C.c_uint32),
-                ("host_threads", C.c_uint32), ("flags", C.c_uint32)]
+                ("host_threads", C.c_uint32), ("flags", C.c_uint32), ("gi_cache_path", C.c_char_p),
+                ("ggx_cache_path", C.c_char_p)]
 
 
 class SceneInfo(C.Structure):
     _fields_ = [("triangle_count", C.c_uint64), ("vertex_count", C.c_uint64), ("device_bytes", C.c_uint64),
                 ("node_count", C.c_uint32), ("draw_count", C.c_uint32), ("bounds_min", C.c_float * 3),
-                ("bounds_max", C.c_float * 3), ("bounds_center", C.c_float * 3), ("bounds_diagonal", C.c_float)]
+                ("bounds_max", C.c_float * 3), ("bounds_center", C.c_float * 3), ("bounds_diagonal", C.c_float),
+                ("gi_cache", C.c_uint32), ("ggx_cache", C.c_uint32)]
 
 
 class TextureView(C.Structure):
@@ -189,7 +194,8 @@ EXPORTS = [
     "swr_batch_create", "swr_batch_destroy", "swr_batch_render", "swr_batch_sync", "swr_batch_output",
     "swr_batch_autotune", "swr_batch_last_ms", "swr_batch_get_tuning", "swr_server_create", "swr_server_destroy", "swr_server_add_scene",
     "swr_server_submit", "swr_server_poll", "swr_server_release", "swr_server_get_stats", "swr_copy_to_host",
-    "swr_selftest_rsqrt", "swr_scene_load_gltf", "swr_selftest_depth_floor",
+    "swr_selftest_rsqrt", "swr_scene_load_gltf", "swr_selftest_depth_floor", "swr_scene_save_gi_cache",
+    "swr_scene_save_ggx_cache",
 ]
 STAGES = ["draws", "frontend", "clip", "scan", "scatter", "raster", "shade", "resolve"]
 
@@ -249,6 +255,8 @@ def lib():
         "swr_copy_to_host": ([vp, vp, C.c_size_t, vp], C.c_int),
         "swr_last_error": ([], C.c_char_p),
         "swr_abi_version": ([], C.c_int32),
+        "swr_scene_save_gi_cache": ([vp, C.c_char_p], C.c_int),
+        "swr_scene_save_ggx_cache": ([vp, C.c_char_p], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -281,10 +289,10 @@ def texref(index=-1, wrap_s=WRAP_REPEAT, wrap_t=WRAP_REPEAT):
     return TexRef(index, wrap_s, wrap_t, 0)
 
 
-def scene_desc(sd, flags=0, host_threads=0):
+def scene_desc(sd, flags=0, host_threads=0, gi_cache=None, ggx_cache=None):
     """swr_scene_desc of a scene dict (see scenes.py), and the arrays it points
     into (keep them alive while the descriptor is used). Builds structures
-    only: the library is not loaded."""
+    only: the library is not loaded. gi_cache / ggx_cache: cache file paths."""
     keep = []
     meshes = (MeshDesc * len(sd["meshes"]))()
     for mi, prims in enumerate(sd["meshes"]):
@@ -347,15 +355,17 @@ def scene_desc(sd, flags=0, host_threads=0):
     desc.sky_visibility = sd.get("sky_visibility", 1.0)
     desc.host_threads = host_threads
     desc.flags = flags
+    desc.gi_cache_path = None if gi_cache is None else os.fsencode(gi_cache)
+    desc.ggx_cache_path = None if ggx_cache is None else os.fsencode(ggx_cache)
     return desc, keep
 
 
 class Scene:
     """Owns a swr_scene built from a scene dict (see scenes.py)."""
 
-    def __init__(self, sd, host_only=False, host_threads=0, gi=False):
+    def __init__(self, sd, host_only=False, host_threads=0, gi=False, gi_cache=None, ggx_cache=None):
         flags = (SCENE_HOST_ONLY if host_only else 0) | (SCENE_GI if gi else 0)
-        desc, keep = scene_desc(sd, flags, host_threads)
+        desc, keep = scene_desc(sd, flags, host_threads, gi_cache, ggx_cache)
         h = C.c_void_p()
         check(lib().swr_scene_create(C.byref(desc), C.byref(h)))
         self.handle = h
@@ -365,8 +375,11 @@ class Scene:
 
     @classmethod
     def load_gltf(cls, path, cubemap_faces=None, cubemap_face_size=0, cubemap_path=None, voxel_grid_size=0,
-                  specular_samples=0, brdf_lut_size=0, host_only=False, host_threads=0, gi=False):
-        """swr_scene_load_gltf: a .gltf/.glb file; the cubemap as raw faces or a cross image path."""
+                  specular_samples=0, brdf_lut_size=0, host_only=False, host_threads=0, gi=False, gi_cache=None,
+                  ggx_cache=None):
+        """swr_scene_load_gltf: a .gltf/.glb file; the cubemap as raw faces or a cross image path.
+        gi_cache: a path, or True for the reference's (the file's path with
+        extension .gi, Path::with_extension); ggx_cache: a path."""
         o = GltfOpts()
         faces = None
         if cubemap_faces is not None:
@@ -380,12 +393,24 @@ class Scene:
         o.brdf_lut_size = brdf_lut_size
         o.host_threads = host_threads
         o.flags = (SCENE_HOST_ONLY if host_only else 0) | (SCENE_GI if gi else 0)
+        if gi_cache is True:
+            gi_cache = os.path.splitext(os.fspath(path))[0] + ".gi"
+        if gi_cache is not None:
+            o.gi_cache_path = os.fsencode(gi_cache)
+        if ggx_cache is not None:
+            o.ggx_cache_path = os.fsencode(ggx_cache)
         h = C.c_void_p()
         check(lib().swr_scene_load_gltf(os.fsencode(path), C.byref(o), C.byref(h)))
         self = cls.__new__(cls)
         self.handle = h
         self.source, self.flags = None, o.flags
         return self
+
+    def save_gi_cache(self, path):
+        check(lib().swr_scene_save_gi_cache(self.handle, os.fsencode(path)))
+
+    def save_ggx_cache(self, path):
+        check(lib().swr_scene_save_ggx_cache(self.handle, os.fsencode(path)))
 
     def info(self):
         i = SceneInfo()

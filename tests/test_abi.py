@@ -29,7 +29,7 @@ def test_every_declared_symbol_is_exported():
 
 
 def test_abi_version():
-    assert swr.lib().swr_abi_version() == 1
+    assert swr.lib().swr_abi_version() == 2
 
 
 def test_null_arguments_are_rejected():

@@ -66,3 +66,34 @@ def test_frames_with_baked_grid_match_oracle(kind):
     cam = swr.make_camera(*scenes.default_camera_params(s.info(), 256, 160))
     compare(s, cam, 256, 160)
     s.close()
+
+
+@pytest.mark.gpu
+def test_gi_cache_replaces_the_bake(tmp_path):
+    """The reference's .gi cache (src/main.rs:248-279): the first load bakes
+    and writes the file, the second reads it instead of baking; grids and
+    frames are identical. The prefiltered environment goes through its
+    cache file the same way."""
+    sd = gi_scene("spheres", voxel=16)
+    gi_path, ggx_path = tmp_path / "scene.gi", tmp_path / "cubemap.ggx"
+    a = swr.Scene(sd, gi=True, gi_cache=gi_path, ggx_cache=ggx_path)
+    ia = a.info()
+    if swr.CACHE_NO_CODEC in (ia.gi_cache, ia.ggx_cache):
+        pytest.skip("no brotli library on this system")
+    assert (ia.gi_cache, ia.ggx_cache) == (swr.CACHE_WRITTEN, swr.CACHE_WRITTEN)
+    b = swr.Scene(sd, gi=True, gi_cache=gi_path, ggx_cache=ggx_path)
+    ib = b.info()
+    assert (ib.gi_cache, ib.ggx_cache) == (swr.CACHE_LOADED, swr.CACHE_LOADED)
+    ga, _ = baked(a)
+    gb, _ = baked(b)
+    assert np.array_equal(ga.view(np.uint32), gb.view(np.uint32))
+    cam = swr.make_camera(*scenes.default_camera_params(ia, 256, 160))
+    out = []
+    for s in (a, b):
+        r = swr.Renderer(256, 160)
+        r.render(s, cam, 0.0)
+        out.append((r.blit(), r.visbuffer()))
+        r.close()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    a.close()
+    b.close()
