@@ -253,6 +253,11 @@ typedef struct swr_scene_info {
     float bounds_diagonal;
     uint32_t gi_cache;          /* SWR_CACHE_* */
     uint32_t ggx_cache;         /* SWR_CACHE_* */
+    /* Scenes built on the device compute mip chains, the BRDF LUT and the
+     * GGX-prefiltered environment there, bit-exact with the host: where
+     * the device's powf leaves a texel's byte open, the texel is computed
+     * again on the host. This counts those texels (0 for host-only scenes). */
+    uint64_t precompute_host_texels;
 } swr_scene_info;
 
 swr_status swr_scene_get_info(const swr_scene* scene, swr_scene_info* out);
@@ -621,6 +626,12 @@ swr_status swr_copy_to_host(void* dst, const void* src_device, size_t bytes, voi
  * in the given SWR_RSQRT_* mode (the arithmetic every normalize of the
  * shading pass uses, src/math.rs:17-49), written to host `out`. */
 swr_status swr_selftest_rsqrt(const float* in, float* out, uint64_t n, uint32_t rsqrt_mode);
+
+/* Numerics self-test: the device powf of the load-time tables on `n` host
+ * values, powf(x, 2.4) (mode 0, srgb_to_linear_scalar, src/util.rs:49-55) or
+ * powf(x, 1/2.4) (mode 1, linear_to_srgb_scalar, src/util.rs:66-72), written
+ * to host `out`. */
+swr_status swr_selftest_srgb_pow(const float* in, float* out, uint64_t n, uint32_t mode);
 
 /* Numerics self-test, host only: the lower bound the raster's occlusion
  * culling takes on the depths of a packet (subpixel vertices p[6] = x0, y0,

@@ -61,6 +61,8 @@ def lib():
         for n in ("oracle_frsqrte", "oracle_rsqrt_aarch64"):
             getattr(L, n).argtypes = [C.c_float]
             getattr(L, n).restype = C.c_float
+        L.oracle_srgb_pow.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p]
+        L.oracle_srgb_pow.restype = C.c_int
         L.oracle_frsqrts.argtypes = [C.c_float, C.c_float]
         L.oracle_frsqrts.restype = C.c_float
         L.oracle_sun_visibility_ex.argtypes = [C.POINTER(swr.SceneHostView), C.c_uint32, C.c_void_p, C.c_int]
@@ -178,6 +180,16 @@ def packet_depths(p, ooa, zow, oow, rect):
     lib().oracle_packet_depths(p.ctypes.data, float(ooa), zow.ctypes.data, oow.ctypes.data, rect.ctypes.data,
                                C.byref(zmin), C.byref(n))
     return zmin.value, n.value
+
+
+def srgb_pow(x, mode, threads=16):
+    """powf(x, 2.4) (mode 0) or powf(x, 1/2.4) (mode 1) with the host libm."""
+    x = np.ascontiguousarray(x, np.float32)
+    out = np.empty_like(x)
+    if lib().oracle_srgb_pow(x.ctypes.data_as(C.c_void_p), x.size, mode, threads,
+                             out.ctypes.data_as(C.c_void_p)) != 0:
+        raise RuntimeError("oracle_srgb_pow failed")
+    return out
 
 
 def sun_visibility(view, threads=1, brute=False):

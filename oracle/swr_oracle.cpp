@@ -1948,6 +1948,22 @@ int oracle_packet_depths(const int32_t* p, float ooa, const float* zow, const fl
 
 // Arm FRSQRTE/FRSQRTS emulation, exposed for the known-answer tests.
 float oracle_frsqrte(float x) { return orc::frsqrte(x); }
+
+// The powf of srgb_to_linear_scalar (mode 0: powf(x, 2.4)) and of
+// linear_to_srgb_scalar (mode 1: powf(x, 1 / 2.4)), src/util.rs:49-72, with
+// the host libm, over n values on `threads` threads.
+int oracle_srgb_pow(const float* x, uint64_t n, uint32_t mode, uint32_t threads, float* out) {
+    if ((!x || !out) && n) return 1;
+    const float y = mode == 0 ? 2.4f : 1.0f / 2.4f;
+    const uint64_t t = threads ? threads : 1;
+    std::vector<std::thread> pool;
+    for (uint64_t k = 0; k < t; ++k)
+        pool.emplace_back([=] {
+            for (uint64_t i = n * k / t; i < n * (k + 1) / t; ++i) out[i] = std::pow(x[i], y);
+        });
+    for (auto& th : pool) th.join();
+    return 0;
+}
 float oracle_frsqrts(float a, float b) { return orc::frsqrts(a, b); }
 float oracle_rsqrt_aarch64(float x) {
     const float y0 = orc::frsqrte(x);

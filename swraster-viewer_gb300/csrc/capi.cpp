@@ -10,6 +10,7 @@
 
 #include "../../include/swr.h"
 #include "caches.h"
+#include "ibl.h"
 #include "renderer.h"
 #include "scene.h"
 
@@ -94,6 +95,7 @@ swr_status swr_scene_get_info(const swr_scene* s, swr_scene_info* o) {
     o->bounds_diagonal = m.bounds_diagonal;
     o->gi_cache = m.gi_cache;
     o->ggx_cache = m.ggx_cache;
+    o->precompute_host_texels = m.precompute_host_texels;
     return SWR_OK;
 }
 
@@ -581,6 +583,14 @@ swr_status swr_renderer_get_tile_luminance(swr_renderer* r, float* out, uint32_t
     return SWR_OK;
 }
 
+
+swr_status swr_selftest_srgb_pow(const float* in, float* out, uint64_t n, uint32_t mode) {
+    if ((!in || !out) && n > 0) return fail(SWR_INVALID_ARG, "null argument");
+    if (mode > 1) return fail(SWR_INVALID_ARG, "bad mode");
+    std::string err;
+    const swr_status st = srgb_pow_selftest(in, out, n, mode, err);
+    return st == SWR_OK ? SWR_OK : fail(st, err);
+}
 
 swr_status swr_selftest_rsqrt(const float* in, float* out, uint64_t n, uint32_t rsqrt_mode) {
     if ((!in || !out) && n > 0) return fail(SWR_INVALID_ARG, "null argument");

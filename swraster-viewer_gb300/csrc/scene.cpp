@@ -8,6 +8,7 @@
 #include "scene.h"
 
 #include "caches.h"
+#include "ibl.h"
 #include "precompute.h"
 
 #include <cuda_runtime.h>
@@ -78,6 +79,53 @@ inline uint32_t ilog2u(uint32_t v) { return 31u - (uint32_t)__builtin_clz(v); }
 
 }  // namespace
 
+// One texel of the next mip from its 2x2 parents (src/texture.rs:82-113).
+uint32_t mip_texel(uint32_t type, uint32_t q00, uint32_t q10, uint32_t q01, uint32_t q11) {
+    const V4 p00 = unpack4(q00), p10 = unpack4(q10), p01 = unpack4(q01), p11 = unpack4(q11);
+    V4 avg;
+    if (type == SWR_TEX_SRGB) {
+        auto lin = [](V4 c) {
+            return V4{srgb_to_linear_scalar(c.x), srgb_to_linear_scalar(c.y), srgb_to_linear_scalar(c.z), c.w};
+        };
+        const V4 l00 = lin(p00), l10 = lin(p10), l01 = lin(p01), l11 = lin(p11);
+        V4 s = add4(add4(add4(l00, l10), l01), l11);
+        s = {s.x / 4.0f, s.y / 4.0f, s.z / 4.0f, s.w / 4.0f};
+        avg = {linear_to_srgb_scalar(s.x), linear_to_srgb_scalar(s.y), linear_to_srgb_scalar(s.z), s.w};
+    } else if (type == SWR_TEX_METALLIC_ROUGHNESS) {
+        const float r = (((p00.y * p00.y + p10.y * p10.y) + p01.y * p01.y) + p11.y * p11.y) / 4.0f;
+        const float m = (((p00.z + p10.z) + p01.z) + p11.z) / 4.0f;
+        avg = {p00.x, std::sqrt(r), m, p00.w};
+    } else if (type == SWR_TEX_NORMAL) {
+        auto n = [](V4 c) { return V4{c.x * 2.0f - 1.0f, c.y * 2.0f - 1.0f, c.z * 2.0f - 1.0f, c.w * 2.0f - 1.0f}; };
+        V4 s = add4(add4(add4(n(p00), n(p10)), n(p01)), n(p11));
+        s = {s.x / 4.0f, s.y / 4.0f, s.z / 4.0f, s.w / 4.0f};
+        avg = {(s.x + 1.0f) / 2.0f, (s.y + 1.0f) / 2.0f, (s.z + 1.0f) / 2.0f, (s.w + 1.0f) / 2.0f};
+    } else {
+        V4 s = add4(add4(add4(p00, p10), p01), p11);
+        avg = {s.x / 4.0f, s.y / 4.0f, s.z / 4.0f, s.w / 4.0f};
+    }
+    return pack4(avg);
+}
+
+float srgb_to_linear_host(float s) { return srgb_to_linear_scalar(s); }
+
+void HTexture::mip_layout() {
+    const uint32_t num_mips = 1u + ilog2u(std::max(width, height));
+    const uint32_t array_size = type == SWR_TEX_CUBEMAP ? 6u : 1u;
+    size_t size = data.size();
+    for (uint32_t mip = 1; mip < num_mips; ++mip) {
+        mip_offsets.push_back((uint32_t)size);
+        const uint32_t mw = std::max(width >> mip, 1u), mh = std::max(height >> mip, 1u);
+        array_stride.push_back(mw * mh);
+        size += (size_t)mw * mh * array_size;
+        mip_widths.push_back(mw);
+        mip_heights.push_back(mh);
+        mip_widths_f.push_back((float)mw);
+        mip_heights_f.push_back((float)mh);
+        max_mip += 1;
+    }
+}
+
 // Texture::generate_mipmaps (src/texture.rs:45-128).
 void HTexture::generate_mipmaps() {
     const uint32_t num_mips = 1u + ilog2u(std::max(width, height));
@@ -95,34 +143,8 @@ void HTexture::generate_mipmaps() {
                 for (uint32_t x = 0; x < mw; ++x) {
                     const uint32_t x0 = x * 2, y0 = y * 2;
                     const uint32_t x1 = std::min(x0 + 1, pw - 1), y1 = std::min(y0 + 1, ph - 1);
-                    const V4 p00 = unpack4(data[so + y0 * pw + x0]);
-                    const V4 p10 = unpack4(data[so + y0 * pw + x1]);
-                    const V4 p01 = unpack4(data[so + y1 * pw + x0]);
-                    const V4 p11 = unpack4(data[so + y1 * pw + x1]);
-                    V4 avg;
-                    if (type == SWR_TEX_SRGB) {
-                        auto lin = [](V4 c) {
-                            return V4{srgb_to_linear_scalar(c.x), srgb_to_linear_scalar(c.y),
-                                      srgb_to_linear_scalar(c.z), c.w};
-                        };
-                        const V4 l00 = lin(p00), l10 = lin(p10), l01 = lin(p01), l11 = lin(p11);
-                        V4 s = add4(add4(add4(l00, l10), l01), l11);
-                        s = {s.x / 4.0f, s.y / 4.0f, s.z / 4.0f, s.w / 4.0f};
-                        avg = {linear_to_srgb_scalar(s.x), linear_to_srgb_scalar(s.y), linear_to_srgb_scalar(s.z), s.w};
-                    } else if (type == SWR_TEX_METALLIC_ROUGHNESS) {
-                        const float r = (((p00.y * p00.y + p10.y * p10.y) + p01.y * p01.y) + p11.y * p11.y) / 4.0f;
-                        const float m = (((p00.z + p10.z) + p01.z) + p11.z) / 4.0f;
-                        avg = {p00.x, std::sqrt(r), m, p00.w};
-                    } else if (type == SWR_TEX_NORMAL) {
-                        auto n = [](V4 c) { return V4{c.x * 2.0f - 1.0f, c.y * 2.0f - 1.0f, c.z * 2.0f - 1.0f, c.w * 2.0f - 1.0f}; };
-                        V4 s = add4(add4(add4(n(p00), n(p10)), n(p01)), n(p11));
-                        s = {s.x / 4.0f, s.y / 4.0f, s.z / 4.0f, s.w / 4.0f};
-                        avg = {(s.x + 1.0f) / 2.0f, (s.y + 1.0f) / 2.0f, (s.z + 1.0f) / 2.0f, (s.w + 1.0f) / 2.0f};
-                    } else {
-                        V4 s = add4(add4(add4(p00, p10), p01), p11);
-                        avg = {s.x / 4.0f, s.y / 4.0f, s.z / 4.0f, s.w / 4.0f};
-                    }
-                    data.push_back(pack4(avg));
+                    data.push_back(mip_texel(type, data[so + y0 * pw + x0], data[so + y0 * pw + x1],
+                                             data[so + y1 * pw + x0], data[so + y1 * pw + x1]));
                 }
             }
         }
@@ -326,10 +348,50 @@ void compute_irradiance_sh4(const HTexture& cube, float out[4][3]) {
         out[i][2] = sh[i].z;
     }
 }
-HTexture generate_prefiltered_specular(const HTexture& cube, uint32_t sample_count, unsigned threads) {
+}  // namespace
+
+// One texel of the GGX-prefiltered environment (the loop body of
+// generate_prefiltered_specular_cubemap, src/texture.rs:357-393).
+uint32_t prefilter_texel(const HTexture& cube, uint32_t mip, uint32_t max_mip, uint32_t face, uint32_t x, uint32_t y,
+                         uint32_t sample_count, const float* xi_x, const float* xi_y) {
     const uint32_t bw = cube.width, bh = cube.height;
+    const float roughness = max_mip > 0 ? (float)mip / (float)max_mip : 0.0f;
+    const float v = (((float)y + 0.5f) / (float)bh) * 2.0f - 1.0f;
+    const float u = (((float)x + 0.5f) / (float)bw) * 2.0f - 1.0f;
+    const V3 r = face_uv_to_direction(face, u, v);
+    V3 color;
+    if (mip == 0) {
+        color = sample_dir_linear(cube, r);
+    } else {
+        V3 accum = {0, 0, 0};
+        float total = 0.0f;
+        for (uint32_t i = 0; i < sample_count; ++i) {
+            const V3 h = importance_sample_ggx(xi_x[i], xi_y[i], r, std::fmax(roughness, 0.045f));
+            const V3 l = normalize3(sub(mul(h, 2.0f * dot3(r, h)), r));
+            const float ndotl = std::fmax(dot3(r, l), 0.0f);
+            if (ndotl > 0.0f) {
+                accum = add(accum, mul(sample_dir_linear(cube, l), ndotl));
+                total += ndotl;
+            }
+        }
+        color = total > 0.0f ? V3{accum.x / total, accum.y / total, accum.z / total} : sample_dir_linear(cube, r);
+    }
+    return pack4({color.x, color.y, color.z, 1.0f});
+}
+
+void hammersley_table(uint32_t n, float* xi_x, float* xi_y, float* cos_phi, float* sin_phi) {
+    for (uint32_t i = 0; i < n; ++i) {
+        hammersley(i, n, xi_x[i], xi_y[i]);
+        const float phi = (2.0f * kPi) * xi_x[i];
+        if (cos_phi) cos_phi[i] = std::cos(phi);
+        if (sin_phi) sin_phi[i] = std::sin(phi);
+    }
+}
+
+// The prefiltered texture's layout: every mip at full face resolution, six
+// faces each (src/texture.rs:335-356).
+HTexture prefiltered_layout(uint32_t bw, uint32_t bh) {
     const uint32_t num_mips = 1u + ilog2u(std::max(bw, bh));
-    const uint32_t max_mip = num_mips - 1;
     HTexture t;
     t.width = bw;
     t.height = bh;
@@ -344,43 +406,32 @@ HTexture generate_prefiltered_specular(const HTexture& cube, uint32_t sample_cou
         t.mip_heights_f.push_back((float)bh);
         t.array_stride.push_back(bw * bh);
     }
+    t.max_mip = num_mips - 1;
+    t.whv[0] = (float)bw;
+    t.whv[1] = (float)bw;
+    t.whv[2] = (float)bh;
+    t.whv[3] = (float)bh;
+    return t;
+}
+
+namespace {
+
+HTexture generate_prefiltered_specular(const HTexture& cube, uint32_t sample_count, unsigned threads) {
+    const uint32_t bw = cube.width, bh = cube.height;
+    HTexture t = prefiltered_layout(bw, bh);
+    const uint32_t num_mips = t.max_mip + 1;
+    const size_t face_texels = (size_t)bw * bh;
     std::vector<float> xi_x(sample_count), xi_y(sample_count);
-    for (uint32_t i = 0; i < sample_count; ++i) hammersley(i, sample_count, xi_x[i], xi_y[i]);
+    hammersley_table(sample_count, xi_x.data(), xi_y.data(), nullptr, nullptr);
     const size_t rows = (size_t)num_mips * 6 * bh;
     parallel_for(rows, threads, [&](size_t row) {
         const uint32_t mip = (uint32_t)(row / (6 * bh));
         const uint32_t face = (uint32_t)((row / bh) % 6);
         const uint32_t y = (uint32_t)(row % bh);
-        const float roughness = max_mip > 0 ? (float)mip / (float)max_mip : 0.0f;
-        const float v = (((float)y + 0.5f) / (float)bh) * 2.0f - 1.0f;
-        for (uint32_t x = 0; x < bw; ++x) {
-            const float u = (((float)x + 0.5f) / (float)bw) * 2.0f - 1.0f;
-            const V3 r = face_uv_to_direction(face, u, v);
-            V3 color;
-            if (mip == 0) {
-                color = sample_dir_linear(cube, r);
-            } else {
-                V3 accum = {0, 0, 0};
-                float total = 0.0f;
-                for (uint32_t i = 0; i < sample_count; ++i) {
-                    const V3 h = importance_sample_ggx(xi_x[i], xi_y[i], r, std::fmax(roughness, 0.045f));
-                    const V3 l = normalize3(sub(mul(h, 2.0f * dot3(r, h)), r));
-                    const float ndotl = std::fmax(dot3(r, l), 0.0f);
-                    if (ndotl > 0.0f) {
-                        accum = add(accum, mul(sample_dir_linear(cube, l), ndotl));
-                        total += ndotl;
-                    }
-                }
-                color = total > 0.0f ? V3{accum.x / total, accum.y / total, accum.z / total} : sample_dir_linear(cube, r);
-            }
-            t.data[t.mip_offsets[mip] + face * face_texels + (size_t)y * bw + x] = pack4({color.x, color.y, color.z, 1.0f});
-        }
+        for (uint32_t x = 0; x < bw; ++x)
+            t.data[t.mip_offsets[mip] + face * face_texels + (size_t)y * bw + x] =
+                prefilter_texel(cube, mip, t.max_mip, face, x, y, sample_count, xi_x.data(), xi_y.data());
     });
-    t.max_mip = max_mip;
-    t.whv[0] = (float)bw;
-    t.whv[1] = (float)bw;
-    t.whv[2] = (float)bh;
-    t.whv[3] = (float)bh;
     return t;
 }
 
@@ -824,7 +875,18 @@ swr_status build_scene(const swr_scene_desc* desc, SceneImpl* s, std::string& er
         }
         s->textures.push_back(make_texture(t.width, t.height, t.type, t.rgba8, false));
     }
-    parallel_for(s->textures.size(), threads, [&](size_t i) { s->textures[i].generate_mipmaps(); });
+    // Mip chains, the BRDF LUT and the GGX prefilter run on the device for
+    // scenes that go there (ibl.cu, bit-exact with these host loops), on
+    // host threads for host-only scenes.
+    const bool on_device = !(desc->flags & SWR_SCENE_HOST_ONLY);
+    if (on_device) {
+        std::vector<HTexture*> texs;
+        for (HTexture& t : s->textures) texs.push_back(&t);
+        const swr_status mst = mipmaps_device(texs, s->precompute_host_texels, err);
+        if (mst != SWR_OK) return mst;
+    } else {
+        parallel_for(s->textures.size(), threads, [&](size_t i) { s->textures[i].generate_mipmaps(); });
+    }
     // Meshes / primitives (src/scene.rs:422-495).
     for (uint32_t mi = 0; mi < desc->mesh_count; ++mi) {
         const swr_mesh_desc& md = desc->meshes[mi];
@@ -946,7 +1008,12 @@ swr_status build_scene(const swr_scene_desc* desc, SceneImpl* s, std::string& er
         return SWR_INVALID_ARG;
     }
     s->cubemap = make_texture(desc->cubemap_face_size, desc->cubemap_face_size, SWR_TEX_CUBEMAP, desc->cubemap_faces, true);
-    s->cubemap.generate_mipmaps();
+    if (on_device) {
+        const swr_status cst = mipmaps_device({&s->cubemap}, s->precompute_host_texels, err);
+        if (cst != SWR_OK) return cst;
+    } else {
+        s->cubemap.generate_mipmaps();
+    }
     // The GGX-prefiltered environment, read from its cache file when one is
     // given and valid, else computed and written there (src/scene.rs:164-205).
     bool specular_loaded = false;
@@ -957,8 +1024,13 @@ swr_status build_scene(const swr_scene_desc* desc, SceneImpl* s, std::string& er
         s->ggx_cache = specular_loaded ? SWR_CACHE_LOADED : (r == CacheRead::NoCodec ? SWR_CACHE_NO_CODEC : 0u);
     }
     if (!specular_loaded) {
-        s->specular = generate_prefiltered_specular(s->cubemap, desc->specular_samples ? desc->specular_samples : 64u,
-                                                    threads);
+        const uint32_t samples = desc->specular_samples ? desc->specular_samples : 64u;
+        if (on_device) {
+            const swr_status pst = prefiltered_specular_device(s->cubemap, samples, s->specular, s->precompute_host_texels, err);
+            if (pst != SWR_OK) return pst;
+        } else {
+            s->specular = generate_prefiltered_specular(s->cubemap, samples, threads);
+        }
         if (desc->ggx_cache_path && s->ggx_cache != SWR_CACHE_NO_CODEC) {
             std::string werr;
             s->ggx_cache = write_ggx_cache(desc->ggx_cache_path, s->specular, werr) ? SWR_CACHE_WRITTEN
@@ -966,7 +1038,13 @@ swr_status build_scene(const swr_scene_desc* desc, SceneImpl* s, std::string& er
         }
     }
     compute_irradiance_sh4(s->cubemap, s->irradiance_sh);
-    s->brdf_lut = generate_brdf_lut(desc->brdf_lut_size ? desc->brdf_lut_size : 128u, threads);
+    if (on_device) {
+        const swr_status bst = brdf_lut_device(desc->brdf_lut_size ? desc->brdf_lut_size : 128u, s->brdf_lut,
+                                                s->precompute_host_texels, err);
+        if (bst != SWR_OK) return bst;
+    } else {
+        s->brdf_lut = generate_brdf_lut(desc->brdf_lut_size ? desc->brdf_lut_size : 128u, threads);
+    }
     // Voxel grid (src/main.rs:227-281).
     const uint32_t n = desc->voxel_grid_size ? desc->voxel_grid_size : 128u;
     s->voxel_n = n;

@@ -21,6 +21,9 @@ struct HTexture {
     std::vector<float> mip_widths_f, mip_heights_f;
     float whv[4] = {0, 0, 0, 0};
     void generate_mipmaps();
+    // Appends the mip levels' metadata generate_mipmaps would (offsets,
+    // sizes, strides); data keeps level 0.
+    void mip_layout();
     swr_texture_view view() const;
 };
 
@@ -67,6 +70,7 @@ struct SceneImpl {
     uint32_t max_draws = 0, max_chunks = 0;
     bool any_translucent = false;  // some node's mesh has translucent primitives
     uint32_t gi_cache = 0, ggx_cache = 0;  // SWR_CACHE_*
+    uint64_t precompute_host_texels = 0;   // device precompute texels recomputed on the host
 
     // Export views.
     std::vector<swr_primitive_view> prim_views;

@@ -80,7 +80,7 @@ class SceneInfo(C.Structure):
     _fields_ = [("triangle_count", C.c_uint64), ("vertex_count", C.c_uint64), ("device_bytes", C.c_uint64),
                 ("node_count", C.c_uint32), ("draw_count", C.c_uint32), ("bounds_min", C.c_float * 3),
                 ("bounds_max", C.c_float * 3), ("bounds_center", C.c_float * 3), ("bounds_diagonal", C.c_float),
-                ("gi_cache", C.c_uint32), ("ggx_cache", C.c_uint32)]
+                ("gi_cache", C.c_uint32), ("ggx_cache", C.c_uint32), ("precompute_host_texels", C.c_uint64)]
 
 
 class TextureView(C.Structure):
@@ -195,7 +195,7 @@ EXPORTS = [
     "swr_batch_autotune", "swr_batch_last_ms", "swr_batch_get_tuning", "swr_server_create", "swr_server_destroy", "swr_server_add_scene",
     "swr_server_submit", "swr_server_poll", "swr_server_release", "swr_server_get_stats", "swr_copy_to_host",
     "swr_selftest_rsqrt", "swr_scene_load_gltf", "swr_selftest_depth_floor", "swr_scene_save_gi_cache",
-    "swr_scene_save_ggx_cache",
+    "swr_scene_save_ggx_cache", "swr_selftest_srgb_pow",
 ]
 STAGES = ["draws", "frontend", "clip", "scan", "scatter", "raster", "shade", "resolve"]
 
@@ -257,6 +257,7 @@ def lib():
         "swr_abi_version": ([], C.c_int32),
         "swr_scene_save_gi_cache": ([vp, C.c_char_p], C.c_int),
         "swr_scene_save_ggx_cache": ([vp, C.c_char_p], C.c_int),
+        "swr_selftest_srgb_pow": ([f32p, f32p, C.c_uint64, C.c_uint32], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
