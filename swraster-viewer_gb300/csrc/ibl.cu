@@ -14,11 +14,12 @@ namespace swr {
 
 namespace {
 
-// Half-width, in ulps, of the interval taken around the device's powf: it
-// must hold the host libm's powf for every input these tables pass.
-// tests/test_ibl_device.py compares the two functions over every float those
-// inputs can take and requires their difference to stay within half of it.
-constexpr int kPowUlps = 8;
+// Half-width, in ulps, of the interval the GGX prefilter takes around the
+// device's powf: it must hold the host libm's powf for every input.
+// tests/test_ibl_device.py compares the two functions over every float the
+// inputs can take and requires their difference to stay within it (the
+// largest difference measured on GB300 against glibc is 1 ulp).
+constexpr int kPowUlps = 2;
 
 struct F3 {
     float x, y, z;
@@ -65,21 +66,27 @@ __device__ __forceinline__ void srgb_to_linear_iv(float s, float& lo, float& hi)
     widen(pow_24((s + 0.055f) / 1.055f), lo, hi);
 }
 
-// linear_to_srgb_scalar (src/util.rs:66-72) and the byte it packs to; sets
-// `amb` when the interval's ends give different bytes.
-__device__ __forceinline__ uint32_t linear_to_srgb_byte(float s, bool& amb) {
+// The byte linear_to_srgb_scalar (src/util.rs:66-72) packs to. Its powf
+// branch goes through the host's byte thresholds: thr[k - 1] is the smallest
+// float whose byte is at least k, so the byte is the number of thresholds
+// at or below s (the host's byte is non-decreasing in s; the tests check it
+// over every float of the branch).
+__device__ __forceinline__ uint32_t linear_to_srgb_byte(float s, const float* __restrict__ thr) {
     if (s <= 0.0031308f) return to_byte(s * 12.92f);
-    const float p = pow_inv24(s);
-    float lo, hi;
-    widen(p, lo, hi);
-    if (to_byte(lo * 1.055f - 0.055f) != to_byte(hi * 1.055f - 0.055f)) amb = true;
-    return to_byte(p * 1.055f - 0.055f);
+    uint32_t lo = 0, hi = 255;  // count of thresholds <= s lies in [lo, hi]
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (__ldg(thr + mid - 1) <= s) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
 }
 
 // One texel of the next mip (src/texture.rs:82-113). s2l: the 256 values of
-// srgb_to_linear_scalar(b / 255) as the host computes them.
+// srgb_to_linear_scalar(b / 255) as the host computes them; thr: the byte
+// thresholds of linear_to_srgb_byte.
 __device__ uint32_t mip_texel_dev(uint32_t type, uint32_t q00, uint32_t q10, uint32_t q01, uint32_t q11,
-                                  const float* __restrict__ s2l, bool& amb) {
+                                  const float* __restrict__ s2l, const float* __restrict__ thr) {
     const int sh[4] = {24, 16, 8, 0};
     uint32_t out[4];
     if (type == SWR_TEX_SRGB) {
@@ -87,7 +94,7 @@ __device__ uint32_t mip_texel_dev(uint32_t type, uint32_t q00, uint32_t q10, uin
             const float l00 = __ldg(s2l + ((q00 >> sh[c]) & 0xFFu)), l10 = __ldg(s2l + ((q10 >> sh[c]) & 0xFFu));
             const float l01 = __ldg(s2l + ((q01 >> sh[c]) & 0xFFu)), l11 = __ldg(s2l + ((q11 >> sh[c]) & 0xFFu));
             const float s = (((l00 + l10) + l01) + l11) / 4.0f;
-            out[c] = linear_to_srgb_byte(s, amb);
+            out[c] = linear_to_srgb_byte(s, thr);
         }
         const float w = (((byte_unit(q00, 0) + byte_unit(q10, 0)) + byte_unit(q01, 0)) + byte_unit(q11, 0)) / 4.0f;
         out[3] = to_byte(w);
@@ -123,10 +130,8 @@ struct MipJob {
     uint32_t pw, ph, pstride, mw, mh, slices, type;
 };
 
-// One mip level; texels whose byte the interval leaves open are listed as
-// (index, four parents).
-__global__ void k_mip(MipJob j, const float* __restrict__ s2l, uint32_t* __restrict__ flags,
-                      uint32_t* __restrict__ nflags) {
+// One mip level.
+__global__ void k_mip(MipJob j, const float* __restrict__ s2l, const float* __restrict__ thr) {
     const uint32_t plane = j.mw * j.mh;
     const uint32_t n = plane * j.slices;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -137,23 +142,8 @@ __global__ void k_mip(MipJob j, const float* __restrict__ s2l, uint32_t* __restr
         const uint32_t* s = j.src + (size_t)slice * j.pstride;
         const uint32_t q00 = s[y0 * j.pw + x0], q10 = s[y0 * j.pw + x1];
         const uint32_t q01 = s[y1 * j.pw + x0], q11 = s[y1 * j.pw + x1];
-        bool amb = false;
-        j.dst[i] = mip_texel_dev(j.type, q00, q10, q01, q11, s2l, amb);
-        if (amb) {
-            const uint32_t k = atomicAdd(nflags, 1u);
-            uint32_t* f = flags + 5 * (size_t)k;
-            f[0] = i;
-            f[1] = q00;
-            f[2] = q10;
-            f[3] = q01;
-            f[4] = q11;
-        }
+        j.dst[i] = mip_texel_dev(j.type, q00, q10, q01, q11, s2l, thr);
     }
-}
-
-__global__ void k_patch(const uint32_t* __restrict__ pairs, uint32_t n, uint32_t* __restrict__ dst) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        dst[pairs[2 * i]] = pairs[2 * i + 1];
 }
 
 // importance_sample_ggx (src/texture.rs:148-167); the sample's angle enters
@@ -373,31 +363,26 @@ swr_status cuda_status(cudaError_t e, const char* what, std::string& err) {
 
 }  // namespace
 
-swr_status mipmaps_device(const std::vector<HTexture*>& textures, uint64_t& host_texels, std::string& err) {
-    size_t max_total = 0, max_level1 = 0;
+swr_status mipmaps_device(const std::vector<HTexture*>& textures, std::string& err) {
+    size_t max_total = 0;
     for (HTexture* t : textures) {
-        const size_t level0 = t->data.size();
         t->mip_layout();
         const uint32_t slices = t->type == SWR_TEX_CUBEMAP ? 6u : 1u;
-        const size_t total = t->max_mip == 0 ? level0
-                                             : (size_t)t->mip_offsets[t->max_mip] +
-                                                   (size_t)t->mip_widths[t->max_mip] * t->mip_heights[t->max_mip] * slices;
+        const size_t total = (size_t)t->mip_offsets[t->max_mip] +
+                             (size_t)t->mip_widths[t->max_mip] * t->mip_heights[t->max_mip] * slices;
         max_total = std::max(max_total, total);
-        if (t->max_mip > 0) max_level1 = std::max(max_level1, (size_t)t->mip_widths[1] * t->mip_heights[1] * slices);
     }
-    float s2l_host[256];
+    float s2l_host[256], thr_host[255];
     for (int b = 0; b < 256; ++b) s2l_host[b] = srgb_to_linear_host((float)b / 255.0f);
+    srgb_byte_thresholds(thr_host);
     Mem m;
-    uint32_t *d_data = nullptr, *d_flags = nullptr, *d_nflags = nullptr, *d_pairs = nullptr;
-    float* d_s2l = nullptr;
+    uint32_t* d_data = nullptr;
+    float *d_s2l = nullptr, *d_thr = nullptr;
     cudaError_t e = m.alloc(&d_data, max_total);
-    if (e == cudaSuccess) e = m.alloc(&d_flags, 5 * max_level1);
-    if (e == cudaSuccess) e = m.alloc(&d_pairs, 2 * max_level1);
-    if (e == cudaSuccess) e = m.alloc(&d_nflags, 1);
     if (e == cudaSuccess) e = m.alloc(&d_s2l, 256);
+    if (e == cudaSuccess) e = m.alloc(&d_thr, 255);
     if (e == cudaSuccess) e = cudaMemcpy(d_s2l, s2l_host, sizeof(s2l_host), cudaMemcpyHostToDevice);
-    std::vector<uint32_t> flags, pairs;
-    uint64_t fixed = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(d_thr, thr_host, sizeof(thr_host), cudaMemcpyHostToDevice);
     for (HTexture* t : textures) {
         if (e != cudaSuccess) break;
         if (t->max_mip == 0) continue;
@@ -417,42 +402,18 @@ swr_status mipmaps_device(const std::vector<HTexture*>& textures, uint64_t& host
             j.mh = t->mip_heights[mip];
             j.slices = slices;
             j.type = t->type;
-            const uint64_t n = (uint64_t)j.mw * j.mh * slices;
-            e = cudaMemset(d_nflags, 0, sizeof(uint32_t));
-            if (e != cudaSuccess) break;
-            k_mip<<<grid_for(n, 256), 256>>>(j, d_s2l, d_flags, d_nflags);
+            k_mip<<<grid_for((uint64_t)j.mw * j.mh * slices, 256), 256>>>(j, d_s2l, d_thr);
             e = cudaGetLastError();
-            // Only sRGB texels go through powf; the other types are exact.
-            if (e != cudaSuccess || t->type != SWR_TEX_SRGB) continue;
-            uint32_t nf = 0;
-            e = cudaMemcpy(&nf, d_nflags, sizeof(uint32_t), cudaMemcpyDeviceToHost);
-            if (e != cudaSuccess || nf == 0) continue;
-            flags.resize(5 * (size_t)nf);
-            pairs.resize(2 * (size_t)nf);
-            e = cudaMemcpy(flags.data(), d_flags, flags.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost);
-            if (e != cudaSuccess) break;
-            for (uint32_t k = 0; k < nf; ++k) {
-                pairs[2 * k] = flags[5 * k];
-                pairs[2 * k + 1] = mip_texel(t->type, flags[5 * k + 1], flags[5 * k + 2], flags[5 * k + 3],
-                                             flags[5 * k + 4]);
-            }
-            fixed += nf;
-            e = cudaMemcpy(d_pairs, pairs.data(), pairs.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
-            if (e == cudaSuccess) {
-                k_patch<<<grid_for(nf, 256), 256>>>(d_pairs, nf, j.dst);
-                e = cudaGetLastError();
-            }
         }
         if (e != cudaSuccess) break;
         t->data.resize(total);
         e = cudaMemcpy(t->data.data(), d_data, total * sizeof(uint32_t), cudaMemcpyDeviceToHost);
     }
     if (e != cudaSuccess) return cuda_status(e, "device mip chains", err);
-    host_texels += fixed;
     return SWR_OK;
 }
 
-swr_status brdf_lut_device(uint32_t size, HTexture& out, uint64_t& host_texels, std::string& err) {
+swr_status brdf_lut_device(uint32_t size, HTexture& out, std::string& err) {
     const uint32_t kSamples = 128;
     std::vector<float> xi_x(kSamples), xi_y(kSamples), c(kSamples), s(kSamples);
     hammersley_table(kSamples, xi_x.data(), xi_y.data(), c.data(), s.data());
@@ -489,7 +450,7 @@ swr_status brdf_lut_device(uint32_t size, HTexture& out, uint64_t& host_texels, 
         if (e == cudaSuccess) e = cudaMemcpy(out.data.data(), d_out, n * sizeof(uint32_t), cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) return cuda_status(e, "device BRDF LUT", err);
     }
-    return mipmaps_device({&out}, host_texels, err);
+    return mipmaps_device({&out}, err);
 }
 
 swr_status prefiltered_specular_device(const HTexture& cube, uint32_t samples, HTexture& out, uint64_t& host_texels,

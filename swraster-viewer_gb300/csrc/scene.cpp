@@ -109,6 +109,33 @@ uint32_t mip_texel(uint32_t type, uint32_t q00, uint32_t q10, uint32_t q01, uint
 
 float srgb_to_linear_host(float s) { return srgb_to_linear_scalar(s); }
 
+void srgb_byte_thresholds(float out[255]) {
+    auto byte = [](uint32_t bits) {
+        float s;
+        std::memcpy(&s, &bits, 4);
+        return f2u_sat(linear_to_srgb_scalar(s) * 255.0f);
+    };
+    auto as_bits = [](float f) {
+        uint32_t u;
+        std::memcpy(&u, &f, 4);
+        return u;
+    };
+    const uint32_t first = as_bits(0.0031308f) + 1u, last = as_bits(1.0f);
+    for (uint32_t k = 1; k <= 255; ++k) {
+        if (byte(last) < k) {
+            out[k - 1] = INFINITY;
+            continue;
+        }
+        uint32_t lo = first, hi = last;  // the first bits in [lo, hi] whose byte is >= k
+        while (lo < hi) {
+            const uint32_t mid = lo + (hi - lo) / 2;
+            if (byte(mid) >= k) hi = mid;
+            else lo = mid + 1;
+        }
+        std::memcpy(&out[k - 1], &lo, 4);
+    }
+}
+
 void HTexture::mip_layout() {
     const uint32_t num_mips = 1u + ilog2u(std::max(width, height));
     const uint32_t array_size = type == SWR_TEX_CUBEMAP ? 6u : 1u;
@@ -882,7 +909,7 @@ swr_status build_scene(const swr_scene_desc* desc, SceneImpl* s, std::string& er
     if (on_device) {
         std::vector<HTexture*> texs;
         for (HTexture& t : s->textures) texs.push_back(&t);
-        const swr_status mst = mipmaps_device(texs, s->precompute_host_texels, err);
+        const swr_status mst = mipmaps_device(texs, err);
         if (mst != SWR_OK) return mst;
     } else {
         parallel_for(s->textures.size(), threads, [&](size_t i) { s->textures[i].generate_mipmaps(); });
@@ -1009,7 +1036,7 @@ swr_status build_scene(const swr_scene_desc* desc, SceneImpl* s, std::string& er
     }
     s->cubemap = make_texture(desc->cubemap_face_size, desc->cubemap_face_size, SWR_TEX_CUBEMAP, desc->cubemap_faces, true);
     if (on_device) {
-        const swr_status cst = mipmaps_device({&s->cubemap}, s->precompute_host_texels, err);
+        const swr_status cst = mipmaps_device({&s->cubemap}, err);
         if (cst != SWR_OK) return cst;
     } else {
         s->cubemap.generate_mipmaps();
@@ -1039,8 +1066,7 @@ swr_status build_scene(const swr_scene_desc* desc, SceneImpl* s, std::string& er
     }
     compute_irradiance_sh4(s->cubemap, s->irradiance_sh);
     if (on_device) {
-        const swr_status bst = brdf_lut_device(desc->brdf_lut_size ? desc->brdf_lut_size : 128u, s->brdf_lut,
-                                                s->precompute_host_texels, err);
+        const swr_status bst = brdf_lut_device(desc->brdf_lut_size ? desc->brdf_lut_size : 128u, s->brdf_lut, err);
         if (bst != SWR_OK) return bst;
     } else {
         s->brdf_lut = generate_brdf_lut(desc->brdf_lut_size ? desc->brdf_lut_size : 128u, threads);
