@@ -63,7 +63,14 @@ __device__ __forceinline__ void srgb_to_linear_iv(float s, float& lo, float& hi)
         lo = hi = s / 12.92f;
         return;
     }
-    widen(pow_24((s + 0.055f) / 1.055f), lo, hi);
+    const float x = (s + 0.055f) / 1.055f;
+    // powf(1, y) is exactly 1 in every conforming libm (C11 F.10.4.4): white
+    // samples stay exact.
+    if (x == 1.0f) {
+        lo = hi = 1.0f;
+        return;
+    }
+    widen(pow_24(x), lo, hi);
 }
 
 // The byte linear_to_srgb_scalar (src/util.rs:66-72) packs to. Its powf

@@ -938,53 +938,90 @@ __device__ __forceinline__ uint32_t order_bucket(uint32_t c) {
 }
 
 // Exclusive scan of tile counts (single CTA). Also seeds the scatter cursors
-// and writes the raster's tile visiting order.
+// and writes the raster's tile visiting order. Each warp owns a contiguous
+// run of 32-bin chunks and reads kScanUnroll chunks at once, so the loads of
+// a batch of many views (10^5 bins) overlap instead of following one another.
+constexpr int kScanUnroll = 8;
 __global__ void __launch_bounds__(1024) k_scan(FrameArgs a) {
-    __shared__ uint32_t part[1024];
+    __shared__ uint32_t wsum[32];
+    __shared__ uint32_t bucket[kOrderBuckets];
     const uint32_t n = a.dyn->n_bins;
-    const uint32_t per = (n + 1023u) / 1024u;
-    const uint32_t b = threadIdx.x * per;
-    const uint32_t e = min(b + per, n);
-    uint32_t s = 0;
-    for (uint32_t i = b; i < e; ++i) s += a.tile_count[i];
-    part[threadIdx.x] = s;
-    __syncthreads();
-    for (uint32_t off = 1; off < 1024u; off <<= 1) {
-        uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
-        __syncthreads();
-        part[threadIdx.x] += v;
-        __syncthreads();
-    }
-    uint32_t run = part[threadIdx.x] - s;
-    for (uint32_t i = b; i < e; ++i) {
-        a.tile_offset[i] = run;
-        a.tile_cursor[i] = run;
-        run += a.tile_count[i];
-    }
-    if (threadIdx.x == 1023) {
-        a.tile_offset[n] = part[1023];
-        a.counters->pairs = part[1023];
-        if ((uint64_t)part[1023] > a.bin_cap) atomicOr(&a.counters->status, ST_BIN_OVERFLOW);
-    }
+    const uint32_t n_st = a.dyn->n_stiles;
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     // Raster visiting order: opaque scheduling tiles, heaviest bins first
     // (longest job first over the persistent CTAs, so the kernel does not end
     // on a late heavy tile). Bins are bucketed by half-octave of their size;
-    // order within a bucket is arbitrary, since tiles are independent. The
-    // counts are no longer needed, so the order is written over them.
-    if (a.sched_tile < kOrderMinTile) return;
-    __shared__ uint32_t bucket[kOrderBuckets];
+    // order within a bucket is arbitrary, since tiles are independent.
+    const bool order = a.sched_tile >= kOrderMinTile;
     if (threadIdx.x < kOrderBuckets) bucket[threadIdx.x] = 0u;
-    __syncthreads();
-    // Lanes of a warp that share a bucket add to it once (most bins of a
-    // frame fall in a few buckets).
-    const uint32_t n_st = a.dyn->n_stiles;
-    const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t n_st_pad = (n_st + 1023u) & ~1023u;
-    for (uint32_t i = threadIdx.x; i < n_st_pad; i += 1024u) {
-        const uint32_t k = i < n_st ? order_bucket(a.tile_offset[i + 1] - a.tile_offset[i]) : kOrderBuckets;
-        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, k);
-        if (k < kOrderBuckets && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&bucket[k], (uint32_t)__popc(peers));
+    const uint32_t chunks = (n + 31u) >> 5;
+    const uint32_t per = (chunks + 31u) >> 5;
+    const uint32_t cb = min(warp * per, chunks), ce = min(cb + per, chunks);
+    uint32_t s = 0;
+    for (uint32_t c = cb; c < ce; c += kScanUnroll) {
+        uint32_t v[kScanUnroll];
+#pragma unroll
+        for (int k = 0; k < kScanUnroll; ++k) {
+            const uint32_t i = ((c + k) << 5) + lane;
+            v[k] = (c + k < ce && i < n) ? a.tile_count[i] : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < kScanUnroll; ++k) s += v[k];
     }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, off);
+    if (lane == 0) wsum[warp] = s;
+    __syncthreads();
+    uint32_t run, total;
+    {
+        const uint32_t x = wsum[lane];
+        uint32_t incl = x;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, off);
+            if (lane >= (uint32_t)off) incl += y;
+        }
+        run = __shfl_sync(0xFFFFFFFFu, incl - x, warp);
+        total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    }
+    for (uint32_t c = cb; c < ce; c += kScanUnroll) {
+        uint32_t v[kScanUnroll];
+#pragma unroll
+        for (int k = 0; k < kScanUnroll; ++k) {
+            const uint32_t i = ((c + k) << 5) + lane;
+            v[k] = (c + k < ce && i < n) ? a.tile_count[i] : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < kScanUnroll; ++k) {
+            uint32_t incl = v[k];
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, off);
+                if (lane >= (uint32_t)off) incl += y;
+            }
+            const uint32_t i = ((c + k) << 5) + lane;
+            if (c + k < ce && i < n) {
+                const uint32_t o = run + incl - v[k];
+                a.tile_offset[i] = o;
+                a.tile_cursor[i] = o;
+            }
+            if (order) {
+                // Lanes of a warp that share a bucket add to it once (most
+                // bins of a frame fall in a few buckets).
+                const uint32_t key = (c + k < ce && i < n_st) ? order_bucket(v[k]) : (uint32_t)kOrderBuckets;
+                const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
+                if (key < (uint32_t)kOrderBuckets && lane == (uint32_t)(__ffs(peers) - 1))
+                    atomicAdd(&bucket[key], (uint32_t)__popc(peers));
+            }
+            run += __shfl_sync(0xFFFFFFFFu, incl, 31);
+        }
+    }
+    if (threadIdx.x == 0) {
+        a.tile_offset[n] = total;
+        a.counters->pairs = total;
+        if ((uint64_t)total > a.bin_cap) atomicOr(&a.counters->status, ST_BIN_OVERFLOW);
+    }
+    if (!order) return;
     __syncthreads();
     if (threadIdx.x == 0) {
         uint32_t acc = 0;
@@ -995,14 +1032,26 @@ __global__ void __launch_bounds__(1024) k_scan(FrameArgs a) {
         }
     }
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < n_st_pad; i += 1024u) {
-        const uint32_t k = i < n_st ? order_bucket(a.tile_offset[i + 1] - a.tile_offset[i]) : kOrderBuckets;
-        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, k);
-        const uint32_t leader = (uint32_t)(__ffs(peers) - 1);
-        uint32_t base = 0;
-        if (k < kOrderBuckets && lane == leader) base = atomicAdd(&bucket[k], (uint32_t)__popc(peers));
-        base = __shfl_sync(0xFFFFFFFFu, base, leader);
-        if (k < kOrderBuckets) a.tile_count[base + __popc(peers & ((1u << lane) - 1u))] = i;
+    // The counts are no longer needed, so the order is written over them;
+    // bin sizes come from the offsets.
+    constexpr int kPlaceUnroll = 4;
+    const uint32_t n_st_pad = (n_st + 1023u) & ~1023u;
+    for (uint32_t i0 = threadIdx.x; i0 < n_st_pad; i0 += 1024u * kPlaceUnroll) {
+        uint32_t key[kPlaceUnroll];
+#pragma unroll
+        for (int u = 0; u < kPlaceUnroll; ++u) {
+            const uint32_t i = i0 + 1024u * u;
+            key[u] = i < n_st ? order_bucket(a.tile_offset[i + 1] - a.tile_offset[i]) : (uint32_t)kOrderBuckets;
+        }
+#pragma unroll
+        for (int u = 0; u < kPlaceUnroll; ++u) {
+            const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key[u]);
+            const uint32_t leader = (uint32_t)(__ffs(peers) - 1);
+            uint32_t base = 0;
+            if (key[u] < (uint32_t)kOrderBuckets && lane == leader) base = atomicAdd(&bucket[key[u]], (uint32_t)__popc(peers));
+            base = __shfl_sync(0xFFFFFFFFu, base, leader);
+            if (key[u] < (uint32_t)kOrderBuckets) a.tile_count[base + __popc(peers & ((1u << lane) - 1u))] = i0 + 1024u * u;
+        }
     }
 }
 
