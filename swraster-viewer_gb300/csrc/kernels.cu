@@ -1055,6 +1055,12 @@ __global__ void __launch_bounds__(1024) k_scan(FrameArgs a) {
     }
 }
 
+// Triangles whose bounding box spans fewer pixels than this take no depth
+// floor, so their packets are never culled (0: every triangle takes one).
+#ifndef SWR_FLOOR_MIN_PX
+#define SWR_FLOOR_MIN_PX 0
+#endif
+
 // Record slots are the frame's main slots [0, T) and the clipper's extra
 // slots right after them.
 __device__ __forceinline__ void scatter_slot(const FrameArgs& a, uint32_t slot, uint32_t tri_total) {
@@ -1066,7 +1072,9 @@ __device__ __forceinline__ void scatter_slot(const FrameArgs& a, uint32_t slot, 
     const RecRaster& r = a.rec_r[slot];
     const DView& view = a.views[r.view];
     const uint32_t bin_off = (r.material & kRecTransBit) ? a.dyn->n_stiles : 0u;
-    if ((int32_t)a.sched_tile >= SWR_CULL_MIN_TILE && !(r.material & kRecTransBit)) {
+    if ((int32_t)a.sched_tile >= SWR_CULL_MIN_TILE && !(r.material & kRecTransBit) &&
+        (SWR_FLOOR_MIN_PX == 0 ||
+         (uint32_t)(r.bb[2] - r.bb[0] + 1) * (uint32_t)(r.bb[3] - r.bb[1] + 1) >= (uint32_t)SWR_FLOOR_MIN_PX)) {
         // The depth floor of the whole triangle for the raster's occlusion
         // culling: every packet's sample coordinates lie below the bbox end,
         // so one floor bounds the depths of all its packets; taken once here
