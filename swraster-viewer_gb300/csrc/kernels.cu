@@ -1057,6 +1057,9 @@ __global__ void __launch_bounds__(1024) k_scan(FrameArgs a) {
 
 // Triangles whose bounding box spans fewer pixels than this take no depth
 // floor, so their packets are never culled (0: every triangle takes one).
+// Small triangles are most of what culling drops: on the 4K frame, raster +
+// scatter took 0.394 + 0.075 ms with a floor for every triangle, 0.421 +
+// 0.077 from 16 px, 0.467 + 0.061 from 64 px and 0.506 + 0.058 from 256 px.
 #ifndef SWR_FLOOR_MIN_PX
 #define SWR_FLOOR_MIN_PX 0
 #endif
