@@ -180,17 +180,9 @@ struct alignas(16) DDraw {
     uint32_t pad[3];
 };
 
-// Up to kChunkTris triangles of one draw (one front-end CTA). The chunk
-// holds where its triangles' indices and vertices are, so the front end's
-// index and vertex loads follow the chunk load directly instead of waiting
-// for the draw, the scene and the primitive first.
-struct alignas(16) DChunk {
+struct DChunk {
     uint32_t draw;
     uint32_t tri_start;        // local to the draw
-    uint32_t count;            // triangles in the chunk
-    uint32_t pad;
-    const uint32_t* indices;   // indices of the chunk's first triangle
-    const DVertex* vertices;   // vertex 0 of the draw's primitive
 };
 
 // RecRaster.material carries the alpha-test flag in its top bit and the

@@ -568,12 +568,7 @@ __device__ DrawCount node_draws(const FrameArgs& a, uint32_t vi, const DView& v,
                 d.translucent = translucent ? 1u : 0u;
                 d.pad[0] = d.pad[1] = d.pad[2] = 0u;
                 a.draws[di] = d;
-                const DPrimitive pr = sc.prims[me.prim];
-                for (uint32_t j = 0; j < nch; ++j) {
-                    const uint32_t t0 = j * (uint32_t)kChunkTris;
-                    a.chunks[ci + j] = DChunk{di, t0, min((uint32_t)kChunkTris, tc - t0), 0u,
-                                              sc.indices + pr.idx_base + 3u * t0, sc.vertices + pr.vtx_base};
-                }
+                for (uint32_t j = 0; j < nch; ++j) a.chunks[ci + j] = DChunk{di, j * (uint32_t)kChunkTris};
                 trans |= translucent;
             } else {
                 atomicOr(&a.counters->status, ST_DRAW_OVERFLOW);
@@ -790,18 +785,19 @@ __device__ __forceinline__ void frontend_triangle(const FrameArgs& a, uint32_t c
     const DDraw& d = a.draws[ch.draw];
     // The CTA's triangles are one draw's: count the chunk once for the
     // reference's clip path (every triangle of an intersecting primitive).
-    if (threadIdx.x == 0 && d.clip) atomicAdd(&a.counters->clip_path, ch.count);
-    if (threadIdx.x >= ch.count) return;
-    const uint32_t* ib = ch.indices + 3u * threadIdx.x;
-    const uint32_t i0 = __ldg(ib), i1 = __ldg(ib + 1), i2 = __ldg(ib + 2);
+    if (threadIdx.x == 0 && d.clip) atomicAdd(&a.counters->clip_path, min((uint32_t)kChunkTris, d.tri_count - ch.tri_start));
     const uint32_t local = ch.tri_start + threadIdx.x;
+    if (local >= d.tri_count) return;
     const uint32_t g = d.tri_begin + local;
     const DScene& sc = a.scenes[d.scene];
     const DView& view = a.views[d.view];
+    const DPrimitive pr = sc.prims[d.prim];
     const float* model = sc.node_xform + 16u * d.node;
-    const Vtx v0 = transform_vertex(ch.vertices, i0, model, d.mvp);
-    const Vtx v1 = transform_vertex(ch.vertices, i1, model, d.mvp);
-    const Vtx v2 = transform_vertex(ch.vertices, i2, model, d.mvp);
+    const uint32_t* ib = sc.indices + pr.idx_base + 3u * local;
+    const uint32_t i0 = __ldg(ib), i1 = __ldg(ib + 1), i2 = __ldg(ib + 2);
+    const Vtx v0 = transform_vertex(sc.vertices, pr.vtx_base + i0, model, d.mvp);
+    const Vtx v1 = transform_vertex(sc.vertices, pr.vtx_base + i1, model, d.mvp);
+    const Vtx v2 = transform_vertex(sc.vertices, pr.vtx_base + i2, model, d.mvp);
     if (d.clip && !(vtx_inside_all(v0) && vtx_inside_all(v1) && vtx_inside_all(v2))) {
         if (clip_rejects_all(v0, v1, v2)) {  // the clipper would return an empty polygon
             a.tri_state[g] = 3;
@@ -817,7 +813,7 @@ __device__ __forceinline__ void frontend_triangle(const FrameArgs& a, uint32_t c
         return;
     }
     // All three vertices inside: the clipper would return the triangle unchanged.
-    const uint32_t mword = record_material(sc, d, sc.prims[d.prim].material);
+    const uint32_t mword = record_material(sc, d, pr.material);
     RecRaster r;
     RecShade q;
     const bool ok = setup_triangle(a, view, v0, v1, v2, g << 3, d.static_base + local, mword, d.view, r, q);

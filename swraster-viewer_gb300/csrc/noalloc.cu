@@ -28,7 +28,6 @@
 // separate lock held while the tables are staged.
 #include <cuda_runtime.h>
 
-#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -228,10 +227,7 @@ extern "C" swr_status swr_render_frame_noalloc(const swr_scene* scene, const swr
             d.tri_count = tc;
             d.static_base = n.tri_id_base + p.tri_id_base;
             d.scene = 0;
-            for (uint32_t t = 0; t < tc; t += kChunkTris)
-                chunks[nc++] = DChunk{nd, t, std::min<uint32_t>(kChunkTris, tc - t), 0u,
-                                      s.dscene.indices + s.prim_idx_base[gp] + 3u * t,
-                                      s.dscene.vertices + s.prim_vtx_base[gp]};
+            for (uint32_t t = 0; t < tc; t += kChunkTris) chunks[nc++] = {nd, t};
             ++nd;
             tri += tc;
         }

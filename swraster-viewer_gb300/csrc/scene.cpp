@@ -1345,8 +1345,6 @@ DTexture to_dtex(const HTexture& t, uintptr_t addr) {
 
 swr_status upload_scene(SceneImpl* s, std::string& err, bool to_device) {
     Arena ar;
-    s->prim_vtx_base.clear();
-    s->prim_idx_base.clear();
     // Vertices, indices, primitive table.
     std::vector<DVertex> verts;
     verts.reserve(s->vtx_total);
@@ -1359,8 +1357,6 @@ swr_status upload_scene(SceneImpl* s, std::string& err, bool to_device) {
         dp.tri_count = (uint32_t)(p.idx.size() / 3);
         dp.material = p.material;
         prims.push_back(dp);
-        s->prim_vtx_base.push_back(dp.vtx_base);
-        s->prim_idx_base.push_back(dp.idx_base);
         const size_t nv = p.pos4.size() / 4;
         for (size_t v = 0; v < nv; ++v) {
             DVertex d;

@@ -71,8 +71,6 @@ struct SceneImpl {
     bool any_translucent = false;  // some node's mesh has translucent primitives
     uint32_t gi_cache = 0, ggx_cache = 0;  // SWR_CACHE_*
     uint64_t precompute_host_texels = 0;   // device precompute texels recomputed on the host
-    // Per primitive, its first vertex and index in the device arrays.
-    std::vector<uint32_t> prim_vtx_base, prim_idx_base;
 
     // Export views.
     std::vector<swr_primitive_view> prim_views;
