@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <thread>
 #include <vector>
 
 #include "devmath.cuh"
@@ -26,6 +27,8 @@ namespace {
 
 constexpr float kPi = 3.14159265358979323846f;
 constexpr float kRayEps = 1.0e-4f;
+// Active voxels baked per chunk (64 rays each, 6 texture values a ray).
+constexpr uint32_t kBakeChunkVoxels = 16384;
 
 struct V {
     float x, y, z;
@@ -219,12 +222,6 @@ __device__ float trace_transmittance(const Dev& D, V o, V d, float tmin) {
 
 __device__ __forceinline__ float unorm8(uint32_t b) { return (float)b / 255.0f; }
 
-// srgb_to_linear_scalar (src/util.rs:49-55).
-__device__ __forceinline__ float srgb_to_linear(float s) {
-    if (s <= 0.04045f) return s / 12.92f;
-    return powf((s + 0.055f) / 1.055f, 2.4f);
-}
-
 // TextureAndSampler::apply_wrap_mode (src/texture.rs:578-589); WrapMode
 // 0 repeat, 1 mirrored repeat, 2 clamp to edge.
 __device__ __forceinline__ float wrap(float t, float dim, uint32_t mode) {
@@ -238,8 +235,10 @@ __device__ __forceinline__ float wrap(float t, float dim, uint32_t mode) {
     return fminf(t, dim - 1.0f);
 }
 
-// sample_bilinear_rgb at mip 0 (src/texture.rs:730-790), then to linear.
-__device__ V sample_bilinear_linear(const Dev& D, const BakeTexture& T, float u, float v, uint32_t ws, uint32_t wt) {
+// sample_bilinear_rgb at mip 0 (src/texture.rs:730-790): the sRGB values
+// before srgb_to_linear_scalar, which the host applies (its powf).
+__device__ void sample_bilinear_srgb(const Dev& D, const BakeTexture& T, float u, float v, uint32_t ws, uint32_t wt,
+                                     float* c) {
     const float wf = (float)T.width, hf = (float)T.height;
     const float xf = u * wf - 0.5f, yf = v * hf - 0.5f;
     const float x0 = floorf(xf), y0 = floorf(yf);
@@ -251,7 +250,6 @@ __device__ V sample_bilinear_linear(const Dev& D, const BakeTexture& T, float u,
     const uint32_t p00 = D.texels[T.offset + iy0 * T.width + ix0], p10 = D.texels[T.offset + iy0 * T.width + ix1];
     const uint32_t p01 = D.texels[T.offset + iy1 * T.width + ix0], p11 = D.texels[T.offset + iy1 * T.width + ix1];
     const float w00 = ofx * ofy, w10 = fx * ofy, w01 = ofx * fy, w11 = fx * fy;
-    float c[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         const int sh = 24 - 8 * k;
@@ -259,7 +257,6 @@ __device__ V sample_bilinear_linear(const Dev& D, const BakeTexture& T, float u,
                 unorm8((p01 >> sh) & 0xFFu) * w01) +
                unorm8((p11 >> sh) & 0xFFu) * w11;
     }
-    return V{srgb_to_linear(c[0]), srgb_to_linear(c[1]), srgb_to_linear(c[2])};
 }
 
 // sample_sky_radiance (src/gi.rs:580-593): nearest texel of cubemap mip 0.
@@ -295,24 +292,27 @@ __device__ float sky_visibility4(const Dev& D, V origin, V n, float dir_bias, fl
     return sum * 0.25f;
 }
 
-// estimate_surface_bounce_radiance (src/gi.rs:466-547).
+// The hit's texture coordinates (src/gi.rs:480-486).
+__device__ __forceinline__ void hit_uv(const BakeTri& tri, float bu, float bv, float& uvx, float& uvy) {
+    const float bw = (1.0f - bu) - bv;
+    uvx = (tri.uv0[0] * bw + tri.uv1[0] * bu) + tri.uv2[0] * bv;
+    uvy = (tri.uv0[1] * bw + tri.uv1[1] * bu) + tri.uv2[1] * bv;
+}
+
+// estimate_surface_bounce_radiance (src/gi.rs:466-547). lin: the ray's base
+// and emissive texture samples in linear (srgb_to_linear_scalar of the
+// bilinear sample, computed on the host).
 __device__ V bounce_radiance(const Dev& D, uint32_t ti, float t, float bu, float bv, V o, V in_dir, float hit_bias,
-                             float tmin) {
+                             float tmin, const float* lin) {
     const BakeTri& tri = D.tris[ti];
     const BakeMaterial& m = D.mats[tri.material];
     V nrm = ld3(tri.n);
     if (dot(nrm, in_dir * -1.0f) < 0.0f) nrm = nrm * -1.0f;
-    const float bw = (1.0f - bu) - bv;
-    const float uvx = (tri.uv0[0] * bw + tri.uv1[0] * bu) + tri.uv2[0] * bv;
-    const float uvy = (tri.uv0[1] * bw + tri.uv1[1] * bu) + tri.uv2[1] * bv;
     V emissive = ld3(m.emissive);
-    if (m.emissive_tex >= 0)
-        emissive = emissive * sample_bilinear_linear(D, D.textures[m.emissive_tex], uvx, uvy, m.emissive_wrap_s,
-                                                     m.emissive_wrap_t);
+    if (m.emissive_tex >= 0) emissive = emissive * ld3(lin + 3);
     emissive = vmax0(emissive);
     V albedo = ld3(m.base);
-    if (m.base_tex >= 0)
-        albedo = albedo * sample_bilinear_linear(D, D.textures[m.base_tex], uvx, uvy, m.base_wrap_s, m.base_wrap_t);
+    if (m.base_tex >= 0) albedo = albedo * ld3(lin);
     albedo = V{fminf(fmaxf(albedo.x, 0.0f), 1.0f), fminf(fmaxf(albedo.y, 0.0f), 1.0f),
                fminf(fmaxf(albedo.z, 0.0f), 1.0f)} * 1.0f;
     if (dot(albedo, albedo) <= 0.0f && dot(emissive, emissive) <= 0.0f) return mk(0.0f, 0.0f, 0.0f);
@@ -337,32 +337,84 @@ __device__ V bounce_radiance(const Dev& D, uint32_t ti, float t, float bu, float
 
 __device__ __forceinline__ float luminance(V c) { return (0.2126f * c.x + 0.7152f * c.y) + 0.0722f * c.z; }
 
-__global__ void __launch_bounds__(128) k_gi_bake(Dev D) {
+// The bake's per-voxel constants and the primary rays of a voxel.
+struct BakeConsts {
+    V vsz, cmin;
+    float primary_weight, primary_bias, hit_bias, gi_tmin;
+};
+__device__ __forceinline__ BakeConsts bake_consts(const Dev& D) {
+    BakeConsts c;
+    c.vsz = ld3(D.vsz);
+    c.cmin = ld3(D.cmin);
+    const float vlen = __fsqrt_rn(dot(c.vsz, c.vsz));
+    const float min_edge = fmaxf(fminf(fminf(c.vsz.x, c.vsz.y), c.vsz.z), 1.0e-6f);
+    c.primary_weight = (4.0f * kPi) / (float)kGiSamples;
+    c.primary_bias = fmaxf(vlen * 0.35f, kRayEps * 4.0f);
+    c.hit_bias = fmaxf(vlen * 0.05f, kRayEps * 8.0f);
+    c.gi_tmin = fmaxf(min_edge * 0.15f, kRayEps);
+    return c;
+}
+// Voxel idx's centre and its direction set.
+__device__ __forceinline__ void voxel_rays(const Dev& D, const BakeConsts& c, uint32_t idx, V& vc, const float*& dirs) {
     const uint32_t n = D.n;
-    const V vsz = ld3(D.vsz), cmin = ld3(D.cmin);
-    const float vlen = __fsqrt_rn(dot(vsz, vsz));
-    const float min_edge = fmaxf(fminf(fminf(vsz.x, vsz.y), vsz.z), 1.0e-6f);
-    const float primary_weight = (4.0f * kPi) / (float)kGiSamples;
-    const float primary_bias = fmaxf(vlen * 0.35f, kRayEps * 4.0f);
-    const float hit_bias = fmaxf(vlen * 0.05f, kRayEps * 8.0f);
-    const float gi_tmin = fmaxf(min_edge * 0.15f, kRayEps);
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < D.n_active; k += gridDim.x * blockDim.x) {
+    const uint32_t z = idx / (n * n), rem = idx % (n * n);
+    const uint32_t y = rem / n, x = rem % n;
+    vc = c.cmin + mk((float)x, (float)y, (float)z) * c.vsz;
+    const uint32_t set = ((x % 3u) + 3u * (y % 3u) + (z % 3u)) % kGiSets;
+    dirs = D.dirs + (size_t)set * kGiSamples * 3;
+}
+
+// First step over the active voxels [k0, k1): for each primary ray, the
+// bilinear sRGB samples of the base and emissive textures where it hits
+// (6 floats per ray, in ray order; NaN where the hit has no such texture or
+// the ray escapes). The host turns them into linear values with its powf.
+__global__ void __launch_bounds__(128) k_gi_tex(Dev D, uint32_t k0, uint32_t k1, float* srgb) {
+    const BakeConsts bc = bake_consts(D);
+    const uint64_t nr = (uint64_t)(k1 - k0) * kGiSamples;
+    for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < nr; r += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t k = k0 + (uint32_t)(r / kGiSamples), s = (uint32_t)(r % kGiSamples);
+        V vc;
+        const float* dirs;
+        voxel_rays(D, bc, D.active_list[k], vc, dirs);
+        const V dir = ld3(dirs + 3 * s);
+        const V ro = vc + dir * bc.primary_bias;
+        float* o = srgb + r * 6;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) o[c] = __int_as_float(0x7FC00000);
+        uint32_t ti = 0;
+        float th = 0.0f, bu = 0.0f, bv = 0.0f;
+        if (!trace_nearest(D, ro, dir, bc.gi_tmin, ti, th, bu, bv)) continue;
+        const BakeTri& tri = D.tris[ti];
+        const BakeMaterial& m = D.mats[tri.material];
+        float uvx, uvy;
+        hit_uv(tri, bu, bv, uvx, uvy);
+        if (m.base_tex >= 0) sample_bilinear_srgb(D, D.textures[m.base_tex], uvx, uvy, m.base_wrap_s, m.base_wrap_t, o);
+        if (m.emissive_tex >= 0)
+            sample_bilinear_srgb(D, D.textures[m.emissive_tex], uvx, uvy, m.emissive_wrap_s, m.emissive_wrap_t, o + 3);
+    }
+}
+
+// Second step over the active voxels [k0, k1), with the rays' texture samples
+// in linear (`lin`, 6 floats per ray as k_gi_tex wrote them).
+__global__ void __launch_bounds__(128) k_gi_bake(Dev D, uint32_t k0, uint32_t k1, const float* lin) {
+    const BakeConsts bc = bake_consts(D);
+    const float primary_weight = bc.primary_weight, hit_bias = bc.hit_bias, gi_tmin = bc.gi_tmin;
+    for (uint32_t k = k0 + blockIdx.x * blockDim.x + threadIdx.x; k < k1; k += gridDim.x * blockDim.x) {
         const uint32_t idx = D.active_list[k];
-        const uint32_t z = idx / (n * n), rem = idx % (n * n);
-        const uint32_t y = rem / n, x = rem % n;
-        const V vc = cmin + mk((float)x, (float)y, (float)z) * vsz;
-        const uint32_t set = ((x % 3u) + 3u * (y % 3u) + (z % 3u)) % kGiSets;
-        const float* dirs = D.dirs + (size_t)set * kGiSamples * 3;
+        V vc;
+        const float* dirs;
+        voxel_rays(D, bc, idx, vc, dirs);
         V rsh[4] = {mk(0, 0, 0), mk(0, 0, 0), mk(0, 0, 0), mk(0, 0, 0)};
         uint32_t sky_hits = 0;
         for (uint32_t s = 0; s < kGiSamples; ++s) {
             const V dir = ld3(dirs + 3 * s);
-            const V ro = vc + dir * primary_bias;
+            const V ro = vc + dir * bc.primary_bias;
             uint32_t ti = 0;
             float th = 0.0f, bu = 0.0f, bv = 0.0f;
             V radiance;
             if (trace_nearest(D, ro, dir, gi_tmin, ti, th, bu, bv)) {
-                radiance = bounce_radiance(D, ti, th, bu, bv, ro, dir, hit_bias, gi_tmin);
+                radiance = bounce_radiance(D, ti, th, bu, bv, ro, dir, hit_bias, gi_tmin,
+                                           lin + ((uint64_t)(k - k0) * kGiSamples + s) * 6);
             } else {
                 ++sky_hits;
                 radiance = sky_radiance(D, dir);
@@ -541,10 +593,44 @@ swr_status gi_bake_device(const BakeInput& in, float* out, std::string& err) {
         D.out = raw;
         const uint32_t vg = (uint32_t)std::min<uint64_t>((nvox + 255) / 256, (uint64_t)sms * 16);
         k_gi_init<<<vg, 256>>>(D);
-        if (D.n_active > 0)
-            k_gi_bake<<<(uint32_t)std::min<uint64_t>((D.n_active + 127) / 128, (uint64_t)sms * 64), 128>>>(D);
-        k_gi_blur<<<vg, 256>>>(raw, blur, n);
         e = cudaGetLastError();
+        // The active voxels in chunks: the texture samples of a chunk's rays
+        // go to the host, which converts them to linear with its own powf
+        // (bit for bit the reference's srgb_to_linear_scalar), then the
+        // chunk is baked with them.
+        float *d_srgb = nullptr, *d_lin = nullptr;
+        const uint32_t chunk = std::min<uint32_t>(std::max<uint32_t>(D.n_active, 1u), kBakeChunkVoxels);
+        const size_t chunk_vals = (size_t)chunk * kGiSamples * 6;
+        if (e == cudaSuccess) e = m.put(&d_srgb, (const float*)nullptr, chunk_vals);
+        if (e == cudaSuccess) e = m.put(&d_lin, (const float*)nullptr, chunk_vals);
+        std::vector<float> vals(e == cudaSuccess && D.n_active ? chunk_vals : 0);
+        const unsigned threads = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+        for (uint32_t k0 = 0; k0 < D.n_active && e == cudaSuccess; k0 += chunk) {
+            const uint32_t k1 = std::min(D.n_active, k0 + chunk);
+            const size_t nv = (size_t)(k1 - k0) * kGiSamples * 6;
+            k_gi_tex<<<(uint32_t)std::min<uint64_t>(((uint64_t)(k1 - k0) * kGiSamples + 127) / 128,
+                                                    (uint64_t)sms * 64),
+                       128>>>(D, k0, k1, d_srgb);
+            e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaMemcpy(vals.data(), d_srgb, nv * sizeof(float), cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) break;
+            std::vector<std::thread> pool;
+            for (unsigned t = 0; t < threads; ++t)
+                pool.emplace_back([&, t] {
+                    for (size_t i = nv * t / threads; i < nv * (t + 1) / threads; ++i)
+                        if (vals[i] == vals[i]) vals[i] = srgb_to_linear_host(vals[i]);
+                });
+            for (auto& th : pool) th.join();
+            e = cudaMemcpy(d_lin, vals.data(), nv * sizeof(float), cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) break;
+            k_gi_bake<<<(uint32_t)std::min<uint64_t>((k1 - k0 + 127) / 128, (uint64_t)sms * 64), 128>>>(D, k0, k1,
+                                                                                                        d_lin);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) {
+            k_gi_blur<<<vg, 256>>>(raw, blur, n);
+            e = cudaGetLastError();
+        }
     }
     if (e == cudaSuccess) e = cudaMemcpy(out, blur, nvox * 16 * sizeof(float), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) {

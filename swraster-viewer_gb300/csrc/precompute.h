@@ -77,9 +77,11 @@ struct BakeInput {
 constexpr uint32_t kGiSamples = 64, kGiSets = 9;
 
 // bake_voxel_gi + blur_gi_sh4 on the device: `out` gets n^3 voxels of four
-// (r, g, b, w) SH4 coefficients. Surface textures are sampled bilinearly and
-// converted to linear with the device's powf, so results equal the host
-// restatement up to its last-bit differences from the host's powf.
+// (r, g, b, w) SH4 coefficients, equal to the host restatement bit for bit.
+// Surface textures are sampled bilinearly on the device and converted to
+// linear on the host (srgb_to_linear_scalar with the host's powf), between
+// the two kernels of each chunk of voxels.
 swr_status gi_bake_device(const BakeInput& in, float* out, std::string& err);
+float srgb_to_linear_host(float s);
 
 }  // namespace swr
