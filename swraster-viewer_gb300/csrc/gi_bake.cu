@@ -527,6 +527,19 @@ struct Mem {
     }
 };
 
+struct HostPinned {
+    float* p = nullptr;
+    ~HostPinned() {
+        if (p) cudaFreeHost(p);
+    }
+    cudaError_t alloc(size_t count) {
+        void* q = nullptr;
+        const cudaError_t e = cudaMallocHost(&q, count * sizeof(float));
+        p = static_cast<float*>(q);
+        return e;
+    }
+};
+
 }  // namespace
 
 swr_status gi_bake_device(const BakeInput& in, float* out, std::string& err) {
@@ -597,36 +610,71 @@ swr_status gi_bake_device(const BakeInput& in, float* out, std::string& err) {
         // The active voxels in chunks: the texture samples of a chunk's rays
         // go to the host, which converts them to linear with its own powf
         // (bit for bit the reference's srgb_to_linear_scalar), then the
-        // chunk is baked with them.
+        // chunk is baked with them. Pipelined on one stream: the device
+        // samples chunk i+1 and bakes chunk i-1 while the host converts
+        // chunk i (two pinned buffers alternate).
         float *d_srgb = nullptr, *d_lin = nullptr;
         const uint32_t chunk = std::min<uint32_t>(std::max<uint32_t>(D.n_active, 1u), kBakeChunkVoxels);
         const size_t chunk_vals = (size_t)chunk * kGiSamples * 6;
         if (e == cudaSuccess) e = m.put(&d_srgb, (const float*)nullptr, chunk_vals);
         if (e == cudaSuccess) e = m.put(&d_lin, (const float*)nullptr, chunk_vals);
-        std::vector<float> vals(e == cudaSuccess && D.n_active ? chunk_vals : 0);
+        HostPinned hp;
+        cudaStream_t st = nullptr;
+        cudaEvent_t ready[2] = {nullptr, nullptr};
+        if (e == cudaSuccess && D.n_active) e = hp.alloc(2 * chunk_vals);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+        for (int b = 0; b < 2 && e == cudaSuccess; ++b) e = cudaEventCreateWithFlags(&ready[b], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(nullptr);  // k_gi_init and the inputs
         const unsigned threads = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-        for (uint32_t k0 = 0; k0 < D.n_active && e == cudaSuccess; k0 += chunk) {
-            const uint32_t k1 = std::min(D.n_active, k0 + chunk);
+        const uint32_t n_chunks = (D.n_active + chunk - 1) / chunk;
+        auto range = [&](uint32_t i, uint32_t& k0, uint32_t& k1) {
+            k0 = i * chunk;
+            k1 = std::min(D.n_active, k0 + chunk);
+        };
+        // Samples of chunk i into pinned buffer i % 2.
+        auto sample = [&](uint32_t i) {
+            uint32_t k0, k1;
+            range(i, k0, k1);
             const size_t nv = (size_t)(k1 - k0) * kGiSamples * 6;
-            k_gi_tex<<<(uint32_t)std::min<uint64_t>(((uint64_t)(k1 - k0) * kGiSamples + 127) / 128,
-                                                    (uint64_t)sms * 64),
-                       128>>>(D, k0, k1, d_srgb);
-            e = cudaGetLastError();
-            if (e == cudaSuccess) e = cudaMemcpy(vals.data(), d_srgb, nv * sizeof(float), cudaMemcpyDeviceToHost);
+            k_gi_tex<<<(uint32_t)std::min<uint64_t>(((uint64_t)(k1 - k0) * kGiSamples + 127) / 128, (uint64_t)sms * 64),
+                       128, 0, st>>>(D, k0, k1, d_srgb);
+            cudaError_t x = cudaGetLastError();
+            if (x == cudaSuccess)
+                x = cudaMemcpyAsync(hp.p + (i % 2) * chunk_vals, d_srgb, nv * sizeof(float), cudaMemcpyDeviceToHost, st);
+            if (x == cudaSuccess) x = cudaEventRecord(ready[i % 2], st);
+            return x;
+        };
+        if (e == cudaSuccess && n_chunks) e = sample(0);
+        for (uint32_t i = 0; i < n_chunks && e == cudaSuccess; ++i) {
+            uint32_t k0, k1;
+            range(i, k0, k1);
+            const size_t nv = (size_t)(k1 - k0) * kGiSamples * 6;
+            e = cudaEventSynchronize(ready[i % 2]);
+            if (e == cudaSuccess && i + 1 < n_chunks) e = sample(i + 1);
             if (e != cudaSuccess) break;
+            float* vals = hp.p + (i % 2) * chunk_vals;
             std::vector<std::thread> pool;
             for (unsigned t = 0; t < threads; ++t)
-                pool.emplace_back([&, t] {
-                    for (size_t i = nv * t / threads; i < nv * (t + 1) / threads; ++i)
-                        if (vals[i] == vals[i]) vals[i] = srgb_to_linear_host(vals[i]);
+                pool.emplace_back([=] {
+                    for (size_t j = nv * t / threads; j < nv * (t + 1) / threads; ++j)
+                        if (vals[j] == vals[j]) vals[j] = srgb_to_linear_host(vals[j]);
                 });
             for (auto& th : pool) th.join();
-            e = cudaMemcpy(d_lin, vals.data(), nv * sizeof(float), cudaMemcpyHostToDevice);
+            // Stream order keeps this copy ahead of the next write to the
+            // same pinned buffer (chunk i + 2's samples).
+            e = cudaMemcpyAsync(d_lin, vals, nv * sizeof(float), cudaMemcpyHostToDevice, st);
             if (e != cudaSuccess) break;
-            k_gi_bake<<<(uint32_t)std::min<uint64_t>((k1 - k0 + 127) / 128, (uint64_t)sms * 64), 128>>>(D, k0, k1,
-                                                                                                        d_lin);
+            k_gi_bake<<<(uint32_t)std::min<uint64_t>((k1 - k0 + 127) / 128, (uint64_t)sms * 64), 128, 0, st>>>(
+                D, k0, k1, d_lin);
             e = cudaGetLastError();
         }
+        if (st) {
+            const cudaError_t x = cudaStreamSynchronize(st);
+            if (e == cudaSuccess) e = x;
+        }
+        for (cudaEvent_t ev : ready)
+            if (ev) cudaEventDestroy(ev);
+        if (st) cudaStreamDestroy(st);
         if (e == cudaSuccess) {
             k_gi_blur<<<vg, 256>>>(raw, blur, n);
             e = cudaGetLastError();
