@@ -364,11 +364,13 @@ __device__ __forceinline__ void voxel_rays(const Dev& D, const BakeConsts& c, ui
     dirs = D.dirs + (size_t)set * kGiSamples * 3;
 }
 
-// First step over the active voxels [k0, k1): for each primary ray, the
-// bilinear sRGB samples of the base and emissive textures where it hits
-// (6 floats per ray, in ray order; NaN where the hit has no such texture or
-// the ray escapes). The host turns them into linear values with its powf.
-__global__ void __launch_bounds__(128) k_gi_tex(Dev D, uint32_t k0, uint32_t k1, float* srgb) {
+// Rays of a chunk of active voxels [k0, k1) are numbered r = (k - k0) * 64 + s.
+// First step, one thread per ray: trace the primary ray; `hit` gets the
+// nearest hit (triangle, t, u, v; triangle 0xFFFFFFFF when the ray escapes)
+// and `srgb` the bilinear sRGB samples of the hit's base and emissive
+// textures (6 floats; NaN where the hit has no such texture). The host turns
+// the samples into linear values with its powf.
+__global__ void __launch_bounds__(128) k_gi_tex(Dev D, uint32_t k0, uint32_t k1, uint4* hit, float* srgb) {
     const BakeConsts bc = bake_consts(D);
     const uint64_t nr = (uint64_t)(k1 - k0) * kGiSamples;
     for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < nr; r += (uint64_t)gridDim.x * blockDim.x) {
@@ -383,7 +385,11 @@ __global__ void __launch_bounds__(128) k_gi_tex(Dev D, uint32_t k0, uint32_t k1,
         for (int c = 0; c < 6; ++c) o[c] = __int_as_float(0x7FC00000);
         uint32_t ti = 0;
         float th = 0.0f, bu = 0.0f, bv = 0.0f;
-        if (!trace_nearest(D, ro, dir, bc.gi_tmin, ti, th, bu, bv)) continue;
+        if (!trace_nearest(D, ro, dir, bc.gi_tmin, ti, th, bu, bv)) {
+            hit[r] = make_uint4(0xFFFFFFFFu, 0u, 0u, 0u);
+            continue;
+        }
+        hit[r] = make_uint4(ti, __float_as_uint(th), __float_as_uint(bu), __float_as_uint(bv));
         const BakeTri& tri = D.tris[ti];
         const BakeMaterial& m = D.mats[tri.material];
         float uvx, uvy;
@@ -394,11 +400,36 @@ __global__ void __launch_bounds__(128) k_gi_tex(Dev D, uint32_t k0, uint32_t k1,
     }
 }
 
-// Second step over the active voxels [k0, k1), with the rays' texture samples
-// in linear (`lin`, 6 floats per ray as k_gi_tex wrote them).
-__global__ void __launch_bounds__(128) k_gi_bake(Dev D, uint32_t k0, uint32_t k1, const float* lin) {
+// Second step, one thread per ray: its radiance (the bounce at the hit, with
+// the texture samples in linear from `lin`, or the sky) into `rad`.
+__global__ void __launch_bounds__(128) k_gi_ray(Dev D, uint32_t k0, uint32_t k1, const uint4* hit, const float* lin,
+                                                float* rad) {
     const BakeConsts bc = bake_consts(D);
-    const float primary_weight = bc.primary_weight, hit_bias = bc.hit_bias, gi_tmin = bc.gi_tmin;
+    const uint64_t nr = (uint64_t)(k1 - k0) * kGiSamples;
+    for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < nr; r += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t k = k0 + (uint32_t)(r / kGiSamples), s = (uint32_t)(r % kGiSamples);
+        V vc;
+        const float* dirs;
+        voxel_rays(D, bc, D.active_list[k], vc, dirs);
+        const V dir = ld3(dirs + 3 * s);
+        const V ro = vc + dir * bc.primary_bias;
+        const uint4 h = hit[r];
+        const V radiance = h.x == 0xFFFFFFFFu
+                               ? sky_radiance(D, dir)
+                               : bounce_radiance(D, h.x, __uint_as_float(h.y), __uint_as_float(h.z),
+                                                 __uint_as_float(h.w), ro, dir, bc.hit_bias, bc.gi_tmin, lin + r * 6);
+        rad[3 * r] = radiance.x;
+        rad[3 * r + 1] = radiance.y;
+        rad[3 * r + 2] = radiance.z;
+    }
+}
+
+// Third step, one thread per voxel: its 64 radiances projected to SH4 in ray
+// order, convolved, floored, stored with the sun and sky visibility.
+__global__ void __launch_bounds__(128) k_gi_accum(Dev D, uint32_t k0, uint32_t k1, const uint4* hit,
+                                                  const float* rad) {
+    const BakeConsts bc = bake_consts(D);
+    const float primary_weight = bc.primary_weight;
     for (uint32_t k = k0 + blockIdx.x * blockDim.x + threadIdx.x; k < k1; k += gridDim.x * blockDim.x) {
         const uint32_t idx = D.active_list[k];
         V vc;
@@ -407,18 +438,10 @@ __global__ void __launch_bounds__(128) k_gi_bake(Dev D, uint32_t k0, uint32_t k1
         V rsh[4] = {mk(0, 0, 0), mk(0, 0, 0), mk(0, 0, 0), mk(0, 0, 0)};
         uint32_t sky_hits = 0;
         for (uint32_t s = 0; s < kGiSamples; ++s) {
+            const uint64_t r = (uint64_t)(k - k0) * kGiSamples + s;
             const V dir = ld3(dirs + 3 * s);
-            const V ro = vc + dir * bc.primary_bias;
-            uint32_t ti = 0;
-            float th = 0.0f, bu = 0.0f, bv = 0.0f;
-            V radiance;
-            if (trace_nearest(D, ro, dir, gi_tmin, ti, th, bu, bv)) {
-                radiance = bounce_radiance(D, ti, th, bu, bv, ro, dir, hit_bias, gi_tmin,
-                                           lin + ((uint64_t)(k - k0) * kGiSamples + s) * 6);
-            } else {
-                ++sky_hits;
-                radiance = sky_radiance(D, dir);
-            }
+            if (hit[r].x == 0xFFFFFFFFu) ++sky_hits;
+            const V radiance = ld3(rad + 3 * r);
             if (dot(radiance, radiance) <= 0.0f) continue;
             // project_radiance_sh4 (src/gi.rs:437-452).
             const float basis[4] = {0.282095f, 0.488603f * dir.y, 0.488603f * dir.z, 0.488603f * dir.x};
@@ -427,10 +450,10 @@ __global__ void __launch_bounds__(128) k_gi_bake(Dev D, uint32_t k0, uint32_t k1
         }
         // radiance_to_irradiance_sh4 (src/gi.rs:454-461).
         rsh[0] = rsh[0] * (kPi * 0.282095f);
-        const float k1 = ((2.0f * kPi) / 3.0f) * 0.488603f;
-        rsh[1] = rsh[1] * k1;
-        rsh[2] = rsh[2] * k1;
-        rsh[3] = rsh[3] * k1;
+        const float k1c = ((2.0f * kPi) / 3.0f) * 0.488603f;
+        rsh[1] = rsh[1] * k1c;
+        rsh[2] = rsh[2] * k1c;
+        rsh[3] = rsh[3] * k1c;
         V rgb[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) rgb[i] = vmax0(rsh[i]);
@@ -613,11 +636,14 @@ swr_status gi_bake_device(const BakeInput& in, float* out, std::string& err) {
         // chunk is baked with them. Pipelined on one stream: the device
         // samples chunk i+1 and bakes chunk i-1 while the host converts
         // chunk i (two pinned buffers alternate).
-        float *d_srgb = nullptr, *d_lin = nullptr;
+        float *d_srgb = nullptr, *d_lin = nullptr, *d_rad = nullptr;
+        uint4* d_hit[2] = {nullptr, nullptr};  // chunk i's hits in d_hit[i % 2]
         const uint32_t chunk = std::min<uint32_t>(std::max<uint32_t>(D.n_active, 1u), kBakeChunkVoxels);
-        const size_t chunk_vals = (size_t)chunk * kGiSamples * 6;
+        const size_t chunk_rays = (size_t)chunk * kGiSamples, chunk_vals = chunk_rays * 6;
         if (e == cudaSuccess) e = m.put(&d_srgb, (const float*)nullptr, chunk_vals);
         if (e == cudaSuccess) e = m.put(&d_lin, (const float*)nullptr, chunk_vals);
+        if (e == cudaSuccess) e = m.put(&d_rad, (const float*)nullptr, chunk_rays * 3);
+        for (int b = 0; b < 2 && e == cudaSuccess; ++b) e = m.put(&d_hit[b], (const uint4*)nullptr, chunk_rays);
         HostPinned hp;
         cudaStream_t st = nullptr;
         cudaEvent_t ready[2] = {nullptr, nullptr};
@@ -637,7 +663,7 @@ swr_status gi_bake_device(const BakeInput& in, float* out, std::string& err) {
             range(i, k0, k1);
             const size_t nv = (size_t)(k1 - k0) * kGiSamples * 6;
             k_gi_tex<<<(uint32_t)std::min<uint64_t>(((uint64_t)(k1 - k0) * kGiSamples + 127) / 128, (uint64_t)sms * 64),
-                       128, 0, st>>>(D, k0, k1, d_srgb);
+                       128, 0, st>>>(D, k0, k1, d_hit[i % 2], d_srgb);
             cudaError_t x = cudaGetLastError();
             if (x == cudaSuccess)
                 x = cudaMemcpyAsync(hp.p + (i % 2) * chunk_vals, d_srgb, nv * sizeof(float), cudaMemcpyDeviceToHost, st);
@@ -664,8 +690,13 @@ swr_status gi_bake_device(const BakeInput& in, float* out, std::string& err) {
             // same pinned buffer (chunk i + 2's samples).
             e = cudaMemcpyAsync(d_lin, vals, nv * sizeof(float), cudaMemcpyHostToDevice, st);
             if (e != cudaSuccess) break;
-            k_gi_bake<<<(uint32_t)std::min<uint64_t>((k1 - k0 + 127) / 128, (uint64_t)sms * 64), 128, 0, st>>>(
-                D, k0, k1, d_lin);
+            // Chunk i + 1 was sampled above into the other hit buffer; d_lin
+            // and d_rad are next written after these two kernels in stream
+            // order.
+            k_gi_ray<<<(uint32_t)std::min<uint64_t>(((uint64_t)(k1 - k0) * kGiSamples + 127) / 128, (uint64_t)sms * 64),
+                       128, 0, st>>>(D, k0, k1, d_hit[i % 2], d_lin, d_rad);
+            k_gi_accum<<<(uint32_t)std::min<uint64_t>((k1 - k0 + 127) / 128, (uint64_t)sms * 64), 128, 0, st>>>(
+                D, k0, k1, d_hit[i % 2], d_rad);
             e = cudaGetLastError();
         }
         if (st) {
