@@ -1391,30 +1391,31 @@ __device__ __forceinline__ void raster_slow_region(RasterShared<S>& s, const Fra
 // slower.) The floor on a packet's depths, and the argument that it covers
 // every rounding of the raster's arithmetic, are in depthfloor.cuh.
 
-// Farthest key depth of each 8x8-px cell (four threads per cell, two rows
-// each), then a barrier.
+// Farthest key depth of each 8x8-px cell, then a barrier. Warp w takes cell
+// row w: each load reads whole key rows (16 B a lane, consecutive lanes
+// consecutive keys), so the warp's accesses cover distinct banks; four lanes
+// hold a cell's part of a row and shuffles fold the lanes and rows.
 template <int S>
 __device__ __forceinline__ void cell_depths(RasterShared<S>& s) {
-    constexpr int CW = S / 8, NC = CW * CW;
-    const int t = (int)threadIdx.x;
-    if ((t & ~31) < NC * 4) {  // whole warps
+    constexpr int CW = S / 8;      // cells per side
+    constexpr int LPR = S / 2;     // lanes per key row (two keys a lane)
+    constexpr int RPW = 32 / LPR;  // key rows per warp load
+    const int lane = (int)(threadIdx.x & 31u), warp = (int)(threadIdx.x >> 5);
+    if (warp < CW) {
         uint32_t m = 0;
-        if (t < NC * 4) {
-            const int cell = t >> 2, part = t & 3;
-            const int cx = cell % CW, cy = cell / CW;
+        const int col = (lane % LPR) * 2, sub = lane / LPR;
 #pragma unroll
-            for (int r = 0; r < 2; ++r) {
-                const ulonglong2* row = reinterpret_cast<const ulonglong2*>(s.sk + (cy * 8 + part * 2 + r) * S + cx * 8);
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    const ulonglong2 v = row[i];
-                    m = max(m, max((uint32_t)(v.x >> 32), (uint32_t)(v.y >> 32)));
-                }
-            }
+        for (int rr = 0; rr < 8; rr += RPW) {
+            const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(s.sk + (warp * 8 + rr + sub) * S + col);
+            m = max(m, max((uint32_t)(v.x >> 32), (uint32_t)(v.y >> 32)));
         }
+        // The four lanes of a cell in a row, then the rows the warp's
+        // lanes read side by side.
         m = max(m, __shfl_xor_sync(0xFFFFFFFFu, m, 1));
         m = max(m, __shfl_xor_sync(0xFFFFFFFFu, m, 2));
-        if (t < NC * 4 && (t & 3) == 0) s.cell_far[t >> 2] = m;
+#pragma unroll
+        for (int o = LPR; o < 32; o <<= 1) m = max(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
+        if (lane < LPR && (lane & 3) == 0) s.cell_far[warp * CW + (lane >> 2)] = m;
     }
     __syncthreads();
 }
