@@ -2090,7 +2090,20 @@ __device__ __forceinline__ void shade_pixel(const FrameArgs& a, const uint8_t* t
 #define SWR_SHADE_BLOCKS 1
 #endif
 __device__ __forceinline__ void quad_xy(const DView& v, uint32_t lq, int32_t& qx, int32_t& qy) {
-#if SWR_SHADE_BLOCKS
+#if SWR_SHADE_BLOCKS == 2
+    const uint32_t n = lq >> 7;
+    const uint32_t brow = v.tiles_x_magic ? __umulhi(n, v.tiles_x_magic) : n;
+    const uint32_t bcol = (lq >> 3) - brow * (v.quad_pitch >> 1);
+    qx = (int32_t)(bcol * 2u + (lq & 1u));
+    qy = (int32_t)(brow * 4u + ((lq >> 1) & 3u));
+#elif SWR_SHADE_BLOCKS == 3
+    const uint32_t n = lq >> 7;
+    const uint32_t brow = v.tiles_x_magic ? __umulhi(n, v.tiles_x_magic) : n;
+    const uint32_t bcol = (lq >> 5) - brow * (v.quad_pitch >> 3);
+    const uint32_t w = (lq >> 3) & 3u;
+    qx = (int32_t)(bcol * 8u + (w & 1u) * 4u + (lq & 3u));
+    qy = (int32_t)(brow * 4u + (w >> 1) * 2u + ((lq >> 2) & 1u));
+#elif SWR_SHADE_BLOCKS
     const uint32_t n = lq >> 6;
     const uint32_t brow = v.tiles_x_magic ? __umulhi(n, v.tiles_x_magic) : n;
     const uint32_t bcol = (lq >> 3) - brow * (v.quad_pitch >> 2);
