@@ -2081,40 +2081,19 @@ __device__ __forceinline__ void shade_pixel(const FrameArgs& a, const uint8_t* t
 }
 
 // Quad (qx, qy) of view-local quad index lq over the padded quad grid
-// (quad_pitch = tiles_x * 32 quads wide, tiles_y * 32 rows). With
-// SWR_SHADE_BLOCKS each warp's eight quads form a 4x2 block (8x4 pixels),
-// blocks row by row: block row (lq >> 6) / tiles_x. Otherwise the quads run
-// in rows: row (lq >> 5) / tiles_x. Both divisions are a multiply with the
-// view's reciprocal (exact: the dividend is below 2^23, tiles_x <= 512).
-#ifndef SWR_SHADE_BLOCKS
-#define SWR_SHADE_BLOCKS 1
-#endif
+// (quad_pitch = tiles_x * 32 quads wide, tiles_y * 32 rows). Each warp's
+// eight quads form a 4x2 block (8x4 pixels), blocks row by row: a warp's
+// pixels then fall on fewer triangles than in a 16x2 strip, so its record and
+// texture loads hit more often (4K shade 0.604 -> 0.580 ms; 2x4 blocks and
+// 8x4-quad blocks per CTA measured the same). The block row is
+// (lq >> 6) / tiles_x by a multiply with the view's reciprocal (exact:
+// lq >> 6 < 2^23, tiles_x <= 512).
 __device__ __forceinline__ void quad_xy(const DView& v, uint32_t lq, int32_t& qx, int32_t& qy) {
-#if SWR_SHADE_BLOCKS == 2
-    const uint32_t n = lq >> 7;
-    const uint32_t brow = v.tiles_x_magic ? __umulhi(n, v.tiles_x_magic) : n;
-    const uint32_t bcol = (lq >> 3) - brow * (v.quad_pitch >> 1);
-    qx = (int32_t)(bcol * 2u + (lq & 1u));
-    qy = (int32_t)(brow * 4u + ((lq >> 1) & 3u));
-#elif SWR_SHADE_BLOCKS == 3
-    const uint32_t n = lq >> 7;
-    const uint32_t brow = v.tiles_x_magic ? __umulhi(n, v.tiles_x_magic) : n;
-    const uint32_t bcol = (lq >> 5) - brow * (v.quad_pitch >> 3);
-    const uint32_t w = (lq >> 3) & 3u;
-    qx = (int32_t)(bcol * 8u + (w & 1u) * 4u + (lq & 3u));
-    qy = (int32_t)(brow * 4u + (w >> 1) * 2u + ((lq >> 2) & 1u));
-#elif SWR_SHADE_BLOCKS
     const uint32_t n = lq >> 6;
     const uint32_t brow = v.tiles_x_magic ? __umulhi(n, v.tiles_x_magic) : n;
     const uint32_t bcol = (lq >> 3) - brow * (v.quad_pitch >> 2);
     qx = (int32_t)(bcol * 4u + (lq & 3u));
     qy = (int32_t)(brow * 2u + ((lq >> 2) & 1u));
-#else
-    const uint32_t n = lq >> 5;
-    const uint32_t row = v.tiles_x_magic ? __umulhi(n, v.tiles_x_magic) : n;
-    qy = (int32_t)row;
-    qx = (int32_t)(lq - row * v.quad_pitch);
-#endif
 }
 
 // One lane of the shading pass over the padded quad grid of every view.
