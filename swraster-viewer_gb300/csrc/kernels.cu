@@ -1708,13 +1708,10 @@ __global__ void __launch_bounds__(RasterShared<S>::kThreads, RasterShared<S>::kM
             const bool live = t < S * S;
             const int ql = live ? (t >> 2) : 0;
             const int32_t k = t & 3;
-            // Each warp's eight quads form a 4x2 block, as in k_shade.
-            const int bq = ql >> 3;
-            const int lx = (bq % (QS / 4)) * 4 + (ql & 3), ly = (bq / (QS / 4)) * 2 + ((ql >> 2) & 1);
-            const int32_t qx = (sx0 >> 1) + lx, qy = (sy0 >> 1) + ly;
+            const int32_t qx = (sx0 >> 1) + ql % QS, qy = (sy0 >> 1) + ql / QS;
             const bool needed = live && shade_needed(view, qx, qy);
             unsigned long long key = kEmptyKey;
-            if (needed) key = s.sk[(2 * ly + (k >> 1)) * S + 2 * lx + (k & 1)];
+            if (needed) key = s.sk[(2 * (ql / QS) + (k >> 1)) * S + 2 * (ql % QS) + (k & 1)];
             shade_pixel<true, kModeAny>(a, s.tab, view, sc, qx, qy, k, needed, key);
         }
         __syncthreads();
