@@ -59,19 +59,6 @@ constexpr uint32_t kFusedShadeMaxTile = 16;
 namespace swr {
 
 // --------------------------------------------------------------------------
-// Programmatic dependent launch. The frame's kernels are launched so that the
-// next one may be scheduled while the previous one drains: each starts with
-// pdl_wait(), which returns once every earlier kernel of the stream has
-// completed and its writes are visible (so nothing is read or written early),
-// then lets its own successor be scheduled. Launched without the attribute,
-// both are no-ops.
-// --------------------------------------------------------------------------
-__device__ __forceinline__ void pdl_wait() {
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
-
-// --------------------------------------------------------------------------
 // Small vector helpers (one lane of Vec3x4 / Vec4).
 // --------------------------------------------------------------------------
 struct f3 {
@@ -722,7 +709,6 @@ __device__ void draw_count_blocks(const FrameArgs& a) {
 }
 
 __global__ void __launch_bounds__(kSlotBlock) k_draw_emit(FrameArgs a) {
-    pdl_wait();
     __shared__ uint32_t sm[3 * (kSlotBlock / 32)];
     if (blockIdx.x == 0 && threadIdx.x == 0) a.counters->draw_done = 0u;  // for the next frame
     const uint32_t n = a.dyn->n_slots;
@@ -742,7 +728,6 @@ __global__ void __launch_bounds__(kSlotBlock) k_draw_emit(FrameArgs a) {
 }
 
 __global__ void __launch_bounds__(256) k_reset(FrameArgs a) {
-    pdl_wait();
     const uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t n = a.dyn->n_bins;
     for (uint32_t i = i0; i < n; i += gridDim.x * blockDim.x) a.tile_count[i] = 0u;
@@ -845,7 +830,6 @@ __device__ __forceinline__ void frontend_triangle(const FrameArgs& a, uint32_t c
 #define SWR_FRONTEND_MIN_BLOCKS 4
 #endif
 __global__ void __launch_bounds__(kChunkTris, SWR_FRONTEND_MIN_BLOCKS) k_frontend(FrameArgs a) {
-    pdl_wait();
     if (blockIdx.x < a.dyn->n_chunks) frontend_triangle(a, blockIdx.x);
 }
 
@@ -873,7 +857,6 @@ __device__ __forceinline__ float plane_dist(const Vtx& v, int p) {
 }
 
 __global__ void __launch_bounds__(128) k_clip(FrameArgs a) {
-    pdl_wait();
     const uint32_t nq = min(a.counters->clip_queue, a.clip_cap);
     const uint32_t tri_total = a.dyn->tri_total;
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
@@ -960,7 +943,6 @@ __device__ __forceinline__ uint32_t order_bucket(uint32_t c) {
 // a batch of many views (10^5 bins) overlap instead of following one another.
 constexpr int kScanUnroll = 8;
 __global__ void __launch_bounds__(1024) k_scan(FrameArgs a) {
-    pdl_wait();
     __shared__ uint32_t wsum[32];
     __shared__ uint32_t bucket[kOrderBuckets];
     const uint32_t n = a.dyn->n_bins;
@@ -1119,7 +1101,6 @@ __device__ __forceinline__ void scatter_slot(const FrameArgs& a, uint32_t slot, 
 }
 
 __global__ void k_scatter(FrameArgs a) {
-    pdl_wait();
     if (a.counters->status & (ST_BIN_OVERFLOW | ST_CLIP_OVERFLOW | ST_QUEUE_OVERFLOW)) return;
     const uint32_t tri_total = a.dyn->tri_total;
     const uint32_t n = tri_total + min(a.counters->extra_used, a.extra_cap);
@@ -1539,7 +1520,6 @@ __device__ __forceinline__ void shade_pixel(const FrameArgs& a, const uint8_t* t
 // regions' quads flattened over all lanes, pass 3 the sequential regions.
 template <int S, bool FUSE>
 __global__ void __launch_bounds__(RasterShared<S>::kThreads, RasterShared<S>::kMinBlocks) k_raster(FrameArgs a) {
-    pdl_wait();
     using Sh = RasterShared<S>;
     constexpr int NT = Sh::kThreads, R = Sh::kRegions, NW = NT / 32;
     extern __shared__ __align__(16) unsigned char raster_smem[];
@@ -2145,7 +2125,6 @@ template <bool GI> struct ShadeShape {
 // GI: the frame has scenes with a baked voxel grid. MODE: see shade_pixel.
 template <bool GI, int MODE>
 __global__ void __launch_bounds__(ShadeShape<GI>::kThreads, ShadeShape<GI>::kMinBlocks) k_shade(FrameArgs a) {
-    pdl_wait();
     __shared__ uint8_t tab[512];
     for (int i = threadIdx.x; i < 512; i += blockDim.x) tab[i] = a.rsqrt_table[i];
     __syncthreads();
@@ -2208,7 +2187,6 @@ __device__ __forceinline__ void quad_edge_values(const Edge& e, int32_t ox, int3
 // Quads are disjoint, so the per-pixel order is the sorted order.
 template <int S>
 __global__ void __launch_bounds__(kTransThreads) k_translucent(FrameArgs a) {
-    pdl_wait();
     __shared__ unsigned long long tkey[kTransCap];
     __shared__ uint32_t tslot[kTransCap];
     __shared__ uint32_t tsorted[kTransCap];
@@ -2352,7 +2330,6 @@ __global__ void __launch_bounds__(kTransThreads) k_translucent(FrameArgs a) {
 
 // Exposure applied after the host's update_auto_exposure (dt > 0 path).
 __global__ void k_resolve(FrameArgs a) {
-    pdl_wait();
     const uint32_t vi = blockIdx.y;
     if (vi >= a.dyn->n_views) return;
     const DView& v = a.views[vi];
@@ -2419,30 +2396,12 @@ void frame_grids(int num_sms, uint32_t S, bool fuse32, uint32_t* raster_grid, ui
     *shade_grid = (uint32_t)(num_sms * (sb > 0 ? sb : 1));
 }
 
-// Launches a frame kernel with programmatic stream serialization: it may be
-// scheduled while the stream's previous kernel drains, and waits for it in
-// pdl_wait().
-template <typename K>
-void frame_launch(K kernel, dim3 grid, dim3 block, size_t smem, cudaStream_t s, const FrameArgs& a) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = grid;
-    cfg.blockDim = block;
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, kernel, a);
-}
-
 void launch_reset(const FrameArgs& a, void* stream) {
     cudaStream_t s = (cudaStream_t)stream;
     const uint32_t n = a.stile_cap > 0 ? a.stile_cap : 1u;
     // Enough CTAs for the bins and for the draw-list blocks (one per 256 node slots).
     const uint32_t slot_blocks = a.gpu_draws ? (a.slot_cap + kSlotBlock - 1u) / kSlotBlock : 0u;
-    frame_launch(k_reset, min(max((n + 255) / 256, slot_blocks), 1024u), 256, 0, s, a);
+    k_reset<<<min(max((n + 255) / 256, slot_blocks), 1024u), 256, 0, s>>>(a);
 }
 
 uint32_t launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t* ev) {
@@ -2460,7 +2419,7 @@ uint32_t launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t
     if (a.gpu_draws) {
         const uint32_t sg = (a.slot_cap + kSlotBlock - 1u) / kSlotBlock;
         if (sg > 1u) {
-            frame_launch(k_draw_emit, sg, kSlotBlock, 0, s, a);
+            k_draw_emit<<<sg, kSlotBlock, 0, s>>>(a);
             launches++;
         }
     }
@@ -2471,13 +2430,13 @@ uint32_t launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t
     if (a.chunk_cap > 0) {
         // Host-built draw lists (no-alloc frames) size chunk_cap exactly.
         const uint64_t most = a.gpu_draws ? (uint64_t)a.tri_cap / kChunkTris + a.draw_cap + 1u : a.chunk_cap;
-        frame_launch(k_frontend, (uint32_t)std::min<uint64_t>(a.chunk_cap, most), kChunkTris, 0, s, a);
+        k_frontend<<<(uint32_t)std::min<uint64_t>(a.chunk_cap, most), kChunkTris, 0, s>>>(a);
         launches++;
     }
     mark(2);
-    frame_launch(k_clip, num_sms * 4, 128, 0, s, a);
+    k_clip<<<num_sms * 4, 128, 0, s>>>(a);
     mark(3);
-    frame_launch(k_scan, 1, 1024, 0, s, a);
+    k_scan<<<1, 1024, 0, s>>>(a);
     launches += 2;
     mark(4);
     {
@@ -2486,7 +2445,7 @@ uint32_t launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t
         // loads stay coalesced (a grid-stride loop here made k_raster 2% slower).
         const uint64_t n = (uint64_t)a.tri_cap + a.extra_cap;
         if (n > 0) {
-            frame_launch(k_scatter, (unsigned)((n + 255) / 256), 256, 0, s, a);
+            k_scatter<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
             launches++;
         }
     }
@@ -2494,15 +2453,15 @@ uint32_t launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t
     const uint32_t rg = SWR_RASTER_PERSISTENT ? (a.raster_grid > 0 ? a.raster_grid : (uint32_t)num_sms)
                                               : (a.stile_cap > 0 ? a.stile_cap : 1u);
     switch (a.sched_tile) {
-        case 8: frame_launch(k_raster<8, true>, rg, RasterShared<8>::kThreads, sizeof(RasterShared<8>), s, a); break;
-        case 16: frame_launch(k_raster<16, true>, rg, RasterShared<16>::kThreads, sizeof(RasterShared<16>), s, a); break;
+        case 8: k_raster<8, true><<<rg, RasterShared<8>::kThreads, sizeof(RasterShared<8>), s>>>(a); break;
+        case 16: k_raster<16, true><<<rg, RasterShared<16>::kThreads, sizeof(RasterShared<16>), s>>>(a); break;
         case 32:
             if (a.fused_shade)
-                frame_launch(k_raster<32, true>, rg, RasterShared<32>::kThreads, sizeof(RasterShared<32>), s, a);
+                k_raster<32, true><<<rg, RasterShared<32>::kThreads, sizeof(RasterShared<32>), s>>>(a);
             else
-                frame_launch(k_raster<32, false>, rg, RasterShared<32>::kThreads, sizeof(RasterShared<32>), s, a);
+                k_raster<32, false><<<rg, RasterShared<32>::kThreads, sizeof(RasterShared<32>), s>>>(a);
             break;
-        default: frame_launch(k_raster<64, false>, rg, RasterShared<64>::kThreads, sizeof(RasterShared<64>), s, a); break;
+        default: k_raster<64, false><<<rg, RasterShared<64>::kThreads, sizeof(RasterShared<64>), s>>>(a); break;
     }
     launches++;
     mark(6);
@@ -2518,15 +2477,15 @@ uint32_t launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t
             }();
             const uint32_t sg = (uint32_t)num_sms * gi_blocks;
             const uint32_t T = ShadeShape<true>::kThreads;
-            if (a.rsqrt_uniform == 1u + kModeArm) frame_launch(k_shade<true, kModeArm>, sg, T, 0, s, a);
-            else if (a.rsqrt_uniform == 1u + kModeIeee) frame_launch(k_shade<true, kModeIeee>, sg, T, 0, s, a);
-            else frame_launch(k_shade<true, kModeAny>, sg, T, 0, s, a);
+            if (a.rsqrt_uniform == 1u + kModeArm) k_shade<true, kModeArm><<<sg, T, 0, s>>>(a);
+            else if (a.rsqrt_uniform == 1u + kModeIeee) k_shade<true, kModeIeee><<<sg, T, 0, s>>>(a);
+            else k_shade<true, kModeAny><<<sg, T, 0, s>>>(a);
         } else {
             const uint32_t sg = a.shade_grid > 0 ? a.shade_grid : (uint32_t)num_sms;
             const uint32_t T = ShadeShape<false>::kThreads;
-            if (a.rsqrt_uniform == 1u + kModeArm) frame_launch(k_shade<false, kModeArm>, sg, T, 0, s, a);
-            else if (a.rsqrt_uniform == 1u + kModeIeee) frame_launch(k_shade<false, kModeIeee>, sg, T, 0, s, a);
-            else frame_launch(k_shade<false, kModeAny>, sg, T, 0, s, a);
+            if (a.rsqrt_uniform == 1u + kModeArm) k_shade<false, kModeArm><<<sg, T, 0, s>>>(a);
+            else if (a.rsqrt_uniform == 1u + kModeIeee) k_shade<false, kModeIeee><<<sg, T, 0, s>>>(a);
+            else k_shade<false, kModeAny><<<sg, T, 0, s>>>(a);
         }
         launches++;
     }
@@ -2534,10 +2493,10 @@ uint32_t launch_frame(const FrameArgs& a, void* stream, int num_sms, cudaEvent_t
     if (a.has_translucent) {
         const uint32_t tg = (uint32_t)num_sms * 2u;
         switch (a.sched_tile) {
-            case 8: frame_launch(k_translucent<8>, tg, kTransThreads, 0, s, a); break;
-            case 16: frame_launch(k_translucent<16>, tg, kTransThreads, 0, s, a); break;
-            case 32: frame_launch(k_translucent<32>, tg, kTransThreads, 0, s, a); break;
-            default: frame_launch(k_translucent<64>, tg, kTransThreads, 0, s, a); break;
+            case 8: k_translucent<8><<<tg, kTransThreads, 0, s>>>(a); break;
+            case 16: k_translucent<16><<<tg, kTransThreads, 0, s>>>(a); break;
+            case 32: k_translucent<32><<<tg, kTransThreads, 0, s>>>(a); break;
+            default: k_translucent<64><<<tg, kTransThreads, 0, s>>>(a); break;
         }
         launches++;
         if (!a.defer_resolve) {
@@ -2562,7 +2521,7 @@ void launch_resolve(const FrameArgs& a, void* stream) {
     cudaStream_t s = (cudaStream_t)stream;
     const uint32_t maxpx = a.pixel_cap > 0 ? a.pixel_cap : 1u;
     dim3 grid((maxpx + 255) / 256, a.view_cap > 0 ? a.view_cap : 1u);
-    frame_launch(k_resolve, grid, 256, 0, s, a);
+    k_resolve<<<grid, 256, 0, s>>>(a);
 }
 
 }  // namespace swr
