@@ -1265,7 +1265,6 @@ struct RasterShared {
     float p_sx[3][kThreads], p_sy[3][kThreads];
     float p_ooa[kThreads], p_oow[3][kThreads], p_zow[3][kThreads];
     uint32_t p_seq8[kThreads], p_mat[kThreads], p_amip[kThreads], p_slot[kThreads];
-    uint32_t p_zfloor[kThreads];  // the triangle's depth floor (RecRaster.zfloor)
     uint32_t scan[kThreads / 32][2];
     uint32_t cell_far[(S / 8) * (S / 8)];  // farthest key depth of each 8x8-px cell (orderable bits)
     uint32_t n_regions, n_quads, n_slow, cur_tile;
@@ -1277,7 +1276,7 @@ constexpr uint32_t kSlowRegion = 0x8000u;  // region replays the sequential addi
 // Interpolation constants of one packet.
 struct PacketLanes {
     float ooa, oow[3], zow[3];
-    uint32_t seq8, mat, zfloor;
+    uint32_t seq8, mat;
 };
 
 template <int S>
@@ -1291,7 +1290,6 @@ __device__ __forceinline__ PacketLanes packet_lanes(const RasterShared<S>& s, ui
     }
     L.seq8 = s.p_seq8[pk];
     L.mat = s.p_mat[pk];
-    L.zfloor = s.p_zfloor[pk];
     return L;
 }
 
@@ -1302,15 +1300,10 @@ template <int S>
 __device__ __forceinline__ void raster_lane(RasterShared<S>& s, const FrameArgs& a, const DScene& sc,
                                             const PacketLanes& L, uint32_t pk, float w1, float w2, int32_t lx,
                                             int32_t ly) {
-    unsigned long long* slot = s.sk + ly * S + lx;
-    const unsigned long long cur = *slot;
-    // A pixel whose key already lies nearer than every depth the triangle can
-    // take (its floor, orderable bits; 0 when none was taken) keeps its key:
-    // skip the interpolation and the division (keys only decrease, and a tie
-    // needs an equal depth).
-    if (L.zfloor > (uint32_t)(cur >> 32)) return;
     const float b1 = w1 * L.ooa, b2 = w2 * L.ooa;
     const float oi = interp(L.oow, b1, b2), zi = interp(L.zow, b1, b2);
+    unsigned long long* slot = s.sk + ly * S + lx;
+    const unsigned long long cur = *slot;
     const float w = 1.0f / oi;
     const float z = zi * w;
     bool pass = (z == z);
@@ -1663,7 +1656,6 @@ __global__ void __launch_bounds__(RasterShared<S>::kThreads, RasterShared<S>::kM
                 s.p_mat[pk] = c.r.material;
                 s.p_amip[pk] = c.amip;
                 s.p_slot[pk] = slot;
-                s.p_zfloor[pk] = c.r.zfloor;
                 packet_regions<S>(s, c, sx0, sy0, true, pk, pr, pq, bmask);
             }
             cursor += n_taken;
