@@ -1447,7 +1447,7 @@ __device__ __forceinline__ uint32_t packet_floor(const PacketCtx& c) { return c.
 template <int S>
 __device__ __forceinline__ void packet_regions(RasterShared<S>& s, const PacketCtx& c, int32_t sx0, int32_t sy0,
                                                bool write, uint32_t pk, uint32_t& n_r, uint32_t& n_q,
-                                               uint32_t& bmask, bool cull_blocks = false) {
+                                               uint32_t& bmask) {
     auto region = [&](int32_t ox, int32_t oy, int32_t ex, int32_t ey) {
         uint32_t ij = 0;
         const uint32_t nq = clip_quads(ox, oy, ex, ey, sx0, sy0, S, ij);
@@ -1485,10 +1485,6 @@ __device__ __forceinline__ void packet_regions(RasterShared<S>& s, const PacketC
             if (write) {
                 if (bmask & bit) region(ox, oy, min(ox + 256, c.xe), min(oy + 256, c.ye));
             } else if (!block_rejected(c.e12, c.e20, c.e01, ox, oy) &&
-                       !(cull_blocks &&
-                         packet_floor(c) > cells_far<S>(s, ox >> kSubpixelShift, min(ox + 256, c.xe) >> kSubpixelShift,
-                                                        oy >> kSubpixelShift, min(oy + 256, c.ye) >> kSubpixelShift,
-                                                        sx0, sy0)) &&
                        region(ox, oy, min(ox + 256, c.xe), min(oy + 256, c.ye))) {
                 bmask |= bit;
             }
@@ -1597,7 +1593,7 @@ __global__ void __launch_bounds__(RasterShared<S>::kThreads, RasterShared<S>::kM
                                                       c.ys >> kSubpixelShift, c.ye >> kSubpixelShift, sx0, sy0);
                     hidden = far < 0xFF800000u && packet_floor(c) > far;
                 }
-                if (!hidden) packet_regions<S>(s, c, sx0, sy0, false, threadIdx.x, n_r, n_q, bmask, kCull && cells_valid);
+                if (!hidden) packet_regions<S>(s, c, sx0, sy0, false, threadIdx.x, n_r, n_q, bmask);
             }
             if (threadIdx.x == 0) s.n_slow = 0;
             // Block-wide exclusive scan of (regions, quads).
