@@ -1256,15 +1256,18 @@ struct RasterShared {
     static constexpr int kRegions = kThreads + kThreads / 2;  // regions staged per round
     unsigned long long sk[S * S];                             // depth keys of the scheduling tile
     // Regions of the round, in packet order.
-    float r_w[12][kRegions];   // origin edge values
+    float4 r_w[3][kRegions];   // origin edge values: edge e's four sample lanes in r_w[e]
     uint32_t r_geom[kRegions];  // quad range (16 b) | exact << 15 | origin x, y relative to the tile (int8 each)
     uint32_t r_pi[kRegions];    // packet index | kSlowRegion | ceil(2^15 / ni) << 16
     uint32_t r_qbeg[kRegions + 40];  // first flattened quad of each region, then end markers
     uint16_t slow[kRegions];    // regions that replay the sequential additions
     // Packets of the round, one per thread.
-    float p_sx[3][kThreads], p_sy[3][kThreads];
-    float p_ooa[kThreads], p_oow[3][kThreads], p_zow[3][kThreads];
-    uint32_t p_seq8[kThreads], p_mat[kThreads], p_amip[kThreads], p_slot[kThreads];
+    // Per packet, packed for 16-byte loads: (sx12, sx20, sx01, sy12), (sy20, sy01),
+    // (ooa, oow a, da, db), (zow a, da, db, seq8 bits).
+    float4 p_s[kThreads];
+    float2 p_s2[kThreads];
+    float4 p_o[kThreads], p_z[kThreads];
+    uint32_t p_mat[kThreads], p_amip[kThreads], p_slot[kThreads];
     uint32_t scan[kThreads / 32][2];
     uint32_t cell_far[(S / 8) * (S / 8)];  // farthest key depth of each 8x8-px cell (orderable bits)
     uint32_t n_regions, n_quads, n_slow, cur_tile;
@@ -1282,13 +1285,15 @@ struct PacketLanes {
 template <int S>
 __device__ __forceinline__ PacketLanes packet_lanes(const RasterShared<S>& s, uint32_t pk) {
     PacketLanes L;
-    L.ooa = s.p_ooa[pk];
-#pragma unroll
-    for (int t = 0; t < 3; ++t) {
-        L.oow[t] = s.p_oow[t][pk];
-        L.zow[t] = s.p_zow[t][pk];
-    }
-    L.seq8 = s.p_seq8[pk];
+    const float4 o = s.p_o[pk], z = s.p_z[pk];
+    L.ooa = o.x;
+    L.oow[0] = o.y;
+    L.oow[1] = o.z;
+    L.oow[2] = o.w;
+    L.zow[0] = z.x;
+    L.zow[1] = z.y;
+    L.zow[2] = z.z;
+    L.seq8 = __float_as_uint(z.w);
     L.mat = s.p_mat[pk];
     return L;
 }
@@ -1330,12 +1335,18 @@ __device__ __forceinline__ void raster_exact_quad(RasterShared<S>& s, const Fram
     const int32_t jj = (int32_t)((q * (pi >> 16)) >> 15);  // q / ni for q < 2^12
     const int32_t i = ilo + ((int32_t)q - jj * ni), j = jlo + jj;
     const float fi = (float)i, fj = (float)j;
+    const float4 ps = s.p_s[pk];
+    const float2 ps2 = s.p_s2[pk];
+    const float sx[3] = {ps.x, ps.y, ps.z}, sy[3] = {ps.w, ps2.x, ps2.y};
     float w[12];
 #pragma unroll
     for (int e = 0; e < 3; ++e) {
-        const float d = s.p_sy[e][pk] * fj + s.p_sx[e][pk] * fi;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) w[4 * e + k] = s.r_w[4 * e + k][r] + d;
+        const float d = sy[e] * fj + sx[e] * fi;
+        const float4 o = s.r_w[e][r];
+        w[4 * e] = o.x + d;
+        w[4 * e + 1] = o.y + d;
+        w[4 * e + 2] = o.z + d;
+        w[4 * e + 3] = o.w + d;
     }
     uint32_t cov = 0;
 #pragma unroll
@@ -1360,11 +1371,15 @@ __device__ __forceinline__ void raster_slow_region(RasterShared<S>& s, const Fra
     const int32_t ilo = (int32_t)(g & 0xFu), jlo = (int32_t)((g >> 4) & 0xFu);
     const int32_t ihi = (int32_t)((g >> 8) & 0xFu), jhi = (int32_t)((g >> 12) & 0xFu);
     const int32_t lx0 = geom_ox(g) + (k & 1), ly0 = geom_oy(g) + (k >> 1);
-    const float sx0 = s.p_sx[0][pk], sx1 = s.p_sx[1][pk], sx2 = s.p_sx[2][pk];
-    const float sy0 = s.p_sy[0][pk], sy1 = s.p_sy[1][pk], sy2 = s.p_sy[2][pk];
+    const float4 ps = s.p_s[pk];
+    const float2 ps2 = s.p_s2[pk];
+    const float sx0 = ps.x, sx1 = ps.y, sx2 = ps.z;
+    const float sy0 = ps.w, sy1 = ps2.x, sy2 = ps2.y;
     const PacketLanes L = packet_lanes(s, pk);
     for (int32_t j = jlo + (int32_t)(lane >> 2); j < jhi; j += 8) {
-        float w0 = s.r_w[k][r], w1 = s.r_w[4 + k][r], w2 = s.r_w[8 + k][r];
+        const float* rw = reinterpret_cast<const float*>(&s.r_w[0][r]);
+        float w0 = rw[k], w1 = reinterpret_cast<const float*>(&s.r_w[1][r])[k],
+              w2 = reinterpret_cast<const float*>(&s.r_w[2][r])[k];
         for (int32_t t = 0; t < j; ++t) {
             w0 += sy0;
             w1 += sy1;
@@ -1458,7 +1473,7 @@ __device__ __forceinline__ void packet_regions(RasterShared<S>& s, const PacketC
             origin_values(c, ox, oy, w);
             const bool exact = region_exact(c, w, ij);
 #pragma unroll
-            for (int t = 0; t < 12; ++t) s.r_w[t][r] = w[t];
+            for (int e = 0; e < 3; ++e) s.r_w[e][r] = make_float4(w[4 * e], w[4 * e + 1], w[4 * e + 2], w[4 * e + 3]);
             const int32_t ox_rel = (ox >> kSubpixelShift) - sx0, oy_rel = (oy >> kSubpixelShift) - sy0;
             s.r_geom[r] = ij | ((uint32_t)(ox_rel & 0xFF) << 16) | ((uint32_t)(oy_rel & 0xFF) << 24);
             const uint32_t ni = ((ij >> 8) & 0xFu) - (ij & 0xFu);
@@ -1640,19 +1655,10 @@ __global__ void __launch_bounds__(RasterShared<S>::kThreads, RasterShared<S>::kM
             }
             if (taken && n_r > 0u) {
                 const uint32_t pk = threadIdx.x;
-                s.p_sx[0][pk] = c.e12.sx;
-                s.p_sx[1][pk] = c.e20.sx;
-                s.p_sx[2][pk] = c.e01.sx;
-                s.p_sy[0][pk] = c.e12.sy;
-                s.p_sy[1][pk] = c.e20.sy;
-                s.p_sy[2][pk] = c.e01.sy;
-                s.p_ooa[pk] = c.r.ooa;
-#pragma unroll
-                for (int t = 0; t < 3; ++t) {
-                    s.p_oow[t][pk] = c.r.oow[t];
-                    s.p_zow[t][pk] = c.r.zow[t];
-                }
-                s.p_seq8[pk] = c.r.seq8;
+                s.p_s[pk] = make_float4(c.e12.sx, c.e20.sx, c.e01.sx, c.e12.sy);
+                s.p_s2[pk] = make_float2(c.e20.sy, c.e01.sy);
+                s.p_o[pk] = make_float4(c.r.ooa, c.r.oow[0], c.r.oow[1], c.r.oow[2]);
+                s.p_z[pk] = make_float4(c.r.zow[0], c.r.zow[1], c.r.zow[2], __uint_as_float(c.r.seq8));
                 s.p_mat[pk] = c.r.material;
                 s.p_amip[pk] = c.amip;
                 s.p_slot[pk] = slot;
