@@ -412,7 +412,7 @@ def measure_served(args, local=0):
     for rate in [float(x) for x in args.rates.split(",")]:
         fixed[str(int(rate))] = {"served": served_at(rate, args.seconds), "plain": plain_at(rate, args.seconds)}
 
-    def best_rate(fn, bound, lo, hi, iters=4):
+    def best_rate(fn, bound, lo, hi, iters=6):
         """Largest arrival rate in [lo, hi] (bisection on a log scale) whose
         p99 stays within `bound`, with the measurement taken there."""
         ok = fn(lo, args.seconds)
