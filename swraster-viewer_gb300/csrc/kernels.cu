@@ -132,9 +132,7 @@ __device__ __forceinline__ uint32_t sample_texel(const DTexture& t, float u, flo
     const float wf = t.mip_wf[mip], hf = t.mip_hf[mip];
     const uint32_t x = f2u_sat(apply_wrap(floorf(u * wf), wf, t.mip_rwf[mip], ws));
     const uint32_t y = f2u_sat(apply_wrap(floorf(v * hf), hf, t.mip_rhf[mip], wt));
-    // Material textures are stored in 4x4-texel tiles (upload_scene).
-    const uint32_t tw = (t.mip_w[mip] + 3u) >> 2;
-    const uint32_t idx = t.mip_offset[mip] + ((((y >> 2) * tw + (x >> 2)) << 4) | ((y & 3u) << 2) | (x & 3u));
+    const uint32_t idx = t.mip_offset[mip] + y * t.mip_w[mip] + x;
     return __ldg(t.data + idx);
 }
 

@@ -14,7 +14,6 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstring>
@@ -1342,25 +1341,6 @@ DTexture to_dtex(const HTexture& t, uintptr_t addr) {
     }
     return d;
 }
-// Material textures go to the device in 4x4-texel tiles (64 B, row-major
-// tiles, row-major texels inside): a warp's 8x4 pixels then fetch from one or
-// two tiles instead of four texture rows. Each mip level is padded to whole
-// tiles; `offs` gets the levels' tiled offsets.
-std::vector<uint32_t> tile_texture(const HTexture& t, uint32_t offs[16]) {
-    std::vector<uint32_t> out;
-    for (uint32_t m = 0; m <= t.max_mip && m < 16; ++m) {
-        const uint32_t w = t.mip_widths[m], h = t.mip_heights[m];
-        const uint32_t tw = (w + 3u) / 4u, th = (h + 3u) / 4u;
-        offs[m] = (uint32_t)out.size();
-        out.resize(out.size() + (size_t)tw * th * 16u, 0u);
-        const uint32_t* src = t.data.data() + t.mip_offsets[m];
-        uint32_t* dst = out.data() + offs[m];
-        for (uint32_t y = 0; y < h; ++y)
-            for (uint32_t x = 0; x < w; ++x)
-                dst[((size_t)(y >> 2) * tw + (x >> 2)) * 16u + (y & 3u) * 4u + (x & 3u)] = src[(size_t)y * w + x];
-    }
-    return out;
-}
 }  // namespace
 
 swr_status upload_scene(SceneImpl* s, std::string& err, bool to_device) {
@@ -1462,20 +1442,7 @@ swr_status upload_scene(SceneImpl* s, std::string& err, bool to_device) {
     all_tex.push_back(&s->cubemap);
     all_tex.push_back(&s->specular);
     all_tex.push_back(&s->brdf_lut);
-    // Material textures tiled (sample_texel), the environment, the prefiltered
-    // environment and the BRDF LUT row-major (sample_cube, sample_bilinear).
-    std::vector<std::array<uint32_t, 16>> tiled_offs(s->textures.size());
-    std::vector<std::vector<uint32_t>> tiled(s->textures.size());
-    parallel_for(s->textures.size(), hw_threads(0),
-                 [&](size_t i) { tiled[i] = tile_texture(s->textures[i], tiled_offs[i].data()); });
-    for (size_t i = 0; i < all_tex.size(); ++i) {
-        if (i < s->textures.size()) {
-            o_tex.push_back(ar.add(tiled[i].data(), tiled[i].size() * sizeof(uint32_t)));
-            std::vector<uint32_t>().swap(tiled[i]);
-        } else {
-            o_tex.push_back(ar.add(all_tex[i]->data.data(), all_tex[i]->data.size() * sizeof(uint32_t)));
-        }
-    }
+    for (const HTexture* t : all_tex) o_tex.push_back(ar.add(t->data.data(), t->data.size() * sizeof(uint32_t)));
     const uint64_t o_vox = ar.add(s->voxel_light.data(), s->voxel_light.size() * sizeof(float));
     const uint64_t o_sh4 = ar.add(s->voxel_sh4.data(), s->voxel_sh4.size() * sizeof(float));
     const uint64_t o_dtex = ar.add(nullptr, all_tex.size() * sizeof(DTexture));
@@ -1494,11 +1461,7 @@ swr_status upload_scene(SceneImpl* s, std::string& err, bool to_device) {
     const uintptr_t base = reinterpret_cast<uintptr_t>(dblock);
     auto at = [&](uint64_t off) { return base + (uintptr_t)off; };
     std::vector<DTexture> dtex;
-    for (size_t i = 0; i < all_tex.size(); ++i) {
-        dtex.push_back(to_dtex(*all_tex[i], at(o_tex[i])));
-        if (i < s->textures.size())
-            for (uint32_t m = 0; m <= all_tex[i]->max_mip && m < 16; ++m) dtex.back().mip_offset[m] = tiled_offs[i][m];
-    }
+    for (size_t i = 0; i < all_tex.size(); ++i) dtex.push_back(to_dtex(*all_tex[i], at(o_tex[i])));
     std::memcpy(ar.host.data() + o_dtex, dtex.data(), dtex.size() * sizeof(DTexture));
     DScene& ds = s->dscene;
     ds = DScene{};
