@@ -619,7 +619,9 @@ def main():
             "steps": plain["steps"], "warmup": max(3, args.warmup), "ms_per_step": plain["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded scene of the configured shape; inputs larger than L2)",
-            "config": dict(plain["config"], parallelism="replicas" if world > 1 else "single")}
+            "config": dict(plain["config"], parallelism="replicas" if world > 1 else "single",
+                           l2="no flush: inputs larger than L2 (the scene's vertices, indices and textures, "
+                              "and each frame's records, keys and outputs)")}
     for k in ("gtri_per_s", "gpix_per_s", "stage_ms", "frame_stats", "issue_roofline", "roofline", "clocks",
               "gpu_launches", "kernels_per_frame", "e2e"):
         line[k] = plain[k]
